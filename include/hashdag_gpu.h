@@ -1,0 +1,225 @@
+/*
+ * hashdag_gpu.h -- C ABI of the GB300 HashDAG edit engine.
+ *
+ * The engine keeps a HashDAG node pool resident in device memory and applies
+ * stateless geometry edits to it with sm_103a kernels.  The pool keeps the
+ * reference's storage format word for word:
+ *   - a NodePointer is a global word index into a bucketed, paged address space,
+ *     0xFFFFFFFF is Null (include/hashdag/NodePointer.hpp:13-31);
+ *   - an inner node is a mask word (low 8 bits = child mask) followed by the
+ *     non-null children in ascending child order; a leaf is two words holding
+ *     a 4x4x4 bitmask (include/hashdag/NodePool.hpp:214-317);
+ *   - a node lives in bucket  base[level] + (hash(node) & (buckets_at_level-1))
+ *     and never straddles a page; the tail of a page that cannot hold the next
+ *     node is zero-filled (include/hashdag/NodePool.hpp:134-212);
+ *   - hash = MurmurHash3-x86-32 body (seed 0, length in words) for inner nodes
+ *     and the 64-bit finaliser truncated to 32 bits for leaves
+ *     (include/hashdag/Hasher.hpp:21-48).
+ * So a pool downloaded with hd_pool_read_* can be handed to the reference's
+ * CPU NodePoolBase / NodePoolTraversal unchanged, and a pool built by the
+ * reference can be uploaded with hd_pool_upload.
+ *
+ * All entry points return an hd_status.  None falls back silently: where the
+ * reference returns the stale node when a bucket is full
+ * (include/hashdag/NodePool.hpp:138-139,195,210) this library returns
+ * HD_ERR_BUCKET_FULL and leaves *out_root equal to the input root.
+ * Calls on one pool are serialised by an internal mutex; different pools may
+ * be used from different threads and streams at the same time.
+ */
+#ifndef HASHDAG_GPU_H
+#define HASHDAG_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum hd_status {
+	HD_OK = 0,
+	HD_ERR_INVALID_ARG = 1,  /* bad config / argument (reference: Config::Validate false, Create -> nullptr) */
+	HD_ERR_BUCKET_FULL = 2,  /* a node did not fit into its bucket (reference: silent fallback) */
+	HD_ERR_POOL_OOM = 3,     /* the device page heap has no free page left */
+	HD_ERR_INDEX_FULL = 4,   /* the device dedup index has no free slot left */
+	HD_ERR_CAPACITY = 5,     /* edit workspace too small (hd_edit grows it and retries by itself) */
+	HD_ERR_CUDA = 6,         /* a CUDA runtime call failed */
+	HD_ERR_TIMEOUT = 7,      /* a bounded device-side wait ran out */
+	HD_ERR_NO_DEVICE = 8,    /* no CUDA device / extension not usable */
+} hd_status;
+
+#define HD_NULL_PTR 0xFFFFFFFFu
+#define HD_MAX_LEVELS 24
+
+/* WordSpanHasher choice (include/hashdag/NodePool.hpp:23, include/hashdag/Hasher.hpp:21-48).
+ * HD_HASHER_ZERO maps every node to the first bucket of its level, like the
+ * reference test fixture ZeroHasher (test/test.cpp:10-12). */
+typedef enum hd_hasher { HD_HASHER_MURMUR32 = 0, HD_HASHER_ZERO = 1 } hd_hasher;
+
+/* hashdag::Config<uint32_t> (include/hashdag/Config.hpp:15-57).
+ * node_levels = bucket_bits_each_level.size(); resolution = 2^(node_levels+1). */
+typedef struct hd_config {
+	uint32_t word_bits_per_page;
+	uint32_t page_bits_per_bucket;
+	uint32_t node_levels;
+	uint32_t hasher; /* hd_hasher */
+	uint32_t bucket_bits_each_level[HD_MAX_LEVELS];
+} hd_config;
+
+/* Stateless editors of the reference application (src/main.cpp:32-150).
+ *   SPHERE: voxel p is inside iff |p - center|^2 <= r2 (integer voxel corner).
+ *   AABB:   voxel p is inside iff p0 <= p < p1 on every axis (half-open box).
+ * FILL sets the voxels inside, DIG clears them (SphereEditor<kFill/kDig>;
+ * the AABB dig follows the same pattern).  A list of edits is applied in
+ * order: per voxel the last edit whose shape covers it decides. */
+typedef enum hd_shape { HD_SHAPE_SPHERE = 0, HD_SHAPE_AABB = 1 } hd_shape;
+typedef enum hd_op { HD_OP_FILL = 0, HD_OP_DIG = 1 } hd_op;
+
+typedef struct hd_edit_desc {
+	uint32_t shape;  /* hd_shape */
+	uint32_t op;     /* hd_op */
+	uint32_t p0[3];  /* sphere centre, or box min (inclusive), voxel units */
+	uint32_t p1[3];  /* box max (exclusive); ignored for spheres */
+	uint64_t r2;     /* sphere radius squared; ignored for boxes */
+} hd_edit_desc;      /* 40 bytes */
+
+typedef struct hd_pool hd_pool;
+
+typedef struct hd_pool_stats {
+	uint64_t heap_pages;       /* physical pages in the device heap */
+	uint64_t used_pages;       /* physical pages handed out */
+	uint64_t total_buckets;
+	uint64_t total_pages;      /* virtual pages (Config::GetTotalPages) */
+	uint64_t index_slots;
+	uint64_t index_used;       /* dedup index slots holding a node */
+	uint32_t max_bucket_words; /* fullest bucket */
+	uint32_t words_per_bucket;
+} hd_pool_stats;
+
+/* Ray hit of the read path (shader/src/trace.frag:69-270 DAG_RayMarch without LOD).
+ * hit = 0 means the ray left the volume.  voxel = integer voxel coordinate of
+ * the hit cell's minimum corner, size = its edge in voxels (1 for a voxel),
+ * level = voxel_level - log2(size); t = ray parameter at the entry point;
+ * pos = hit position in [0,1]^3 as NodePoolTraversal::Traversal returns it
+ * (include/hashdag/NodePoolTraversal.hpp:253-255). */
+typedef struct hd_hit {
+	uint32_t voxel[3];
+	uint32_t size;
+	uint32_t level;
+	uint32_t hit;
+	float t;
+	float pos[3];
+} hd_hit; /* 40 bytes */
+
+/* Pinhole camera (src/Camera.hpp:36-52, shader/src/trace.frag:366-370):
+ * ray(u,v) = normalize(look - side*(2u-1) - up*(2v-1)), origin = position,
+ * all in [0,1]^3 scene units; u = (px+0.5)/width, v = (py+0.5)/height. */
+typedef struct hd_camera {
+	float position[3];
+	float look[3];
+	float side[3];
+	float up[3];
+} hd_camera;
+
+/* ---- pool lifecycle -------------------------------------------------------
+ * replaces NodePoolBase(Config) (include/hashdag/NodePool.hpp:400-403) and
+ * DAGNodePool::Create (src/DAGNodePool.cpp:9-47).  heap_pages = device pages
+ * reserved for node storage (memory = heap_pages << word_bits_per_page words);
+ * index_log2 = log2 of dedup index slots (0 = sized from heap_pages).
+ * The filled node of every level (make_filled_node_pointers,
+ * include/hashdag/NodePool.hpp:240-262) is inserted at creation. */
+hd_status hd_pool_create(const hd_config *config, uint64_t heap_pages, uint32_t index_log2, int device,
+                         hd_pool **out_pool);
+void hd_pool_destroy(hd_pool *pool);
+/* Config::Validate (include/hashdag/Config.hpp:48-56). */
+int hd_config_validate(const hd_config *config);
+/* DefaultConfig<uint32_t>{...}() (include/hashdag/Config.hpp:59-75). */
+void hd_config_default(uint32_t level_count, uint32_t top_level_count, uint32_t word_bits_per_page,
+                       uint32_t page_bits_per_bucket, uint32_t bucket_bits_per_top_level,
+                       uint32_t bucket_bits_per_bottom_level, hd_config *out);
+/* m_filled_node_pointers (include/hashdag/NodePool.hpp:54), one per level. */
+hd_status hd_pool_filled_pointers(const hd_pool *pool, uint32_t *out_levels);
+hd_status hd_pool_get_stats(const hd_pool *pool, hd_pool_stats *out);
+/* Sticky device error word of the pool (for the *_async entry points); 0 = none.
+ * hd_pool_clear_error resets it. */
+hd_status hd_pool_get_error(const hd_pool *pool, uint32_t *out_error);
+hd_status hd_pool_clear_error(hd_pool *pool);
+
+/* ---- edit path ------------------------------------------------------------
+ * replaces NodePoolBase::Edit (include/hashdag/NodePool.hpp:405-417) and
+ * NodePoolThreadedEdit::ThreadedEdit (include/hashdag/NodePoolThreadedEdit.hpp:104-126)
+ * for the stateless editors (include/hashdag/Editor.hpp:36-55, src/main.cpp:32-150).
+ * Applies edits[0..n) in order to root and returns the new root.  n = 1 is the
+ * plain one-edit form; n > 1 is one level-synchronous batched pass whose
+ * voxel result equals applying the edits one after another.  Host edit array;
+ * blocks until the result is known.  stream = cudaStream_t or NULL. */
+hd_status hd_edit(hd_pool *pool, uint32_t root, const hd_edit_desc *edits, uint32_t n, uint32_t *out_root,
+                  void *stream);
+/* Same work with device-resident inputs and output and no host synchronisation:
+ * d_edits and d_out_root are device pointers; status is reported through the
+ * pool's sticky error word (hd_pool_get_error).  The workspace must have been
+ * sized by hd_edit_reserve (or a previous hd_edit of at least this size). */
+hd_status hd_edit_async(hd_pool *pool, uint32_t root, const hd_edit_desc *d_edits, uint32_t n,
+                        uint32_t *d_out_root, void *stream);
+/* Same as hd_edit_async but the root is read from device memory (d_root), so a
+ * chain of edits can run without any host round trip. */
+hd_status hd_edit_async_droot(hd_pool *pool, const uint32_t *d_root, const hd_edit_desc *d_edits, uint32_t n,
+                              uint32_t *d_out_root, void *stream);
+/* Size the edit workspace for batches of up to max_edits touching up to
+ * max_items nodes per batch and max_list_entries (node, edit) pairs. */
+hd_status hd_edit_reserve(hd_pool *pool, uint64_t max_items, uint64_t max_list_entries, uint32_t max_edits);
+/* Per-level counters of the last edit: items[level] = nodes visited (frontier
+ * size), inserted[level] = nodes newly appended, candidates[level] = nodes
+ * that went through the dedup pass.  Arrays of node_levels entries. */
+hd_status hd_edit_last_counters(hd_pool *pool, uint64_t *items, uint64_t *candidates, uint64_t *inserted);
+
+/* ---- upsert (find-or-insert) ---------------------------------------------
+ * replaces upsert_inner_node / upsert_leaf (include/hashdag/NodePool.hpp:159-238).
+ * words = n packed nodes back to back (host), lens[i] = word count of node i
+ * (2 for a leaf at level node_levels-1, 1+popcount(mask) otherwise).  All
+ * nodes go to `level`.  out_ptrs[i] = pointer of the stored or found node. */
+hd_status hd_upsert(hd_pool *pool, uint32_t level, const uint32_t *words, const uint32_t *lens, uint32_t n,
+                    uint32_t *out_ptrs);
+
+/* ---- host mirror (reference storage hooks) --------------------------------
+ * GetBucketRefWords / ReadPage (include/hashdag/NodePool.hpp:22-29,
+ * src/DAGNodePool.hpp:56-69).  Virtual page ids are the reference's page ids
+ * (bucket << page_bits_per_bucket | page in bucket). */
+hd_status hd_pool_read_bucket_words(const hd_pool *pool, uint32_t first_bucket, uint32_t count, uint32_t *out);
+/* out[i] = 1 if virtual page i holds data, else 0 (count = total pages). */
+hd_status hd_pool_read_page_map(const hd_pool *pool, uint8_t *out);
+/* Copies virtual pages page_ids[0..n) to out (n << word_bits_per_page words). */
+hd_status hd_pool_read_pages(const hd_pool *pool, const uint32_t *page_ids, uint32_t n, uint32_t *out);
+/* Replaces the pool contents with a host pool (e.g. one the reference built):
+ * bucket words for every bucket, n pages with their ids and words, and the
+ * filled-node pointer per level (NULL = recompute).  Rebuilds the dedup index. */
+hd_status hd_pool_upload(hd_pool *pool, const uint32_t *bucket_words, const uint32_t *page_ids, uint32_t n_pages,
+                         const uint32_t *page_words, const uint32_t *filled_levels);
+
+/* ---- read path --------------------------------------------------------------
+ * Point occupancy: out[i] = voxel (xyz[3i], xyz[3i+1], xyz[3i+2]) set under root. */
+hd_status hd_query(hd_pool *pool, uint32_t root, const uint32_t *xyz, uint32_t n, uint8_t *out, void *stream);
+/* NodePoolTraversal::Traversal<float> (include/hashdag/NodePoolTraversal.hpp:93-256)
+ * over n rays: origins/dirs = 3n floats (host), out = n hits (host). */
+hd_status hd_trace(hd_pool *pool, uint32_t root, const float *origins, const float *dirs, uint32_t n, hd_hit *out,
+                   void *stream);
+/* Primary rays of n_cameras pinhole cameras at width x height, device output
+ * (d_out = device pointer to n_cameras*width*height hits, camera-major,
+ * row-major).  Async on stream. */
+hd_status hd_trace_pinhole_async(hd_pool *pool, uint32_t root, const hd_camera *cameras, uint32_t n_cameras,
+                                 uint32_t width, uint32_t height, hd_hit *d_out, void *stream);
+
+/* ---- workload helpers ------------------------------------------------------
+ * Number of grid voxels inside each edit's shape clipped to [0,resolution)^3,
+ * summed over the edits (the voxel-edits unit of the benchmark). */
+uint64_t hd_count_voxel_edits(const hd_edit_desc *edits, uint32_t n, uint32_t resolution);
+
+const char *hd_status_string(hd_status s);
+/* 1 if a CUDA device is usable, else 0. */
+int hd_device_available(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HASHDAG_GPU_H */

@@ -1,0 +1,883 @@
+// hashdag_oracle.cpp -- CPU restatement of the reference HashDAG edit path.
+//
+// TEST INFRASTRUCTURE ONLY.  This file is the oracle: the parity tests, the
+// smoke check and the CPU-baseline leg of the benchmark call it to check or
+// time the CUDA engine.  The engine itself (vkhashdag_gb300/) never links,
+// loads or calls it.
+//
+// It restates, in plain C++, the algorithm of the reference's header library
+// include/hashdag/ (AdamYuan/VkHashDAG) for the stateless sphere and box
+// editors of src/main.cpp, with the same storage layout, hash functions and
+// page padding rule, so that a serial edit here produces a pool that is word
+// for word the pool the reference's serial NodePoolBase::Edit produces.  Each
+// function names the reference lines it follows.  The threaded edit follows
+// NodePoolThreadedEdit (libfork fork-join) with OpenMP tasks.
+//
+// Exported through a small C ABI (orc_*) for ctypes.
+
+#include "../include/hashdag_gpu.h"
+
+#include <algorithm>
+#include <array>
+#include <atomic>
+#include <bit>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <unordered_map>
+#include <unordered_set>
+#include <vector>
+
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace orc {
+
+using Word = uint32_t;
+static constexpr Word kNull = 0xFFFFFFFFu;
+
+// ---------------------------------------------------------------- Config
+// include/hashdag/Config.hpp:15-57
+struct Config {
+	Word wbpp = 9, pbpb = 2, hasher = HD_HASHER_MURMUR32;
+	std::vector<Word> bucket_bits;
+	Word words_per_page() const { return Word(1) << wbpp; }
+	Word pages_per_bucket() const { return Word(1) << pbpb; }
+	Word words_per_bucket() const { return Word(1) << (wbpp + pbpb); }
+	Word buckets_at(Word l) const { return Word(1) << bucket_bits[l]; }
+	Word node_levels() const { return (Word)bucket_bits.size(); }
+	Word voxel_level() const { return node_levels() + 1; }
+	std::vector<Word> level_bases() const { // Config.hpp:33-38
+		std::vector<Word> b(bucket_bits.size(), 0);
+		for (size_t i = 1; i < bucket_bits.size(); ++i)
+			b[i] = buckets_at(Word(i - 1)) + b[i - 1];
+		return b;
+	}
+	uint64_t total_buckets() const {
+		uint64_t t = 0;
+		for (Word b : bucket_bits)
+			t += uint64_t(1) << b;
+		return t;
+	}
+	uint64_t total_pages() const { return total_buckets() << pbpb; }
+};
+
+// ---------------------------------------------------------------- hashers
+// include/hashdag/Hasher.hpp:21-39 (span of any length: MurmurHash3 x86-32 body, seed 0)
+static inline Word murmur_words(const Word *w, size_t n) {
+	Word h = 0;
+	for (size_t i = 0; i < n; ++i) {
+		Word k = w[i];
+		k *= 0xcc9e2d51u;
+		k = (k << 15) | (k >> 17);
+		k *= 0x1b873593u;
+		h ^= k;
+		h = (h << 13) | (h >> 19);
+		h = h * 5u + 0xe6546b64u;
+	}
+	h ^= Word(n);
+	h ^= h >> 16;
+	h *= 0x85ebca6bu;
+	h ^= h >> 13;
+	h *= 0xc2b2ae35u;
+	h ^= h >> 16;
+	return h;
+}
+// include/hashdag/Hasher.hpp:40-48 (fixed extent 2: 64-bit finaliser, truncated)
+static inline Word murmur_leaf(Word w0, Word w1) {
+	uint64_t h = uint64_t(w0) | (uint64_t(w1) << 32);
+	h ^= h >> 33;
+	h *= 0xff51afd7ed558ccdull;
+	h ^= h >> 33;
+	h *= 0xc4ceb9fe1a85ec53ull;
+	h ^= h >> 33;
+	return Word(h);
+}
+
+// include/hashdag/NodePool.hpp:214-226 (popcount(mask)+1, 0 for an empty mask)
+static inline Word inner_node_words(const Word *p) {
+	Word m = *p & 0xFFu;
+	return m ? Word(std::popcount(m)) + 1u : 0u;
+}
+
+// ---------------------------------------------------------------- editors
+// src/main.cpp:32-150, stateless forms, restated for hd_edit_desc.
+enum EditType { kNotAffected = 0, kProceed = 1, kFill = 2, kClear = 3 };
+
+static inline EditType edit_node_type(const hd_edit_desc &e, Word voxel_level, Word level, const Word pos[3]) {
+	Word bits = voxel_level - level; // NodeCoord::GetLower/UpperBoundAtLevel (NodeCoord.hpp:86-93)
+	Word lb[3], ub[3];
+	for (int a = 0; a < 3; ++a) {
+		lb[a] = pos[a] << bits;
+		ub[a] = (pos[a] + 1u) << bits;
+	}
+	if (e.shape == HD_SHAPE_AABB) { // AABBEditor::EditNode (src/main.cpp:36-47)
+		for (int a = 0; a < 3; ++a)
+			if (ub[a] <= e.p0[a] || lb[a] >= e.p1[a])
+				return kNotAffected;
+		bool inside = true;
+		for (int a = 0; a < 3; ++a)
+			inside = inside && lb[a] >= e.p0[a] && ub[a] <= e.p1[a];
+		if (inside)
+			return e.op == HD_OP_DIG ? kClear : kFill;
+		return kProceed;
+	}
+	// SphereEditor::EditNode (src/main.cpp:77-106)
+	int64_t lbd[3], ubd[3];
+	uint64_t lb2[3], ub2[3], mx = 0;
+	for (int a = 0; a < 3; ++a) {
+		lbd[a] = int64_t(lb[a]) - int64_t(e.p0[a]);
+		ubd[a] = int64_t(ub[a]) - int64_t(e.p0[a]);
+		lb2[a] = uint64_t(lbd[a]) * uint64_t(lbd[a]);
+		ub2[a] = uint64_t(ubd[a]) * uint64_t(ubd[a]);
+		mx += std::max(lb2[a], ub2[a]);
+	}
+	if (mx <= e.r2)
+		return e.op == HD_OP_DIG ? kClear : kFill;
+	uint64_t mn = 0;
+	for (int a = 0; a < 3; ++a) {
+		if (lbd[a] > 0)
+			mn += lb2[a];
+		if (ubd[a] < 0)
+			mn += ub2[a];
+	}
+	return mn > e.r2 ? kNotAffected : kProceed;
+}
+
+static inline bool voxel_in_shape(const hd_edit_desc &e, const Word p[3]) {
+	if (e.shape == HD_SHAPE_AABB) // AABBEditor::VoxelInRange (src/main.cpp:55-57)
+		return p[0] >= e.p0[0] && p[1] >= e.p0[1] && p[2] >= e.p0[2] && p[0] < e.p1[0] && p[1] < e.p1[1] &&
+		       p[2] < e.p1[2];
+	// SphereEditor::VoxelInRange (src/main.cpp:121-126)
+	uint64_t n2 = 0;
+	for (int a = 0; a < 3; ++a) {
+		int64_t d = int64_t(p[a]) - int64_t(e.p0[a]);
+		n2 += uint64_t(d) * uint64_t(d);
+	}
+	return n2 <= e.r2;
+}
+// EditVoxel (src/main.cpp:58-60 fill, :127-136 fill/dig)
+static inline bool edit_voxel(const hd_edit_desc &e, const Word p[3], bool voxel) {
+	bool in = voxel_in_shape(e, p);
+	return e.op == HD_OP_DIG ? (voxel && !in) : (voxel || in);
+}
+
+// ---------------------------------------------------------------- pool
+struct Pool {
+	Config cfg;
+	std::vector<Word> bases;
+	std::unique_ptr<Word[]> bucket_words;
+	std::vector<std::unique_ptr<Word[]>> pages;
+	std::vector<Word> filled;
+	std::unique_ptr<std::mutex[]> mutexes; // striped like src/DAGNodePool.hpp:43,56
+	static constexpr Word kMutexes = 1024;
+
+	explicit Pool(Config c) : cfg(std::move(c)) {
+		bases = cfg.level_bases();
+		bucket_words = std::make_unique<Word[]>(cfg.total_buckets());
+		std::fill(bucket_words.get(), bucket_words.get() + cfg.total_buckets(), 0u);
+		pages.resize(cfg.total_pages());
+		mutexes = std::make_unique<std::mutex[]>(kMutexes);
+	}
+
+	// storage hooks, pattern of src/DAGNodePool.hpp:56-69
+	const Word *read_page(Word page) const { return pages[page].get(); }
+	Word *page_for_write(Word page) {
+		if (!pages[page]) {
+			pages[page] = std::make_unique<Word[]>(cfg.words_per_page()); // zero-initialised
+		}
+		return pages[page].get();
+	}
+	void write_page(Word page, Word off, const Word *w, Word n) { std::memcpy(page_for_write(page) + off, w, n * 4); }
+	void zero_page(Word page, Word off, Word n) { std::memset(page_for_write(page) + off, 0, size_t(n) * 4); }
+
+	// NodePool.hpp:75-77
+	const Word *read_node(Word node) const {
+		return read_page(node >> cfg.wbpp) + (node & (cfg.words_per_page() - 1u));
+	}
+
+	// NodePool.hpp:79-91
+	template <bool Leaf>
+	static Word find_in_span(Word base, const Word *span, Word span_len, const Word *node, Word node_len) {
+		Word i = 0;
+		while (node_len <= span_len - i) {
+			Word w = Leaf ? 2u : inner_node_words(span + i);
+			if (w == 0)
+				break;
+			if (w == node_len && std::equal(node, node + node_len, span + i))
+				return base + i;
+			i += w;
+		}
+		return kNull;
+	}
+
+	// NodePool.hpp:93-132
+	template <bool Leaf>
+	Word find_node(Word bucket, Word bucket_words_now, Word bucket_word_offset, const Word *node, Word node_len) const {
+		if (bucket_words_now <= bucket_word_offset)
+			return kNull;
+		Word find_words = bucket_words_now - bucket_word_offset;
+		Word page_index = (bucket << cfg.pbpb) | (bucket_word_offset >> cfg.wbpp);
+		Word page_word_offset = bucket_word_offset & (cfg.words_per_page() - 1u);
+		while (page_word_offset + find_words >= cfg.words_per_page()) {
+			Word r = find_in_span<Leaf>((page_index << cfg.wbpp) | page_word_offset, read_page(page_index) + page_word_offset,
+			                            cfg.words_per_page() - page_word_offset, node, node_len);
+			if (r != kNull)
+				return r;
+			find_words -= cfg.words_per_page() - page_word_offset;
+			page_word_offset = 0;
+			++page_index;
+		}
+		if (find_words) {
+			Word r = find_in_span<Leaf>((page_index << cfg.wbpp) | page_word_offset, read_page(page_index) + page_word_offset,
+			                            find_words, node, node_len);
+			if (r != kNull)
+				return r;
+		}
+		return kNull;
+	}
+
+	// NodePool.hpp:134-157; returns {ptr, new_bucket_words}
+	std::pair<Word, Word> append_node(Word bucket, Word bw, const Word *node, Word node_len) {
+		if (uint64_t(bw) + node_len > cfg.words_per_bucket())
+			return {kNull, 0};
+		Word slot = bw >> cfg.wbpp;
+		Word off = bw & (cfg.words_per_page() - 1u);
+		Word page = (bucket << cfg.pbpb) | slot;
+		if (off + node_len > cfg.words_per_page()) {
+			zero_page(page, off, cfg.words_per_page() - off);
+			++slot;
+			++page;
+			off = 0;
+		}
+		write_page(page, off, node, node_len);
+		Word nbw = ((slot << cfg.wbpp) | off) + node_len;
+		return {(page << cfg.wbpp) | off, nbw};
+	}
+
+	Word node_hash(bool leaf, const Word *node, Word len) const {
+		if (cfg.hasher == HD_HASHER_ZERO)
+			return 0;
+		return leaf ? murmur_leaf(node[0], node[1]) : murmur_words(node, len);
+	}
+
+	// NodePool.hpp:159-212; `ok` is cleared when the bucket is full (the
+	// reference silently returns fallback there; the oracle returns it too but
+	// records the event).
+	template <bool ThreadSafe>
+	Word upsert(bool leaf, Word level, const Word *node, Word len, Word fallback, bool *ok) {
+		const Word bucket = bases[level] + (node_hash(leaf, node, len) & (cfg.buckets_at(level) - 1u));
+		Word &ref = bucket_words[bucket];
+		if constexpr (ThreadSafe) {
+			std::atomic_ref<Word> aref{ref};
+			Word shared = aref.load(std::memory_order_acquire);
+			Word r = leaf ? find_node<true>(bucket, shared, 0, node, len) : find_node<false>(bucket, shared, 0, node, len);
+			if (r != kNull)
+				return r;
+			std::lock_guard<std::mutex> lk{mutexes[bucket % kMutexes]};
+			Word uniq = aref.load(std::memory_order_relaxed);
+			r = leaf ? find_node<true>(bucket, uniq, shared, node, len) : find_node<false>(bucket, uniq, shared, node, len);
+			if (r != kNull)
+				return r;
+			auto [p, nbw] = append_node(bucket, uniq, node, len);
+			if (p != kNull) {
+				// release so that a lock-free reader that sees the new count also
+				// sees the node words (the reference stores relaxed under the lock)
+				aref.store(nbw, std::memory_order_release);
+				return p;
+			}
+			if (ok)
+				*ok = false;
+			return fallback;
+		} else {
+			const Word bw = ref;
+			Word r = leaf ? find_node<true>(bucket, bw, 0, node, len) : find_node<false>(bucket, bw, 0, node, len);
+			if (r != kNull)
+				return r;
+			auto [p, nbw] = append_node(bucket, bw, node, len);
+			if (p != kNull) {
+				ref = nbw;
+				return p;
+			}
+			if (ok)
+				*ok = false;
+			return fallback;
+		}
+	}
+
+	// NodePool.hpp:240-262
+	void make_filled(bool *ok) {
+		if (!filled.empty())
+			return;
+		Word L = cfg.node_levels();
+		filled.assign(L, kNull);
+		Word leaf[2] = {kNull, kNull};
+		filled[L - 1] = upsert<false>(true, L - 1, leaf, 2, kNull, ok);
+		if (L == 1)
+			return;
+		for (Word l = L - 2; l != Word(-1); --l) {
+			Word p = filled[l + 1];
+			Word node[9] = {0xFFu, p, p, p, p, p, p, p, p};
+			filled[l] = upsert<false>(false, l, node, 9, kNull, ok);
+		}
+	}
+
+	// NodePool.hpp:278-309
+	std::array<Word, 9> unpack(Word ptr) const {
+		std::array<Word, 9> u;
+		u.fill(kNull);
+		u[0] = 0;
+		if (ptr == kNull)
+			return u;
+		const Word *p = read_node(ptr);
+		Word mask = p[0];
+		u[0] = mask;
+		const Word *nx = p + 1;
+		for (Word m = mask & 0xFFu; m; m &= m - 1)
+			u[1 + std::countr_zero(m)] = *nx++;
+		return u;
+	}
+	// NodePool.hpp:272-277
+	static Word pack_inplace(std::array<Word, 9> &u) {
+		Word mask = u[0], *c = u.data() + 1, *nx = c;
+		for (Word m = mask & 0xFFu; m; m &= m - 1)
+			*nx++ = c[std::countr_zero(m)];
+		return Word(nx - u.data());
+	}
+
+	// NodePool.hpp:319-343 with NodeCoord::GetLeafCoord (NodeCoord.hpp:32-43)
+	template <bool ThreadSafe>
+	Word edit_leaf(const hd_edit_desc &e, Word leaf_ptr, Word level, const Word pos[3], bool *ok) {
+		Word leaf[2] = {0, 0};
+		if (leaf_ptr != kNull) {
+			const Word *p = read_node(leaf_ptr);
+			leaf[0] = p[0];
+			leaf[1] = p[1];
+		}
+		bool changed = false;
+		for (Word i = 0; i < 64; ++i) {
+			Word vp[3] = {(pos[0] << 2) | ((i >> 2) & 2u) | (i & 1u), (pos[1] << 2) | ((i >> 3) & 2u) | ((i >> 1) & 1u),
+			              (pos[2] << 2) | ((i >> 4) & 2u) | ((i >> 2) & 1u)};
+			bool v = (leaf[i >> 5] >> (i & 31)) & 1u;
+			bool nv = edit_voxel(e, vp, v);
+			changed |= nv != v;
+			leaf[i >> 5] ^= Word(nv != v) << (i & 31);
+		}
+		if (!changed)
+			return leaf_ptr;
+		if (leaf[0] == 0 && leaf[1] == 0)
+			return kNull;
+		return upsert<ThreadSafe>(true, level, leaf, 2, leaf_ptr, ok);
+	}
+
+	// NodePool.hpp:345-360 (terminal part); returns true if the child must be recursed
+	bool edit_switch(const hd_edit_desc &e, Word ptr, Word level, const Word pos[3], Word *out) const {
+		EditType t = edit_node_type(e, cfg.voxel_level(), level, pos);
+		if (t == kClear) {
+			*out = kNull;
+			return false;
+		}
+		if (t == kFill) {
+			*out = filled[level];
+			return false;
+		}
+		if (t == kNotAffected) {
+			*out = ptr;
+			return false;
+		}
+		return true;
+	}
+
+	static void child_pos(const Word pos[3], Word c, Word out[3]) { // NodeCoord.hpp:18-28
+		out[0] = (pos[0] << 1) | (c & 1u);
+		out[1] = (pos[1] << 1) | ((c >> 1) & 1u);
+		out[2] = (pos[2] << 1) | ((c >> 2) & 1u);
+	}
+
+	// NodePool.hpp:362-396
+	template <bool ThreadSafe>
+	Word edit_node(const hd_edit_desc &e, Word ptr, Word level, const Word pos[3], bool *ok) {
+		if (level == cfg.node_levels() - 1)
+			return edit_leaf<ThreadSafe>(e, ptr, level, pos, ok);
+		std::array<Word, 9> u = unpack(ptr);
+		bool changed = false;
+		for (Word i = 0; i < 8; ++i) {
+			Word cp[3];
+			child_pos(pos, i, cp);
+			Word old = u[1 + i], nw;
+			if (edit_switch(e, old, level + 1, cp, &nw))
+				nw = edit_node<ThreadSafe>(e, old, level + 1, cp, ok);
+			changed |= nw != old;
+			u[1 + i] = nw;
+			u[0] ^= Word((nw != kNull) != (old != kNull)) << i;
+		}
+		if (!changed)
+			return ptr;
+		if (!u[0])
+			return kNull;
+		Word len = pack_inplace(u);
+		return upsert<ThreadSafe>(false, level, u.data(), len, ptr, ok);
+	}
+
+	// NodePool.hpp:405-417
+	Word edit(Word root, const hd_edit_desc &e, bool *ok) {
+		make_filled(ok);
+		Word zero[3] = {0, 0, 0}, out;
+		if (!edit_switch(e, root, 0, zero, &out))
+			return out;
+		return edit_node<false>(e, root, 0, zero, ok);
+	}
+
+	// NodePoolThreadedEdit.hpp:27-99 (lf_edit_node), fork-join with OpenMP tasks
+	Word t_edit_node(const hd_edit_desc &e, Word ptr, Word level, const Word pos[3], Word max_task_level, bool *ok) {
+		if (level == cfg.node_levels() - 1)
+			return edit_leaf<true>(e, ptr, level, pos, ok);
+		if (level >= max_task_level)
+			return edit_node<true>(e, ptr, level, pos, ok);
+		std::array<Word, 9> u = unpack(ptr);
+		Word nc[8];
+		Word cps[8][3];
+		bool fork[8];
+		for (Word i = 0; i < 8; ++i) {
+			child_pos(pos, i, cps[i]);
+			fork[i] = edit_switch(e, u[1 + i], level + 1, cps[i], &nc[i]);
+		}
+		for (Word i = 0; i < 8; ++i) {
+			if (!fork[i])
+				continue;
+#pragma omp task default(none) firstprivate(i, level, max_task_level) shared(e, u, nc, cps, ok)
+			nc[i] = t_edit_node(e, u[1 + i], level + 1, cps[i], max_task_level, ok);
+		}
+#pragma omp taskwait
+		bool changed = false;
+		for (Word i = 0; i < 8; ++i) {
+			Word old = u[1 + i];
+			changed |= nc[i] != old;
+			u[0] ^= Word((nc[i] != kNull) != (old != kNull)) << i;
+			u[1 + i] = nc[i];
+		}
+		if (!changed)
+			return ptr;
+		if (!u[0])
+			return kNull;
+		Word len = pack_inplace(u);
+		return upsert<true>(false, level, u.data(), len, ptr, ok);
+	}
+
+	// NodePoolThreadedEdit.hpp:104-126
+	Word threaded_edit(Word root, const hd_edit_desc &e, Word max_task_level, int threads, bool *ok) {
+		make_filled(ok);
+		Word zero[3] = {0, 0, 0}, out;
+		if (!edit_switch(e, root, 0, zero, &out))
+			return out;
+		Word r = kNull;
+#pragma omp parallel num_threads(threads) default(none) shared(r, e, zero, max_task_level, ok, root)
+		{
+#pragma omp single
+			r = t_edit_node(e, root, 0, zero, max_task_level, ok);
+		}
+		return r;
+	}
+
+	// occupancy of one voxel
+	bool query(Word root, const Word v[3]) const {
+		Word L = cfg.node_levels(), ptr = root;
+		if (ptr == kNull)
+			return false;
+		for (Word l = 0; l + 1 < L; ++l) {
+			Word sh = cfg.voxel_level() - l - 1;
+			Word c = ((v[0] >> sh) & 1u) | (((v[1] >> sh) & 1u) << 1) | (((v[2] >> sh) & 1u) << 2);
+			const Word *p = read_node(ptr);
+			Word mask = p[0] & 0xFFu;
+			if (!((mask >> c) & 1u))
+				return false;
+			ptr = p[1 + std::popcount(mask & ((1u << c) - 1u))];
+			if (ptr == kNull)
+				return false;
+		}
+		const Word *p = read_node(ptr);
+		Word i = ((v[0] >> 1) & 1u) << 3 | ((v[1] >> 1) & 1u) << 4 | ((v[2] >> 1) & 1u) << 5 | (v[0] & 1u) |
+		         (v[1] & 1u) << 1 | (v[2] & 1u) << 2;
+		return (p[i >> 5] >> (i & 31)) & 1u;
+	}
+};
+
+// ---------------------------------------------------------------- canonical DAG
+// Canonical form of the reachable DAG: per level, the sorted set of node tuples
+// whose child pointers are replaced by the child's rank in the sorted tuple
+// list of the level below.  Equal canonical forms <=> equal voxel occupancy.
+static inline uint64_t mix64(uint64_t x) {
+	x ^= x >> 30;
+	x *= 0xbf58476d1ce4e5b9ull;
+	x ^= x >> 27;
+	x *= 0x94d049bb133111ebull;
+	x ^= x >> 31;
+	return x;
+}
+
+struct Canon {
+	std::vector<uint64_t> counts, digests;
+	bool ok = true;
+};
+
+static Canon canonical(const Pool &pool, Word root) {
+	Word L = pool.cfg.node_levels();
+	Canon c;
+	c.counts.assign(L, 0);
+	c.digests.assign(L, 0);
+	if (root == kNull)
+		return c;
+	// reachable node pointers per level
+	std::vector<std::vector<Word>> lv(L);
+	lv[0].push_back(root);
+	for (Word l = 0; l + 1 < L; ++l) {
+		std::unordered_set<Word> seen;
+		for (Word p : lv[l]) {
+			const Word *n = pool.read_node(p);
+			Word k = std::popcount(n[0] & 0xFFu);
+			for (Word j = 0; j < k; ++j)
+				if (seen.insert(n[1 + j]).second)
+					lv[l + 1].push_back(n[1 + j]);
+		}
+	}
+	std::unordered_map<Word, Word> rank_below, rank_here;
+	for (Word l = L; l-- > 0;) {
+		std::vector<std::vector<Word>> tuples;
+		tuples.reserve(lv[l].size());
+		for (Word p : lv[l]) {
+			const Word *n = pool.read_node(p);
+			std::vector<Word> t;
+			if (l == L - 1) {
+				t = {n[0], n[1]};
+			} else {
+				Word k = std::popcount(n[0] & 0xFFu);
+				t.push_back(n[0]);
+				for (Word j = 0; j < k; ++j) {
+					auto it = rank_below.find(n[1 + j]);
+					if (it == rank_below.end()) {
+						c.ok = false;
+						t.push_back(kNull);
+					} else
+						t.push_back(it->second);
+				}
+			}
+			tuples.push_back(std::move(t));
+		}
+		std::vector<Word> order(tuples.size());
+		for (Word i = 0; i < order.size(); ++i)
+			order[i] = i;
+		std::sort(order.begin(), order.end(), [&](Word a, Word b) { return tuples[a] < tuples[b]; });
+		rank_here.clear();
+		uint64_t d = 0x6a09e667f3bcc909ull ^ l;
+		Word rank = 0;
+		for (Word i = 0; i < order.size(); ++i) {
+			if (i > 0 && tuples[order[i]] == tuples[order[i - 1]]) {
+				c.ok = false; // duplicate content at one level: the DAG is not reduced
+			} else if (i > 0)
+				++rank;
+			rank_here[lv[l][order[i]]] = rank;
+			if (i == 0 || tuples[order[i]] != tuples[order[i - 1]]) {
+				d = mix64(d ^ tuples[order[i]].size());
+				for (Word w : tuples[order[i]])
+					d = mix64(d ^ w);
+			}
+		}
+		c.counts[l] = tuples.empty() ? 0 : rank + 1;
+		c.digests[l] = d;
+		rank_below.swap(rank_here);
+	}
+	return c;
+}
+
+// ---------------------------------------------------------------- ray traversal
+// NodePoolTraversal::Traversal<float> (include/hashdag/NodePoolTraversal.hpp:93-256)
+// extended with the voxel position / size output of shader/src/trace.frag:223-246.
+// Compiled with -ffp-contract=off so every float operation rounds like the GPU
+// kernel built with -fmad=false.
+static inline Word f2w(float f) {
+	Word w;
+	std::memcpy(&w, &f, 4);
+	return w;
+}
+static inline float w2f(Word w) {
+	float f;
+	std::memcpy(&f, &w, 4);
+	return f;
+}
+static inline int find_msb(Word x) { return x ? 31 - std::countl_zero(x) : -1; }
+// glm::abs for float (x >= 0 ? x : -x)
+static inline float abs_ref(float x) { return x >= 0.0f ? x : -x; }
+
+static hd_hit trace_ray(const Pool &pool, Word root, const float o_in[3], const float d_in[3]) {
+	hd_hit out{};
+	out.hit = 0;
+	if (root == kNull)
+		return out;
+	constexpr int kStack = 23;
+	const float eps = w2f((127u - 23u) << 23); // exp2(-23) == FLT_EPSILON
+	Word stack[kStack];
+	for (int k = 0; k < kStack; ++k) // every entry holds a node pointer before the first push
+		stack[k] = root;
+	float o[3] = {o_in[0] + 1.0f, o_in[1] + 1.0f, o_in[2] + 1.0f};
+	float d[3];
+	for (int a = 0; a < 3; ++a)
+		d[a] = abs_ref(d_in[a]) > eps ? d_in[a] : (d_in[a] >= 0 ? eps : -eps);
+	float tc[3], tb[3];
+	for (int a = 0; a < 3; ++a) {
+		tc[a] = 1.0f / -abs_ref(d[a]);
+		tb[a] = tc[a] * o[a];
+	}
+	Word octant = 0;
+	for (int a = 0; a < 3; ++a)
+		if (d[a] > 0.0f)
+			octant ^= 1u << a, tb[a] = 3.0f * tc[a] - tb[a];
+	float t_min = std::max(std::max(2.0f * tc[0] - tb[0], 2.0f * tc[1] - tb[1]), 2.0f * tc[2] - tb[2]);
+	float t_max = std::min(std::min(tc[0] - tb[0], tc[1] - tb[1]), tc[2] - tb[2]);
+	float h = t_max;
+	t_min = std::max(t_min, 0.0f);
+	t_max = std::min(t_max, 1.0f);
+	Word parent = root, child_bits = 0;
+	float pos[3] = {1.0f, 1.0f, 1.0f};
+	Word idx = 0;
+	for (int a = 0; a < 3; ++a)
+		if (1.5f * tc[a] - tb[a] > t_min)
+			idx ^= 1u << a, pos[a] = 1.5f;
+	int scale = kStack - 1;
+	float scale_exp2 = 0.5f;
+	const Word leaf_level = pool.cfg.node_levels();
+	const int leaf_scale = kStack - int(leaf_level);
+	for (;;) {
+		if (child_bits == 0u) {
+			if (scale > leaf_scale)
+				child_bits = pool.read_node(parent)[0];
+			else if (scale == leaf_scale) {
+				const Word *p = pool.read_node(parent);
+				Word l0 = p[0], l1 = p[1];
+				child_bits = ((l0 & 0xFFu) ? 1u : 0u) | ((l0 & 0xFF00u) ? 2u : 0u) | ((l0 & 0xFF0000u) ? 4u : 0u) |
+				             ((l0 & 0xFF000000u) ? 8u : 0u) | ((l1 & 0xFFu) ? 16u : 0u) | ((l1 & 0xFF00u) ? 32u : 0u) |
+				             ((l1 & 0xFF0000u) ? 64u : 0u) | ((l1 & 0xFF000000u) ? 128u : 0u);
+			} else
+				child_bits = parent;
+		}
+		float tcorner[3] = {pos[0] * tc[0] - tb[0], pos[1] * tc[1] - tb[1], pos[2] * tc[2] - tb[2]};
+		float tc_max = std::min(std::min(tcorner[0], tcorner[1]), tcorner[2]);
+		Word child_shift = idx ^ octant;
+		Word child_mask = 1u << child_shift;
+		if ((child_bits & child_mask) != 0 && t_min <= t_max) {
+			float half = scale_exp2 * 0.5f;
+			float tcen[3] = {half * tc[0] + tcorner[0], half * tc[1] + tcorner[1], half * tc[2] + tcorner[2]};
+			if (scale < leaf_scale)
+				break;
+			if (tc_max < h)
+				stack[scale] = parent;
+			h = tc_max;
+			if (scale > leaf_scale)
+				parent = pool.read_node(parent + 1u + std::popcount(child_bits & (child_mask - 1u)))[0];
+			else
+				parent = (pool.read_node(parent + (child_shift >> 2u))[0] >> ((child_shift & 3u) << 3u)) & 0xFFu;
+			idx = 0;
+			--scale;
+			scale_exp2 = half;
+			for (int a = 0; a < 3; ++a)
+				if (tcen[a] > t_min)
+					idx ^= 1u << a, pos[a] += scale_exp2;
+			child_bits = 0;
+			continue;
+		}
+		Word step = 0;
+		for (int a = 0; a < 3; ++a)
+			if (tcorner[a] <= tc_max)
+				step ^= 1u << a, pos[a] -= scale_exp2;
+		t_min = tc_max;
+		idx ^= step;
+		if ((idx & step) != 0) {
+			Word diff = 0;
+			for (int a = 0; a < 3; ++a)
+				if (step & (1u << a))
+					diff |= f2w(pos[a]) ^ f2w(pos[a] + scale_exp2);
+			scale = find_msb(diff);
+			if (scale >= kStack || scale < 0) {
+				scale = kStack;
+				break;
+			}
+			scale_exp2 = w2f(Word(scale - kStack + 127) << 23);
+			parent = stack[scale];
+			Word sh[3];
+			for (int a = 0; a < 3; ++a) {
+				sh[a] = f2w(pos[a]) >> scale;
+				pos[a] = w2f(sh[a] << scale);
+			}
+			idx = (sh[0] & 1u) | ((sh[1] & 1u) << 1) | ((sh[2] & 1u) << 2);
+			h = 0.0f;
+			child_bits = 0;
+		}
+	}
+	bool hit = scale < kStack && t_min <= t_max;
+	out.hit = hit ? 1u : 0u;
+	out.t = t_min;
+	const Word voxel_level = leaf_level + 1u;
+	const int voxel_scale = kStack - int(voxel_level);
+	if (hit) {
+		Word size = 1u << (scale - voxel_scale);
+		for (int a = 0; a < 3; ++a) {
+			Word vp = (f2w(pos[a]) & 0x7FFFFFu) >> voxel_scale;
+			if (octant & (1u << a))
+				vp = (1u << voxel_level) - size - vp;
+			out.voxel[a] = vp;
+		}
+		out.size = size;
+		out.level = voxel_level - Word(find_msb(size));
+		for (int a = 0; a < 3; ++a) {
+			float p = pos[a];
+			if (octant & (1u << a))
+				p = 3.0f - scale_exp2 - p;
+			float q = o[a] + t_min * d[a];
+			q = std::min(std::max(q, p), p + scale_exp2);
+			out.pos[a] = q - 1.0f;
+		}
+	}
+	return out;
+}
+
+} // namespace orc
+
+// ---------------------------------------------------------------- C ABI
+using orc::Pool;
+using orc::Word;
+
+struct orc_pool {
+	Pool pool;
+	bool ok = true; // cleared when a bucket overflowed (reference: silent fallback)
+	explicit orc_pool(orc::Config c) : pool(std::move(c)) {}
+};
+
+extern "C" {
+
+orc_pool *orc_pool_create(uint32_t wbpp, uint32_t pbpb, uint32_t node_levels, const uint32_t *bucket_bits,
+                          uint32_t hasher) {
+	orc::Config c;
+	c.wbpp = wbpp;
+	c.pbpb = pbpb;
+	c.hasher = hasher;
+	c.bucket_bits.assign(bucket_bits, bucket_bits + node_levels);
+	return new orc_pool(std::move(c));
+}
+
+void orc_pool_destroy(orc_pool *p) { delete p; }
+
+int orc_pool_ok(const orc_pool *p) { return p->ok ? 1 : 0; }
+
+void orc_make_filled(orc_pool *p, uint32_t *out) {
+	p->pool.make_filled(&p->ok);
+	if (out)
+		for (size_t i = 0; i < p->pool.filled.size(); ++i)
+			out[i] = p->pool.filled[i];
+}
+
+// Serial edits applied one after another (NodePoolBase::Edit per edit).
+uint32_t orc_edit(orc_pool *p, uint32_t root, const hd_edit_desc *e, uint32_t n) {
+	for (uint32_t i = 0; i < n; ++i)
+		root = p->pool.edit(root, e[i], &p->ok);
+	return root;
+}
+
+// Threaded edits (NodePoolThreadedEdit::ThreadedEdit per edit).
+uint32_t orc_threaded_edit(orc_pool *p, uint32_t root, const hd_edit_desc *e, uint32_t n, uint32_t max_task_level,
+                           int threads) {
+	for (uint32_t i = 0; i < n; ++i)
+		root = p->pool.threaded_edit(root, e[i], max_task_level, threads, &p->ok);
+	return root;
+}
+
+int orc_max_threads(void) {
+#ifdef _OPENMP
+	return omp_get_max_threads();
+#else
+	return 1;
+#endif
+}
+
+uint32_t orc_upsert(orc_pool *p, uint32_t level, const uint32_t *words, uint32_t len) {
+	bool leaf = level == p->pool.cfg.node_levels() - 1;
+	bool ok = true;
+	Word r = p->pool.upsert<false>(leaf, level, words, len, orc::kNull, &ok);
+	return ok ? r : orc::kNull;
+}
+
+uint32_t orc_bucket_words(const orc_pool *p, uint32_t bucket) { return p->pool.bucket_words[bucket]; }
+
+uint64_t orc_total_buckets(const orc_pool *p) { return p->pool.cfg.total_buckets(); }
+uint64_t orc_total_pages(const orc_pool *p) { return p->pool.cfg.total_pages(); }
+
+// 1 if the virtual page exists, copies its words to out when out != NULL
+int orc_read_page(const orc_pool *p, uint32_t page, uint32_t *out) {
+	if (page >= p->pool.pages.size() || !p->pool.pages[page])
+		return 0;
+	if (out)
+		std::memcpy(out, p->pool.pages[page].get(), size_t(p->pool.cfg.words_per_page()) * 4);
+	return 1;
+}
+
+// Replace the pool contents (e.g. with a pool downloaded from the GPU).
+void orc_pool_load(orc_pool *p, const uint32_t *bucket_words, const uint32_t *page_ids, uint32_t n_pages,
+                   const uint32_t *page_words, const uint32_t *filled) {
+	auto &pool = p->pool;
+	uint64_t tb = pool.cfg.total_buckets();
+	std::memcpy(pool.bucket_words.get(), bucket_words, tb * 4);
+	for (auto &pg : pool.pages)
+		pg.reset();
+	Word wpp = pool.cfg.words_per_page();
+	for (uint32_t i = 0; i < n_pages; ++i) {
+		Word *dst = pool.page_for_write(page_ids[i]);
+		std::memcpy(dst, page_words + size_t(i) * wpp, size_t(wpp) * 4);
+	}
+	if (filled)
+		pool.filled.assign(filled, filled + pool.cfg.node_levels());
+}
+
+// Per-level canonical node counts and digests; returns 1 if the reachable DAG
+// is fully reduced (no duplicate node content on a level) and well formed.
+int orc_canonical(const orc_pool *p, uint32_t root, uint64_t *counts, uint64_t *digests) {
+	orc::Canon c = orc::canonical(p->pool, root);
+	for (size_t i = 0; i < c.counts.size(); ++i) {
+		counts[i] = c.counts[i];
+		digests[i] = c.digests[i];
+	}
+	return c.ok ? 1 : 0;
+}
+
+void orc_query(const orc_pool *p, uint32_t root, const uint32_t *xyz, uint32_t n, uint8_t *out) {
+	for (uint32_t i = 0; i < n; ++i)
+		out[i] = p->pool.query(root, xyz + 3 * size_t(i)) ? 1 : 0;
+}
+
+// Dense occupancy of the whole grid (small resolutions only): out[x + y*R + z*R*R].
+void orc_dense(const orc_pool *p, uint32_t root, uint8_t *out) {
+	Word R = 1u << p->pool.cfg.voxel_level();
+	for (Word z = 0; z < R; ++z)
+		for (Word y = 0; y < R; ++y)
+			for (Word x = 0; x < R; ++x) {
+				Word v[3] = {x, y, z};
+				out[x + size_t(y) * R + size_t(z) * R * R] = p->pool.query(root, v) ? 1 : 0;
+			}
+}
+
+void orc_trace(const orc_pool *p, uint32_t root, const float *o, const float *d, uint32_t n, hd_hit *out) {
+	for (uint32_t i = 0; i < n; ++i)
+		out[i] = orc::trace_ray(p->pool, root, o + 3 * size_t(i), d + 3 * size_t(i));
+}
+
+void orc_trace_threads(const orc_pool *p, uint32_t root, const float *o, const float *d, uint32_t n, hd_hit *out,
+                       int threads) {
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 4096)
+	for (int64_t i = 0; i < int64_t(n); ++i)
+		out[i] = orc::trace_ray(p->pool, root, o + 3 * size_t(i), d + 3 * size_t(i));
+}
+
+uint32_t orc_hash_inner(const uint32_t *w, uint32_t n) { return orc::murmur_words(w, n); }
+uint32_t orc_hash_leaf(uint32_t w0, uint32_t w1) { return orc::murmur_leaf(w0, w1); }
+
+} // extern "C"

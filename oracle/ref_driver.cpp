@@ -1,0 +1,239 @@
+// ref_driver.cpp -- runs the reference's own hashdag header library.
+//
+// TEST INFRASTRUCTURE ONLY.  Built by oracle/build_ref.sh against the
+// reference headers (include/hashdag/*.hpp, dep/libfork, dep/glm) where the
+// reference tree is present, into oracle/_ref/.  It executes the reference's
+// NodePoolBase::Edit, NodePoolThreadedEdit::ThreadedEdit,
+// NodePoolBase::upsert_inner_node / upsert_leaf and
+// NodePoolTraversal::Traversal on a vector-backed pool whose storage hooks
+// follow src/DAGNodePool.hpp:56-69, and dumps the resulting pool, so the
+// oracle restatement can be pinned against the reference and golden fixtures
+// can be generated.  The editors restate the stateless SphereEditor<kFill/kDig>
+// and AABBEditor of src/main.cpp:32-150 (they live in the application, not the
+// library) plus an AABB dig by symmetry.
+//
+// Protocol (all little-endian uint32 unless noted), input file:
+//   magic 'HDRQ', mode (0 edit, 1 threaded edit, 2 upsert, 3 trace-after-edit),
+//   wbpp, pbpb, node_levels, hasher, bucket_bits[node_levels],
+//   threads, max_task_level, n_edits, edits[n_edits] (40 bytes each),
+//   mode 2: n_ops, then per op: level, len, words[len]
+//   mode 3: n_rays, then origins[3n] and dirs[3n] (float)
+// output file:
+//   magic 'HDRS', root, ok, elapsed_ns (uint64), filled[node_levels],
+//   total_buckets, bucket_words[total_buckets], n_pages, then per page: id, words[wpp]
+//   mode 2: n_ops, ptrs[n_ops] (after the pool dump)
+//   mode 3: n_rays, per ray: hit, pos[3] (float)
+
+#include <hashdag/NodePool.hpp>
+#include <hashdag/NodePoolThreadedEdit.hpp>
+#include <hashdag/NodePoolTraversal.hpp>
+
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <vector>
+
+#include "../include/hashdag_gpu.h"
+
+struct ZeroHasher {
+	inline uint32_t operator()(auto &&) const { return 0; }
+};
+
+template <typename HasherT>
+struct RefPool final : public hashdag::NodePoolBase<RefPool<HasherT>, uint32_t>,
+                       public hashdag::NodePoolThreadedEdit<RefPool<HasherT>, uint32_t>,
+                       public hashdag::NodePoolTraversal<RefPool<HasherT>, uint32_t> {
+	using WordSpanHasher = HasherT;
+	using Base = hashdag::NodePoolBase<RefPool<HasherT>, uint32_t>;
+
+	std::unique_ptr<uint32_t[]> bucket_words;
+	std::vector<std::unique_ptr<uint32_t[]>> pages;
+	std::array<std::mutex, 1024> mutexes{};
+
+	explicit RefPool(const hashdag::Config<uint32_t> &config) : Base(config) {
+		bucket_words = std::make_unique<uint32_t[]>(this->GetConfig().GetTotalBuckets());
+		pages.resize(this->GetConfig().GetTotalPages());
+	}
+	~RefPool() final = default;
+
+	std::mutex &GetBucketRefMutex(uint32_t b) { return mutexes[b % mutexes.size()]; }
+	uint32_t &GetBucketRefWords(uint32_t b) { return bucket_words[b]; }
+	const uint32_t *ReadPage(uint32_t p) const { return pages[p].get(); }
+	uint32_t *page(uint32_t p) {
+		if (!pages[p])
+			pages[p] = std::make_unique<uint32_t[]>(this->GetConfig().GetWordsPerPage()); // zeroed
+		return pages[p].get();
+	}
+	void ZeroPage(uint32_t p, uint32_t off, uint32_t n) { std::fill(page(p) + off, page(p) + off + n, 0u); }
+	void WritePage(uint32_t p, uint32_t off, std::span<const uint32_t> s) {
+		std::copy(s.begin(), s.end(), page(p) + off);
+	}
+};
+
+// Stateless editors (src/main.cpp:32-150) for one hd_edit_desc.
+struct DescEditor {
+	hd_edit_desc e;
+	inline hashdag::EditType EditNode(const hashdag::Config<uint32_t> &config, const hashdag::NodeCoord<uint32_t> &coord,
+	                                  hashdag::NodePointer<uint32_t>) const {
+		auto lb = coord.GetLowerBoundAtLevel(config.GetVoxelLevel()), ub = coord.GetUpperBoundAtLevel(config.GetVoxelLevel());
+		if (e.shape == HD_SHAPE_AABB) {
+			glm::u32vec3 mn{e.p0[0], e.p0[1], e.p0[2]}, mx{e.p1[0], e.p1[1], e.p1[2]};
+			if (glm::any(glm::lessThanEqual(ub, mn)) || glm::any(glm::greaterThanEqual(lb, mx)))
+				return hashdag::EditType::kNotAffected;
+			if (glm::all(glm::greaterThanEqual(lb, mn)) && glm::all(glm::lessThanEqual(ub, mx)))
+				return e.op == HD_OP_DIG ? hashdag::EditType::kClear : hashdag::EditType::kFill;
+			return hashdag::EditType::kProceed;
+		}
+		glm::u32vec3 center{e.p0[0], e.p0[1], e.p0[2]};
+		glm::i64vec3 lb_dist = glm::i64vec3{lb} - glm::i64vec3(center);
+		glm::i64vec3 ub_dist = glm::i64vec3{ub} - glm::i64vec3(center);
+		glm::u64vec3 lb_dist_2 = lb_dist * lb_dist;
+		glm::u64vec3 ub_dist_2 = ub_dist * ub_dist;
+		glm::u64vec3 max_dist_2 = glm::max(lb_dist_2, ub_dist_2);
+		uint64_t max_n2 = max_dist_2.x + max_dist_2.y + max_dist_2.z;
+		if (max_n2 <= e.r2)
+			return e.op == HD_OP_DIG ? hashdag::EditType::kClear : hashdag::EditType::kFill;
+		uint64_t min_n2 = 0;
+		if (lb_dist.x > 0)
+			min_n2 += lb_dist_2.x;
+		if (ub_dist.x < 0)
+			min_n2 += ub_dist_2.x;
+		if (lb_dist.y > 0)
+			min_n2 += lb_dist_2.y;
+		if (ub_dist.y < 0)
+			min_n2 += ub_dist_2.y;
+		if (lb_dist.z > 0)
+			min_n2 += lb_dist_2.z;
+		if (ub_dist.z < 0)
+			min_n2 += ub_dist_2.z;
+		return min_n2 > e.r2 ? hashdag::EditType::kNotAffected : hashdag::EditType::kProceed;
+	}
+	inline bool EditVoxel(const hashdag::Config<uint32_t> &, const hashdag::NodeCoord<uint32_t> &coord, bool voxel) const {
+		bool in;
+		if (e.shape == HD_SHAPE_AABB) {
+			glm::u32vec3 mn{e.p0[0], e.p0[1], e.p0[2]}, mx{e.p1[0], e.p1[1], e.p1[2]};
+			in = glm::all(glm::greaterThanEqual(coord.pos, mn)) && glm::all(glm::lessThan(coord.pos, mx));
+		} else {
+			glm::i64vec3 d = glm::i64vec3{coord.pos.x, coord.pos.y, coord.pos.z} -
+			                 glm::i64vec3(glm::u32vec3{e.p0[0], e.p0[1], e.p0[2]});
+			uint64_t n2 = d.x * d.x + d.y * d.y + d.z * d.z;
+			in = n2 <= e.r2;
+		}
+		return e.op == HD_OP_DIG ? (voxel && !in) : (voxel || in);
+	}
+};
+
+static uint32_t rd(FILE *f) {
+	uint32_t v = 0;
+	if (fread(&v, 4, 1, f) != 1) {
+		fprintf(stderr, "short read\n");
+		exit(2);
+	}
+	return v;
+}
+static void wr(FILE *f, uint32_t v) { fwrite(&v, 4, 1, f); }
+
+template <typename HasherT> static int run(FILE *in, FILE *out, uint32_t mode, const hashdag::Config<uint32_t> &config) {
+	uint32_t threads = rd(in), max_task_level = rd(in), n_edits = rd(in);
+	std::vector<hd_edit_desc> edits(n_edits);
+	if (n_edits && fread(edits.data(), sizeof(hd_edit_desc), n_edits, in) != n_edits)
+		return 2;
+	auto pool = std::make_unique<RefPool<HasherT>>(config);
+	hashdag::NodePointer<uint32_t> root{};
+	std::vector<uint32_t> upsert_ptrs;
+	std::vector<float> rays;
+	auto t0 = std::chrono::steady_clock::now();
+	if (mode == 0 || mode == 3) {
+		for (auto &e : edits)
+			root = pool->Edit(root, hashdag::StatelessEditorWrapper<uint32_t, DescEditor>{.editor = DescEditor{e}});
+	} else if (mode == 1) {
+		lf::busy_pool busy(threads ? threads : 1);
+		for (auto &e : edits)
+			root = pool->ThreadedEdit(&busy, root, hashdag::StatelessEditorWrapper<uint32_t, DescEditor>{.editor = DescEditor{e}},
+			                          max_task_level);
+	} else if (mode == 2) {
+		pool->make_filled_node_pointers();
+		uint32_t n_ops = rd(in);
+		for (uint32_t i = 0; i < n_ops; ++i) {
+			uint32_t level = rd(in), len = rd(in);
+			std::vector<uint32_t> w(len);
+			for (auto &x : w)
+				x = rd(in);
+			hashdag::NodePointer<uint32_t> p;
+			if (level == config.GetNodeLevels() - 1 && len == 2)
+				p = pool->template upsert_leaf<false>(level, std::span<const uint32_t, 2>{w.data(), 2}, {});
+			else
+				p = pool->template upsert_inner_node<false>(level, std::span<const uint32_t>{w}, {});
+			upsert_ptrs.push_back(*p);
+		}
+	}
+	auto t1 = std::chrono::steady_clock::now();
+	uint64_t ns = std::chrono::duration_cast<std::chrono::nanoseconds>(t1 - t0).count();
+
+	fwrite("HDRS", 1, 4, out);
+	wr(out, *root);
+	wr(out, 1);
+	fwrite(&ns, 8, 1, out);
+	for (uint32_t l = 0; l < config.GetNodeLevels(); ++l)
+		wr(out, pool->m_filled_node_pointers.empty() ? 0xFFFFFFFFu : *pool->m_filled_node_pointers[l]);
+	uint32_t tb = config.GetTotalBuckets();
+	wr(out, tb);
+	fwrite(pool->bucket_words.get(), 4, tb, out);
+	uint32_t np = 0;
+	for (auto &p : pool->pages)
+		np += p ? 1 : 0;
+	wr(out, np);
+	for (uint32_t i = 0; i < pool->pages.size(); ++i)
+		if (pool->pages[i]) {
+			wr(out, i);
+			fwrite(pool->pages[i].get(), 4, config.GetWordsPerPage(), out);
+		}
+	if (mode == 2) {
+		wr(out, (uint32_t)upsert_ptrs.size());
+		fwrite(upsert_ptrs.data(), 4, upsert_ptrs.size(), out);
+	}
+	if (mode == 3) {
+		uint32_t n = rd(in);
+		std::vector<float> o(3 * size_t(n)), d(3 * size_t(n));
+		if (n && (fread(o.data(), 4, o.size(), in) != o.size() || fread(d.data(), 4, d.size(), in) != d.size()))
+			return 2;
+		wr(out, n);
+		for (uint32_t i = 0; i < n; ++i) {
+			auto r = pool->template Traversal<float>(root, glm::vec3{o[3 * i], o[3 * i + 1], o[3 * i + 2]},
+			                                          glm::vec3{d[3 * i], d[3 * i + 1], d[3 * i + 2]});
+			wr(out, r ? 1u : 0u);
+			float p[3] = {r ? r->x : 0.f, r ? r->y : 0.f, r ? r->z : 0.f};
+			fwrite(p, 4, 3, out);
+		}
+	}
+	return 0;
+}
+
+int main(int argc, char **argv) {
+	if (argc != 3) {
+		fprintf(stderr, "usage: ref_driver <request> <response>\n");
+		return 2;
+	}
+	FILE *in = fopen(argv[1], "rb"), *out = fopen(argv[2], "wb");
+	if (!in || !out)
+		return 2;
+	char magic[4];
+	if (fread(magic, 1, 4, in) != 4 || memcmp(magic, "HDRQ", 4) != 0)
+		return 2;
+	uint32_t mode = rd(in);
+	hashdag::Config<uint32_t> config;
+	config.word_bits_per_page = rd(in);
+	config.page_bits_per_bucket = rd(in);
+	uint32_t L = rd(in), hasher = rd(in);
+	for (uint32_t l = 0; l < L; ++l)
+		config.bucket_bits_each_level.push_back(rd(in));
+	if (!hashdag::Config<uint32_t>::Validate(config))
+		return 3;
+	int rc = hasher == HD_HASHER_ZERO ? run<ZeroHasher>(in, out, mode, config)
+	                                  : run<hashdag::MurmurHasher32>(in, out, mode, config);
+	fclose(in);
+	fclose(out);
+	return rc;
+}

@@ -1,0 +1,90 @@
+"""The C ABI library and the host-side logic, without a GPU."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    src = open(os.path.join(ROOT, "include", "hashdag_gpu.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?[a-z_0-9]+\s*\*?\s*(hd_[a-z_0-9]+)\s*\(", src, re.M)))
+
+
+def test_library_exports_every_declared_symbol(hd):
+    syms = declared_symbols()
+    assert len(syms) >= 24
+    lib = ctypes.CDLL(hd.library_path)
+    missing = [s for s in syms if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+def test_edit_desc_layout_matches_header(hd):
+    assert hd.EDIT_DTYPE.itemsize == 40 and hd.HIT_DTYPE.itemsize == 40
+    assert hd.EDIT_DTYPE.fields["r2"][1] == 32
+
+
+def test_config_mirror(hd):
+    """DefaultConfig / Config derived quantities (include/hashdag/Config.hpp)."""
+    c = hd.DefaultConfig()()
+    assert c.get_node_levels() == 16 and c.get_voxel_level() == 17 and c.get_resolution() == 1 << 17
+    assert c.get_words_per_bucket() == 2048
+    assert c.get_level_base_bucket_indices()[9] == 9 * 1024
+    assert c.validate()
+    big = hd.Config(9, 2, [21] * 3)
+    assert not big.validate()
+    lib = hd.lib()
+    assert lib.hd_config_validate(ctypes.byref(c.to_c())) == 1
+    assert lib.hd_config_validate(ctypes.byref(big.to_c())) == 0
+    out = hd._Config()
+    lib.hd_config_default(17, 9, 9, 2, 10, 16, ctypes.byref(out))
+    assert out.node_levels == 16 and list(out.bucket_bits_each_level[:16]) == [10] * 9 + [16] * 7
+
+
+def test_status_strings(hd):
+    lib = hd.lib()
+    assert lib.hd_status_string(2) == b"bucket full"
+
+
+def test_pool_create_fails_loudly_without_device(hd):
+    if hd.device_available():
+        pytest.skip("device present")
+    with pytest.raises(hd.HashDagError) as e:
+        hd.NodePool(hd.DefaultConfig(level_count=6)(), heap_pages=64)
+    assert e.value.status == 8  # HD_ERR_NO_DEVICE: no CPU fallback
+
+
+def test_count_voxel_edits_matches_brute_force(hd):
+    from vkhashdag_gb300 import workloads as W
+    res = 64
+    e = W.mixed_batch(res, 60, seed=5, r_max=20, side_max=30)
+    e = np.concatenate([e, W.sphere_scene(res, 4, seed=1)])
+    g = np.stack(np.meshgrid(np.arange(res), np.arange(res), np.arange(res), indexing="ij"), -1).reshape(-1, 3)
+    want = 0
+    for x in e:
+        if x["shape"] == 0:
+            d = g.astype(np.int64) - x["p0"].astype(np.int64)
+            want += int(((d * d).sum(1) <= int(x["r2"])).sum())
+        else:
+            want += int(np.all((g >= x["p0"]) & (g < x["p1"]), 1).sum())
+    assert hd.count_voxel_edits(e, res) == want
+
+
+def test_workloads_deterministic_and_in_range():
+    from vkhashdag_gb300 import workloads as W
+    a = W.mixed_batch(32768, 1000, seed=1)
+    b = W.mixed_batch(32768, 1000, seed=1)
+    assert a.tobytes() == b.tobytes()
+    sph = a[a["shape"] == 0]
+    r = np.sqrt(sph["r2"].astype(np.float64))
+    assert r.min() >= 1 and r.max() <= 512
+    box = a[a["shape"] == 1]
+    side = box["p1"].astype(np.int64) - box["p0"].astype(np.int64)
+    assert side.min() >= 1 and side.max() <= 1024
+    assert 0.6 < len(sph) / len(a) < 0.8
+    assert 0.4 < (a["op"] == 1).mean() < 0.6
+    t = W.terrain_columns(256, 8, seed=0)
+    assert len(t) == 32 * 32 and t["p1"][:, 1].min() >= 1

@@ -1,0 +1,82 @@
+"""Read path parity: the CUDA traversal against the oracle restatement
+(bit-identical fp32) and the reference's own Traversal positions."""
+import numpy as np
+import pytest
+
+from helpers import config_from, rays_for, scenario, scenario_edits
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("idx", [0, 1, 2])
+def test_trace_matches_reference_positions(golden, orc, hd, idx):
+    t = golden["traversal"][idx]
+    s = scenario(golden, t["scenario"])
+    pool = hd.NodePool(config_from(s["config"]), heap_pages=1 << 12)
+    root = pool.edit(hd.NULL, scenario_edits(s))
+    o, d = rays_for(t["n"], t["seed"])
+    hits = pool.traversal(root, o, d)
+    assert hits["hit"].tolist() == t["hit"]
+    m = hits["hit"] == 1
+    assert np.array_equal(hits["pos"].view(np.uint32)[m], np.array(t["pos_bits"], np.uint32)[m])
+
+
+@pytest.mark.parametrize("name", ["scene1024", "mixed512", "terrain256", "full_then_dig"])
+def test_trace_bit_identical_to_oracle(golden, orc, hd, name):
+    s = scenario(golden, name)
+    cfg = config_from(s["config"])
+    pool = hd.NodePool(cfg, heap_pages=1 << 14)
+    edits = scenario_edits(s)
+    root = pool.edit(hd.NULL, edits)
+    ref = orc.OraclePool.from_config(cfg)
+    rr = ref.edit(orc.NULL, edits)
+    o, d = rays_for(20000, 5)
+    a = pool.traversal(root, o, d)
+    b = ref.trace(rr, o, d)
+    for f in ("hit", "voxel", "size", "level"):
+        assert np.array_equal(a[f], b[f]), f
+    m = a["hit"] == 1
+    assert np.array_equal(a["t"].view(np.uint32)[m], b["t"].view(np.uint32)[m])
+    assert np.array_equal(a["pos"].view(np.uint32)[m], b["pos"].view(np.uint32)[m])
+    assert m.mean() > 0.2
+
+
+def test_pinhole_cameras_match_host_rays(orc, hd):
+    """Camera_GenRay on the device equals the same float ops on the host."""
+    import ctypes
+    from vkhashdag_gb300 import workloads as W
+    import torch
+    res = 512
+    cfg = W.config_for_resolution(res)
+    pool = hd.NodePool(cfg, heap_pages=1 << 13)
+    edits = np.concatenate([W.terrain_columns(res, 8, 1), W.surface_spheres(res, 100, 1, 16, 8, 2, 20)])
+    root = pool.edit(hd.NULL, edits)
+    ref = orc.OraclePool.from_config(cfg)
+    rr = ref.edit(orc.NULL, edits)
+    cams = np.zeros(2, hd.CAMERA_DTYPE)
+    cams["position"] = [[0.2, 0.9, 0.3], [0.7, 0.95, 0.6]]
+    cams["look"] = [[0.3, -0.5, 0.8], [-0.4, -0.6, -0.7]]
+    cams["look"] /= np.linalg.norm(cams["look"], axis=1, keepdims=True)
+    cams["side"] = [[0.5, 0.0, -0.2], [0.4, 0.0, -0.3]]
+    cams["up"] = [[0.0, 0.5, 0.3], [0.1, 0.5, 0.0]]
+    w, h = 64, 48
+    out = torch.empty(2 * w * h * 40, dtype=torch.uint8, device="cuda")
+    st = hd.lib().hd_trace_pinhole_async(pool.handle, root, cams.ctypes.data_as(ctypes.c_void_p), 2, w, h,
+                                         ctypes.c_void_p(out.data_ptr()), None)
+    assert st == 0
+    torch.cuda.synchronize()
+    got = out.cpu().numpy().view(hd.HIT_DTYPE)
+    px, py = np.meshgrid(np.arange(w, dtype=np.float32), np.arange(h, dtype=np.float32))
+    u = ((px.ravel() + np.float32(0.5)) / np.float32(w)) * np.float32(2) - np.float32(1)
+    v = ((py.ravel() + np.float32(0.5)) / np.float32(h)) * np.float32(2) - np.float32(1)
+    o_all, d_all = [], []
+    for c in cams:
+        dd = (c["look"][None, :] - c["side"][None, :] * u[:, None]) - c["up"][None, :] * v[:, None]
+        len2 = (dd[:, 0] * dd[:, 0] + dd[:, 1] * dd[:, 1]) + dd[:, 2] * dd[:, 2]
+        inv = np.float32(1) / np.sqrt(len2)
+        d_all.append((dd * inv[:, None]).astype(np.float32))
+        o_all.append(np.tile(c["position"], (len(u), 1)).astype(np.float32))
+    want = ref.trace(rr, np.concatenate(o_all), np.concatenate(d_all))
+    for f in ("hit", "voxel", "size", "level"):
+        assert np.array_equal(got[f], want[f]), f
+    assert got["hit"].mean() > 0.3

@@ -1,0 +1,133 @@
+"""The oracle restatement against the golden vectors produced by the
+reference's own headers (tests/golden/golden.json), and -- where the reference
+tree is present -- against the live reference driver.  CPU only."""
+import numpy as np
+import pytest
+
+from helpers import config_from, scenario, scenario_edits, sha, rays_for
+
+
+def test_generators_are_stable(golden):
+    for s in golden["scenarios"]:
+        assert sha(scenario_edits(s)) == s["edits_sha"], s["name"]
+
+
+@pytest.mark.parametrize("name", ["scene64", "scene256", "scene1024", "mixed256", "mixed512", "terrain256",
+                                  "aabb_kat", "full_then_dig", "zero_hasher16", "tiny_pages64"])
+def test_serial_edit_pool_is_word_identical(golden, orc, name):
+    """NodePoolBase::Edit restated: same root, same pool words as the reference."""
+    s = scenario(golden, name)
+    cfg = config_from(s["config"])
+    pool = orc.OraclePool.from_config(cfg)
+    root = pool.edit(orc.NULL, scenario_edits(s))
+    assert pool.ok
+    assert root == s["root"]
+    bw, ids, pages = pool.dump()
+    assert sha(bw, ids, pages) == s["pool_sha"]
+    ok, counts, digests = pool.canonical(root)
+    assert ok and counts == s["canonical_counts"] and [str(d) for d in digests] == s["canonical_digests"]
+    from vkhashdag_gb300 import workloads as W
+    occ = pool.query(root, W.point_queries(s["res"], s["n_queries"], s["query_seed"]))
+    assert sha(occ) == s["query_sha"] and int(occ.sum()) == s["query_set"]
+
+
+@pytest.mark.parametrize("name", ["scene256", "mixed256", "terrain256"])
+def test_threaded_edit_same_canonical_dag(golden, orc, name):
+    """NodePoolThreadedEdit restated (OpenMP tasks): canonical DAG equals the serial one."""
+    s = scenario(golden, name)
+    assert s["threaded_canonical_equal"]
+    cfg = config_from(s["config"])
+    pool = orc.OraclePool.from_config(cfg)
+    root = pool.threaded_edit(orc.NULL, scenario_edits(s), max(0, cfg.get_node_levels() - 4), 4)
+    ok, counts, digests = pool.canonical(root)
+    assert ok and [str(d) for d in digests] == s["canonical_digests"]
+
+
+def test_aabb_known_answers(golden, orc):
+    """test/test.cpp:161-199: fill twice keeps the root, (3,3,3) set, (4,3,3)
+    clear, a sub-box fill inside a filled box keeps the root."""
+    s = scenario(golden, "aabb_kat")
+    cfg = config_from(s["config"])
+    edits = scenario_edits(s)
+    pool = orc.OraclePool.from_config(cfg)
+    roots = []
+    r = orc.NULL
+    for k in range(len(edits)):
+        r = pool.edit(r, edits[k:k + 1])
+        roots.append(r)
+    assert roots == s["roots_after_each"]
+    assert roots[0] == roots[1] and roots[2] == roots[3] and roots[1] != roots[2]
+    assert pool.query(roots[1], [[3, 3, 3], [4, 3, 3]]).tolist() == [1, 0]
+    assert pool.query(orc.NULL, [[3, 3, 3]]).tolist() == [0]
+    assert pool.query(roots[3], [[4, 3, 3]]).tolist() == [1]
+
+
+def test_upsert_known_answers(golden, orc):
+    """test/test.cpp:118-147: idempotent upsert, bucket word counts 3/9/2,
+    same node at another level gets another pointer."""
+    k = golden["upsert_kat"]
+    cfg = config_from(k["config"])
+    pool = orc.OraclePool.from_config(cfg)
+    pool.make_filled()
+    ptrs = [pool.upsert(level, words) for level, words in k["ops"]]
+    assert ptrs == k["ptrs"]
+    assert ptrs[0] == ptrs[1] and ptrs[2] != ptrs[0] and ptrs[3] != ptrs[2]
+    wpb = cfg.get_words_per_bucket()
+    bw = pool.bucket_words()
+    assert [int(bw[p // wpb]) for p in ptrs] == k["bucket_words_of_ptrs"]
+
+
+def test_bucket_full_known_answer(golden, orc):
+    """test/test.cpp:148-160: with every node in one bucket, exactly the words
+    of the bucket minus the filled node fit, pointers stay 3-word aligned in a page."""
+    k = golden["bucket_full_kat"]
+    cfg = config_from(k["config"])
+    pool = orc.OraclePool.from_config(cfg)
+    pool.make_filled()
+    ptrs = []
+    for c in range(k["n_ops"]):
+        p = pool.upsert(0, [0b11, c, 0x45])
+        if p == orc.NULL:
+            break
+        ptrs.append(p)
+    assert len(ptrs) == k["fit"]
+    assert (cfg.get_words_per_page() // 3) * cfg.get_pages_per_bucket() == k["fit"] + 3  # 9-word filled node
+    assert all((p % cfg.get_words_per_page()) % 3 == 0 for p in ptrs)
+    assert sha(np.array(ptrs, np.uint32)) == k["ptrs_sha"]
+
+
+@pytest.mark.parametrize("idx", [0, 1, 2])
+def test_traversal_matches_reference(golden, orc, idx):
+    """NodePoolTraversal::Traversal restated: same hit flags and bit-identical positions."""
+    t = golden["traversal"][idx]
+    s = scenario(golden, t["scenario"])
+    cfg = config_from(s["config"])
+    pool = orc.OraclePool.from_config(cfg)
+    root = pool.edit(orc.NULL, scenario_edits(s))
+    o, d = rays_for(t["n"], t["seed"])
+    hits = pool.trace(root, o, d)
+    assert hits["hit"].tolist() == t["hit"]
+    got = hits["pos"].view(np.uint32)
+    want = np.array(t["pos_bits"], np.uint32)
+    m = hits["hit"] == 1
+    assert np.array_equal(got[m], want[m])
+    # the hit voxel contains the hit position
+    R = 1 << cfg.get_voxel_level()
+    vox = hits["voxel"][m].astype(np.int64)
+    p = hits["pos"][m].astype(np.float64) * R
+    assert np.all(p >= vox - 1e-3) and np.all(p <= vox + hits["size"][m, None] + 1e-3)
+
+
+def test_live_reference_when_present(orc):
+    """Where the reference tree exists, re-run one scenario through its headers."""
+    if orc.build_ref() is None:
+        pytest.skip("reference tree not present on this machine")
+    from vkhashdag_gb300 import workloads as W
+    cfg = W.config_for_resolution(128)
+    e = W.mixed_batch(128, 300, seed=17, r_max=20, side_max=40)
+    r = orc.run_reference(orc.MODE_EDIT, cfg.word_bits_per_page, cfg.page_bits_per_bucket,
+                          cfg.bucket_bits_each_level, e)
+    pool = orc.OraclePool.from_config(cfg)
+    root = pool.edit(orc.NULL, e)
+    bw, ids, pages = pool.dump()
+    assert root == r["root"] and np.array_equal(pages, r["pages"]) and np.array_equal(bw, r["bucket_words"])

@@ -1,0 +1,382 @@
+"""vkhashdag_gb300 -- GB300 HashDAG edit engine (Python host mirror of the C ABI).
+
+The names follow the reference's hashdag API (include/hashdag/): ``Config`` and
+``DefaultConfig`` (Config.hpp:15-75), ``NodePointer`` values as plain ints with
+``NULL`` = 0xFFFFFFFF (NodePointer.hpp:13-31), ``EditType``/editors
+(Editor.hpp:18-55, src/main.cpp:32-150) and ``NodePool`` with ``edit``
+(NodePool.hpp:405-417), ``upsert_inner_node``/``upsert_leaf``
+(NodePool.hpp:228-238) and ``traversal`` (NodePoolTraversal.hpp:93-256).
+
+Every call goes through ``libhashdag_gb300.so`` (CUDA, sm_103a).  There is no
+CPU fallback: constructing a ``NodePool`` without the built library or without a
+CUDA device raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import enum
+import os
+from dataclasses import dataclass, field
+from typing import Iterable, List, Optional, Sequence
+
+import numpy as np
+
+__all__ = [
+    "NULL", "Config", "DefaultConfig", "EditMode", "SphereEditor", "AABBEditor", "NodePool",
+    "HashDagError", "EDIT_DTYPE", "HIT_DTYPE", "CAMERA_DTYPE", "edits_to_array", "lib", "library_path",
+    "count_voxel_edits", "device_available",
+]
+
+NULL = 0xFFFFFFFF
+MAX_LEVELS = 24
+_HERE = os.path.dirname(os.path.abspath(__file__))
+library_path = os.path.join(_HERE, "libhashdag_gb300.so")
+
+# hd_edit_desc (include/hashdag_gpu.h): 40 bytes
+EDIT_DTYPE = np.dtype([("shape", "<u4"), ("op", "<u4"), ("p0", "<u4", (3,)), ("p1", "<u4", (3,)), ("r2", "<u8")],
+                      align=True)
+assert EDIT_DTYPE.itemsize == 40
+HIT_DTYPE = np.dtype([("voxel", "<u4", (3,)), ("size", "<u4"), ("level", "<u4"), ("hit", "<u4"), ("t", "<f4"),
+                      ("pos", "<f4", (3,))])
+assert HIT_DTYPE.itemsize == 40
+CAMERA_DTYPE = np.dtype([("position", "<f4", (3,)), ("look", "<f4", (3,)), ("side", "<f4", (3,)),
+                         ("up", "<f4", (3,))])
+
+SHAPE_SPHERE, SHAPE_AABB = 0, 1
+OP_FILL, OP_DIG = 0, 1
+
+STATUS = {0: "ok", 1: "invalid argument", 2: "bucket full", 3: "device page heap exhausted", 4: "dedup index full",
+          5: "edit workspace capacity exceeded", 6: "CUDA error", 7: "device wait timed out", 8: "no CUDA device"}
+
+
+class HashDagError(RuntimeError):
+    def __init__(self, status: int, what: str = ""):
+        self.status = status
+        super().__init__(f"{what}: {STATUS.get(status, status)} (status {status})")
+
+
+class _Config(ctypes.Structure):
+    _fields_ = [("word_bits_per_page", ctypes.c_uint32), ("page_bits_per_bucket", ctypes.c_uint32),
+                ("node_levels", ctypes.c_uint32), ("hasher", ctypes.c_uint32),
+                ("bucket_bits_each_level", ctypes.c_uint32 * MAX_LEVELS)]
+
+
+class _Stats(ctypes.Structure):
+    _fields_ = [("heap_pages", ctypes.c_uint64), ("used_pages", ctypes.c_uint64), ("total_buckets", ctypes.c_uint64),
+                ("total_pages", ctypes.c_uint64), ("index_slots", ctypes.c_uint64), ("index_used", ctypes.c_uint64),
+                ("max_bucket_words", ctypes.c_uint32), ("words_per_bucket", ctypes.c_uint32)]
+
+
+_lib = None
+
+
+def lib():
+    """The loaded C ABI library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(library_path):
+        raise RuntimeError(f"{library_path} is missing: build it with vkhashdag_gb300._build.build()")
+    L = ctypes.CDLL(library_path)
+    P, U32, U64, I = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_int
+    sig = {
+        "hd_pool_create": (I, [ctypes.POINTER(_Config), U64, U32, I, ctypes.POINTER(P)]),
+        "hd_pool_destroy": (None, [P]),
+        "hd_config_validate": (I, [ctypes.POINTER(_Config)]),
+        "hd_config_default": (None, [U32, U32, U32, U32, U32, U32, ctypes.POINTER(_Config)]),
+        "hd_pool_filled_pointers": (I, [P, P]),
+        "hd_pool_get_stats": (I, [P, ctypes.POINTER(_Stats)]),
+        "hd_pool_get_error": (I, [P, P]),
+        "hd_pool_clear_error": (I, [P]),
+        "hd_edit": (I, [P, U32, P, U32, P, P]),
+        "hd_edit_async": (I, [P, U32, P, U32, P, P]),
+        "hd_edit_async_droot": (I, [P, P, P, U32, P, P]),
+        "hd_edit_reserve": (I, [P, U64, U64, U32]),
+        "hd_edit_last_counters": (I, [P, P, P, P]),
+        "hd_upsert": (I, [P, U32, P, P, U32, P]),
+        "hd_pool_read_bucket_words": (I, [P, U32, U32, P]),
+        "hd_pool_read_page_map": (I, [P, P]),
+        "hd_pool_read_pages": (I, [P, P, U32, P]),
+        "hd_pool_upload": (I, [P, P, P, U32, P, P]),
+        "hd_query": (I, [P, U32, P, U32, P, P]),
+        "hd_trace": (I, [P, U32, P, P, U32, P, P]),
+        "hd_trace_pinhole_async": (I, [P, U32, P, U32, U32, U32, P, P]),
+        "hd_count_voxel_edits": (U64, [P, U32, U32]),
+        "hd_status_string": (ctypes.c_char_p, [I]),
+        "hd_device_available": (I, []),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def device_available() -> bool:
+    return bool(lib().hd_device_available())
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def _check(status: int, what: str):
+    if status != 0:
+        raise HashDagError(status, what)
+
+
+@dataclass
+class Config:
+    """hashdag::Config<uint32_t> (include/hashdag/Config.hpp:15-57)."""
+    word_bits_per_page: int
+    page_bits_per_bucket: int
+    bucket_bits_each_level: List[int]
+    hasher: int = 0  # 0 MurmurHasher32, 1 all nodes to bucket 0 of their level (test ZeroHasher)
+
+    def get_node_levels(self) -> int:
+        return len(self.bucket_bits_each_level)
+
+    def get_leaf_level(self) -> int:
+        return self.get_node_levels()
+
+    def get_voxel_level(self) -> int:
+        return self.get_node_levels() + 1
+
+    def get_resolution(self) -> int:
+        return 1 << self.get_voxel_level()
+
+    def get_words_per_page(self) -> int:
+        return 1 << self.word_bits_per_page
+
+    def get_pages_per_bucket(self) -> int:
+        return 1 << self.page_bits_per_bucket
+
+    def get_words_per_bucket(self) -> int:
+        return 1 << (self.word_bits_per_page + self.page_bits_per_bucket)
+
+    def get_buckets_at_level(self, level: int) -> int:
+        return 1 << self.bucket_bits_each_level[level]
+
+    def get_level_base_bucket_indices(self) -> List[int]:
+        out, b = [], 0
+        for bits in self.bucket_bits_each_level:
+            out.append(b)
+            b += 1 << bits
+        return out
+
+    def get_total_buckets(self) -> int:
+        return sum(1 << b for b in self.bucket_bits_each_level)
+
+    def get_total_pages(self) -> int:
+        return self.get_total_buckets() << self.page_bits_per_bucket
+
+    def get_total_words(self) -> int:
+        return self.get_total_buckets() << (self.word_bits_per_page + self.page_bits_per_bucket)
+
+    def to_c(self) -> _Config:
+        c = _Config()
+        c.word_bits_per_page = self.word_bits_per_page
+        c.page_bits_per_bucket = self.page_bits_per_bucket
+        c.node_levels = len(self.bucket_bits_each_level)
+        c.hasher = self.hasher
+        for i, b in enumerate(self.bucket_bits_each_level):
+            c.bucket_bits_each_level[i] = b
+        return c
+
+    def validate(self) -> bool:
+        """Config::Validate (include/hashdag/Config.hpp:48-56)."""
+        if self.word_bits_per_page < 4:
+            return False
+        total = sum(1 << b for b in self.bucket_bits_each_level) << (self.word_bits_per_page + self.page_bits_per_bucket)
+        return total - 1 <= 0xFFFFFFFE
+
+
+@dataclass
+class DefaultConfig:
+    """hashdag::DefaultConfig<uint32_t> (include/hashdag/Config.hpp:59-75)."""
+    level_count: int = 17
+    top_level_count: int = 9
+    word_bits_per_page: int = 9
+    page_bits_per_bucket: int = 2
+    bucket_bits_per_top_level: int = 10
+    bucket_bits_per_bottom_level: int = 16
+
+    def __call__(self) -> Config:
+        bits = [self.bucket_bits_per_top_level if l < self.top_level_count else self.bucket_bits_per_bottom_level
+                for l in range(self.level_count - 1)]
+        return Config(self.word_bits_per_page, self.page_bits_per_bucket, bits)
+
+
+class EditMode(enum.IntEnum):
+    """EditMode of src/main.cpp:72 (kPaint only recolours and is out of scope here)."""
+    kFill = OP_FILL
+    kDig = OP_DIG
+
+
+@dataclass
+class SphereEditor:
+    """SphereEditor<Mode> (src/main.cpp:73-150): voxel p inside iff |p-center|^2 <= r2."""
+    center: Sequence[int]
+    r2: int
+    mode: EditMode = EditMode.kFill
+
+    def desc(self):
+        return (SHAPE_SPHERE, int(self.mode), tuple(int(c) for c in self.center), (0, 0, 0), int(self.r2))
+
+
+@dataclass
+class AABBEditor:
+    """AABBEditor (src/main.cpp:32-63): voxel p inside iff aabb_min <= p < aabb_max; kDig by symmetry."""
+    aabb_min: Sequence[int]
+    aabb_max: Sequence[int]
+    mode: EditMode = EditMode.kFill
+
+    def desc(self):
+        return (SHAPE_AABB, int(self.mode), tuple(int(c) for c in self.aabb_min), tuple(int(c) for c in self.aabb_max), 0)
+
+
+def edits_to_array(editors: Iterable) -> np.ndarray:
+    items = [e.desc() for e in editors]
+    return np.array(items, dtype=EDIT_DTYPE)
+
+
+def count_voxel_edits(edits: np.ndarray, resolution: int) -> int:
+    edits = np.ascontiguousarray(edits, dtype=EDIT_DTYPE)
+    return int(lib().hd_count_voxel_edits(_ptr(edits), len(edits), resolution))
+
+
+class NodePool:
+    """A device-resident node pool (NodePoolBase + DAGNodePool storage, on the GPU).
+
+    ``heap_pages`` is the number of physical pages reserved on the device
+    (``heap_pages << word_bits_per_page`` 32-bit words).
+    """
+
+    def __init__(self, config: Config, heap_pages: int = 1 << 16, index_log2: int = 0, device: int = 0):
+        L = lib()
+        self.config = config
+        self._cfg = config.to_c()
+        h = ctypes.c_void_p()
+        _check(L.hd_pool_create(ctypes.byref(self._cfg), heap_pages, index_log2, device, ctypes.byref(h)),
+               "hd_pool_create")
+        self._h = h
+        self.root = NULL
+
+    # -- lifecycle -------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().hd_pool_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def get_config(self) -> Config:
+        return self.config
+
+    def filled_node_pointers(self) -> List[int]:
+        out = np.zeros(self.config.get_node_levels(), np.uint32)
+        _check(lib().hd_pool_filled_pointers(self._h, _ptr(out)), "hd_pool_filled_pointers")
+        return [int(x) for x in out]
+
+    def stats(self) -> dict:
+        s = _Stats()
+        _check(lib().hd_pool_get_stats(self._h, ctypes.byref(s)), "hd_pool_get_stats")
+        return {k: getattr(s, k) for k, _ in _Stats._fields_}
+
+    # -- edit path ---------------------------------------------------------
+    def edit(self, root: int, editors, stream: int = 0) -> int:
+        """Apply one editor or an ordered list of editors / an EDIT_DTYPE array to root."""
+        if isinstance(editors, np.ndarray):
+            arr = np.ascontiguousarray(editors, dtype=EDIT_DTYPE)
+        elif isinstance(editors, (SphereEditor, AABBEditor)):
+            arr = edits_to_array([editors])
+        else:
+            arr = edits_to_array(editors)
+        out = ctypes.c_uint32(NULL)
+        _check(lib().hd_edit(self._h, root & 0xFFFFFFFF, _ptr(arr), len(arr), ctypes.byref(out),
+                             ctypes.c_void_p(stream)), "hd_edit")
+        return out.value
+
+    def last_counters(self):
+        n = self.config.get_node_levels()
+        it, ca, ins = (np.zeros(n, np.uint64) for _ in range(3))
+        _check(lib().hd_edit_last_counters(self._h, _ptr(it), _ptr(ca), _ptr(ins)), "hd_edit_last_counters")
+        return it, ca, ins
+
+    def reserve(self, max_items: int, max_list_entries: int, max_edits: int):
+        _check(lib().hd_edit_reserve(self._h, max_items, max_list_entries, max_edits), "hd_edit_reserve")
+
+    # -- upsert ------------------------------------------------------------
+    def upsert_nodes(self, level: int, nodes: Sequence[Sequence[int]]) -> List[int]:
+        words = np.array([w for n in nodes for w in n], dtype=np.uint32)
+        lens = np.array([len(n) for n in nodes], dtype=np.uint32)
+        out = np.zeros(len(nodes), np.uint32)
+        _check(lib().hd_upsert(self._h, level, _ptr(words), _ptr(lens), len(nodes), _ptr(out)), "hd_upsert")
+        return [int(x) for x in out]
+
+    def upsert_inner_node(self, level: int, node: Sequence[int]) -> int:
+        return self.upsert_nodes(level, [node])[0]
+
+    def upsert_leaf(self, level: int, leaf: Sequence[int]) -> int:
+        return self.upsert_nodes(level, [leaf])[0]
+
+    # -- host mirror -------------------------------------------------------
+    def bucket_words(self) -> np.ndarray:
+        n = self.config.get_total_buckets()
+        out = np.zeros(n, np.uint32)
+        _check(lib().hd_pool_read_bucket_words(self._h, 0, n, _ptr(out)), "hd_pool_read_bucket_words")
+        return out
+
+    def page_map(self) -> np.ndarray:
+        out = np.zeros(self.config.get_total_pages(), np.uint8)
+        _check(lib().hd_pool_read_page_map(self._h, _ptr(out)), "hd_pool_read_page_map")
+        return out
+
+    def read_pages(self, page_ids) -> np.ndarray:
+        ids = np.ascontiguousarray(page_ids, dtype=np.uint32)
+        out = np.zeros((len(ids), self.config.get_words_per_page()), np.uint32)
+        _check(lib().hd_pool_read_pages(self._h, _ptr(ids), len(ids), _ptr(out)), "hd_pool_read_pages")
+        return out
+
+    def download(self):
+        """(bucket_words, page_ids, pages) of the whole pool."""
+        pm = self.page_map()
+        ids = np.nonzero(pm)[0].astype(np.uint32)
+        return self.bucket_words(), ids, self.read_pages(ids)
+
+    def upload(self, bucket_words, page_ids, pages, filled=None):
+        bw = np.ascontiguousarray(bucket_words, dtype=np.uint32)
+        ids = np.ascontiguousarray(page_ids, dtype=np.uint32)
+        pg = np.ascontiguousarray(pages, dtype=np.uint32)
+        fl = None if filled is None else np.ascontiguousarray(filled, dtype=np.uint32)
+        _check(lib().hd_pool_upload(self._h, _ptr(bw), _ptr(ids), len(ids), _ptr(pg),
+                                    None if fl is None else _ptr(fl)), "hd_pool_upload")
+
+    # -- read path ---------------------------------------------------------
+    def query(self, root: int, xyz) -> np.ndarray:
+        pts = np.ascontiguousarray(xyz, dtype=np.uint32).reshape(-1, 3)
+        out = np.zeros(len(pts), np.uint8)
+        _check(lib().hd_query(self._h, root & 0xFFFFFFFF, _ptr(pts), len(pts), _ptr(out), None), "hd_query")
+        return out
+
+    def traversal(self, root: int, origins, dirs) -> np.ndarray:
+        o = np.ascontiguousarray(origins, dtype=np.float32).reshape(-1, 3)
+        d = np.ascontiguousarray(dirs, dtype=np.float32).reshape(-1, 3)
+        out = np.zeros(len(o), HIT_DTYPE)
+        _check(lib().hd_trace(self._h, root & 0xFFFFFFFF, _ptr(o), _ptr(d), len(o), _ptr(out), None), "hd_trace")
+        return out

@@ -1,0 +1,268 @@
+// hd_device.cuh -- device-side building blocks of the HashDAG edit engine:
+// pool view, node addressing, hashes, editor predicates, the dedup index
+// encoding and the edit workspace layout.  Included by every .cu file.
+#pragma once
+
+#include "../../include/hashdag_gpu.h"
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace hd {
+
+using u32 = uint32_t;
+using u64 = uint64_t;
+
+static constexpr u32 kNull = 0xFFFFFFFFu;
+static constexpr u32 kMaxNodeLevels = 21; // node coordinates packed 21 bits per axis
+static constexpr u32 kUnallocPage = 0xFFFFFFFFu;
+static constexpr u32 kZeroPage = 0u; // physical page 0 is never handed out (failed allocations map here)
+
+// device error codes (sticky, first error wins)
+enum DevError : u32 {
+	kErrNone = 0,
+	kErrBucketFull = HD_ERR_BUCKET_FULL,
+	kErrOom = HD_ERR_POOL_OOM,
+	kErrIndexFull = HD_ERR_INDEX_FULL,
+	kErrCapacity = HD_ERR_CAPACITY,
+	kErrTimeout = HD_ERR_TIMEOUT,
+	kErrInvalidRoot = HD_ERR_INVALID_ARG,
+};
+
+// Config<uint32_t> with the derived per-level tables (include/hashdag/Config.hpp:15-57)
+// and the filled node of every level (include/hashdag/NodePool.hpp:54).
+struct DevConfig {
+	u32 wbpp, pbpb, L, hasher;
+	u32 bucket_bits[HD_MAX_LEVELS];
+	u32 bucket_base[HD_MAX_LEVELS];
+	u32 filled[HD_MAX_LEVELS];
+};
+
+// Device-resident node pool.  Pointers are the reference's virtual word
+// indices; page_table maps a virtual page (bucket << pbpb | slot) to a
+// physical page of the heap.
+struct DevPool {
+	DevConfig cfg;
+	u32 *bucket_words; // [total_buckets]
+	u32 *page_table;   // [total_pages] physical page or kUnallocPage
+	u32 *heap;         // [heap_pages << wbpp]
+	u32 *counters;     // [0] next physical page, [1] sticky error, [2] index slots used
+	unsigned long long *index; // dedup index [index_mask+1]
+	u64 index_mask;
+	u64 total_pages;
+	u32 heap_pages;
+	u32 pad_;
+};
+
+enum CounterSlot : u32 { kCtrHeapNext = 0, kCtrError = 1, kCtrIndexUsed = 2, kCtrCount = 4 };
+
+__device__ __forceinline__ u32 wpp(const DevConfig &c) { return 1u << c.wbpp; }
+
+// NodePool.hpp:75-77 read_node, through the page table
+__device__ __forceinline__ const u32 *node_addr(const DevPool &p, u32 ptr) {
+	u32 phys = __ldg(p.page_table + (ptr >> p.cfg.wbpp));
+	return p.heap + ((u64)phys << p.cfg.wbpp) + (ptr & (wpp(p.cfg) - 1u));
+}
+__device__ __forceinline__ u32 *node_addr_w(const DevPool &p, u32 ptr) {
+	u32 phys = p.page_table[ptr >> p.cfg.wbpp];
+	return p.heap + ((u64)phys << p.cfg.wbpp) + (ptr & (wpp(p.cfg) - 1u));
+}
+
+__device__ __forceinline__ void set_error(u32 *slot, u32 code) { atomicCAS(slot, 0u, code); }
+
+// ------------------------------------------------------------------ hashes
+// include/hashdag/Hasher.hpp:21-39: MurmurHash3 x86-32 body, seed 0, length = words
+struct Murmur {
+	u32 h = 0;
+	__device__ __forceinline__ void add(u32 k) {
+		k *= 0xcc9e2d51u;
+		k = (k << 15) | (k >> 17);
+		k *= 0x1b873593u;
+		h ^= k;
+		h = (h << 13) | (h >> 19);
+		h = h * 5u + 0xe6546b64u;
+	}
+	__device__ __forceinline__ u32 finish(u32 n) const {
+		u32 x = h ^ n;
+		x ^= x >> 16;
+		x *= 0x85ebca6bu;
+		x ^= x >> 13;
+		x *= 0xc2b2ae35u;
+		x ^= x >> 16;
+		return x;
+	}
+};
+// include/hashdag/Hasher.hpp:40-48: 64-bit finaliser truncated to 32 bits (leaves)
+__device__ __forceinline__ u32 hash_leaf(u64 v) {
+	v ^= v >> 33;
+	v *= 0xff51afd7ed558ccdull;
+	v ^= v >> 33;
+	v *= 0xc4ceb9fe1a85ec53ull;
+	v ^= v >> 33;
+	return (u32)v;
+}
+
+__device__ __forceinline__ u64 mix64(u64 x) {
+	x ^= x >> 30;
+	x *= 0xbf58476d1ce4e5b9ull;
+	x ^= x >> 27;
+	x *= 0x94d049bb133111ebull;
+	x ^= x >> 31;
+	return x;
+}
+
+// ------------------------------------------------------------------ dedup index
+// 64-bit slots of an open-addressing table over all nodes of the pool:
+//   empty      ~0
+//   committed  tag31 << 32 | node pointer           (bit 63 clear)
+//   pending    1 << 63 | tag31 << 32 | item index    (claimed in this pass, not yet written)
+//   tombstone  1 << 63 | 0x7FFFFFFF << 32 | 0xFFFFFFFE (claim of a failed insert)
+// tag31 = low 31 bits of the node's content hash.
+static constexpr unsigned long long kSlotEmpty = ~0ull;
+static constexpr unsigned long long kSlotTomb = (1ull << 63) | (0x7FFFFFFFull << 32) | 0xFFFFFFFEull;
+__device__ __forceinline__ u64 index_start(u32 h, u32 level, u64 mask) {
+	return mix64(((u64)h << 8) | level) & mask;
+}
+
+// ------------------------------------------------------------------ editors
+// src/main.cpp:32-150 (stateless forms).  Classification of a node at `level`
+// with integer position pos[] against one edit: 0 kNotAffected, 1 kProceed,
+// 2 full cover (kFill for FILL, kClear for DIG).
+enum Cls : u32 { kClsNone = 0, kClsPartial = 1, kClsFull = 2 };
+
+__device__ __forceinline__ u32 classify(const hd_edit_desc &e, u32 shift, u32 px, u32 py, u32 pz) {
+	u32 lb[3] = {px << shift, py << shift, pz << shift};
+	u32 ub[3] = {(px + 1u) << shift, (py + 1u) << shift, (pz + 1u) << shift};
+	if (e.shape == HD_SHAPE_AABB) { // AABBEditor::EditNode (src/main.cpp:36-47)
+		bool out = false, in = true;
+#pragma unroll
+		for (int a = 0; a < 3; ++a) {
+			out |= (ub[a] <= e.p0[a]) | (lb[a] >= e.p1[a]);
+			in &= (lb[a] >= e.p0[a]) & (ub[a] <= e.p1[a]);
+		}
+		return out ? kClsNone : (in ? kClsFull : kClsPartial);
+	}
+	// SphereEditor::EditNode (src/main.cpp:77-106), same integer formulas
+	u64 mx = 0, mn = 0;
+#pragma unroll
+	for (int a = 0; a < 3; ++a) {
+		long long lbd = (long long)lb[a] - (long long)e.p0[a];
+		long long ubd = (long long)ub[a] - (long long)e.p0[a];
+		u64 l2 = (u64)lbd * (u64)lbd, u2 = (u64)ubd * (u64)ubd;
+		mx += l2 > u2 ? l2 : u2;
+		mn += (lbd > 0 ? l2 : 0ull) + (ubd < 0 ? u2 : 0ull);
+	}
+	if (mx <= e.r2)
+		return kClsFull;
+	return mn > e.r2 ? kClsNone : kClsPartial;
+}
+
+// Leaf voxel index i in [0,64) -> offset inside the 4^3 leaf (NodeCoord.hpp:32-43):
+//   x = (i>>2 & 2) | (i & 1), y = (i>>3 & 2) | (i>>1 & 1), z = (i>>4 & 2) | (i>>2 & 1)
+// 64-bit mask of the leaf voxels at origin (ox,oy,oz) inside the edit's shape
+// (SphereEditor/AABBEditor::VoxelInRange, src/main.cpp:55-57,121-126).
+__device__ __forceinline__ u64 shape_mask(const hd_edit_desc &e, u32 ox, u32 oy, u32 oz) {
+	if (e.shape == HD_SHAPE_AABB) {
+		u32 mx = 0, my = 0, mz = 0;
+#pragma unroll
+		for (u32 k = 0; k < 4; ++k) {
+			mx |= u32((ox + k) >= e.p0[0] && (ox + k) < e.p1[0]) << k;
+			my |= u32((oy + k) >= e.p0[1] && (oy + k) < e.p1[1]) << k;
+			mz |= u32((oz + k) >= e.p0[2] && (oz + k) < e.p1[2]) << k;
+		}
+		u64 m = 0;
+#pragma unroll
+		for (u32 i = 0; i < 64; ++i) {
+			u32 x = ((i >> 2) & 2u) | (i & 1u), y = ((i >> 3) & 2u) | ((i >> 1) & 1u), z = ((i >> 4) & 2u) | ((i >> 2) & 1u);
+			m |= (u64)((mx >> x) & (my >> y) & (mz >> z) & 1u) << i;
+		}
+		return m;
+	}
+	u64 dx2[4], dy2[4], dz2[4];
+#pragma unroll
+	for (u32 k = 0; k < 4; ++k) {
+		long long dx = (long long)(ox + k) - (long long)e.p0[0];
+		long long dy = (long long)(oy + k) - (long long)e.p0[1];
+		long long dz = (long long)(oz + k) - (long long)e.p0[2];
+		dx2[k] = (u64)dx * (u64)dx;
+		dy2[k] = (u64)dy * (u64)dy;
+		dz2[k] = (u64)dz * (u64)dz;
+	}
+	u64 m = 0;
+#pragma unroll
+	for (u32 i = 0; i < 64; ++i) {
+		u32 x = ((i >> 2) & 2u) | (i & 1u), y = ((i >> 3) & 2u) | ((i >> 1) & 1u), z = ((i >> 4) & 2u) | ((i >> 2) & 1u);
+		m |= (u64)(dx2[x] + dy2[y] + dz2[z] <= e.r2) << i;
+	}
+	return m;
+}
+
+__device__ __forceinline__ u64 pack_pos(u32 x, u32 y, u32 z) { return (u64)x | ((u64)y << 21) | ((u64)z << 42); }
+__device__ __forceinline__ u32 pos_x(u64 p) { return (u32)(p & 0x1FFFFFu); }
+__device__ __forceinline__ u32 pos_y(u64 p) { return (u32)((p >> 21) & 0x1FFFFFu); }
+__device__ __forceinline__ u32 pos_z(u64 p) { return (u32)((p >> 42) & 0x1FFFFFu); }
+
+// ------------------------------------------------------------------ edit workspace
+// Frontier items of one batched edit pass.  Inner items (levels 0..L-2) and
+// leaf items (level L-1) live in two index spaces; every level's items are a
+// contiguous range of its space.
+enum ItemState : u32 {
+	kStUnchanged = 0, // result = base pointer
+	kStEmpty = 1,     // result = Null
+	kStFound = 2,     // result = existing node res[]
+	kStRep = 3,       // result = node inserted by this item (res[]); link = index slot
+	kStAlias = 4,     // result = res[link] (another item of the pass with equal content)
+	kStFail = 5,      // insertion failed (error recorded)
+	kStCand = 6,      // leaf computed, dedup pending
+};
+
+struct Items {
+	u64 *pos;     // packed node coordinate
+	u32 *base;    // node the edit list applies to (original node, filled node or Null)
+	u32 *parent;  // child slot of the parent (inner index*8 + child) or kNull for the root
+	u32 *lst_off; // edit list [lst_off, lst_off+lst_len) in Workspace::lists
+	u32 *lst_len;
+	u32 *res;     // result pointer
+	u32 *state;   // ItemState
+	u32 *link;    // index slot (kStRep) or representative item (kStAlias)
+	u32 *pad;     // bucket word offset where zero padding starts (kStRep), or kNull
+	u64 cap;
+};
+
+struct Workspace {
+	Items inner, leaf;
+	u32 *bchild; // [inner.cap*8] children of the base node
+	u32 *cnew;   // [inner.cap*8] new children
+	u64 *leaf_new; // [leaf.cap] new leaf bits
+	u32 *lists;    // edit lists
+	u64 list_cap;
+	u32 *long_q;   // per inner level: items with long edit lists (same index space as inner)
+	const hd_edit_desc *edits;
+	u32 n_edits;
+	u32 long_threshold; // lists longer than this are expanded by a warp
+	// device counters (u64 so that overflow counts stay exact):
+	//   [0..L)       items per level
+	//   [32..32+L)   long items per level
+	//   [64]         list entries used
+	//   [65]         workspace error
+	//   [66]         root result
+	//   [96..96+L)   candidates per level, [128..) words of candidates,
+	//   [160..) inserted per level, [192..) words inserted
+	unsigned long long *ctr;
+};
+
+enum WsCtr : u32 {
+	kWsItems = 0,
+	kWsLong = 32,
+	kWsList = 64,
+	kWsError = 65,
+	kWsRoot = 66,
+	kWsRootIn = 67,
+	kWsCand = 96,
+	kWsCandWords = 128,
+	kWsIns = 160,
+	kWsInsWords = 192,
+	kWsCtrCount = 224,
+};
+
+} // namespace hd

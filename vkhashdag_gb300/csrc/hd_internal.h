@@ -1,0 +1,33 @@
+// hd_internal.h -- host-side state of a device node pool (shared by the .cu files).
+#pragma once
+
+#include "hd_device.cuh"
+
+#include <mutex>
+#include <vector>
+
+struct hd_ws_host {
+	hd::Workspace d{};          // device view handed to kernels
+	std::vector<void *> allocs; // everything cudaMalloc'ed for the workspace
+	hd_edit_desc *edits = nullptr;
+	uint32_t edit_cap = 0;
+	unsigned long long *ctr_host = nullptr; // pinned copy of the counters
+};
+
+struct hd_pool {
+	int device = 0;
+	int num_sms = 152;
+	hd_config cfg{};
+	hd::DevPool P{};
+	uint64_t total_buckets = 0, total_pages = 0;
+	uint32_t *d_out_root = nullptr; // device word for synchronous calls
+	uint32_t *h_small = nullptr;    // pinned scratch (root, error)
+	cudaEvent_t ws_free = nullptr;  // orders passes that share the workspace
+	hd_ws_host ws;
+	std::mutex mtx;
+	uint64_t last_items[HD_MAX_LEVELS] = {}, last_cand[HD_MAX_LEVELS] = {}, last_ins[HD_MAX_LEVELS] = {};
+};
+
+// hd_engine.cu
+hd_status hd_check(cudaError_t e);
+void hd_grid_for_levels(const hd_pool *pool, const hd_edit_desc *host_edits, uint32_t n, uint32_t *grid_per_level);

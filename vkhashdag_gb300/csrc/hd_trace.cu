@@ -1,0 +1,274 @@
+// hd_trace.cu -- read path: DAG ray traversal and point queries.
+//
+// k_trace restates NodePoolTraversal::Traversal<float>
+// (include/hashdag/NodePoolTraversal.hpp:93-256), the Laine-Karras style
+// traversal of the DAG mapped to [1,2]^3, with the voxel position / size
+// output of shader/src/trace.frag:223-246 and without the LOD cut.  One thread
+// per ray; this file is compiled with -fmad=false and IEEE division / square
+// root so every float operation rounds exactly like the CPU restatement built
+// with -ffp-contract=off.
+#include "hd_internal.h"
+
+#include <algorithm>
+#include <cstdio>
+
+using namespace hd;
+
+namespace {
+
+__device__ __forceinline__ float fmin_ref(float x, float y) { return (y < x) ? y : x; } // glm::min
+__device__ __forceinline__ float fmax_ref(float x, float y) { return (x < y) ? y : x; } // glm::max
+__device__ __forceinline__ float abs_ref(float x) { return x >= 0.0f ? x : -x; }
+
+__device__ hd_hit trace_one(const DevPool &P, u32 root, float ox, float oy, float oz, float dx, float dy, float dz) {
+	hd_hit out;
+	out.voxel[0] = out.voxel[1] = out.voxel[2] = 0;
+	out.size = 0;
+	out.level = 0;
+	out.hit = 0;
+	out.t = 0.0f;
+	out.pos[0] = out.pos[1] = out.pos[2] = 0.0f;
+	if (root == kNull)
+		return out;
+	constexpr int kStack = 23;
+	const float eps = __uint_as_float((127u - 23u) << 23);
+	u32 stack[kStack];
+#pragma unroll
+	for (int k = 0; k < kStack; ++k) // every entry holds a node pointer before the first push
+		stack[k] = root;
+	float o[3] = {ox + 1.0f, oy + 1.0f, oz + 1.0f};
+	float din[3] = {dx, dy, dz}, d[3];
+#pragma unroll
+	for (int a = 0; a < 3; ++a)
+		d[a] = abs_ref(din[a]) > eps ? din[a] : (din[a] >= 0.0f ? eps : -eps);
+	float tc[3], tb[3];
+#pragma unroll
+	for (int a = 0; a < 3; ++a) {
+		tc[a] = __fdiv_rn(1.0f, -abs_ref(d[a]));
+		tb[a] = __fmul_rn(tc[a], o[a]);
+	}
+	u32 octant = 0;
+#pragma unroll
+	for (int a = 0; a < 3; ++a)
+		if (d[a] > 0.0f) {
+			octant ^= 1u << a;
+			tb[a] = __fsub_rn(__fmul_rn(3.0f, tc[a]), tb[a]);
+		}
+	float t_min = fmax_ref(fmax_ref(__fsub_rn(__fmul_rn(2.0f, tc[0]), tb[0]), __fsub_rn(__fmul_rn(2.0f, tc[1]), tb[1])),
+	                       __fsub_rn(__fmul_rn(2.0f, tc[2]), tb[2]));
+	float t_max = fmin_ref(fmin_ref(__fsub_rn(tc[0], tb[0]), __fsub_rn(tc[1], tb[1])), __fsub_rn(tc[2], tb[2]));
+	float h = t_max;
+	t_min = fmax_ref(t_min, 0.0f);
+	t_max = fmin_ref(t_max, 1.0f);
+	u32 parent = root, child_bits = 0;
+	float pos[3] = {1.0f, 1.0f, 1.0f};
+	u32 idx = 0;
+#pragma unroll
+	for (int a = 0; a < 3; ++a)
+		if (__fsub_rn(__fmul_rn(1.5f, tc[a]), tb[a]) > t_min) {
+			idx ^= 1u << a;
+			pos[a] = 1.5f;
+		}
+	int scale = kStack - 1;
+	float scale_exp2 = 0.5f;
+	const u32 leaf_level = P.cfg.L;
+	const int leaf_scale = kStack - (int)leaf_level;
+	for (int guard = 0; guard < (1 << 20); ++guard) { // a ray crosses at most a few thousand cells
+		if (child_bits == 0u) {
+			if (scale > leaf_scale)
+				child_bits = node_addr(P, parent)[0];
+			else if (scale == leaf_scale) {
+				const u32 *p = node_addr(P, parent);
+				const u32 l0 = p[0], l1 = p[1];
+				child_bits = ((l0 & 0xFFu) ? 1u : 0u) | ((l0 & 0xFF00u) ? 2u : 0u) | ((l0 & 0xFF0000u) ? 4u : 0u) |
+				             ((l0 & 0xFF000000u) ? 8u : 0u) | ((l1 & 0xFFu) ? 16u : 0u) | ((l1 & 0xFF00u) ? 32u : 0u) |
+				             ((l1 & 0xFF0000u) ? 64u : 0u) | ((l1 & 0xFF000000u) ? 128u : 0u);
+			} else
+				child_bits = parent;
+		}
+		float tcor[3];
+#pragma unroll
+		for (int a = 0; a < 3; ++a)
+			tcor[a] = __fsub_rn(__fmul_rn(pos[a], tc[a]), tb[a]);
+		const float tc_max = fmin_ref(fmin_ref(tcor[0], tcor[1]), tcor[2]);
+		const u32 child_shift = idx ^ octant;
+		const u32 child_mask = 1u << child_shift;
+		if ((child_bits & child_mask) != 0 && t_min <= t_max) {
+			const float half = __fmul_rn(scale_exp2, 0.5f);
+			float tcen[3];
+#pragma unroll
+			for (int a = 0; a < 3; ++a)
+				tcen[a] = __fadd_rn(__fmul_rn(half, tc[a]), tcor[a]);
+			if (scale < leaf_scale)
+				break;
+			if (tc_max < h)
+				stack[scale] = parent;
+			h = tc_max;
+			if (scale > leaf_scale)
+				parent = node_addr(P, parent + 1u + __popc(child_bits & (child_mask - 1u)))[0];
+			else
+				parent = (node_addr(P, parent + (child_shift >> 2u))[0] >> ((child_shift & 3u) << 3u)) & 0xFFu;
+			idx = 0;
+			--scale;
+			scale_exp2 = half;
+#pragma unroll
+			for (int a = 0; a < 3; ++a)
+				if (tcen[a] > t_min) {
+					idx ^= 1u << a;
+					pos[a] = __fadd_rn(pos[a], scale_exp2);
+				}
+			child_bits = 0;
+			continue;
+		}
+		u32 step = 0;
+#pragma unroll
+		for (int a = 0; a < 3; ++a)
+			if (tcor[a] <= tc_max) {
+				step ^= 1u << a;
+				pos[a] = __fsub_rn(pos[a], scale_exp2);
+			}
+		t_min = tc_max;
+		idx ^= step;
+		if ((idx & step) != 0) {
+			u32 diff = 0;
+#pragma unroll
+			for (int a = 0; a < 3; ++a)
+				if (step & (1u << a))
+					diff |= __float_as_uint(pos[a]) ^ __float_as_uint(__fadd_rn(pos[a], scale_exp2));
+			scale = diff ? 31 - __clz(diff) : -1;
+			if (scale >= kStack || scale < 0) {
+				scale = kStack;
+				break;
+			}
+			scale_exp2 = __uint_as_float((u32)(scale - kStack + 127) << 23);
+			parent = stack[scale];
+			u32 sh[3];
+#pragma unroll
+			for (int a = 0; a < 3; ++a) {
+				sh[a] = __float_as_uint(pos[a]) >> scale;
+				pos[a] = __uint_as_float(sh[a] << scale);
+			}
+			idx = (sh[0] & 1u) | ((sh[1] & 1u) << 1) | ((sh[2] & 1u) << 2);
+			h = 0.0f;
+			child_bits = 0;
+		}
+	}
+	const bool hit = scale < kStack && t_min <= t_max;
+	out.hit = hit ? 1u : 0u;
+	out.t = t_min;
+	const u32 voxel_level = leaf_level + 1u;
+	const int voxel_scale = kStack - (int)voxel_level;
+	if (hit) {
+		const u32 size = 1u << (scale - voxel_scale);
+#pragma unroll
+		for (int a = 0; a < 3; ++a) {
+			u32 vp = (__float_as_uint(pos[a]) & 0x7FFFFFu) >> voxel_scale;
+			if (octant & (1u << a))
+				vp = (1u << voxel_level) - size - vp;
+			out.voxel[a] = vp;
+		}
+		out.size = size;
+		out.level = voxel_level - (31u - __clz(size));
+#pragma unroll
+		for (int a = 0; a < 3; ++a) {
+			float p = pos[a];
+			if (octant & (1u << a))
+				p = __fsub_rn(__fsub_rn(3.0f, scale_exp2), p);
+			float q = __fadd_rn(o[a], __fmul_rn(t_min, d[a]));
+			q = fmin_ref(fmax_ref(q, p), __fadd_rn(p, scale_exp2));
+			out.pos[a] = __fsub_rn(q, 1.0f);
+		}
+	}
+	return out;
+}
+
+__global__ void k_trace(DevPool P, u32 root, const float *o, const float *d, u32 n, hd_hit *out) {
+	for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (u64)gridDim.x * blockDim.x)
+		out[i] = trace_one(P, root, o[3 * i], o[3 * i + 1], o[3 * i + 2], d[3 * i], d[3 * i + 1], d[3 * i + 2]);
+}
+
+// Camera_GenRay (shader/src/trace.frag:366-370) at pixel centres, then the traversal.
+__global__ void k_trace_pinhole(DevPool P, u32 root, const hd_camera *cams, u32 n_cams, u32 w, u32 h, hd_hit *out) {
+	const u64 per = (u64)w * h, total = per * n_cams;
+	for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (u64)gridDim.x * blockDim.x) {
+		const u32 c = (u32)(i / per);
+		const u32 px = (u32)(i % per % w), py = (u32)(i % per / w);
+		const hd_camera cam = cams[c];
+		const float u = __fsub_rn(__fmul_rn(__fdiv_rn(__fadd_rn((float)px, 0.5f), (float)w), 2.0f), 1.0f);
+		const float v = __fsub_rn(__fmul_rn(__fdiv_rn(__fadd_rn((float)py, 0.5f), (float)h), 2.0f), 1.0f);
+		float dd[3];
+#pragma unroll
+		for (int a = 0; a < 3; ++a)
+			dd[a] = __fsub_rn(__fsub_rn(cam.look[a], __fmul_rn(cam.side[a], u)), __fmul_rn(cam.up[a], v));
+		const float len2 = __fadd_rn(__fadd_rn(__fmul_rn(dd[0], dd[0]), __fmul_rn(dd[1], dd[1])), __fmul_rn(dd[2], dd[2]));
+		const float inv = __fdiv_rn(1.0f, __fsqrt_rn(len2));
+		out[i] = trace_one(P, root, cam.position[0], cam.position[1], cam.position[2], __fmul_rn(dd[0], inv),
+		                   __fmul_rn(dd[1], inv), __fmul_rn(dd[2], inv));
+	}
+}
+
+} // namespace
+
+extern "C" {
+
+hd_status hd_trace(hd_pool *pool, uint32_t root, const float *origins, const float *dirs, uint32_t n, hd_hit *out,
+                   void *stream) {
+	if (!pool || (n && (!origins || !dirs || !out)))
+		return HD_ERR_INVALID_ARG;
+	if (!n)
+		return HD_OK;
+	std::lock_guard<std::mutex> lk(pool->mtx);
+	if (cudaSetDevice(pool->device) != cudaSuccess)
+		return HD_ERR_CUDA;
+	cudaStream_t st = (cudaStream_t)stream;
+	float *d_o = nullptr, *d_d = nullptr;
+	hd_hit *d_out = nullptr;
+	hd_status s = HD_OK;
+	if (cudaMalloc(&d_o, n * 12ull) != cudaSuccess || cudaMalloc(&d_d, n * 12ull) != cudaSuccess ||
+	    cudaMalloc(&d_out, n * sizeof(hd_hit)) != cudaSuccess)
+		s = HD_ERR_CUDA;
+	if (!s && (cudaStreamWaitEvent(st, pool->ws_free, 0) != cudaSuccess ||
+	           cudaMemcpyAsync(d_o, origins, n * 12ull, cudaMemcpyHostToDevice, st) != cudaSuccess ||
+	           cudaMemcpyAsync(d_d, dirs, n * 12ull, cudaMemcpyHostToDevice, st) != cudaSuccess))
+		s = HD_ERR_CUDA;
+	if (!s) {
+		const uint32_t grid = std::max(1u, std::min((n + 255u) / 256u, (uint32_t)pool->num_sms * 16u));
+		k_trace<<<grid, 256, 0, st>>>(pool->P, root, d_o, d_d, n, d_out);
+		if (cudaGetLastError() != cudaSuccess ||
+		    cudaMemcpyAsync(out, d_out, n * sizeof(hd_hit), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+		    cudaStreamSynchronize(st) != cudaSuccess)
+			s = HD_ERR_CUDA;
+	}
+	cudaFree(d_o);
+	cudaFree(d_d);
+	cudaFree(d_out);
+	return s;
+}
+
+hd_status hd_trace_pinhole_async(hd_pool *pool, uint32_t root, const hd_camera *cameras, uint32_t n_cameras,
+                                 uint32_t width, uint32_t height, hd_hit *d_out, void *stream) {
+	if (!pool || !cameras || !d_out || !n_cameras || !width || !height)
+		return HD_ERR_INVALID_ARG;
+	std::lock_guard<std::mutex> lk(pool->mtx);
+	if (cudaSetDevice(pool->device) != cudaSuccess)
+		return HD_ERR_CUDA;
+	cudaStream_t st = (cudaStream_t)stream;
+	hd_camera *d_cams = nullptr;
+	if (cudaMallocAsync((void **)&d_cams, n_cameras * sizeof(hd_camera), st) != cudaSuccess)
+		return HD_ERR_CUDA;
+	hd_status s = HD_OK;
+	if (cudaStreamWaitEvent(st, pool->ws_free, 0) != cudaSuccess ||
+	    cudaMemcpyAsync(d_cams, cameras, n_cameras * sizeof(hd_camera), cudaMemcpyHostToDevice, st) != cudaSuccess)
+		s = HD_ERR_CUDA;
+	if (!s) {
+		const uint64_t total = (uint64_t)width * height * n_cameras;
+		const uint32_t grid = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((total + 255) / 256, pool->num_sms * 16ull));
+		k_trace_pinhole<<<grid, 256, 0, st>>>(pool->P, root, d_cams, n_cameras, width, height, d_out);
+		if (cudaGetLastError() != cudaSuccess)
+			s = HD_ERR_CUDA;
+	}
+	cudaFreeAsync(d_cams, st);
+	return s;
+}
+
+} // extern "C"
