@@ -1,0 +1,414 @@
+#!/usr/bin/env python3
+"""Benchmark of the HashDAG edit path on one GB300 (or N replicas).
+
+A step applies one batch of 65,536 mixed edits (70 % spheres with radius
+log-uniform in [1,512], 30 % boxes with sides log-uniform in [1,1024], 50/50
+fill/dig, seed order) to a 32768^3 DAG seeded with the sphere scene scaled x32
+(one r=9600 sphere fill, 64 sphere digs with r in [512,2048]).  Every step
+first rolls the pool back to the seeded state (stream-ordered device copies,
+inside the timed region) and then runs one batched level-synchronous pass, so
+every step inserts its nodes afresh.  Metric: voxel-edits/s, where a batch's
+voxel-edits = sum over its edits of the grid voxels inside the shape.
+
+  value      device-resident edits, CUDA events on the pass's stream
+  e2e        the public C-ABI call hd_edit() with host edits (H2D copy of the
+             edit array and D2H of root/status inside the timed region)
+  per_edit   the plain form on the same edit list: one pass per edit
+  roofline   the dedup pass (k_probe + k_commit over all levels) against the
+             measured HBM copy bandwidth
+  cpu_baseline  the CPU restatement of the reference's threaded edit
+             (oracle, OpenMP on all host cores) on a bounded sample
+
+--impl reference times that CPU editor alone (all host cores) on the same
+workload and prints the same JSON line with "impl": "reference".
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+RES = 32768
+BUCKET_BITS = [10, 10, 10, 10, 10, 12, 14, 15, 16, 17, 17, 18, 18, 15]
+N_EDITS = 65536
+METRIC = "voxel-edits/s batched vs per-edit on 1 GB300 (bit-exact DAG); p99 edit latency"
+
+
+def peaks():
+    try:
+        with open(os.path.join(HERE, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.lines = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(2)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def build_if_needed():
+    import vkhashdag_gb300
+    if not os.path.exists(vkhashdag_gb300.library_path):
+        from vkhashdag_gb300 import _build
+        _build.build()
+
+
+def bench_config():
+    from vkhashdag_gb300 import Config
+    return Config(9, 2, list(BUCKET_BITS))
+
+
+def workload(rank, n_batches, n_edits, res):
+    from vkhashdag_gb300 import workloads as W
+    base = W.sphere_scene(res, 64, seed=0)
+    batches = [W.mixed_batch(res, n_edits, seed=1000 + 100 * rank + k) for k in range(n_batches)]
+    return base, batches
+
+
+# ---------------------------------------------------------------------- CPU (oracle) timing
+def cpu_sample_rate(orc_pool, root, edits, res, budget_s, threads, max_task_level):
+    """Threaded CPU editor over a growing prefix of `edits` until budget_s is spent."""
+    import vkhashdag_gb300 as hd
+    done, t_used, ve = 0, 0.0, 0
+    r = root
+    chunk = 8
+    while done < len(edits) and t_used < budget_s:
+        e = edits[done:done + chunk]
+        t0 = time.perf_counter()
+        r = orc_pool.threaded_edit(r, e, max_task_level, threads)
+        t_used += time.perf_counter() - t0
+        ve += hd.count_voxel_edits(e, res)
+        done += len(e)
+        chunk = min(chunk * 2, 256)
+    return ve / t_used, done, t_used
+
+
+def run_reference(args):
+    """--impl reference: the CPU restatement of the reference's threaded editor,
+    all host threads, same workload (bounded samples per step)."""
+    world, rank, _ = dist_setup()
+    if rank != 0:
+        return
+    import oracle
+    oracle.build()
+    import vkhashdag_gb300 as hd  # host helpers only (voxel counting, workload arrays)
+    cfg = bench_config()
+    L = cfg.get_node_levels()
+    threads = os.cpu_count() or 1
+    mtl = max(0, L - 4)
+    base, batches = workload(0, args.warmup + args.steps, args.n_edits, args.resolution)
+    pool = oracle.OraclePool.from_config(cfg)
+    t0 = time.perf_counter()
+    root0 = pool.threaded_edit(oracle.NULL, base, mtl, threads)
+    t_base = time.perf_counter() - t0
+    rates, samples = [], []
+    for k in range(args.warmup + args.steps):
+        rate, n_done, t_used = cpu_sample_rate(pool, root0, batches[k], args.resolution, args.ref_step_seconds,
+                                              threads, mtl)
+        if k >= args.warmup:
+            rates.append(rate)
+            samples.append((n_done, t_used))
+    value = float(np.mean(rates))
+    n_done = sum(s[0] for s in samples)
+    t_all = sum(s[1] for s in samples)
+    sample = (f"first {n_done // max(1, len(samples))} edits (on average) of each of {args.steps} batches of "
+              f"{args.n_edits}, applied one by one by the threaded CPU editor to the seeded {args.resolution}^3 scene "
+              f"(scene build {t_base:.1f} s untimed)")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "voxel-edits/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_all / max(1, len(samples)),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": f"batched-{args.n_edits}-mixed-edits-{args.resolution}^3", "node_levels": L,
+                   "bucket_bits": BUCKET_BITS, "max_task_level": mtl},
+        "cpu_baseline": {"value": value, "unit": "voxel-edits/s", "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "voxel-edits/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------- GPU arm
+def run_ours(args):
+    world, rank, local = dist_setup()
+    import torch
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    build_if_needed()
+    import vkhashdag_gb300 as hd
+
+    from vkhashdag_gb300 import workloads as W
+    res, n_edits = args.resolution, args.n_edits
+    cfg = bench_config() if res == RES else W.config_for_resolution(res, bottom_bits=16, top_levels=6)
+    L = cfg.get_node_levels()
+    heap_pages = min(cfg.get_total_pages(), args.heap_pages)
+    n_batches = args.warmup + args.steps
+    base, batches = workload(rank, n_batches, n_edits, res)
+    ve = [hd.count_voxel_edits(b, res) for b in batches]
+
+    stream = torch.cuda.Stream(device=local)
+    sp = stream.cuda_stream
+    pool = hd.NodePool(cfg, heap_pages=heap_pages, device=local)
+    root0 = pool.edit(hd.NULL, base)
+    pool.checkpoint()
+    d_batches = [torch.from_numpy(b.view(np.uint8).copy()).to(f"cuda:{local}") for b in batches]
+    d_out = torch.zeros(n_batches, dtype=torch.int32, device=f"cuda:{local}")
+    # size the edit workspace on every batch (sync path grows it), then restore
+    for b in batches:
+        pool.edit(root0, b)
+        pool.rollback(0)
+    torch.cuda.synchronize()
+
+    def step(k):
+        pool.rollback(sp)
+        pool.edit_async(root0, d_batches[k].data_ptr(), n_edits, d_out[k:k + 1].data_ptr(), sp)
+
+    with torch.cuda.stream(stream):
+        for k in range(args.warmup):
+            step(k)
+    torch.cuda.synchronize()
+    if pool.error():
+        raise RuntimeError(f"device error {pool.error()} during warm-up")
+
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = pool.kernel_launches()
+    pool.profile_begin(args.steps)
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        start.record(stream)
+        for k in range(args.warmup, n_batches):
+            step(k)
+        end.record(stream)
+        torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    elapsed_ms = start.elapsed_time(end)
+    launches = pool.kernel_launches() - launches0
+    phases, npass = pool.profile_end()
+    err = pool.error()
+    if err:
+        raise RuntimeError(f"device error {err} in the timed region")
+    counters = pool.last_counters_full()
+    # self-check: re-running the last batch on the same pool finds every node it
+    # inserted, so the synchronous path must return the very same root
+    last_root = int(d_out[n_batches - 1].item()) & 0xFFFFFFFF
+    same_roots = pool.edit(root0, batches[n_batches - 1]) == last_root
+    t = torch.tensor([elapsed_ms], dtype=torch.float64, device=f"cuda:{local}")
+    total_ve = torch.tensor([float(sum(ve[args.warmup:]))], dtype=torch.float64, device=f"cuda:{local}")
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        torch.distributed.all_reduce(total_ve, op=torch.distributed.ReduceOp.SUM)
+    elapsed_ms = float(t.item())
+    value = float(total_ve.item()) / (elapsed_ms / 1e3)
+
+    # ---------------- e2e through the public call with host buffers
+    e2e_times = []
+    for k in range(args.warmup, n_batches):
+        pool.rollback(0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        pool.edit(root0, batches[k])
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_value = sum(ve[args.warmup:]) / sum(e2e_times)
+
+    # ---------------- plain form: one pass per edit, same edit list
+    pool.rollback(0)
+    torch.cuda.synchronize()
+    plain = batches[args.warmup][: args.per_edit]
+    lat = []
+    r = root0
+    for k in range(len(plain)):
+        t0 = time.perf_counter()
+        r = pool.edit(r, plain[k:k + 1])
+        lat.append(time.perf_counter() - t0)
+    lat_ms = np.array(lat) * 1e3
+    plain_ve = hd.count_voxel_edits(plain, res)
+    plain_rate = plain_ve / (lat_ms.sum() / 1e3)
+    # device time of the same plain passes, back to back on the stream
+    pool.rollback(0)
+    d_plain = d_batches[args.warmup]
+    d_root = torch.zeros(1, dtype=torch.int32, device=f"cuda:{local}")
+    torch.cuda.synchronize()
+    s2, e2 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s2.record(stream)
+    d_root_ptr = d_root.data_ptr()
+    for k in range(len(plain)):
+        if k == 0:
+            pool.edit_async(root0, d_plain.data_ptr(), 1, d_root_ptr, sp)
+        else:
+            pool.edit_async_droot(d_root_ptr, d_plain.data_ptr() + 40 * k, 1, d_root_ptr, sp)
+    e2.record(stream)
+    torch.cuda.synchronize()
+    plain_dev_ms = s2.elapsed_time(e2)
+    # re-running the chain finds every node: same final root
+    rr = root0
+    for k in range(len(plain)):
+        rr = pool.edit(rr, plain[k:k + 1])
+    plain_same = (int(d_root.item()) & 0xFFFFFFFF) == rr
+    plain_dev_rate = plain_ve / (plain_dev_ms / 1e3)
+
+    # ---------------- roofline of the dedup pass
+    hbm, peak_kind = peaks()
+    per_step_dedup_ms = float(sum(phases[2:2 + 2 * L])) / max(1, npass)
+    cw, c, iw = counters["candidate_words"], counters["candidates"], counters["inserted_words"]
+    dedup_bytes = float(8 * cw.sum() + 8 * c.sum() + 4 * iw.sum())
+    achieved = dedup_bytes / (per_step_dedup_ms / 1e3) / 1e9
+    phase_ms = {"root+expand": float(phases[0]) / npass, "leaf_voxels": float(phases[1]) / npass}
+    for k in range(L):
+        lvl = L - 1 - k
+        phase_ms[f"probe_l{lvl}"] = float(phases[2 + 2 * k]) / npass
+        phase_ms[f"commit_l{lvl}"] = float(phases[3 + 2 * k]) / npass
+    phase_ms["finish"] = float(phases[-1]) / npass
+    traffic = None
+    tf = os.path.join(HERE, "profiles", "dedup_traffic.json")
+    if os.path.exists(tf):
+        try:
+            traffic = json.load(open(tf)).get("bytes_per_step")
+        except Exception:
+            traffic = None
+
+    # ---------------- CPU baseline (rank 0, bounded sample), oracle on host cores
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        import oracle
+        oracle.build()
+        pool.rollback(0)
+        torch.cuda.synchronize()
+        bw, ids, pages = pool.download()
+        opool = oracle.OraclePool.from_config(cfg)
+        opool.load(bw, ids, pages, pool.filled_node_pointers())
+        threads = os.cpu_count() or 1
+        rate, n_done, t_used = cpu_sample_rate(opool, root0, batches[args.warmup], res, args.cpu_seconds, threads,
+                                               max(0, L - 4))
+        cpu = {"value": rate, "unit": "voxel-edits/s", "cores": threads, "kind": "port",
+               "sample": f"first {n_done} edits of the first timed batch, one ThreadedEdit each, on the seeded "
+                         f"scene downloaded from the device ({t_used:.1f} s of CPU time)"}
+        del opool
+
+    if rank != 0:
+        return
+    clk = clocks.summary()
+    line = {
+        "metric": METRIC, "value": value, "unit": "voxel-edits/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": f"batched-{n_edits}-mixed-edits-{res}^3", "resolution": res, "edits_per_step": n_edits,
+                   "voxel_edits_per_step": float(np.mean(ve[args.warmup:])),
+                   "seeded_scene": "sphere r=9600 fill + 64 sphere digs r in [512,2048] (1024^3 scene x32)",
+                   "node_levels": L, "bucket_bits": list(cfg.bucket_bits_each_level), "word_bits_per_page": 9,
+                   "page_bits_per_bucket": 2, "rollback_to_seeded_scene_each_step": True,
+                   "l2": "working set of a step (pool + frontier, tens of GB) far above L2; no flush",
+                   "parallelism": f"replicas x{world}"},
+        "e2e": {"value": e2e_value, "unit": "voxel-edits/s", "h2d_bytes_per_step": int(n_edits * 40),
+                "d2h_bytes_per_step": int(224 * 8 + 4), "ms_per_step": 1e3 * float(np.mean(e2e_times))},
+        "per_edit": {"edits": len(plain), "voxel_edits_per_s_e2e": plain_rate, "voxel_edits_per_s_device": plain_dev_rate,
+                     "p50_ms": float(np.percentile(lat_ms, 50)), "p99_ms": float(np.percentile(lat_ms, 99)),
+                     "mean_ms": float(lat_ms.mean()), "device_ms_per_edit": plain_dev_ms / len(plain),
+                     "same_root_as_sync": bool(plain_same)},
+        "batched_vs_per_edit": {"e2e": e2e_value / plain_rate, "device": value / plain_dev_rate},
+        "roofline": {"bound": "hbm", "kernel": "dedup pass (k_probe+k_commit, all levels)", "achieved": achieved,
+                     "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm,
+                     "traffic": traffic, "algorithmic_bytes_per_step": dedup_bytes,
+                     "dedup_ms_per_step": per_step_dedup_ms},
+        "phases_ms_per_step": phase_ms,
+        "cpu_baseline": cpu,
+        "gpu_launches": int(launches),
+        "clocks": clk,
+        "checks": {"rerun_of_last_batch_finds_same_root": bool(same_roots)},
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--resolution", type=int, default=RES)
+    ap.add_argument("--n-edits", type=int, default=N_EDITS)
+    ap.add_argument("--heap-pages", type=int, default=1 << 22)
+    ap.add_argument("--per-edit", type=int, default=1024)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--ref-step-seconds", type=float, default=6.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -168,10 +168,28 @@ hd_status hd_edit_async_droot(hd_pool *pool, const uint32_t *d_root, const hd_ed
 /* Size the edit workspace for batches of up to max_edits touching up to
  * max_items nodes per batch and max_list_entries (node, edit) pairs. */
 hd_status hd_edit_reserve(hd_pool *pool, uint64_t max_items, uint64_t max_list_entries, uint32_t max_edits);
-/* Per-level counters of the last edit: items[level] = nodes visited (frontier
- * size), inserted[level] = nodes newly appended, candidates[level] = nodes
- * that went through the dedup pass.  Arrays of node_levels entries. */
-hd_status hd_edit_last_counters(hd_pool *pool, uint64_t *items, uint64_t *candidates, uint64_t *inserted);
+/* Per-level counters of the last edit pass (arrays of node_levels entries,
+ * any may be NULL): items = nodes visited (frontier size), candidates = nodes
+ * that went through the dedup pass and their words, inserted = nodes newly
+ * appended to buckets and their words. */
+hd_status hd_edit_last_counters(hd_pool *pool, uint64_t *items, uint64_t *candidates, uint64_t *candidate_words,
+                                uint64_t *inserted, uint64_t *inserted_words);
+/* Checkpoint / rollback of the whole pool state (bucket word counts, page
+ * table, heap and index counters, dedup index), kept in device memory.
+ * Rollback (stream-ordered) forgets every node inserted after the checkpoint;
+ * roots created after it become invalid.  Words past a bucket's word count in
+ * reused pages keep stale values (no scan ever reads them). */
+hd_status hd_pool_checkpoint(hd_pool *pool);
+hd_status hd_pool_rollback(hd_pool *pool, void *stream);
+/* Phase timing of edit passes with CUDA events recorded on the pass's own
+ * stream: after hd_edit_profile_begin, the next max_passes passes record
+ * events; hd_edit_profile_end waits for them and writes, summed over those
+ * passes, node_levels*2+3 phase durations in ms: [0] root+expand (all levels),
+ * [1] leaf voxels, then for level L-1 down to 0: probe, commit; [last] finish. */
+hd_status hd_edit_profile_begin(hd_pool *pool, uint32_t max_passes);
+hd_status hd_edit_profile_end(hd_pool *pool, float *out_ms, uint32_t *out_passes);
+/* Kernels this pool has launched since creation. */
+uint64_t hd_pool_kernel_launches(const hd_pool *pool);
 
 /* ---- upsert (find-or-insert) ---------------------------------------------
  * replaces upsert_inner_node / upsert_leaf (include/hashdag/NodePool.hpp:159-238).

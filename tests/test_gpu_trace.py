@@ -38,7 +38,7 @@ def test_trace_bit_identical_to_oracle(golden, orc, hd, name):
     m = a["hit"] == 1
     assert np.array_equal(a["t"].view(np.uint32)[m], b["t"].view(np.uint32)[m])
     assert np.array_equal(a["pos"].view(np.uint32)[m], b["pos"].view(np.uint32)[m])
-    assert m.mean() > 0.2
+    assert m.sum() > 200  # some rays hit (half of them start outside the cube)
 
 
 def test_pinhole_cameras_match_host_rays(orc, hd):

@@ -92,8 +92,13 @@ def lib():
         "hd_edit_async": (I, [P, U32, P, U32, P, P]),
         "hd_edit_async_droot": (I, [P, P, P, U32, P, P]),
         "hd_edit_reserve": (I, [P, U64, U64, U32]),
-        "hd_edit_last_counters": (I, [P, P, P, P]),
+        "hd_edit_last_counters": (I, [P, P, P, P, P, P]),
+        "hd_pool_checkpoint": (I, [P]),
+        "hd_pool_rollback": (I, [P, P]),
         "hd_upsert": (I, [P, U32, P, P, U32, P]),
+        "hd_edit_profile_begin": (I, [P, U32]),
+        "hd_edit_profile_end": (I, [P, P, P]),
+        "hd_pool_kernel_launches": (U64, [P]),
         "hd_pool_read_bucket_words": (I, [P, U32, U32, P]),
         "hd_pool_read_page_map": (I, [P, P]),
         "hd_pool_read_pages": (I, [P, P, U32, P]),
@@ -299,6 +304,24 @@ class NodePool:
         return {k: getattr(s, k) for k, _ in _Stats._fields_}
 
     # -- edit path ---------------------------------------------------------
+    def edit_async(self, root: int, d_edits: int, n: int, d_out_root: int, stream: int = 0):
+        """Device edits (pointer to n hd_edit_desc) -> device root; no host sync."""
+        _check(lib().hd_edit_async(self._h, root & 0xFFFFFFFF, ctypes.c_void_p(d_edits), n,
+                                   ctypes.c_void_p(d_out_root), ctypes.c_void_p(stream)), "hd_edit_async")
+
+    def edit_async_droot(self, d_root: int, d_edits: int, n: int, d_out_root: int, stream: int = 0):
+        """Like edit_async, with the input root read from device memory."""
+        _check(lib().hd_edit_async_droot(self._h, ctypes.c_void_p(d_root), ctypes.c_void_p(d_edits), n,
+                                         ctypes.c_void_p(d_out_root), ctypes.c_void_p(stream)), "hd_edit_async_droot")
+
+    def error(self) -> int:
+        e = ctypes.c_uint32(0)
+        _check(lib().hd_pool_get_error(self._h, ctypes.byref(e)), "hd_pool_get_error")
+        return e.value
+
+    def clear_error(self):
+        _check(lib().hd_pool_clear_error(self._h), "hd_pool_clear_error")
+
     def edit(self, root: int, editors, stream: int = 0) -> int:
         """Apply one editor or an ordered list of editors / an EDIT_DTYPE array to root."""
         if isinstance(editors, np.ndarray):
@@ -313,10 +336,38 @@ class NodePool:
         return out.value
 
     def last_counters(self):
+        """Per-level (items, candidates, inserted) of the last pass."""
+        c = self.last_counters_full()
+        return c["items"], c["candidates"], c["inserted"]
+
+    def last_counters_full(self) -> dict:
         n = self.config.get_node_levels()
-        it, ca, ins = (np.zeros(n, np.uint64) for _ in range(3))
-        _check(lib().hd_edit_last_counters(self._h, _ptr(it), _ptr(ca), _ptr(ins)), "hd_edit_last_counters")
-        return it, ca, ins
+        names = ["items", "candidates", "candidate_words", "inserted", "inserted_words"]
+        arrs = {k: np.zeros(n, np.uint64) for k in names}
+        _check(lib().hd_edit_last_counters(self._h, *[_ptr(arrs[k]) for k in names]), "hd_edit_last_counters")
+        return arrs
+
+    def checkpoint(self):
+        _check(lib().hd_pool_checkpoint(self._h), "hd_pool_checkpoint")
+
+    def rollback(self, stream: int = 0):
+        _check(lib().hd_pool_rollback(self._h, ctypes.c_void_p(stream)), "hd_pool_rollback")
+
+    def profile_begin(self, max_passes: int):
+        _check(lib().hd_edit_profile_begin(self._h, max_passes), "hd_edit_profile_begin")
+
+    def profile_end(self):
+        """(phase times in ms summed over the profiled passes, number of passes).
+        Phases: [0] root+expand, [1] leaf voxels, then probe/commit for level
+        L-1 down to 0, [last] finish."""
+        n = 2 * self.config.get_node_levels() + 3
+        out = np.zeros(n, np.float32)
+        passes = ctypes.c_uint32(0)
+        _check(lib().hd_edit_profile_end(self._h, _ptr(out), ctypes.byref(passes)), "hd_edit_profile_end")
+        return out, passes.value
+
+    def kernel_launches(self) -> int:
+        return int(lib().hd_pool_kernel_launches(self._h))
 
     def reserve(self, max_items: int, max_list_entries: int, max_edits: int):
         _check(lib().hd_edit_reserve(self._h, max_items, max_list_entries, max_edits), "hd_edit_reserve")

@@ -202,22 +202,44 @@ hd_status launch_pass(hd_pool *pool, const hd_edit_desc *d_edits, uint32_t n, ui
 	uint32_t grid[HD_MAX_LEVELS];
 	hd_grid_for_levels(pool, host_edits, n, grid);
 	const uint32_t long_grid = (uint32_t)pool->num_sms * 4u;
+	cudaEvent_t *ev = nullptr;
+	if (pool->prof_passes < pool->prof_max_passes)
+		ev = pool->prof_events.data() + (uint64_t)pool->prof_passes++ * hd_prof_events_per_pass(L);
+	uint32_t e = 0;
+	auto mark = [&]() {
+		if (ev)
+			cudaEventRecord(ev[e++], st);
+	};
 	HD_TRY(cudaStreamWaitEvent(st, pool->ws_free, 0));
+	mark();
 	HD_TRY(cudaMemsetAsync(W.ctr, 0, kWsCtrCount * sizeof(unsigned long long), st));
 	k_root<<<1, 32, 0, st>>>(P, W, root_val, root_ptr);
+	uint64_t launches = 1;
 	for (uint32_t l = 0; l + 1 < L; ++l) {
 		k_expand_short<<<grid[l], kBlock, 0, st>>>(P, W, l);
-		if (n > W.long_threshold)
+		++launches;
+		if (n > W.long_threshold) {
 			k_expand_long<<<long_grid, kBlock, 0, st>>>(P, W, l);
+			++launches;
+		}
 	}
+	mark();
 	k_leaf<<<grid[L - 1], kBlock, 0, st>>>(P, W);
+	mark();
 	k_probe<true><<<grid[L - 1], kBlock, 0, st>>>(P, W, L - 1);
+	mark();
 	k_commit<true><<<grid[L - 1], kBlock, 0, st>>>(P, W, L - 1);
+	mark();
 	for (uint32_t l = L - 1; l-- > 0;) {
 		k_probe<false><<<grid[l], kBlock, 0, st>>>(P, W, l);
+		mark();
 		k_commit<false><<<grid[l], kBlock, 0, st>>>(P, W, l);
+		mark();
 	}
 	k_finish<<<1, 32, 0, st>>>(P, W, d_out);
+	mark();
+	launches += 2 + 2ull * L;
+	pool->kernel_launches += launches;
 	HD_TRY(cudaGetLastError());
 	HD_TRY(cudaEventRecord(pool->ws_free, st));
 	return HD_OK;
@@ -482,6 +504,7 @@ hd_status upsert_impl(hd_pool *pool, uint32_t level, const uint32_t *words, cons
 		k_commit<false><<<grid, kBlock, 0, st>>>(pool->P, W, level);
 	}
 	k_finish<<<1, 32, 0, st>>>(pool->P, W, nullptr);
+	pool->kernel_launches += 3;
 	HD_TRY(cudaGetLastError());
 	HD_TRY(cudaEventRecord(pool->ws_free, st));
 	HD_TRY(cudaMemcpyAsync(out, it.res, n * 4ull, cudaMemcpyDeviceToHost, st));
@@ -525,6 +548,12 @@ void pool_free(hd_pool *p) {
 		cudaFreeHost(p->ws.ctr_host);
 	if (p->ws_free)
 		cudaEventDestroy(p->ws_free);
+	for (cudaEvent_t e : p->prof_events)
+		cudaEventDestroy(e);
+	cudaFree(p->ck_bucket_words);
+	cudaFree(p->ck_page_table);
+	cudaFree(p->ck_counters);
+	cudaFree(p->ck_index);
 	delete p;
 }
 
@@ -757,6 +786,7 @@ hd_status hd_edit_async(hd_pool *pool, uint32_t root, const hd_edit_desc *d_edit
 	if (s)
 		return s;
 	k_error_from_ws<<<1, 32, 0, st>>>(pool->P, pool->ws.d);
+	pool->kernel_launches++;
 	return hd_check(cudaGetLastError());
 }
 
@@ -771,10 +801,106 @@ hd_status hd_edit_async_droot(hd_pool *pool, const uint32_t *d_root, const hd_ed
 	if (s)
 		return s;
 	k_error_from_ws<<<1, 32, 0, st>>>(pool->P, pool->ws.d);
+	pool->kernel_launches++;
 	return hd_check(cudaGetLastError());
 }
 
-hd_status hd_edit_last_counters(hd_pool *pool, uint64_t *items, uint64_t *candidates, uint64_t *inserted) {
+hd_status hd_edit_profile_begin(hd_pool *pool, uint32_t max_passes) {
+	if (!pool)
+		return HD_ERR_INVALID_ARG;
+	std::lock_guard<std::mutex> lk(pool->mtx);
+	HD_TRY(cudaSetDevice(pool->device));
+	const uint64_t need = (uint64_t)max_passes * hd_prof_events_per_pass(pool->cfg.node_levels);
+	while (pool->prof_events.size() < need) {
+		cudaEvent_t e;
+		HD_TRY(cudaEventCreate(&e));
+		pool->prof_events.push_back(e);
+	}
+	pool->prof_passes = 0;
+	pool->prof_max_passes = max_passes;
+	return HD_OK;
+}
+
+hd_status hd_edit_profile_end(hd_pool *pool, float *out_ms, uint32_t *out_passes) {
+	if (!pool || !out_ms)
+		return HD_ERR_INVALID_ARG;
+	std::lock_guard<std::mutex> lk(pool->mtx);
+	HD_TRY(cudaSetDevice(pool->device));
+	const uint32_t L = pool->cfg.node_levels, per = hd_prof_events_per_pass(L);
+	for (uint32_t k = 0; k + 1 < per; ++k)
+		out_ms[k] = 0.0f;
+	for (uint32_t p = 0; p < pool->prof_passes; ++p) {
+		cudaEvent_t *ev = pool->prof_events.data() + (uint64_t)p * per;
+		HD_TRY(cudaEventSynchronize(ev[per - 1]));
+		for (uint32_t k = 0; k + 1 < per; ++k) {
+			float ms = 0.0f;
+			HD_TRY(cudaEventElapsedTime(&ms, ev[k], ev[k + 1]));
+			out_ms[k] += ms;
+		}
+	}
+	if (out_passes)
+		*out_passes = pool->prof_passes;
+	pool->prof_max_passes = 0;
+	pool->prof_passes = 0;
+	return HD_OK;
+}
+
+uint64_t hd_pool_kernel_launches(const hd_pool *pool) { return pool ? pool->kernel_launches : 0; }
+
+hd_status hd_pool_checkpoint(hd_pool *pool) {
+	if (!pool)
+		return HD_ERR_INVALID_ARG;
+	std::lock_guard<std::mutex> lk(pool->mtx);
+	HD_TRY(cudaSetDevice(pool->device));
+	HD_TRY(cudaDeviceSynchronize());
+	const uint64_t slots = pool->P.index_mask + 1;
+	if (!pool->ck_bucket_words) {
+		if (cudaMalloc(&pool->ck_bucket_words, pool->total_buckets * 4) != cudaSuccess ||
+		    cudaMalloc(&pool->ck_page_table, pool->total_pages * 4) != cudaSuccess ||
+		    cudaMalloc(&pool->ck_counters, kCtrCount * 4) != cudaSuccess ||
+		    cudaMalloc(&pool->ck_index, slots * 8) != cudaSuccess) {
+			cudaGetLastError();
+			cudaFree(pool->ck_bucket_words);
+			cudaFree(pool->ck_page_table);
+			cudaFree(pool->ck_counters);
+			cudaFree(pool->ck_index);
+			pool->ck_bucket_words = pool->ck_page_table = pool->ck_counters = nullptr;
+			pool->ck_index = nullptr;
+			return HD_ERR_POOL_OOM;
+		}
+	}
+	HD_TRY(cudaMemcpy(pool->ck_bucket_words, pool->P.bucket_words, pool->total_buckets * 4, cudaMemcpyDeviceToDevice));
+	HD_TRY(cudaMemcpy(pool->ck_page_table, pool->P.page_table, pool->total_pages * 4, cudaMemcpyDeviceToDevice));
+	HD_TRY(cudaMemcpy(pool->ck_counters, pool->P.counters, kCtrCount * 4, cudaMemcpyDeviceToDevice));
+	HD_TRY(cudaMemcpy(pool->ck_index, pool->P.index, slots * 8, cudaMemcpyDeviceToDevice));
+	for (uint32_t l = 0; l < pool->cfg.node_levels; ++l)
+		pool->ck_filled[l] = pool->P.cfg.filled[l];
+	pool->has_checkpoint = true;
+	return HD_OK;
+}
+
+hd_status hd_pool_rollback(hd_pool *pool, void *stream) {
+	if (!pool)
+		return HD_ERR_INVALID_ARG;
+	std::lock_guard<std::mutex> lk(pool->mtx);
+	if (!pool->has_checkpoint)
+		return HD_ERR_INVALID_ARG;
+	HD_TRY(cudaSetDevice(pool->device));
+	cudaStream_t st = (cudaStream_t)stream;
+	HD_TRY(cudaStreamWaitEvent(st, pool->ws_free, 0));
+	HD_TRY(cudaMemcpyAsync(pool->P.bucket_words, pool->ck_bucket_words, pool->total_buckets * 4,
+	                       cudaMemcpyDeviceToDevice, st));
+	HD_TRY(cudaMemcpyAsync(pool->P.page_table, pool->ck_page_table, pool->total_pages * 4, cudaMemcpyDeviceToDevice, st));
+	HD_TRY(cudaMemcpyAsync(pool->P.counters, pool->ck_counters, kCtrCount * 4, cudaMemcpyDeviceToDevice, st));
+	HD_TRY(cudaMemcpyAsync(pool->P.index, pool->ck_index, (pool->P.index_mask + 1) * 8, cudaMemcpyDeviceToDevice, st));
+	for (uint32_t l = 0; l < pool->cfg.node_levels; ++l)
+		pool->P.cfg.filled[l] = pool->ck_filled[l];
+	HD_TRY(cudaEventRecord(pool->ws_free, st));
+	return HD_OK;
+}
+
+hd_status hd_edit_last_counters(hd_pool *pool, uint64_t *items, uint64_t *candidates, uint64_t *candidate_words,
+                                uint64_t *inserted, uint64_t *inserted_words) {
 	if (!pool)
 		return HD_ERR_INVALID_ARG;
 	std::lock_guard<std::mutex> lk(pool->mtx);
@@ -787,8 +913,12 @@ hd_status hd_edit_last_counters(hd_pool *pool, uint64_t *items, uint64_t *candid
 			items[l] = c[kWsItems + l];
 		if (candidates)
 			candidates[l] = c[kWsCand + l];
+		if (candidate_words)
+			candidate_words[l] = c[kWsCandWords + l];
 		if (inserted)
 			inserted[l] = c[kWsIns + l];
+		if (inserted_words)
+			inserted_words[l] = c[kWsInsWords + l];
 	}
 	return HD_OK;
 }

@@ -26,7 +26,20 @@ struct hd_pool {
 	hd_ws_host ws;
 	std::mutex mtx;
 	uint64_t last_items[HD_MAX_LEVELS] = {}, last_cand[HD_MAX_LEVELS] = {}, last_ins[HD_MAX_LEVELS] = {};
+	uint64_t kernel_launches = 0; // kernels launched by this pool since creation
+	// phase timing: one set of events per profiled pass
+	std::vector<cudaEvent_t> prof_events;
+	uint32_t prof_passes = 0, prof_max_passes = 0;
+	// checkpoint: device copies of the pool's mutable state
+	uint32_t *ck_bucket_words = nullptr, *ck_page_table = nullptr, *ck_counters = nullptr;
+	unsigned long long *ck_index = nullptr;
+	uint32_t ck_filled[HD_MAX_LEVELS] = {};
+	bool has_checkpoint = false;
 };
+
+// events per profiled pass: start, after expand, after leaf, after probe/commit of
+// every level (2 per level), after finish
+inline uint32_t hd_prof_events_per_pass(uint32_t L) { return 3u + 2u * L + 1u; }
 
 // hd_engine.cu
 hd_status hd_check(cudaError_t e);
