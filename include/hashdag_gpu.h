@@ -46,6 +46,7 @@ typedef enum hd_status {
 	HD_ERR_CUDA = 6,         /* a CUDA runtime call failed */
 	HD_ERR_TIMEOUT = 7,      /* a bounded device-side wait ran out */
 	HD_ERR_NO_DEVICE = 8,    /* no CUDA device / extension not usable */
+	HD_ERR_INTERNAL = 9,     /* a device-side consistency check failed (work skipped, nothing corrupted) */
 } hd_status;
 
 #define HD_NULL_PTR 0xFFFFFFFFu

@@ -46,7 +46,8 @@ SHAPE_SPHERE, SHAPE_AABB = 0, 1
 OP_FILL, OP_DIG = 0, 1
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "bucket full", 3: "device page heap exhausted", 4: "dedup index full",
-          5: "edit workspace capacity exceeded", 6: "CUDA error", 7: "device wait timed out", 8: "no CUDA device"}
+          5: "edit workspace capacity exceeded", 6: "CUDA error", 7: "device wait timed out", 8: "no CUDA device",
+          9: "device consistency check failed"}
 
 
 class HashDagError(RuntimeError):

@@ -27,6 +27,7 @@ enum DevError : u32 {
 	kErrCapacity = HD_ERR_CAPACITY,
 	kErrTimeout = HD_ERR_TIMEOUT,
 	kErrInvalidRoot = HD_ERR_INVALID_ARG,
+	kErrInternal = HD_ERR_INTERNAL,
 };
 
 // Config<uint32_t> with the derived per-level tables (include/hashdag/Config.hpp:15-57)
@@ -178,6 +179,33 @@ __device__ __forceinline__ u64 shape_mask(const hd_edit_desc &e, u32 ox, u32 oy,
 		}
 		return m;
 	}
+	// A leaf that the sphere only partially covers lies within r+4 of the centre
+	// on every axis, so for r2 <= 2^30 every square and every sum of three fits
+	// in 32 bits (3 * 32772^2 < 2^32); the wider form handles the rest.
+	if (e.r2 <= (1ull << 30)) {
+		u32 dx2[4], dy2[4], dz2[4];
+		const int cx = (int)e.p0[0], cy = (int)e.p0[1], cz = (int)e.p0[2];
+#pragma unroll
+		for (u32 k = 0; k < 4; ++k) {
+			const int dx = (int)(ox + k) - cx, dy = (int)(oy + k) - cy, dz = (int)(oz + k) - cz;
+			dx2[k] = (u32)(dx * dx);
+			dy2[k] = (u32)(dy * dy);
+			dz2[k] = (u32)(dz * dz);
+		}
+		const u32 r2 = (u32)e.r2;
+		u32 lo = 0, hi = 0;
+#pragma unroll
+		for (u32 i = 0; i < 64; ++i) {
+			const u32 x = ((i >> 2) & 2u) | (i & 1u), y = ((i >> 3) & 2u) | ((i >> 1) & 1u),
+			          z = ((i >> 4) & 2u) | ((i >> 2) & 1u);
+			const u32 in = (dx2[x] + dy2[y] + dz2[z] <= r2) ? 1u : 0u;
+			if (i < 32)
+				lo |= in << i;
+			else
+				hi |= in << (i - 32);
+		}
+		return (u64)lo | ((u64)hi << 32);
+	}
 	u64 dx2[4], dy2[4], dz2[4];
 #pragma unroll
 	for (u32 k = 0; k < 4; ++k) {
@@ -197,15 +225,26 @@ __device__ __forceinline__ u64 shape_mask(const hd_edit_desc &e, u32 ox, u32 oy,
 	return m;
 }
 
+// One voxel inside the edit's shape (VoxelInRange, src/main.cpp:55-57,121-126).
+__device__ __forceinline__ bool voxel_in(const hd_edit_desc &e, u32 x, u32 y, u32 z) {
+	if (e.shape == HD_SHAPE_AABB)
+		return x >= e.p0[0] && y >= e.p0[1] && z >= e.p0[2] && x < e.p1[0] && y < e.p1[1] && z < e.p1[2];
+	const long long dx = (long long)x - (long long)e.p0[0], dy = (long long)y - (long long)e.p0[1],
+	                dz = (long long)z - (long long)e.p0[2];
+	return (u64)dx * (u64)dx + (u64)dy * (u64)dy + (u64)dz * (u64)dz <= e.r2;
+}
+
 __device__ __forceinline__ u64 pack_pos(u32 x, u32 y, u32 z) { return (u64)x | ((u64)y << 21) | ((u64)z << 42); }
 __device__ __forceinline__ u32 pos_x(u64 p) { return (u32)(p & 0x1FFFFFu); }
 __device__ __forceinline__ u32 pos_y(u64 p) { return (u32)((p >> 21) & 0x1FFFFFu); }
 __device__ __forceinline__ u32 pos_z(u64 p) { return (u32)((p >> 42) & 0x1FFFFFu); }
 
 // ------------------------------------------------------------------ edit workspace
-// Frontier items of one batched edit pass.  Inner items (levels 0..L-2) and
-// leaf items (level L-1) live in two index spaces; every level's items are a
-// contiguous range of its space.
+// Frontier items of one batched edit pass.  Inner items (levels 0..L-2) live
+// in one index space, every level a contiguous range in level order.  The
+// leaf level has no items: the kernel of level L-2 computes the 8 child leaves
+// of each node itself and emits only the changed leaves as candidates
+// (Workspace::leaf, with their bits in leaf_new).
 enum ItemState : u32 {
 	kStUnchanged = 0, // result = base pointer
 	kStEmpty = 1,     // result = Null
@@ -213,39 +252,39 @@ enum ItemState : u32 {
 	kStRep = 3,       // result = node inserted by this item (res[]); link = index slot
 	kStAlias = 4,     // result = res[link] (another item of the pass with equal content)
 	kStFail = 5,      // insertion failed (error recorded)
-	kStCand = 6,      // leaf computed, dedup pending
+	kStCand = 6,      // leaf candidate, dedup pending
 };
 
 struct Items {
-	u64 *pos;     // packed node coordinate
-	u32 *base;    // node the edit list applies to (original node, filled node or Null)
+	u64 *pos;     // packed node coordinate (inner items)
+	u32 *base;    // node the edit list applies to (original node, filled node or Null) (inner items)
 	u32 *parent;  // child slot of the parent (inner index*8 + child) or kNull for the root
-	u32 *lst_off; // edit list [lst_off, lst_off+lst_len) in Workspace::lists
+	u32 *lst_off; // edit list [lst_off, lst_off+lst_len) in Workspace::lists (inner items)
 	u32 *lst_len;
 	u32 *res;     // result pointer
 	u32 *state;   // ItemState
 	u32 *link;    // index slot (kStRep) or representative item (kStAlias)
-	u32 *pad;     // bucket word offset where zero padding starts (kStRep), or kNull
+	u32 *pad;     // bucket word offset where zero padding starts (kStRep), or kNull (inner items)
 	u64 cap;
 };
 
 struct Workspace {
-	Items inner, leaf;
-	u32 *bchild; // [inner.cap*8] children of the base node
-	u32 *cnew;   // [inner.cap*8] new children
-	u64 *leaf_new; // [leaf.cap] new leaf bits
-	u32 *lists;    // edit lists
+	Items inner, leaf; // leaf: candidates (parent, res, state, link)
+	u32 *bchild;       // [inner.cap*8] children of the base node
+	u32 *cnew;         // [inner.cap*8] new children
+	u64 *leaf_new;     // [leaf.cap] bits of the leaf candidates
+	u32 *lists;        // edit lists
 	u64 list_cap;
-	u32 *long_q;   // per inner level: items with long edit lists (same index space as inner)
+	u32 *long_q;       // per inner level: items with long edit lists (same index space as inner)
 	const hd_edit_desc *edits;
 	u32 n_edits;
-	u32 long_threshold; // lists longer than this are expanded by a warp
+	u32 long_threshold; // lists longer than this are expanded by a block (inner) or a warp (level L-2)
 	// device counters (u64 so that overflow counts stay exact):
-	//   [0..L)       items per level
-	//   [32..32+L)   long items per level
+	//   [0..L-1)     items per inner level, [L-1] leaf candidates
+	//   [32..)       long items per level
 	//   [64]         list entries used
 	//   [65]         workspace error
-	//   [66]         root result
+	//   [66]         root result, [67] input root
 	//   [96..96+L)   candidates per level, [128..) words of candidates,
 	//   [160..) inserted per level, [192..) words inserted
 	unsigned long long *ctr;
@@ -258,6 +297,9 @@ enum WsCtr : u32 {
 	kWsError = 65,
 	kWsRoot = 66,
 	kWsRootIn = 67,
+	kWsMaxProbe = 68,   // longest index probe of the pass
+	kWsProbeSteps = 69, // index slots visited in the pass
+	kWsCasRetry = 70,   // failed bucket-count CAS attempts
 	kWsCand = 96,
 	kWsCandWords = 128,
 	kWsIns = 160,

@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <unordered_map>
 
@@ -89,6 +90,17 @@ hd_status alloc_items(hd_ws_host &ws, Items &it, uint64_t cap) {
 	return HD_OK;
 }
 
+// Leaf candidates carry only parent slot, result, state and link (bits in leaf_new).
+hd_status alloc_leaf_candidates(hd_ws_host &ws, Items &it, uint64_t cap) {
+	it = Items{};
+	it.cap = cap;
+	hd_status s;
+	if ((s = ws_alloc(ws, &it.parent, cap)) || (s = ws_alloc(ws, &it.res, cap)) || (s = ws_alloc(ws, &it.state, cap)) ||
+	    (s = ws_alloc(ws, &it.link, cap)))
+		return s;
+	return HD_OK;
+}
+
 // (Re)allocates the workspace with at least the given capacities; keeps the
 // counters.  Frees the old one first.
 hd_status ws_reserve(hd_pool *pool, uint64_t inner_cap, uint64_t leaf_cap, uint64_t list_cap, uint32_t edit_cap) {
@@ -106,7 +118,7 @@ hd_status ws_reserve(hd_pool *pool, uint64_t inner_cap, uint64_t leaf_cap, uint6
 	ws_free_all(ws);
 	Workspace d{};
 	hd_status s;
-	if ((s = alloc_items(ws, d.inner, inner_cap)) || (s = alloc_items(ws, d.leaf, leaf_cap)) ||
+	if ((s = alloc_items(ws, d.inner, inner_cap)) || (s = alloc_leaf_candidates(ws, d.leaf, leaf_cap)) ||
 	    (s = ws_alloc(ws, &d.bchild, inner_cap * 8)) || (s = ws_alloc(ws, &d.cnew, inner_cap * 8)) ||
 	    (s = ws_alloc(ws, &d.leaf_new, leaf_cap)) || (s = ws_alloc(ws, &d.lists, list_cap)) ||
 	    (s = ws_alloc(ws, &d.long_q, inner_cap)) || (s = ws_alloc(ws, &d.ctr, (uint64_t)kWsCtrCount)) ||
@@ -202,6 +214,7 @@ hd_status launch_pass(hd_pool *pool, const hd_edit_desc *d_edits, uint32_t n, ui
 	uint32_t grid[HD_MAX_LEVELS];
 	hd_grid_for_levels(pool, host_edits, n, grid);
 	const uint32_t long_grid = (uint32_t)pool->num_sms * 4u;
+	static const bool debug_sync = getenv("HD_DEBUG_SYNC") != nullptr;
 	cudaEvent_t *ev = nullptr;
 	if (pool->prof_passes < pool->prof_max_passes)
 		ev = pool->prof_events.data() + (uint64_t)pool->prof_passes++ * hd_prof_events_per_pass(L);
@@ -210,35 +223,66 @@ hd_status launch_pass(hd_pool *pool, const hd_edit_desc *d_edits, uint32_t n, ui
 		if (ev)
 			cudaEventRecord(ev[e++], st);
 	};
+	auto dbg = [&](const char *what, uint32_t l) {
+		if (!debug_sync)
+			return;
+		cudaError_t err = cudaStreamSynchronize(st);
+		unsigned long long c[kWsCtrCount];
+		cudaMemcpy(c, W.ctr, sizeof(c), cudaMemcpyDeviceToHost);
+		uint32_t perr = 0;
+		cudaMemcpy(&perr, pool->P.counters + kCtrError, 4, cudaMemcpyDeviceToHost);
+		fprintf(stderr,
+		        "hd_debug %s l=%u err=%s ws_err=%llu pool_err=%u items=%llu list=%llu long=%llu max_probe=%llu "
+		        "probe_steps=%llu cas_retry=%llu\n",
+		        what, l, cudaGetErrorString(err), c[kWsError], perr, l < HD_MAX_LEVELS ? c[kWsItems + l] : 0ull,
+		        c[kWsList], l < HD_MAX_LEVELS ? c[kWsLong + l] : 0ull, c[kWsMaxProbe], c[kWsProbeSteps], c[kWsCasRetry]);
+	};
 	HD_TRY(cudaStreamWaitEvent(st, pool->ws_free, 0));
 	mark();
 	HD_TRY(cudaMemsetAsync(W.ctr, 0, kWsCtrCount * sizeof(unsigned long long), st));
-	k_root<<<1, 32, 0, st>>>(P, W, root_val, root_ptr);
+	k_root<<<1, kLongBlock, 0, st>>>(P, W, root_val, root_ptr);
+	dbg("root", 0);
 	uint64_t launches = 1;
-	for (uint32_t l = 0; l + 1 < L; ++l) {
+	const bool longs = n > W.long_threshold; // no list can be longer than the batch
+	for (uint32_t l = 0; l + 2 < L; ++l) {
 		k_expand_short<<<grid[l], kBlock, 0, st>>>(P, W, l);
+		dbg("expand_short", l + 1);
 		++launches;
-		if (n > W.long_threshold) {
-			k_expand_long<<<long_grid, kBlock, 0, st>>>(P, W, l);
+		if (longs) {
+			k_expand_long<<<long_grid, kLongBlock, 0, st>>>(P, W, l);
+			dbg("expand_long", l + 1);
 			++launches;
 		}
 	}
 	mark();
-	k_leaf<<<grid[L - 1], kBlock, 0, st>>>(P, W);
+	if (L >= 2) {
+		k_leafparent_short<<<grid[L - 2], kBlock, 0, st>>>(P, W);
+		dbg("leafparent_short", L - 1);
+		++launches;
+		if (longs) {
+			k_leafparent_long<<<long_grid, kBlock, 0, st>>>(P, W);
+			dbg("leafparent_long", L - 1);
+			++launches;
+		}
+	}
 	mark();
 	k_probe<true><<<grid[L - 1], kBlock, 0, st>>>(P, W, L - 1);
+	dbg("probe_leaf", L - 1);
 	mark();
 	k_commit<true><<<grid[L - 1], kBlock, 0, st>>>(P, W, L - 1);
+	dbg("commit_leaf", L - 1);
 	mark();
 	for (uint32_t l = L - 1; l-- > 0;) {
 		k_probe<false><<<grid[l], kBlock, 0, st>>>(P, W, l);
+		dbg("probe", l);
 		mark();
 		k_commit<false><<<grid[l], kBlock, 0, st>>>(P, W, l);
+		dbg("commit", l);
 		mark();
 	}
 	k_finish<<<1, 32, 0, st>>>(P, W, d_out);
 	mark();
-	launches += 2 + 2ull * L;
+	launches += 1 + 2ull * L;
 	pool->kernel_launches += launches;
 	HD_TRY(cudaGetLastError());
 	HD_TRY(cudaEventRecord(pool->ws_free, st));
@@ -264,6 +308,10 @@ hd_status status_of(uint32_t err) {
 		return HD_ERR_CAPACITY;
 	case kErrTimeout:
 		return HD_ERR_TIMEOUT;
+	case kErrInternal:
+		return HD_ERR_INTERNAL;
+	case kErrInvalidRoot:
+		return HD_ERR_INVALID_ARG;
 	default:
 		return HD_ERR_CUDA;
 	}
@@ -291,9 +339,9 @@ hd_status run_pass_sync(hd_pool *pool, const hd_edit_desc *h_edits, uint32_t n, 
 			pool->last_cand[l] = c[kWsCand + l];
 			pool->last_ins[l] = c[kWsIns + l];
 		}
-		if (c[kWsError] == kErrInvalidRoot) {
+		if (c[kWsError] == kErrInvalidRoot || c[kWsError] == kErrInternal) {
 			*out_root = root;
-			return HD_ERR_INVALID_ARG;
+			return status_of((uint32_t)c[kWsError]);
 		}
 		if (c[kWsError] == kErrCapacity) {
 			uint64_t inner = 0;
@@ -627,6 +675,8 @@ const char *hd_status_string(hd_status s) {
 		return "device wait timed out";
 	case HD_ERR_NO_DEVICE:
 		return "no CUDA device";
+	case HD_ERR_INTERNAL:
+		return "device consistency check failed";
 	}
 	return "unknown";
 }

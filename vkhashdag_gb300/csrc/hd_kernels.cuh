@@ -5,16 +5,22 @@
 // (include/hashdag/NodePool.hpp:319-396) applied edit after edit, but with
 // every level of every edit processed by one set of launches:
 //
-//   k_root            classify the root against the whole edit list
-//   k_expand_short(l) thread per level-l node: classify its 8 children against
-//                     the node's edit list, keep the edits after the last full
-//                     cover (EditType kFill/kClear), emit children to recurse
-//   k_expand_long(l)  same, a warp per node, for nodes with long edit lists
-//   k_leaf            thread per leaf: apply the leaf's edit list to its 64 voxels
-//   k_probe(l)        build each level-l node, hash it (Hasher.hpp:21-48) and
-//                     find-or-claim it in the dedup index; claimed nodes
-//                     reserve words in their bucket (page padding rule of
-//                     NodePool.hpp:134-157) and open pages from the heap
+//   k_root            classify the root against the whole edit list (one block)
+//   k_expand_short(l) thread per level-l node (l <= L-3): classify its 8
+//                     children against the node's edit list, keep the edits
+//                     after the last full cover (EditType kFill/kClear), emit
+//                     the children that still need work as level-(l+1) items
+//   k_expand_long(l)  the same for nodes with long edit lists, a block per
+//                     (node, child) with an order-preserving block compaction
+//   k_leafparent      thread per level-(L-2) node (warp for long lists): apply
+//                     the node's edit list to the 64 voxels of each of its 8
+//                     child leaves (NodePool.hpp:319-343) and emit the changed
+//                     leaves as dedup candidates
+//   k_probe(l)        hash each candidate (Hasher.hpp:21-48), merge equal
+//                     candidates of a warp (__match_any_sync), find-or-claim
+//                     it in the dedup index; claimed nodes reserve words in
+//                     their bucket (page padding rule of NodePool.hpp:134-157)
+//                     and open pages from the heap
 //   k_commit(l)       write claimed nodes, publish them in the index, hand
 //                     every node's pointer to its parent's child slot
 //   k_finish          report the root
@@ -30,6 +36,7 @@ namespace hd {
 
 static constexpr u32 kFullMask = 0xFFFFFFFFu;
 static constexpr int kBlock = 256;
+static constexpr int kLongBlock = 256;
 
 __device__ __forceinline__ u32 lane_id() { return threadIdx.x & 31u; }
 
@@ -52,27 +59,8 @@ __device__ __forceinline__ u64 warp_reserve(unsigned long long *ctr, u32 count) 
 	return base + incl - count;
 }
 
-// Level ranges: inner levels 0..L-2 share the inner index space in level order,
-// the leaf level starts at 0 of the leaf space.
-__device__ __forceinline__ void level_range(const Workspace &W, u32 L, u32 l, u64 &begin, u64 &n) {
-	if (l == L - 1) {
-		begin = 0;
-		n = W.ctr[kWsItems + l];
-		if (n > W.leaf.cap)
-			n = W.leaf.cap;
-		return;
-	}
-	u64 b = 0;
-	for (u32 k = 0; k < l; ++k)
-		b += W.ctr[kWsItems + k];
-	begin = b;
-	n = W.ctr[kWsItems + l];
-	if (begin >= W.inner.cap)
-		n = 0;
-	else if (begin + n > W.inner.cap)
-		n = W.inner.cap - begin;
-}
-// First index of level l in its space (used when emitting level l items).
+// Level ranges: inner levels 0..L-2 share the inner index space in level order;
+// the leaf candidates start at 0 of the leaf space.
 __device__ __forceinline__ u64 level_begin(const Workspace &W, u32 L, u32 l) {
 	if (l == L - 1)
 		return 0;
@@ -81,9 +69,19 @@ __device__ __forceinline__ u64 level_begin(const Workspace &W, u32 L, u32 l) {
 		b += W.ctr[kWsItems + k];
 	return b;
 }
+__device__ __forceinline__ void level_range(const Workspace &W, u32 L, u32 l, u64 &begin, u64 &n) {
+	begin = level_begin(W, L, l);
+	n = W.ctr[kWsItems + l];
+	const u64 cap = l == L - 1 ? W.leaf.cap : W.inner.cap;
+	if (begin >= cap)
+		n = 0;
+	else if (begin + n > cap)
+		n = cap - begin;
+}
 
 __device__ __forceinline__ bool ws_failed(const Workspace &W) { return *(volatile unsigned long long *)&W.ctr[kWsError] != 0; }
 __device__ __forceinline__ bool pool_failed(const DevPool &P) { return *(volatile u32 *)&P.counters[kCtrError] != 0; }
+__device__ __forceinline__ void ws_error(Workspace &W, u32 code) { atomicCAS(&W.ctr[kWsError], 0ull, (unsigned long long)code); }
 
 // Children of a base node (NodePool.hpp:278-309 get_unpacked_node_array; the
 // filled node's children are the filled node of the level below).
@@ -113,6 +111,15 @@ __device__ __forceinline__ void base_children(const DevPool &P, u32 l, u32 b, u3
 	}
 }
 
+__device__ __forceinline__ u64 leaf_bits(const DevPool &P, u32 ptr) {
+	if (ptr == kNull)
+		return 0ull;
+	if (ptr == P.cfg.filled[P.cfg.L - 1])
+		return ~0ull;
+	const u32 *p = node_addr(P, ptr);
+	return (u64)p[0] | ((u64)p[1] << 32);
+}
+
 // Whether an edit that only partially covers a node can change it, given the
 // node's base: a dig cannot change an empty node and a fill cannot change a
 // full one.  Leading edits that cannot change the node are dropped.
@@ -124,30 +131,44 @@ __device__ __forceinline__ bool effective(u32 op, u32 base, u32 filled) {
 	return true;
 }
 
-template <bool Identity>
-__device__ __forceinline__ u32 list_at(const Workspace &W, u32 off, u32 p) {
+// Consistency check of an inner item's edit list before it is walked.
+__device__ __forceinline__ bool list_ok(Workspace &W, u32 off, u32 len) {
+	if (len > W.n_edits || (u64)off + len > W.list_cap) {
+		ws_error(W, kErrInternal);
+		return false;
+	}
+	return true;
+}
+
+template <bool Identity> __device__ __forceinline__ u32 list_at(const Workspace &W, u32 off, u32 p) {
 	return Identity ? p : W.lists[off + p];
 }
 
+__device__ __forceinline__ void child_pos(u64 pos, u32 c, u32 &cx, u32 &cy, u32 &cz) {
+	cx = (pos_x(pos) << 1) | (c & 1u);
+	cy = (pos_y(pos) << 1) | ((c >> 1) & 1u);
+	cz = (pos_z(pos) << 1) | ((c >> 2) & 1u);
+}
+
+// ------------------------------------------------------------------ thread planning (short lists)
 // Plan of one child against the parent's edit list, by one thread.
 // Returns the number of edits to keep (0 = terminal, result in *base_out).
-template <bool Identity>
 __device__ __forceinline__ u32 plan_child_thread(const Workspace &W, u32 off, u32 len, u32 shift, u32 cx, u32 cy,
                                                  u32 cz, u32 old, u32 filled, u32 *base_out, u32 *first_out) {
 	int lastfull = -1;
 	u32 lastop = 0;
 	for (u32 p = 0; p < len; ++p) {
-		const hd_edit_desc &e = W.edits[list_at<Identity>(W, off, p)];
+		const hd_edit_desc &e = W.edits[W.lists[off + p]];
 		if (classify(e, shift, cx, cy, cz) == kClsFull) {
 			lastfull = (int)p;
 			lastop = e.op;
 		}
 	}
-	u32 base = lastfull >= 0 ? (lastop == HD_OP_FILL ? filled : kNull) : old;
+	const u32 base = lastfull >= 0 ? (lastop == HD_OP_FILL ? filled : kNull) : old;
 	*base_out = base;
 	u32 first = kNull, cnt = 0;
 	for (u32 p = (u32)(lastfull + 1); p < len; ++p) {
-		const hd_edit_desc &e = W.edits[list_at<Identity>(W, off, p)];
+		const hd_edit_desc &e = W.edits[W.lists[off + p]];
 		if (classify(e, shift, cx, cy, cz) == kClsPartial) {
 			if (first == kNull && effective(e.op, base, filled))
 				first = p;
@@ -160,27 +181,19 @@ __device__ __forceinline__ u32 plan_child_thread(const Workspace &W, u32 off, u3
 }
 
 // Writes the kept edits of a planned child (positions >= first, partial) in order.
-template <bool Identity>
 __device__ __forceinline__ void write_child_list_thread(const Workspace &W, u32 off, u32 len, u32 first, u32 shift,
                                                         u32 cx, u32 cy, u32 cz, u32 *dst) {
 	u32 k = 0;
 	for (u32 p = first; p < len; ++p) {
-		u32 id = list_at<Identity>(W, off, p);
+		const u32 id = W.lists[off + p];
 		if (classify(W.edits[id], shift, cx, cy, cz) == kClsPartial)
 			dst[k++] = id;
 	}
 }
 
-struct ChildSpace {
-	Items *it;
-	u64 begin;
-	u64 cap;
-};
-
-__device__ __forceinline__ Items &items_of(Workspace &W, u32 L, u32 l) { return l == L - 1 ? W.leaf : W.inner; }
-
 // ------------------------------------------------------------------ k_expand_short
-// Thread per level-l inner node with an edit list of at most long_threshold edits.
+// Thread per level-l inner node (l <= L-3) with an edit list of at most
+// long_threshold edits.  Children are inner items of level l+1.
 __global__ void __launch_bounds__(kBlock) k_expand_short(DevPool P, Workspace W, u32 l) {
 	if (ws_failed(W)) // an earlier launch overflowed: some items were never written
 		return;
@@ -189,9 +202,9 @@ __global__ void __launch_bounds__(kBlock) k_expand_short(DevPool P, Workspace W,
 	u64 begin, n;
 	level_range(W, L, l, begin, n);
 	const u64 child_begin = level_begin(W, L, cl);
-	Items &child = items_of(W, L, cl);
-	const u32 shift = P.cfg.L + 1u - cl; // child bounds at voxel level
+	const u32 shift = L + 1u - cl; // child bounds at voxel level
 	const u32 filled_c = P.cfg.filled[cl];
+	const u32 T = W.long_threshold;
 	const u64 stride = (u64)gridDim.x * blockDim.x;
 	for (u64 w0 = (u64)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); w0 < n; w0 += stride) {
 		const u64 t = w0 + lane_id();
@@ -205,32 +218,30 @@ __global__ void __launch_bounds__(kBlock) k_expand_short(DevPool P, Workspace W,
 			b = W.inner.base[i];
 			pos = W.inner.pos[i];
 		}
-		const bool mine = valid && len <= W.long_threshold;
-		u32 cbase[8], cfirst[8], ccnt[8];
+		const bool mine = valid && len <= T && list_ok(W, off, len);
+		u32 cbase[8], cfirst[8], ccnt[8], old[8];
 		u32 n_emit = 0, n_list = 0, n_long = 0;
-		u32 old[8];
 		if (mine) {
 			base_children(P, l, b, old);
-			const u32 px = pos_x(pos), py = pos_y(pos), pz = pos_z(pos);
 #pragma unroll 1
 			for (u32 c = 0; c < 8; ++c) {
-				const u32 cx = (px << 1) | (c & 1u), cy = (py << 1) | ((c >> 1) & 1u), cz = (pz << 1) | ((c >> 2) & 1u);
-				ccnt[c] = plan_child_thread<false>(W, off, len, shift, cx, cy, cz, old[c], filled_c, &cbase[c], &cfirst[c]);
+				u32 cx, cy, cz;
+				child_pos(pos, c, cx, cy, cz);
+				ccnt[c] = plan_child_thread(W, off, len, shift, cx, cy, cz, old[c], filled_c, &cbase[c], &cfirst[c]);
 				if (ccnt[c]) {
 					++n_emit;
 					n_list += ccnt[c];
-					n_long += (cl < L - 1 && ccnt[c] > W.long_threshold) ? 1u : 0u;
+					n_long += ccnt[c] > T ? 1u : 0u;
 				}
 			}
 		}
 		const u64 item0 = warp_reserve(&W.ctr[kWsItems + cl], n_emit);
 		const u64 list0 = warp_reserve(&W.ctr[kWsList], n_list);
-		const u64 long0 = (cl < L - 1) ? warp_reserve(&W.ctr[kWsLong + cl], n_long) : 0;
+		const u64 long0 = warp_reserve(&W.ctr[kWsLong + cl], n_long);
 		if (!mine)
 			continue;
 		u32 res[8];
 		u64 it = child_begin + item0, lo = list0, lg = long0;
-		const u32 px = pos_x(pos), py = pos_y(pos), pz = pos_z(pos);
 #pragma unroll 1
 		for (u32 c = 0; c < 8; ++c) {
 			if (!ccnt[c]) {
@@ -238,23 +249,24 @@ __global__ void __launch_bounds__(kBlock) k_expand_short(DevPool P, Workspace W,
 				continue;
 			}
 			res[c] = kNull; // overwritten by the child's commit
-			const u32 cx = (px << 1) | (c & 1u), cy = (py << 1) | ((c >> 1) & 1u), cz = (pz << 1) | ((c >> 2) & 1u);
-			if (it < child.cap && lo + ccnt[c] <= W.list_cap) {
-				child.pos[it] = pack_pos(cx, cy, cz);
-				child.base[it] = cbase[c];
-				child.parent[it] = (u32)(i * 8u + c);
-				child.lst_off[it] = (u32)lo;
-				child.lst_len[it] = ccnt[c];
-				write_child_list_thread<false>(W, off, len, cfirst[c], shift, cx, cy, cz, W.lists + lo);
-				if (cl < L - 1 && ccnt[c] > W.long_threshold) {
+			u32 cx, cy, cz;
+			child_pos(pos, c, cx, cy, cz);
+			if (it < W.inner.cap && lo + ccnt[c] <= W.list_cap) {
+				W.inner.pos[it] = pack_pos(cx, cy, cz);
+				W.inner.base[it] = cbase[c];
+				W.inner.parent[it] = (u32)(i * 8u + c);
+				W.inner.lst_off[it] = (u32)lo;
+				W.inner.lst_len[it] = ccnt[c];
+				write_child_list_thread(W, off, len, cfirst[c], shift, cx, cy, cz, W.lists + lo);
+				if (ccnt[c] > T) {
 					if (child_begin + lg < W.inner.cap)
 						W.long_q[child_begin + lg] = (u32)it;
 					else
-						atomicCAS(&W.ctr[kWsError], 0ull, (unsigned long long)kErrCapacity);
+						ws_error(W, kErrCapacity);
 					++lg;
 				}
 			} else {
-				atomicCAS(&W.ctr[kWsError], 0ull, (unsigned long long)kErrCapacity);
+				ws_error(W, kErrCapacity);
 			}
 			++it;
 			lo += ccnt[c];
@@ -268,24 +280,43 @@ __global__ void __launch_bounds__(kBlock) k_expand_short(DevPool P, Workspace W,
 	}
 }
 
-// ------------------------------------------------------------------ warp planning (long lists)
-// Plan of one child by a whole warp: returns kept-count upper bound, base and first.
-template <bool Identity>
-__device__ __forceinline__ u32 plan_child_warp(const Workspace &W, u32 off, u32 len, u32 shift, u32 cx, u32 cy, u32 cz,
-                                               u32 old, u32 filled, u32 *base_out, u32 *first_out) {
-	const u32 lane = lane_id();
-	u32 lf1 = 0; // lastfull + 1
-	for (u32 p = lane; p < len; p += 32) {
-		const hd_edit_desc &e = W.edits[list_at<Identity>(W, off, p)];
-		if (classify(e, shift, cx, cy, cz) == kClsFull)
-			lf1 = p + 1;
+// ------------------------------------------------------------------ block planning (long lists)
+// Block-wide reductions through a shared scratch of at least 33 words.
+template <int Op> __device__ __forceinline__ u32 warp_red(u32 v) {
+	return Op == 0 ? __reduce_max_sync(kFullMask, v) : (Op == 1 ? __reduce_min_sync(kFullMask, v) : __reduce_add_sync(kFullMask, v));
+}
+template <int Op> __device__ __forceinline__ u32 block_reduce(u32 v, u32 *sm) {
+	const u32 warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+	v = warp_red<Op>(v);
+	if (lane_id() == 0)
+		sm[warp] = v;
+	__syncthreads();
+	if (warp == 0) {
+		u32 x = lane_id() < nw ? sm[lane_id()] : (Op == 1 ? kNull : 0u);
+		x = warp_red<Op>(x);
+		if (lane_id() == 0)
+			sm[32] = x;
 	}
-	lf1 = __reduce_max_sync(kFullMask, lf1);
+	__syncthreads();
+	const u32 r = sm[32];
+	__syncthreads();
+	return r;
+}
+
+// Plan of one child by a whole block: returns kept-count upper bound (0 = terminal).
+template <bool Identity>
+__device__ u32 plan_child_block(const Workspace &W, u32 off, u32 len, u32 shift, u32 cx, u32 cy, u32 cz, u32 old,
+                                u32 filled, u32 *base_out, u32 *first_out, u32 *sm) {
+	u32 lf1 = 0; // lastfull + 1
+	for (u32 p = threadIdx.x; p < len; p += blockDim.x)
+		if (classify(W.edits[list_at<Identity>(W, off, p)], shift, cx, cy, cz) == kClsFull)
+			lf1 = p + 1;
+	lf1 = block_reduce<0>(lf1, sm);
 	u32 base = old;
 	if (lf1)
 		base = W.edits[list_at<Identity>(W, off, lf1 - 1)].op == HD_OP_FILL ? filled : kNull;
 	u32 first = kNull, cnt = 0;
-	for (u32 p = lf1 + lane; p < len; p += 32) {
+	for (u32 p = lf1 + threadIdx.x; p < len; p += blockDim.x) {
 		const hd_edit_desc &e = W.edits[list_at<Identity>(W, off, p)];
 		if (classify(e, shift, cx, cy, cz) == kClsPartial) {
 			++cnt;
@@ -293,21 +324,21 @@ __device__ __forceinline__ u32 plan_child_warp(const Workspace &W, u32 off, u32 
 				first = p;
 		}
 	}
-	first = __reduce_min_sync(kFullMask, first);
-	cnt = __reduce_add_sync(kFullMask, cnt);
+	first = block_reduce<1>(first, sm);
+	cnt = block_reduce<2>(cnt, sm);
 	*base_out = base;
 	*first_out = first;
-	return first == kNull ? 0u : cnt; // cnt bounds the kept edits (positions >= first)
+	return first == kNull ? 0u : cnt;
 }
 
-// Writes kept edits (positions >= first, partial) in order; returns the count.
+// Writes the kept edits (positions >= first, partial) in order; returns the count.
 template <bool Identity>
-__device__ __forceinline__ u32 write_child_list_warp(const Workspace &W, u32 off, u32 len, u32 first, u32 shift, u32 cx,
-                                                     u32 cy, u32 cz, u32 *dst) {
-	const u32 lane = lane_id();
+__device__ u32 write_child_list_block(const Workspace &W, u32 off, u32 len, u32 first, u32 shift, u32 cx, u32 cy, u32 cz,
+                                      u32 *dst, u32 *sm) {
+	const u32 warp = threadIdx.x >> 5, nw = blockDim.x >> 5, lane = lane_id();
 	u32 k = 0;
-	for (u32 p0 = first; p0 < len; p0 += 32) {
-		const u32 p = p0 + lane;
+	for (u32 p0 = first; p0 < len; p0 += blockDim.x) {
+		const u32 p = p0 + threadIdx.x;
 		u32 id = 0;
 		bool keep = false;
 		if (p < len) {
@@ -315,161 +346,356 @@ __device__ __forceinline__ u32 write_child_list_warp(const Workspace &W, u32 off
 			keep = classify(W.edits[id], shift, cx, cy, cz) == kClsPartial;
 		}
 		const u32 bal = __ballot_sync(kFullMask, keep);
+		if (lane == 0)
+			sm[warp] = __popc(bal);
+		__syncthreads();
+		u32 before = 0, total = 0;
+		for (u32 w = 0; w < nw; ++w) {
+			const u32 c = sm[w];
+			before += w < warp ? c : 0u;
+			total += c;
+		}
 		if (keep)
-			dst[k + __popc(bal & ((1u << lane) - 1u))] = id;
-		k += __popc(bal);
+			dst[k + before + __popc(bal & ((1u << lane) - 1u))] = id;
+		k += total;
+		__syncthreads();
 	}
 	return k;
 }
 
-// Emits one child planned by a warp; lane 0 reserves.  The list gets the
-// upper bound `cnt` of entries and the exact kept count is stored as its length.
+// Emits one inner child item planned by a block; errors go to the workspace.
 template <bool Identity>
-__device__ __forceinline__ void emit_child_warp(Workspace &W, u32 L, u32 cl, u64 child_begin, u32 parent_slot, u32 off,
-                                                u32 len, u32 shift, u32 cx, u32 cy, u32 cz, u32 base, u32 first, u32 cnt) {
-	Items &child = items_of(W, L, cl);
-	unsigned long long it = 0, lo = 0;
-	if (lane_id() == 0) {
-		it = atomicAdd(&W.ctr[kWsItems + cl], 1ull);
-		lo = atomicAdd(&W.ctr[kWsList], (unsigned long long)cnt);
+__device__ void emit_child_block(Workspace &W, u32 cl, u64 child_begin, u32 parent_slot, u32 off, u32 len, u32 shift,
+                                 u32 cx, u32 cy, u32 cz, u32 base, u32 first, u32 cnt, u32 *sm) {
+	if (threadIdx.x == 0) {
+		sm[34] = (u32)atomicAdd(&W.ctr[kWsItems + cl], 1ull);
+		const unsigned long long lo = atomicAdd(&W.ctr[kWsList], (unsigned long long)cnt);
+		sm[35] = (u32)lo;
+		sm[36] = lo + cnt <= W.list_cap ? 1u : 0u;
 	}
-	it = __shfl_sync(kFullMask, it, 0) + child_begin;
-	lo = __shfl_sync(kFullMask, lo, 0);
-	if (it < child.cap && lo + cnt <= W.list_cap) {
-		const u32 k = write_child_list_warp<Identity>(W, off, len, first, shift, cx, cy, cz, W.lists + lo);
-		if (lane_id() == 0) {
-			child.pos[it] = pack_pos(cx, cy, cz);
-			child.base[it] = base;
-			child.parent[it] = parent_slot;
-			child.lst_off[it] = (u32)lo;
-			child.lst_len[it] = k;
-			if (cl < L - 1 && k > W.long_threshold) {
+	__syncthreads();
+	const u64 it = child_begin + sm[34];
+	const u32 lo = sm[35];
+	const bool fits = it < W.inner.cap && sm[36];
+	__syncthreads();
+	if (fits) {
+		const u32 k = write_child_list_block<Identity>(W, off, len, first, shift, cx, cy, cz, W.lists + lo, sm);
+		if (threadIdx.x == 0) {
+			W.inner.pos[it] = pack_pos(cx, cy, cz);
+			W.inner.base[it] = base;
+			W.inner.parent[it] = parent_slot;
+			W.inner.lst_off[it] = lo;
+			W.inner.lst_len[it] = k;
+			if (k > W.long_threshold) {
 				const unsigned long long lg = atomicAdd(&W.ctr[kWsLong + cl], 1ull);
 				if (child_begin + lg < W.inner.cap)
 					W.long_q[child_begin + lg] = (u32)it;
 				else
-					atomicCAS(&W.ctr[kWsError], 0ull, (unsigned long long)kErrCapacity);
+					ws_error(W, kErrCapacity);
 			}
 		}
-	} else if (lane_id() == 0) {
-		atomicCAS(&W.ctr[kWsError], 0ull, (unsigned long long)kErrCapacity);
+	} else if (threadIdx.x == 0) {
+		ws_error(W, kErrCapacity);
 	}
+	__syncthreads();
 }
 
 // ------------------------------------------------------------------ k_expand_long
-// Warp per level-l node whose edit list is longer than long_threshold.
-__global__ void __launch_bounds__(kBlock) k_expand_long(DevPool P, Workspace W, u32 l) {
+// Block per (level-l node with a long edit list, child), l <= L-3.
+__global__ void __launch_bounds__(kLongBlock) k_expand_long(DevPool P, Workspace W, u32 l) {
 	if (ws_failed(W))
 		return;
+	__shared__ u32 sm[40];
 	const u32 L = P.cfg.L;
 	const u32 cl = l + 1;
 	const u64 begin = level_begin(W, L, l);
-	u64 n = W.ctr[kWsLong + l];
+	const u64 n = W.ctr[kWsLong + l];
 	const u64 child_begin = level_begin(W, L, cl);
-	const u32 shift = P.cfg.L + 1u - cl;
+	const u32 shift = L + 1u - cl;
 	const u32 filled_c = P.cfg.filled[cl];
-	const u64 warps = (u64)gridDim.x * (blockDim.x / 32);
-	for (u64 q = (u64)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32; q < n; q += warps) {
-		const u64 qi = begin + q;
+	for (u64 pair = blockIdx.x; pair < n * 8; pair += gridDim.x) {
+		const u64 qi = begin + (pair >> 3);
+		const u32 c = (u32)(pair & 7u);
 		if (qi >= W.inner.cap)
 			break;
 		const u64 i = W.long_q[qi];
+		if (i >= W.inner.cap) { // uniform over the block
+			if (threadIdx.x == 0)
+				ws_error(W, kErrInternal);
+			break;
+		}
 		const u32 len = W.inner.lst_len[i], off = W.inner.lst_off[i], b = W.inner.base[i];
 		const u64 pos = W.inner.pos[i];
-		u32 old[8], res[8];
+		if (len > W.n_edits || (u64)off + len > W.list_cap) {
+			if (threadIdx.x == 0)
+				ws_error(W, kErrInternal);
+			break;
+		}
+		u32 old[8];
 		base_children(P, l, b, old);
-		const u32 px = pos_x(pos), py = pos_y(pos), pz = pos_z(pos);
-		for (u32 c = 0; c < 8; ++c) {
-			const u32 cx = (px << 1) | (c & 1u), cy = (py << 1) | ((c >> 1) & 1u), cz = (pz << 1) | ((c >> 2) & 1u);
-			u32 cb, cf;
-			u32 cnt = plan_child_warp<false>(W, off, len, shift, cx, cy, cz, old[c], filled_c, &cb, &cf);
-			if (!cnt) {
-				res[c] = cb;
+		u32 cx, cy, cz;
+		child_pos(pos, c, cx, cy, cz);
+		u32 cb, cf;
+		const u32 cnt = plan_child_block<false>(W, off, len, shift, cx, cy, cz, old[c], filled_c, &cb, &cf, sm);
+		if (threadIdx.x == 0) {
+			W.bchild[i * 8u + c] = old[c];
+			W.cnew[i * 8u + c] = cnt ? kNull : cb;
+		}
+		if (cnt)
+			emit_child_block<false>(W, cl, child_begin, (u32)(i * 8u + c), off, len, shift, cx, cy, cz, cb, cf, cnt, sm);
+	}
+}
+
+// ------------------------------------------------------------------ leaf level
+// New bits of the leaf at leaf coordinate (lx,ly,lz) after one edit.  A leaf
+// fully covered by the edit takes the edit's value; a partially covered one
+// applies the edit's 64-voxel mask (edit_leaf, NodePool.hpp:319-343).
+__device__ __forceinline__ u64 apply_edit_leaf(const hd_edit_desc &e, u32 lx, u32 ly, u32 lz, u64 bits) {
+	const u32 cls = classify(e, 2u, lx, ly, lz);
+	if (cls == kClsNone)
+		return bits;
+	if (cls == kClsFull)
+		return e.op == HD_OP_FILL ? ~0ull : 0ull;
+	const u64 m = shape_mask(e, lx << 2, ly << 2, lz << 2);
+	return e.op == HD_OP_FILL ? (bits | m) : (bits & ~m);
+}
+
+// Result of a rebuilt leaf: unchanged / Null / filled leaf, or a dedup candidate (kNull).
+__device__ __forceinline__ u32 leaf_result(const DevPool &P, u64 bits, u64 bits0, u32 old, bool *cand) {
+	*cand = false;
+	if (bits == bits0)
+		return old;
+	if (bits == 0ull)
+		return kNull;
+	if (bits == ~0ull)
+		return P.cfg.filled[P.cfg.L - 1];
+	*cand = true;
+	return kNull;
+}
+
+// Thread per level-(L-2) node with a short edit list: computes its 8 leaves.
+__global__ void __launch_bounds__(kBlock) k_leafparent_short(DevPool P, Workspace W) {
+	if (ws_failed(W))
+		return;
+	const u32 L = P.cfg.L, l = L - 2;
+	u64 begin, n;
+	level_range(W, L, l, begin, n);
+	const u32 T = W.long_threshold;
+	const u64 stride = (u64)gridDim.x * blockDim.x;
+	for (u64 w0 = (u64)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); w0 < n; w0 += stride) {
+		const u64 t = w0 + lane_id();
+		const u64 i = begin + t;
+		const bool valid = t < n;
+		u32 len = 0, off = 0, b = kNull;
+		u64 pos = 0;
+		if (valid) {
+			len = W.inner.lst_len[i];
+			off = W.inner.lst_off[i];
+			b = W.inner.base[i];
+			pos = W.inner.pos[i];
+		}
+		const bool mine = valid && len <= T && list_ok(W, off, len);
+		u32 old[8], res[8];
+		u64 bits[8];
+		u32 cand_mask = 0;
+		if (mine) {
+			base_children(P, l, b, old);
+			u64 bits0[8];
+#pragma unroll
+			for (int c = 0; c < 8; ++c) {
+				bits[c] = leaf_bits(P, old[c]);
+				bits0[c] = bits[c];
+			}
+			for (u32 p = 0; p < len; ++p) {
+				const hd_edit_desc e = W.edits[W.lists[off + p]];
+#pragma unroll
+				for (u32 c = 0; c < 8; ++c) {
+					u32 cx, cy, cz;
+					child_pos(pos, c, cx, cy, cz);
+					bits[c] = apply_edit_leaf(e, cx, cy, cz, bits[c]);
+				}
+			}
+#pragma unroll
+			for (int c = 0; c < 8; ++c) {
+				bool cand;
+				res[c] = leaf_result(P, bits[c], bits0[c], old[c], &cand);
+				cand_mask |= (cand ? 1u : 0u) << c;
+			}
+		}
+		const u64 c0 = warp_reserve(&W.ctr[kWsItems + L - 1], __popc(cand_mask));
+		if (!mine)
+			continue;
+		u64 ci = c0;
+#pragma unroll
+		for (int c = 0; c < 8; ++c) {
+			if (!((cand_mask >> c) & 1u))
+				continue;
+			if (ci < W.leaf.cap) {
+				W.leaf_new[ci] = bits[c];
+				W.leaf.parent[ci] = (u32)(i * 8u + c);
+				W.leaf.state[ci] = kStCand;
+			} else {
+				ws_error(W, kErrCapacity);
+			}
+			++ci;
+		}
+		uint4 *bc = reinterpret_cast<uint4 *>(W.bchild + i * 8u);
+		uint4 *cn = reinterpret_cast<uint4 *>(W.cnew + i * 8u);
+		bc[0] = make_uint4(old[0], old[1], old[2], old[3]);
+		bc[1] = make_uint4(old[4], old[5], old[6], old[7]);
+		cn[0] = make_uint4(res[0], res[1], res[2], res[3]);
+		cn[1] = make_uint4(res[4], res[5], res[6], res[7]);
+	}
+}
+
+// Warp per level-(L-2) node with a long edit list: lane = (leaf c = lane/4,
+// quarter q = lane%4) owns voxels 16q..16q+15 of leaf c and walks the whole
+// list in order.
+__global__ void __launch_bounds__(kBlock) k_leafparent_long(DevPool P, Workspace W) {
+	if (ws_failed(W))
+		return;
+	const u32 L = P.cfg.L, l = L - 2;
+	const u64 begin = level_begin(W, L, l);
+	const u64 n = W.ctr[kWsLong + l];
+	const u32 lane = lane_id(), c = lane >> 2, q = lane & 3u;
+	const u64 warps = (u64)gridDim.x * (blockDim.x / 32);
+	for (u64 k = (u64)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32; k < n; k += warps) {
+		const u64 qi = begin + k;
+		if (qi >= W.inner.cap)
+			break;
+		const u64 i = W.long_q[qi];
+		if (i >= W.inner.cap) { // uniform over the warp
+			if (lane == 0)
+				ws_error(W, kErrInternal);
+			break;
+		}
+		const u32 len = W.inner.lst_len[i], off = W.inner.lst_off[i], b = W.inner.base[i];
+		const u64 pos = W.inner.pos[i];
+		if (len > W.n_edits || (u64)off + len > W.list_cap) {
+			if (lane == 0)
+				ws_error(W, kErrInternal);
+			break;
+		}
+		u32 old[8];
+		base_children(P, l, b, old);
+		u32 cx, cy, cz;
+		child_pos(pos, c, cx, cy, cz);
+		const u64 b0 = leaf_bits(P, old[c]);
+		u32 mine = (u32)(b0 >> (16u * q)) & 0xFFFFu;
+		for (u32 p = 0; p < len; ++p) {
+			const hd_edit_desc e = W.edits[W.lists[off + p]];
+			const u32 cls = classify(e, 2u, cx, cy, cz);
+			if (cls == kClsNone)
+				continue;
+			if (cls == kClsFull) {
+				mine = e.op == HD_OP_FILL ? 0xFFFFu : 0u;
 				continue;
 			}
-			res[c] = kNull;
-			emit_child_warp<false>(W, L, cl, child_begin, (u32)(i * 8u + c), off, len, shift, cx, cy, cz, cb, cf, cnt);
+			for (u32 v = 0; v < 16; ++v) {
+				const u32 iv = 16u * q + v;
+				const u32 x = (cx << 2) | ((iv >> 2) & 2u) | (iv & 1u), y = (cy << 2) | ((iv >> 3) & 2u) | ((iv >> 1) & 1u),
+				          z = (cz << 2) | ((iv >> 4) & 2u) | ((iv >> 2) & 1u);
+				if (voxel_in(e, x, y, z))
+					mine = e.op == HD_OP_FILL ? (mine | (1u << v)) : (mine & ~(1u << v));
+			}
 		}
-		if (lane_id() == 0) {
-			uint4 *bc = reinterpret_cast<uint4 *>(W.bchild + i * 8u);
-			uint4 *cn = reinterpret_cast<uint4 *>(W.cnew + i * 8u);
-			bc[0] = make_uint4(old[0], old[1], old[2], old[3]);
-			bc[1] = make_uint4(old[4], old[5], old[6], old[7]);
-			cn[0] = make_uint4(res[0], res[1], res[2], res[3]);
-			cn[1] = make_uint4(res[4], res[5], res[6], res[7]);
+		// gather the 4 quarters of each leaf
+		u64 bits = 0;
+#pragma unroll
+		for (u32 s = 0; s < 4; ++s)
+			bits |= (u64)__shfl_sync(kFullMask, mine, (lane & ~3u) | s) << (16u * s);
+		bool cand = false;
+		const u32 r = leaf_result(P, bits, b0, old[c], &cand);
+		const bool lead = q == 0;
+		const u64 ci = warp_reserve(&W.ctr[kWsItems + L - 1], lead && cand ? 1u : 0u);
+		if (lead) {
+			if (cand) {
+				if (ci < W.leaf.cap) {
+					W.leaf_new[ci] = bits;
+					W.leaf.parent[ci] = (u32)(i * 8u + c);
+					W.leaf.state[ci] = kStCand;
+				} else {
+					ws_error(W, kErrCapacity);
+				}
+			}
+			W.bchild[i * 8u + c] = old[c];
+			W.cnew[i * 8u + c] = r;
 		}
 	}
 }
 
 // ------------------------------------------------------------------ k_root
-// One warp: NodePool.hpp:405-414 edit_switch on the root for the whole list.
-__global__ void k_root(DevPool P, Workspace W, u32 root_val, const u32 *root_ptr) {
-	if (threadIdx.x >= 32)
-		return;
+// NodePool.hpp:405-414 edit_switch on the root for the whole list (one block).
+// With a single node level the root is a leaf and is rebuilt here directly.
+__global__ void __launch_bounds__(kLongBlock) k_root(DevPool P, Workspace W, u32 root_val, const u32 *root_ptr) {
+	__shared__ u32 sm[40];
 	const u32 L = P.cfg.L;
 	const u32 root = root_ptr ? *root_ptr : root_val;
-	if (lane_id() == 0)
+	if (threadIdx.x == 0)
 		W.ctr[kWsRootIn] = root;
 	// a root must be Null or point into a page that holds data
 	if (root != kNull) {
 		const u64 vp = root >> P.cfg.wbpp;
 		const u32 phys = vp < P.total_pages ? P.page_table[vp] : kUnallocPage;
 		if (phys == kUnallocPage || phys == kZeroPage) {
-			if (lane_id() == 0) {
+			if (threadIdx.x == 0) {
 				W.ctr[kWsRoot] = root;
-				atomicCAS(&W.ctr[kWsError], 0ull, (unsigned long long)kErrInvalidRoot);
+				ws_error(W, kErrInvalidRoot);
 			}
 			return;
 		}
 	}
+	if (L == 1) { // the root is a leaf: warp 0, two voxels per lane, edits in order
+		if (threadIdx.x >= 32)
+			return;
+		const u64 b0 = leaf_bits(P, root);
+		u32 v2 = (u32)(b0 >> (2u * lane_id())) & 3u;
+		for (u32 p = 0; p < W.n_edits; ++p) {
+			const hd_edit_desc e = W.edits[p];
+#pragma unroll
+			for (u32 s = 0; s < 2; ++s) {
+				const u32 iv = 2u * lane_id() + s;
+				const u32 x = ((iv >> 2) & 2u) | (iv & 1u), y = ((iv >> 3) & 2u) | ((iv >> 1) & 1u),
+				          z = ((iv >> 4) & 2u) | ((iv >> 2) & 1u);
+				if (voxel_in(e, x, y, z))
+					v2 = e.op == HD_OP_FILL ? (v2 | (1u << s)) : (v2 & ~(1u << s));
+			}
+		}
+		const u32 lo = __ballot_sync(kFullMask, v2 & 1u), hi = __ballot_sync(kFullMask, (v2 >> 1) & 1u);
+		u64 bits = 0;
+		for (u32 k = 0; k < 32; ++k)
+			bits |= ((u64)((lo >> k) & 1u) << (2 * k)) | ((u64)((hi >> k) & 1u) << (2 * k + 1));
+		if (lane_id() == 0) {
+			bool cand;
+			const u32 r = leaf_result(P, bits, b0, root, &cand);
+			W.ctr[kWsRoot] = r;
+			if (cand) {
+				W.ctr[kWsItems + 0] = 1;
+				W.leaf_new[0] = bits;
+				W.leaf.parent[0] = kNull;
+				W.leaf.state[0] = kStCand;
+			}
+		}
+		return;
+	}
 	u32 b, f;
-	u32 cnt = plan_child_warp<true>(W, 0, W.n_edits, L + 1u, 0, 0, 0, root, P.cfg.filled[0], &b, &f);
+	const u32 cnt = plan_child_block<true>(W, 0, W.n_edits, L + 1u, 0, 0, 0, root, P.cfg.filled[0], &b, &f, sm);
 	if (!cnt) {
-		if (lane_id() == 0)
+		if (threadIdx.x == 0)
 			W.ctr[kWsRoot] = b;
 		return;
 	}
-	emit_child_warp<true>(W, L, 0, 0, kNull, 0, W.n_edits, L + 1u, 0, 0, 0, b, f, cnt);
-}
-
-// ------------------------------------------------------------------ k_leaf
-// Thread per leaf: NodePool.hpp:319-343 for the leaf's edit list, 64 voxels at a time.
-__global__ void __launch_bounds__(kBlock) k_leaf(DevPool P, Workspace W) {
-	if (ws_failed(W))
-		return;
-	const u32 L = P.cfg.L;
-	u64 begin, n;
-	level_range(W, L, L - 1, begin, n);
-	const u32 filled = P.cfg.filled[L - 1];
-	const u64 stride = (u64)gridDim.x * blockDim.x;
-	for (u64 t = (u64)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
-		const u64 i = begin + t;
-		const u32 b = W.leaf.base[i];
-		u64 bits0 = 0;
-		if (b == filled)
-			bits0 = ~0ull;
-		else if (b != kNull) {
-			const u32 *p = node_addr(P, b);
-			bits0 = (u64)p[0] | ((u64)p[1] << 32);
-		}
-		const u64 pos = W.leaf.pos[i];
-		const u32 ox = pos_x(pos) << 2, oy = pos_y(pos) << 2, oz = pos_z(pos) << 2;
-		const u32 off = W.leaf.lst_off[i], len = W.leaf.lst_len[i];
-		u64 bits = bits0;
-		for (u32 p = 0; p < len; ++p) {
-			const hd_edit_desc &e = W.edits[W.lists[off + p]];
-			const u64 m = shape_mask(e, ox, oy, oz);
-			bits = e.op == HD_OP_FILL ? (bits | m) : (bits & ~m);
-		}
-		W.leaf_new[i] = bits;
-		W.leaf.state[i] = bits == bits0 ? kStUnchanged : (bits == 0 ? kStEmpty : kStCand);
-	}
+	emit_child_block<true>(W, 0, 0, kNull, 0, W.n_edits, L + 1u, 0, 0, 0, b, f, cnt, sm);
 }
 
 // ------------------------------------------------------------------ dedup: find or claim
 struct NodeWords {
 	u32 w[9];
 	u32 n;
+};
+
+struct Outcome {
+	u32 state, res, link, pad;
 };
 
 __device__ __forceinline__ bool equal_resident(const DevPool &P, u32 ptr, const NodeWords &nw) {
@@ -482,20 +708,25 @@ __device__ __forceinline__ bool equal_resident(const DevPool &P, u32 ptr, const 
 
 // Reserve space for a node of w words in bucket b (NodePool.hpp:134-157 on an
 // atomic word count).  Returns false when the bucket is full.
-__device__ __forceinline__ bool reserve(const DevPool &P, u32 b, u32 w, u32 *ptr_out, u32 *pad_out) {
+__device__ __forceinline__ bool reserve(const DevPool &P, Workspace &W, u32 b, u32 w, u32 *ptr_out, u32 *pad_out) {
 	const u32 wp = wpp(P.cfg), wpb = 1u << (P.cfg.wbpp + P.cfg.pbpb);
 	u32 old = *(volatile u32 *)&P.bucket_words[b];
 	u32 off, nw;
-	for (;;) {
+	for (u32 tries = 0;; ++tries) { // lock-free: a failed CAS means another thread advanced the count
+		if (tries > (1u << 22)) {  // cannot happen with fewer than 2^22 contenders; report, do not spin
+			set_error(&P.counters[kCtrError], kErrTimeout);
+			return false;
+		}
 		off = old;
 		if ((off & (wp - 1u)) + w > wp)
 			off = (off | (wp - 1u)) + 1u;
 		nw = off + w;
 		if (nw > wpb)
 			return false;
-		u32 prev = atomicCAS(&P.bucket_words[b], old, nw);
+		const u32 prev = atomicCAS(&P.bucket_words[b], old, nw);
 		if (prev == old)
 			break;
+		atomicAdd(&W.ctr[kWsCasRetry], 1ull);
 		old = prev;
 	}
 	*pad_out = off != old ? old : kNull;
@@ -512,32 +743,34 @@ __device__ __forceinline__ bool reserve(const DevPool &P, u32 b, u32 w, u32 *ptr
 	return true;
 }
 
-// Find-or-claim of one candidate.  Compare(j) tests equality with pending item j.
+// Find-or-claim of one candidate.  cmp_pending(j) tests equality with pending item j.
+// The probe walks at most kMaxProbe slots (a table at its load limit needs a
+// few dozen); longer walks are reported as a full index instead of scanned.
+static constexpr u64 kMaxProbe = 1u << 16;
 template <typename CmpPending>
-__device__ __forceinline__ void find_or_claim(const DevPool &P, Items &it, u64 i, u32 level, u32 h, u32 bucket,
-                                              const NodeWords &nw, CmpPending &&cmp_pending) {
+__device__ __forceinline__ Outcome find_or_claim(const DevPool &P, Workspace &W, u64 i, u32 level, u32 h, u32 bucket,
+                                                 const NodeWords &nw, u32 *probes, CmpPending &&cmp_pending) {
 	const u64 mask = P.index_mask;
 	const unsigned long long tag = (unsigned long long)(h & 0x7FFFFFFFu) << 32;
 	const u32 bucket_shift = P.cfg.wbpp + P.cfg.pbpb;
+	const u64 limit = mask < kMaxProbe ? mask + 1 : kMaxProbe;
 	u64 s = index_start(h, level, mask);
-	for (u64 probe = 0; probe <= mask; ++probe, s = (s + 1) & mask) {
+	Outcome out = {kStFail, kNull, kNull, kNull};
+	u64 probe = 0;
+	for (; probe < limit; ++probe, s = (s + 1) & mask) {
 		unsigned long long v = *(volatile unsigned long long *)&P.index[s];
 		if (v == kSlotEmpty) {
 			const unsigned long long claim = (1ull << 63) | tag | (unsigned long long)i;
-			unsigned long long prev = atomicCAS(&P.index[s], kSlotEmpty, claim);
+			const unsigned long long prev = atomicCAS(&P.index[s], kSlotEmpty, claim);
 			if (prev == kSlotEmpty) {
 				u32 ptr, pad;
-				if (reserve(P, bucket, nw.n, &ptr, &pad)) {
-					it.state[i] = kStRep;
-					it.res[i] = ptr;
-					it.pad[i] = pad;
-				} else {
+				if (reserve(P, W, bucket, nw.n, &ptr, &pad))
+					out = {kStRep, ptr, (u32)s, pad};
+				else {
 					set_error(&P.counters[kCtrError], kErrBucketFull);
-					it.state[i] = kStFail;
-					it.res[i] = kNull;
+					out = {kStFail, kNull, (u32)s, kNull};
 				}
-				it.link[i] = (u32)s; // index slot
-				return;
+				break;
 			}
 			v = prev;
 		}
@@ -546,20 +779,18 @@ __device__ __forceinline__ void find_or_claim(const DevPool &P, Items &it, u64 i
 		const u32 val = (u32)v;
 		if (v >> 63) { // pending in this pass
 			if (cmp_pending(val)) {
-				it.state[i] = kStAlias;
-				it.link[i] = val;
-				return;
+				out = {kStAlias, kNull, val, kNull};
+				break;
 			}
 		} else if ((val >> bucket_shift) == bucket && equal_resident(P, val, nw)) {
-			it.state[i] = kStFound;
-			it.res[i] = val;
-			return;
+			out = {kStFound, val, kNull, kNull};
+			break;
 		}
 	}
-	set_error(&P.counters[kCtrError], kErrIndexFull);
-	it.state[i] = kStFail;
-	it.res[i] = kNull;
-	it.link[i] = kNull;
+	if (probe == limit)
+		set_error(&P.counters[kCtrError], kErrIndexFull);
+	*probes = (u32)probe + 1u;
+	return out;
 }
 
 __device__ __forceinline__ void warp_count(unsigned long long *ctr, u32 v) {
@@ -569,6 +800,7 @@ __device__ __forceinline__ void warp_count(unsigned long long *ctr, u32 v) {
 }
 
 // ------------------------------------------------------------------ k_probe
+// Leaf: the leaf candidates.  Inner: the level-l items, rebuilt from cnew.
 template <bool Leaf>
 __global__ void __launch_bounds__(kBlock) k_probe(DevPool P, Workspace W, u32 l) {
 	if (ws_failed(W))
@@ -585,29 +817,31 @@ __global__ void __launch_bounds__(kBlock) k_probe(DevPool P, Workspace W, u32 l)
 	const u32 nb_mask = (1u << P.cfg.bucket_bits[l]) - 1u;
 	const u32 bbase = P.cfg.bucket_base[l];
 	const bool zero_hash = P.cfg.hasher == HD_HASHER_ZERO;
+	const u32 lane = lane_id();
 	const u64 stride = (u64)gridDim.x * blockDim.x;
 	for (u64 w0 = (u64)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); w0 < n; w0 += stride) {
-		const u64 t = w0 + lane_id();
-		u32 cand = 0, cwords = 0;
+		const u64 t = w0 + lane;
+		const u64 i = begin + t;
+		bool cand = false;
+		NodeWords nw;
+		nw.n = 0;
+#pragma unroll
+		for (int k = 0; k < 9; ++k)
+			nw.w[k] = 0;
+		u32 h = 0;
 		if (t < n) {
-			const u64 i = begin + t;
-			NodeWords nw;
-			u32 h;
 			if (skip) { // an earlier level failed: insert nothing more
 				if (!Leaf || it.state[i] == kStCand) {
 					it.state[i] = kStFail;
 					it.link[i] = kNull;
 				}
-				goto next;
-			}
-			if (Leaf) {
-				if (it.state[i] != kStCand)
-					goto next;
+			} else if (Leaf) {
 				const u64 bits = W.leaf_new[i];
 				nw.w[0] = (u32)bits;
 				nw.w[1] = (u32)(bits >> 32);
 				nw.n = 2;
 				h = hash_leaf(bits);
+				cand = true;
 			} else {
 				const uint4 *cn4 = reinterpret_cast<const uint4 *>(W.cnew + i * 8u);
 				const uint4 *bc4 = reinterpret_cast<const uint4 *>(W.bchild + i * 8u);
@@ -616,48 +850,83 @@ __global__ void __launch_bounds__(kBlock) k_probe(DevPool P, Workspace W, u32 l)
 				if (a0.x == b0.x && a0.y == b0.y && a0.z == b0.z && a0.w == b0.w && a1.x == b1.x && a1.y == b1.y &&
 				    a1.z == b1.z && a1.w == b1.w) {
 					it.state[i] = kStUnchanged;
-					goto next;
-				}
-				u32 mask = 0, k = 1;
-				Murmur mm;
-#pragma unroll
-				for (int q = 0; q < 8; ++q)
-					if (c[q] != kNull) {
-						mask |= 1u << q;
-						nw.w[k++] = c[q];
-					}
-				if (!mask) {
-					it.state[i] = kStEmpty;
-					goto next;
-				}
-				nw.w[0] = mask;
-				nw.n = k;
-				for (u32 q = 0; q < k; ++q)
-					mm.add(nw.w[q]);
-				h = mm.finish(k);
-			}
-			{
-				const u32 bucket = bbase + ((zero_hash ? 0u : h) & nb_mask);
-				cand = 1;
-				cwords = nw.n;
-				if (Leaf) {
-					const u64 mine = W.leaf_new[i];
-					find_or_claim(P, it, i, l, h, bucket, nw, [&](u32 j) { return W.leaf_new[j] == mine; });
 				} else {
-					const uint4 *cn4 = reinterpret_cast<const uint4 *>(W.cnew + i * 8u);
-					const uint4 a0 = cn4[0], a1 = cn4[1];
-					find_or_claim(P, it, i, l, h, bucket, nw, [&](u32 j) {
-						const uint4 *o4 = reinterpret_cast<const uint4 *>(W.cnew + (u64)j * 8u);
-						const uint4 c0 = o4[0], c1 = o4[1];
-						return c0.x == a0.x && c0.y == a0.y && c0.z == a0.z && c0.w == a0.w && c1.x == a1.x &&
-						       c1.y == a1.y && c1.z == a1.z && c1.w == a1.w;
-					});
+					u32 mask = 0, k = 1;
+#pragma unroll
+					for (int q = 0; q < 8; ++q)
+						if (c[q] != kNull) {
+							mask |= 1u << q;
+							nw.w[k++] = c[q];
+						}
+					if (!mask) {
+						it.state[i] = kStEmpty;
+					} else {
+						nw.w[0] = mask;
+						nw.n = k;
+						Murmur mm;
+						for (u32 q = 0; q < k; ++q)
+							mm.add(nw.w[q]);
+						h = mm.finish(k);
+						cand = true;
+					}
 				}
 			}
 		}
-	next:
-		warp_count(&W.ctr[kWsCand + l], cand);
-		warp_count(&W.ctr[kWsCandWords + l], cwords);
+		// merge equal candidates of the warp: one leader probes, the others follow
+		const unsigned long long key = cand ? (unsigned long long)h : (0x100000000ull | lane);
+		const u32 same = __match_any_sync(kFullMask, key);
+		const u32 leader = __ffs(same) - 1u;
+		// every lane executes every shuffle (no short-circuit around a full-mask shuffle)
+		const u32 leader_n = __shfl_sync(kFullMask, nw.n, leader);
+		bool eq = cand && leader != lane && leader_n == nw.n;
+#pragma unroll
+		for (int k = 0; k < 9; ++k) {
+			const u32 lw = __shfl_sync(kFullMask, nw.w[k], leader);
+			eq = eq && lw == nw.w[k];
+		}
+		const bool follower = eq;
+		Outcome o = {kStFail, kNull, kNull, kNull};
+		u32 probes = 0;
+		if (cand && !follower) {
+			const u32 bucket = bbase + ((zero_hash ? 0u : h) & nb_mask);
+			if (Leaf) {
+				const u64 mine = W.leaf_new[i];
+				o = find_or_claim(P, W, i, l, h, bucket, nw, &probes, [&](u32 j) { return W.leaf_new[j] == mine; });
+			} else {
+				const uint4 *cn4 = reinterpret_cast<const uint4 *>(W.cnew + i * 8u);
+				const uint4 a0 = cn4[0], a1 = cn4[1];
+				o = find_or_claim(P, W, i, l, h, bucket, nw, &probes, [&](u32 j) {
+					const uint4 *o4 = reinterpret_cast<const uint4 *>(W.cnew + (u64)j * 8u);
+					const uint4 c0 = o4[0], c1 = o4[1];
+					return c0.x == a0.x && c0.y == a0.y && c0.z == a0.z && c0.w == a0.w && c1.x == a1.x &&
+					       c1.y == a1.y && c1.z == a1.z && c1.w == a1.w;
+				});
+			}
+		}
+		const u32 lst = __shfl_sync(kFullMask, o.state, leader), lres = __shfl_sync(kFullMask, o.res, leader),
+		          llink = __shfl_sync(kFullMask, o.link, leader);
+		const u64 litem = __shfl_sync(kFullMask, i, leader);
+		if (follower) {
+			if (lst == kStRep)
+				o = {kStAlias, kNull, (u32)litem, kNull};
+			else if (lst == kStFail)
+				o = {kStFail, kNull, kNull, kNull};
+			else
+				o = {lst, lres, llink, kNull};
+		}
+		if (cand) {
+			it.state[i] = o.state;
+			it.res[i] = o.res;
+			it.link[i] = o.link;
+			if (!Leaf)
+				it.pad[i] = o.pad;
+		}
+		warp_count(&W.ctr[kWsCand + l], cand ? 1u : 0u);
+		warp_count(&W.ctr[kWsCandWords + l], cand ? nw.n : 0u);
+		warp_count(&W.ctr[kWsProbeSteps], probes);
+		const u32 pmax = __reduce_max_sync(kFullMask, probes);
+		if (lane == 0 && pmax)
+			atomicMax(&W.ctr[kWsMaxProbe], (unsigned long long)pmax);
 	}
 }
 
@@ -721,15 +990,15 @@ __global__ void __launch_bounds__(kBlock) k_commit(DevPool P, Workspace W, u32 l
 						}
 					dst[0] = mask;
 					insw = k;
-				}
-				const u32 pad = it.pad[i];
-				if (pad != kNull) {
-					const u32 vp = ((r >> bucket_shift) << P.cfg.pbpb) | (pad >> P.cfg.wbpp);
-					const u32 zp = P.page_table[vp];
-					if (zp != kUnallocPage && zp != kZeroPage) {
-						u32 *z = P.heap + ((u64)zp << P.cfg.wbpp);
-						for (u32 q = pad & (wp - 1u); q < wp; ++q)
-							z[q] = 0u;
+					const u32 pad = it.pad[i];
+					if (pad != kNull) {
+						const u32 vp = ((r >> bucket_shift) << P.cfg.pbpb) | (pad >> P.cfg.wbpp);
+						const u32 zp = P.page_table[vp];
+						if (zp != kUnallocPage && zp != kZeroPage) {
+							u32 *z = P.heap + ((u64)zp << P.cfg.wbpp);
+							for (u32 q = pad & (wp - 1u); q < wp; ++q)
+								z[q] = 0u;
+						}
 					}
 				}
 				ins = 1;
