@@ -378,6 +378,7 @@ def run_ours(args):
                      "traffic": traffic, "algorithmic_bytes_per_step": dedup_bytes,
                      "dedup_ms_per_step": per_step_dedup_ms},
         "phases_ms_per_step": phase_ms,
+        "counters_last_step": {k: [int(x) for x in v] for k, v in counters.items()},
         "cpu_baseline": cpu,
         "gpu_launches": int(launches),
         "clocks": clk,

@@ -233,3 +233,25 @@ def test_batched_equals_chunked_at_scale(hd):
     for k in range(0, 96):
         r = pool.edit(r, e[k:k + 1])
     assert r == pool.edit(base, e[:96])
+
+
+def test_identity_and_paged_heaps_agree(golden, orc, hd):
+    """The identity-mapped heap (heap spans every virtual page) and the paged
+    heap (pages handed out on first use) store the same DAG."""
+    s = scenario(golden, "mixed512")
+    cfg = config_from(s["config"])
+    edits = scenario_edits(s)
+    paged = hd.NodePool(cfg, heap_pages=1 << 14)
+    ident = hd.NodePool(cfg, heap_pages=cfg.get_total_pages())
+    assert paged.stats()["heap_pages"] == 1 << 14 < cfg.get_total_pages()
+    assert ident.stats()["heap_pages"] == cfg.get_total_pages()
+    for pool in (paged, ident):
+        root = pool.edit(hd.NULL, edits)
+        check_against_golden(orc, pool, root, s)
+        check_pool_structure(orc, pool)
+    # an identity-mapped pool uploads and downloads like a paged one
+    bw, ids, pages = paged.download()
+    ident2 = hd.NodePool(cfg, heap_pages=cfg.get_total_pages())
+    ident2.upload(bw, ids, pages, paged.filled_node_pointers())
+    bw2, ids2, pages2 = ident2.download()
+    assert np.array_equal(bw, bw2) and np.array_equal(ids, ids2) and np.array_equal(pages, pages2)

@@ -52,22 +52,23 @@ struct DevPool {
 	u64 index_mask;
 	u64 total_pages;
 	u32 heap_pages;
-	u32 pad_;
+	u32 identity; // 1: the heap spans every virtual page, page i is physical page i
 };
 
 enum CounterSlot : u32 { kCtrHeapNext = 0, kCtrError = 1, kCtrIndexUsed = 2, kCtrCount = 4 };
 
 __device__ __forceinline__ u32 wpp(const DevConfig &c) { return 1u << c.wbpp; }
 
-// NodePool.hpp:75-77 read_node, through the page table
+// NodePool.hpp:75-77 read_node: one load with an identity-mapped heap, else
+// through the page table.
 __device__ __forceinline__ const u32 *node_addr(const DevPool &p, u32 ptr) {
+	if (p.identity)
+		return p.heap + ptr;
 	u32 phys = __ldg(p.page_table + (ptr >> p.cfg.wbpp));
 	return p.heap + ((u64)phys << p.cfg.wbpp) + (ptr & (wpp(p.cfg) - 1u));
 }
-__device__ __forceinline__ u32 *node_addr_w(const DevPool &p, u32 ptr) {
-	u32 phys = p.page_table[ptr >> p.cfg.wbpp];
-	return p.heap + ((u64)phys << p.cfg.wbpp) + (ptr & (wpp(p.cfg) - 1u));
-}
+// A page whose allocation failed maps to the zero page (paged heaps only).
+__device__ __forceinline__ bool page_lost(const DevPool &p, u32 phys) { return !p.identity && phys == kZeroPage; }
 
 __device__ __forceinline__ void set_error(u32 *slot, u32 code) { atomicCAS(slot, 0u, code); }
 
@@ -162,7 +163,36 @@ __device__ __forceinline__ u32 classify(const hd_edit_desc &e, u32 shift, u32 px
 //   x = (i>>2 & 2) | (i & 1), y = (i>>3 & 2) | (i>>1 & 1), z = (i>>4 & 2) | (i>>2 & 1)
 // 64-bit mask of the leaf voxels at origin (ox,oy,oz) inside the edit's shape
 // (SphereEditor/AABBEditor::VoxelInRange, src/main.cpp:55-57,121-126).
+// Sphere mask in 64-bit arithmetic (r2 > 2^30); rare, kept out of line.
+static __device__ __noinline__ u64 sphere_mask_wide(const hd_edit_desc &e, u32 ox, u32 oy, u32 oz) {
+	u64 dx2[4], dy2[4], dz2[4];
+#pragma unroll
+	for (u32 k = 0; k < 4; ++k) {
+		const long long dx = (long long)(ox + k) - (long long)e.p0[0];
+		const long long dy = (long long)(oy + k) - (long long)e.p0[1];
+		const long long dz = (long long)(oz + k) - (long long)e.p0[2];
+		dx2[k] = (u64)dx * (u64)dx;
+		dy2[k] = (u64)dy * (u64)dy;
+		dz2[k] = (u64)dz * (u64)dz;
+	}
+	u64 m = 0;
+	for (u32 yo = 0; yo < 4; ++yo)
+		for (u32 zo = 0; zo < 4; ++zo) {
+			const u64 t = dy2[yo] + dz2[zo];
+			const u32 base = ((yo & 1u) << 1) | ((zo & 1u) << 2) | ((yo >> 1) << 4) | ((zo >> 1) << 5);
+			if (t > e.r2)
+				continue;
+			const u64 rem = e.r2 - t;
+			const u32 nib = u32(dx2[0] <= rem) | u32(dx2[1] <= rem) << 1 | u32(dx2[2] <= rem) << 8 | u32(dx2[3] <= rem) << 9;
+			m |= (u64)nib << base;
+		}
+	return m;
+}
+
 __device__ __forceinline__ u64 shape_mask(const hd_edit_desc &e, u32 ox, u32 oy, u32 oz) {
+	// The leaf's voxels are 16 x-rows of 4 (one per (y,z) offset pair).  Row
+	// (yo,zo) holds voxel indices base+{0,1,8,9} for x offsets 0..3, with
+	// base = (yo&1)<<1 | (zo&1)<<2 | (yo>>1)<<4 | (zo>>1)<<5.
 	if (e.shape == HD_SHAPE_AABB) {
 		u32 mx = 0, my = 0, mz = 0;
 #pragma unroll
@@ -171,12 +201,16 @@ __device__ __forceinline__ u64 shape_mask(const hd_edit_desc &e, u32 ox, u32 oy,
 			my |= u32((oy + k) >= e.p0[1] && (oy + k) < e.p1[1]) << k;
 			mz |= u32((oz + k) >= e.p0[2] && (oz + k) < e.p1[2]) << k;
 		}
+		const u64 nib = (u64)((mx & 1u) | ((mx >> 1) & 1u) << 1 | ((mx >> 2) & 1u) << 8 | ((mx >> 3) & 1u) << 9);
 		u64 m = 0;
 #pragma unroll
-		for (u32 i = 0; i < 64; ++i) {
-			u32 x = ((i >> 2) & 2u) | (i & 1u), y = ((i >> 3) & 2u) | ((i >> 1) & 1u), z = ((i >> 4) & 2u) | ((i >> 2) & 1u);
-			m |= (u64)((mx >> x) & (my >> y) & (mz >> z) & 1u) << i;
-		}
+		for (u32 yo = 0; yo < 4; ++yo)
+#pragma unroll
+			for (u32 zo = 0; zo < 4; ++zo) {
+				const u32 base = ((yo & 1u) << 1) | ((zo & 1u) << 2) | ((yo >> 1) << 4) | ((zo >> 1) << 5);
+				if ((my >> yo) & (mz >> zo) & 1u)
+					m |= nib << base;
+			}
 		return m;
 	}
 	// A leaf that the sphere only partially covers lies within r+4 of the centre
@@ -193,36 +227,22 @@ __device__ __forceinline__ u64 shape_mask(const hd_edit_desc &e, u32 ox, u32 oy,
 			dz2[k] = (u32)(dz * dz);
 		}
 		const u32 r2 = (u32)e.r2;
-		u32 lo = 0, hi = 0;
+		u64 m = 0;
 #pragma unroll
-		for (u32 i = 0; i < 64; ++i) {
-			const u32 x = ((i >> 2) & 2u) | (i & 1u), y = ((i >> 3) & 2u) | ((i >> 1) & 1u),
-			          z = ((i >> 4) & 2u) | ((i >> 2) & 1u);
-			const u32 in = (dx2[x] + dy2[y] + dz2[z] <= r2) ? 1u : 0u;
-			if (i < 32)
-				lo |= in << i;
-			else
-				hi |= in << (i - 32);
-		}
-		return (u64)lo | ((u64)hi << 32);
-	}
-	u64 dx2[4], dy2[4], dz2[4];
+		for (u32 yo = 0; yo < 4; ++yo)
 #pragma unroll
-	for (u32 k = 0; k < 4; ++k) {
-		long long dx = (long long)(ox + k) - (long long)e.p0[0];
-		long long dy = (long long)(oy + k) - (long long)e.p0[1];
-		long long dz = (long long)(oz + k) - (long long)e.p0[2];
-		dx2[k] = (u64)dx * (u64)dx;
-		dy2[k] = (u64)dy * (u64)dy;
-		dz2[k] = (u64)dz * (u64)dz;
+			for (u32 zo = 0; zo < 4; ++zo) {
+				const u32 t = dy2[yo] + dz2[zo];
+				const u32 rem = t <= r2 ? r2 - t : 0u;
+				const u32 ok = t <= r2 ? 1u : 0u;
+				const u32 nib = (ok & (dx2[0] <= rem)) | (ok & (dx2[1] <= rem)) << 1 | (ok & (dx2[2] <= rem)) << 8 |
+				                (ok & (dx2[3] <= rem)) << 9;
+				const u32 base = ((yo & 1u) << 1) | ((zo & 1u) << 2) | ((yo >> 1) << 4) | ((zo >> 1) << 5);
+				m |= (u64)nib << base;
+			}
+		return m;
 	}
-	u64 m = 0;
-#pragma unroll
-	for (u32 i = 0; i < 64; ++i) {
-		u32 x = ((i >> 2) & 2u) | (i & 1u), y = ((i >> 3) & 2u) | ((i >> 1) & 1u), z = ((i >> 4) & 2u) | ((i >> 2) & 1u);
-		m |= (u64)(dx2[x] + dy2[y] + dz2[z] <= e.r2) << i;
-	}
-	return m;
+	return sphere_mask_wide(e, ox, oy, oz);
 }
 
 // One voxel inside the edit's shape (VoxelInRange, src/main.cpp:55-57,121-126).

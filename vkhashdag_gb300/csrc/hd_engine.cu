@@ -388,7 +388,7 @@ __global__ void k_index_rebuild(DevPool P, u32 total_buckets) {
 		while (off < bw) {
 			const u32 ptr = ((u32)b << (P.cfg.wbpp + P.cfg.pbpb)) | off;
 			const u32 phys = P.page_table[ptr >> P.cfg.wbpp];
-			if (phys == kUnallocPage || phys == kZeroPage) { // page lost: skip it
+			if (phys == kUnallocPage || page_lost(P, phys)) { // page lost: skip it
 				off = (off | (wp - 1u)) + 1u;
 				continue;
 			}
@@ -710,6 +710,11 @@ hd_status hd_pool_create(const hd_config *config, uint64_t heap_pages, uint32_t 
 	p->total_buckets = total_buckets_of(*config);
 	p->total_pages = p->total_buckets << c.pbpb;
 	p->P.total_pages = p->total_pages;
+	// a heap that can hold every virtual page is identity-mapped: node reads skip the page table
+	if (heap_pages >= p->total_pages) {
+		heap_pages = p->total_pages;
+		p->P.identity = 1;
+	}
 	const uint64_t heap_words = heap_pages << c.wbpp;
 	uint64_t slots = 1;
 	if (index_log2)
@@ -1056,14 +1061,16 @@ hd_status hd_pool_upload(hd_pool *pool, const uint32_t *bucket_words, const uint
 	for (uint32_t i = 0; i < n_pages; ++i) {
 		if (page_ids[i] >= pool->total_pages)
 			return HD_ERR_INVALID_ARG;
-		pt[page_ids[i]] = i + 1;
+		pt[page_ids[i]] = pool->P.identity ? page_ids[i] : i + 1;
 	}
 	HD_TRY(cudaMemcpy(pool->P.bucket_words, bucket_words, pool->total_buckets * 4, cudaMemcpyHostToDevice));
 	HD_TRY(cudaMemcpy(pool->P.page_table, pt.data(), pool->total_pages * 4, cudaMemcpyHostToDevice));
-	HD_TRY(cudaMemset(pool->P.heap, 0, wp * 4));
-	if (n_pages)
-		HD_TRY(cudaMemcpy(pool->P.heap + wp, page_words, (uint64_t)n_pages * wp * 4, cudaMemcpyHostToDevice));
-	HD_TRY(cudaMemset(pool->P.heap + wp * (n_pages + 1ull), 0, ((uint64_t)pool->P.heap_pages - n_pages - 1) * wp * 4));
+	HD_TRY(cudaMemset(pool->P.heap, 0, (uint64_t)pool->P.heap_pages * wp * 4));
+	for (uint32_t i = 0; i < n_pages; ++i) { // one copy per page: the layout differs per mode
+		const uint64_t phys = pt[page_ids[i]];
+		HD_TRY(cudaMemcpyAsync(pool->P.heap + phys * wp, page_words + (uint64_t)i * wp, wp * 4, cudaMemcpyHostToDevice));
+	}
+	HD_TRY(cudaDeviceSynchronize());
 	uint32_t ctr0[kCtrCount] = {n_pages + 1u, 0u, 0u, 0u};
 	HD_TRY(cudaMemcpy(pool->P.counters, ctr0, sizeof(ctr0), cudaMemcpyHostToDevice));
 	HD_TRY(cudaMemset(pool->P.index, 0xFF, (pool->P.index_mask + 1) * 8));

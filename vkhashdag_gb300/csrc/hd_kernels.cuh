@@ -460,6 +460,14 @@ __device__ __forceinline__ u64 apply_edit_leaf(const hd_edit_desc &e, u32 lx, u3
 	return e.op == HD_OP_FILL ? (bits | m) : (bits & ~m);
 }
 
+// New bits of one leaf after the edits of a list (kept out of line so the
+// caller keeps its 8 children in registers).
+__device__ __noinline__ u64 rebuild_leaf(const Workspace &W, u32 off, u32 len, u32 lx, u32 ly, u32 lz, u64 bits) {
+	for (u32 p = 0; p < len; ++p)
+		bits = apply_edit_leaf(W.edits[W.lists[off + p]], lx, ly, lz, bits);
+	return bits;
+}
+
 // Result of a rebuilt leaf: unchanged / Null / filled leaf, or a dedup candidate (kNull).
 __device__ __forceinline__ u32 leaf_result(const DevPool &P, u64 bits, u64 bits0, u32 old, bool *cand) {
 	*cand = false;
@@ -496,49 +504,32 @@ __global__ void __launch_bounds__(kBlock) k_leafparent_short(DevPool P, Workspac
 		}
 		const bool mine = valid && len <= T && list_ok(W, off, len);
 		u32 old[8], res[8];
-		u64 bits[8];
-		u32 cand_mask = 0;
-		if (mine) {
+		if (mine)
 			base_children(P, l, b, old);
-			u64 bits0[8];
-#pragma unroll
-			for (int c = 0; c < 8; ++c) {
-				bits[c] = leaf_bits(P, old[c]);
-				bits0[c] = bits[c];
+#pragma unroll 1
+		for (u32 c = 0; c < 8; ++c) { // not unrolled: one copy of the leaf code keeps the i-cache warm
+			u64 bits = 0;
+			bool cand = false;
+			if (mine) {
+				u32 cx, cy, cz;
+				child_pos(pos, c, cx, cy, cz);
+				const u64 b0 = leaf_bits(P, old[c]);
+				bits = rebuild_leaf(W, off, len, cx, cy, cz, b0);
+				res[c] = leaf_result(P, bits, b0, old[c], &cand);
 			}
-			for (u32 p = 0; p < len; ++p) {
-				const hd_edit_desc e = W.edits[W.lists[off + p]];
-#pragma unroll
-				for (u32 c = 0; c < 8; ++c) {
-					u32 cx, cy, cz;
-					child_pos(pos, c, cx, cy, cz);
-					bits[c] = apply_edit_leaf(e, cx, cy, cz, bits[c]);
+			const u64 ci = warp_reserve(&W.ctr[kWsItems + L - 1], cand ? 1u : 0u);
+			if (cand) {
+				if (ci < W.leaf.cap) {
+					W.leaf_new[ci] = bits;
+					W.leaf.parent[ci] = (u32)(i * 8u + c);
+					W.leaf.state[ci] = kStCand;
+				} else {
+					ws_error(W, kErrCapacity);
 				}
 			}
-#pragma unroll
-			for (int c = 0; c < 8; ++c) {
-				bool cand;
-				res[c] = leaf_result(P, bits[c], bits0[c], old[c], &cand);
-				cand_mask |= (cand ? 1u : 0u) << c;
-			}
 		}
-		const u64 c0 = warp_reserve(&W.ctr[kWsItems + L - 1], __popc(cand_mask));
 		if (!mine)
 			continue;
-		u64 ci = c0;
-#pragma unroll
-		for (int c = 0; c < 8; ++c) {
-			if (!((cand_mask >> c) & 1u))
-				continue;
-			if (ci < W.leaf.cap) {
-				W.leaf_new[ci] = bits[c];
-				W.leaf.parent[ci] = (u32)(i * 8u + c);
-				W.leaf.state[ci] = kStCand;
-			} else {
-				ws_error(W, kErrCapacity);
-			}
-			++ci;
-		}
 		uint4 *bc = reinterpret_cast<uint4 *>(W.bchild + i * 8u);
 		uint4 *cn = reinterpret_cast<uint4 *>(W.cnew + i * 8u);
 		bc[0] = make_uint4(old[0], old[1], old[2], old[3]);
@@ -637,7 +628,7 @@ __global__ void __launch_bounds__(kLongBlock) k_root(DevPool P, Workspace W, u32
 	if (root != kNull) {
 		const u64 vp = root >> P.cfg.wbpp;
 		const u32 phys = vp < P.total_pages ? P.page_table[vp] : kUnallocPage;
-		if (phys == kUnallocPage || phys == kZeroPage) {
+		if (phys == kUnallocPage || page_lost(P, phys)) {
 			if (threadIdx.x == 0) {
 				W.ctr[kWsRoot] = root;
 				ws_error(W, kErrInvalidRoot);
@@ -731,9 +722,11 @@ __device__ __forceinline__ bool reserve(const DevPool &P, Workspace &W, u32 b, u
 	}
 	*pad_out = off != old ? old : kNull;
 	const u32 vpage = (b << P.cfg.pbpb) | (off >> P.cfg.wbpp);
-	if ((off & (wp - 1u)) == 0u) {
+	if ((off & (wp - 1u)) == 0u) { // this node opens the page
 		u32 phys = atomicAdd(&P.counters[kCtrHeapNext], 1u);
-		if (phys >= P.heap_pages) {
+		if (P.identity)
+			phys = vpage;
+		else if (phys >= P.heap_pages) {
 			phys = kZeroPage;
 			set_error(&P.counters[kCtrError], kErrOom);
 		}
@@ -801,11 +794,22 @@ __device__ __forceinline__ void warp_count(unsigned long long *ctr, u32 v) {
 
 // ------------------------------------------------------------------ k_probe
 // Leaf: the leaf candidates.  Inner: the level-l items, rebuilt from cnew.
+// Leaves repeat a few patterns many times: each block keeps a direct-mapped
+// shared-memory cache of leaf bits -> pointer for leaves found resident, so
+// repeated patterns are answered without touching the index.
+static constexpr u32 kLeafCache = 2048;
 template <bool Leaf>
 __global__ void __launch_bounds__(kBlock) k_probe(DevPool P, Workspace W, u32 l) {
 	if (ws_failed(W))
 		return;
 	__shared__ int s_skip;
+	__shared__ unsigned long long s_key[Leaf ? kLeafCache : 1];
+	__shared__ u32 s_val[Leaf ? kLeafCache : 1];
+	if (Leaf)
+		for (u32 e = threadIdx.x; e < kLeafCache; e += blockDim.x) {
+			s_key[e] = 0ull; // no leaf candidate is all-empty
+			s_val[e] = kNull;
+		}
 	if (threadIdx.x == 0)
 		s_skip = pool_failed(P) ? 1 : 0;
 	__syncthreads();
@@ -872,13 +876,25 @@ __global__ void __launch_bounds__(kBlock) k_probe(DevPool P, Workspace W, u32 l)
 				}
 			}
 		}
+		// cached leaf: found without a probe
+		bool hit = false;
+		u32 hit_ptr = kNull, slot_e = 0;
+		if (Leaf && cand) {
+			const u64 bits = (u64)nw.w[0] | ((u64)nw.w[1] << 32);
+			slot_e = (h ^ (h >> 13)) & (kLeafCache - 1u);
+			if (s_key[slot_e] == bits) {
+				hit_ptr = *(volatile u32 *)&s_val[slot_e];
+				hit = hit_ptr != kNull;
+			}
+		}
+		const bool probe_me = cand && !hit;
 		// merge equal candidates of the warp: one leader probes, the others follow
-		const unsigned long long key = cand ? (unsigned long long)h : (0x100000000ull | lane);
+		const unsigned long long key = probe_me ? (unsigned long long)h : (0x100000000ull | lane);
 		const u32 same = __match_any_sync(kFullMask, key);
 		const u32 leader = __ffs(same) - 1u;
 		// every lane executes every shuffle (no short-circuit around a full-mask shuffle)
 		const u32 leader_n = __shfl_sync(kFullMask, nw.n, leader);
-		bool eq = cand && leader != lane && leader_n == nw.n;
+		bool eq = probe_me && leader != lane && leader_n == nw.n;
 #pragma unroll
 		for (int k = 0; k < 9; ++k) {
 			const u32 lw = __shfl_sync(kFullMask, nw.w[k], leader);
@@ -887,7 +903,7 @@ __global__ void __launch_bounds__(kBlock) k_probe(DevPool P, Workspace W, u32 l)
 		const bool follower = eq;
 		Outcome o = {kStFail, kNull, kNull, kNull};
 		u32 probes = 0;
-		if (cand && !follower) {
+		if (probe_me && !follower) {
 			const u32 bucket = bbase + ((zero_hash ? 0u : h) & nb_mask);
 			if (Leaf) {
 				const u64 mine = W.leaf_new[i];
@@ -913,6 +929,13 @@ __global__ void __launch_bounds__(kBlock) k_probe(DevPool P, Workspace W, u32 l)
 				o = {kStFail, kNull, kNull, kNull};
 			else
 				o = {lst, lres, llink, kNull};
+		}
+		if (hit)
+			o = {kStFound, hit_ptr, kNull, kNull};
+		else if (Leaf && probe_me && !follower && o.state == kStFound) {
+			const u64 bits = (u64)nw.w[0] | ((u64)nw.w[1] << 32);
+			if (s_key[slot_e] == 0ull && atomicCAS(&s_key[slot_e], 0ull, (unsigned long long)bits) == 0ull)
+				*(volatile u32 *)&s_val[slot_e] = o.res;
 		}
 		if (cand) {
 			it.state[i] = o.state;
@@ -966,7 +989,7 @@ __global__ void __launch_bounds__(kBlock) k_commit(DevPool P, Workspace W, u32 l
 				r = it.res[i];
 				const u32 slot = it.link[i];
 				const u32 phys = P.page_table[r >> P.cfg.wbpp];
-				if (phys == kZeroPage) {
+				if (page_lost(P, phys)) {
 					P.index[slot] = kSlotTomb;
 					r = kNull;
 					break;
@@ -994,7 +1017,7 @@ __global__ void __launch_bounds__(kBlock) k_commit(DevPool P, Workspace W, u32 l
 					if (pad != kNull) {
 						const u32 vp = ((r >> bucket_shift) << P.cfg.pbpb) | (pad >> P.cfg.wbpp);
 						const u32 zp = P.page_table[vp];
-						if (zp != kUnallocPage && zp != kZeroPage) {
+						if (zp != kUnallocPage && !page_lost(P, zp)) {
 							u32 *z = P.heap + ((u64)zp << P.cfg.wbpp);
 							for (u32 q = pad & (wp - 1u); q < wp; ++q)
 								z[q] = 0u;
