@@ -296,6 +296,7 @@ struct Workspace {
 	u32 *lists;        // edit lists
 	u64 list_cap;
 	u32 *long_q;       // per inner level: items with long edit lists (same index space as inner)
+	u64 *leafcand;     // [inner.cap] level-(L-2) items: first leaf candidate | child mask << 32
 	const hd_edit_desc *edits;
 	u32 n_edits;
 	u32 long_threshold; // lists longer than this are expanded by a block (inner) or a warp (level L-2)

@@ -90,13 +90,13 @@ hd_status alloc_items(hd_ws_host &ws, Items &it, uint64_t cap) {
 	return HD_OK;
 }
 
-// Leaf candidates carry only parent slot, result, state and link (bits in leaf_new).
+// Leaf candidates carry only result, state and link (bits in leaf_new); the
+// level-(L-2) node finds its candidates through Workspace::leafcand.
 hd_status alloc_leaf_candidates(hd_ws_host &ws, Items &it, uint64_t cap) {
 	it = Items{};
 	it.cap = cap;
 	hd_status s;
-	if ((s = ws_alloc(ws, &it.parent, cap)) || (s = ws_alloc(ws, &it.res, cap)) || (s = ws_alloc(ws, &it.state, cap)) ||
-	    (s = ws_alloc(ws, &it.link, cap)))
+	if ((s = ws_alloc(ws, &it.res, cap)) || (s = ws_alloc(ws, &it.state, cap)) || (s = ws_alloc(ws, &it.link, cap)))
 		return s;
 	return HD_OK;
 }
@@ -121,7 +121,8 @@ hd_status ws_reserve(hd_pool *pool, uint64_t inner_cap, uint64_t leaf_cap, uint6
 	if ((s = alloc_items(ws, d.inner, inner_cap)) || (s = alloc_leaf_candidates(ws, d.leaf, leaf_cap)) ||
 	    (s = ws_alloc(ws, &d.bchild, inner_cap * 8)) || (s = ws_alloc(ws, &d.cnew, inner_cap * 8)) ||
 	    (s = ws_alloc(ws, &d.leaf_new, leaf_cap)) || (s = ws_alloc(ws, &d.lists, list_cap)) ||
-	    (s = ws_alloc(ws, &d.long_q, inner_cap)) || (s = ws_alloc(ws, &d.ctr, (uint64_t)kWsCtrCount)) ||
+	    (s = ws_alloc(ws, &d.long_q, inner_cap)) || (s = ws_alloc(ws, &d.leafcand, inner_cap)) ||
+	    (s = ws_alloc(ws, &d.ctr, (uint64_t)kWsCtrCount)) ||
 	    (s = ws_alloc(ws, &ws.edits, (uint64_t)edit_cap))) {
 		ws_free_all(ws);
 		return s;
@@ -535,7 +536,8 @@ hd_status upsert_impl(hd_pool *pool, uint32_t level, const uint32_t *words, cons
 	ctr[kWsItems + level] = n;
 	HD_TRY(cudaStreamWaitEvent(st, pool->ws_free, 0));
 	HD_TRY(cudaMemcpyAsync(W.ctr, ctr.data(), kWsCtrCount * 8, cudaMemcpyHostToDevice, st));
-	HD_TRY(cudaMemcpyAsync(it.parent, parents.data(), n * 4ull, cudaMemcpyHostToDevice, st));
+	if (!leaf)
+		HD_TRY(cudaMemcpyAsync(it.parent, parents.data(), n * 4ull, cudaMemcpyHostToDevice, st));
 	if (leaf) {
 		HD_TRY(cudaMemcpyAsync(W.leaf_new, leafbits.data(), n * 8ull, cudaMemcpyHostToDevice, st));
 		HD_TRY(cudaMemcpyAsync(it.state, states.data(), n * 4ull, cudaMemcpyHostToDevice, st));

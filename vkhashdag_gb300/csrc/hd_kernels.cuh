@@ -481,8 +481,35 @@ __device__ __forceinline__ u32 leaf_result(const DevPool &P, u64 bits, u64 bits0
 	return kNull;
 }
 
+// Read-only lookup of a leaf among the resident nodes.  No slot is pending
+// while the leaves are rebuilt, so a committed entry with equal bits is the
+// node; a short walk that misses leaves the leaf to the claiming probe.
+__device__ __forceinline__ u32 lookup_leaf(const DevPool &P, u64 bits) {
+	const u32 L = P.cfg.L, l = L - 1;
+	const u32 h = hash_leaf(bits);
+	const u32 bucket = P.cfg.bucket_base[l] + ((P.cfg.hasher == HD_HASHER_ZERO ? 0u : h) & ((1u << P.cfg.bucket_bits[l]) - 1u));
+	const u32 bucket_shift = P.cfg.wbpp + P.cfg.pbpb;
+	const u64 mask = P.index_mask;
+	const unsigned long long tag = h & 0x7FFFFFFFu;
+	u64 s = index_start(h, l, mask);
+	for (u32 probe = 0; probe < 32u; ++probe, s = (s + 1) & mask) {
+		const unsigned long long v = __ldg(&P.index[s]);
+		if (v == kSlotEmpty)
+			return kNull;
+		if ((v >> 63) || ((v >> 32) & 0x7FFFFFFFull) != tag)
+			continue;
+		const u32 val = (u32)v;
+		if ((val >> bucket_shift) != bucket)
+			continue;
+		const u32 *p = node_addr(P, val);
+		if (p[0] == (u32)bits && p[1] == (u32)(bits >> 32))
+			return val;
+	}
+	return kNull;
+}
+
 // Thread per level-(L-2) node with a short edit list: computes its 8 leaves.
-__global__ void __launch_bounds__(kBlock) k_leafparent_short(DevPool P, Workspace W) {
+__global__ void __launch_bounds__(kBlock, 3) k_leafparent_short(DevPool P, Workspace W) {
 	if (ws_failed(W))
 		return;
 	const u32 L = P.cfg.L, l = L - 2;
@@ -504,32 +531,46 @@ __global__ void __launch_bounds__(kBlock) k_leafparent_short(DevPool P, Workspac
 		}
 		const bool mine = valid && len <= T && list_ok(W, off, len);
 		u32 old[8], res[8];
-		if (mine)
+		u64 cb[8];
+		u32 cand_mask = 0;
+		if (mine) {
 			base_children(P, l, b, old);
 #pragma unroll 1
-		for (u32 c = 0; c < 8; ++c) { // not unrolled: one copy of the leaf code keeps the i-cache warm
-			u64 bits = 0;
-			bool cand = false;
-			if (mine) {
+			for (u32 c = 0; c < 8; ++c) { // not unrolled: one copy of the leaf code keeps the i-cache warm
 				u32 cx, cy, cz;
 				child_pos(pos, c, cx, cy, cz);
 				const u64 b0 = leaf_bits(P, old[c]);
-				bits = rebuild_leaf(W, off, len, cx, cy, cz, b0);
-				res[c] = leaf_result(P, bits, b0, old[c], &cand);
-			}
-			const u64 ci = warp_reserve(&W.ctr[kWsItems + L - 1], cand ? 1u : 0u);
-			if (cand) {
-				if (ci < W.leaf.cap) {
-					W.leaf_new[ci] = bits;
-					W.leaf.parent[ci] = (u32)(i * 8u + c);
-					W.leaf.state[ci] = kStCand;
-				} else {
-					ws_error(W, kErrCapacity);
+				const u64 bits = rebuild_leaf(W, off, len, cx, cy, cz, b0);
+				bool cand;
+				u32 r = leaf_result(P, bits, b0, old[c], &cand);
+				if (cand) {
+					r = lookup_leaf(P, bits);
+					if (r == kNull) {
+						cb[c] = bits;
+						cand_mask |= 1u << c;
+					}
 				}
+				res[c] = r;
 			}
 		}
+		// the node's leaf candidates are contiguous, in child order
+		const u64 c0 = warp_reserve(&W.ctr[kWsItems + L - 1], __popc(cand_mask));
 		if (!mine)
 			continue;
+		u64 ci = c0;
+#pragma unroll 1
+		for (u32 c = 0; c < 8; ++c) {
+			if (!((cand_mask >> c) & 1u))
+				continue;
+			if (ci < W.leaf.cap) {
+				W.leaf_new[ci] = cb[c];
+				W.leaf.state[ci] = kStCand;
+			} else {
+				ws_error(W, kErrCapacity);
+			}
+			++ci;
+		}
+		W.leafcand[i] = c0 | ((u64)cand_mask << 32);
 		uint4 *bc = reinterpret_cast<uint4 *>(W.bchild + i * 8u);
 		uint4 *cn = reinterpret_cast<uint4 *>(W.cnew + i * 8u);
 		bc[0] = make_uint4(old[0], old[1], old[2], old[3]);
@@ -595,23 +636,38 @@ __global__ void __launch_bounds__(kBlock) k_leafparent_long(DevPool P, Workspace
 #pragma unroll
 		for (u32 s = 0; s < 4; ++s)
 			bits |= (u64)__shfl_sync(kFullMask, mine, (lane & ~3u) | s) << (16u * s);
-		bool cand = false;
-		const u32 r = leaf_result(P, bits, b0, old[c], &cand);
 		const bool lead = q == 0;
-		const u64 ci = warp_reserve(&W.ctr[kWsItems + L - 1], lead && cand ? 1u : 0u);
+		bool cand = false;
+		u32 r = leaf_result(P, bits, b0, old[c], &cand);
+		if (lead && cand) {
+			r = lookup_leaf(P, bits);
+			cand = r == kNull;
+		}
+		cand = lead && cand;
+		const u32 cmask_lanes = __ballot_sync(kFullMask, cand); // bit 4c set for candidate child c
+		u32 cmask = 0;
+#pragma unroll
+		for (u32 k = 0; k < 8; ++k)
+			cmask |= ((cmask_lanes >> (4u * k)) & 1u) << k;
+		unsigned long long c0 = 0;
+		if (lane == 0 && cmask)
+			c0 = atomicAdd(&W.ctr[kWsItems + L - 1], (unsigned long long)__popc(cmask));
+		c0 = __shfl_sync(kFullMask, c0, 0);
 		if (lead) {
 			if (cand) {
+				const u64 ci = c0 + __popc(cmask & ((1u << c) - 1u));
 				if (ci < W.leaf.cap) {
 					W.leaf_new[ci] = bits;
-					W.leaf.parent[ci] = (u32)(i * 8u + c);
 					W.leaf.state[ci] = kStCand;
 				} else {
 					ws_error(W, kErrCapacity);
 				}
 			}
 			W.bchild[i * 8u + c] = old[c];
-			W.cnew[i * 8u + c] = r;
+			W.cnew[i * 8u + c] = cand ? kNull : r;
 		}
+		if (lane == 0)
+			W.leafcand[i] = c0 | ((u64)cmask << 32);
 	}
 }
 
@@ -660,10 +716,9 @@ __global__ void __launch_bounds__(kLongBlock) k_root(DevPool P, Workspace W, u32
 			bool cand;
 			const u32 r = leaf_result(P, bits, b0, root, &cand);
 			W.ctr[kWsRoot] = r;
-			if (cand) {
+			if (cand) { // the root leaf is the only candidate; its commit reports the root
 				W.ctr[kWsItems + 0] = 1;
 				W.leaf_new[0] = bits;
-				W.leaf.parent[0] = kNull;
 				W.leaf.state[0] = kStCand;
 			}
 		}
@@ -847,9 +902,26 @@ __global__ void __launch_bounds__(kBlock) k_probe(DevPool P, Workspace W, u32 l)
 				h = hash_leaf(bits);
 				cand = true;
 			} else {
-				const uint4 *cn4 = reinterpret_cast<const uint4 *>(W.cnew + i * 8u);
+				uint4 *cn4 = reinterpret_cast<uint4 *>(W.cnew + i * 8u);
 				const uint4 *bc4 = reinterpret_cast<const uint4 *>(W.bchild + i * 8u);
-				const uint4 a0 = cn4[0], a1 = cn4[1], b0 = bc4[0], b1 = bc4[1];
+				uint4 a0 = cn4[0], a1 = cn4[1];
+				const uint4 b0 = bc4[0], b1 = bc4[1];
+				if (l == L - 2) { // pick up the results of this node's leaf candidates
+					const u64 lc = W.leafcand[i];
+					const u32 cm = (u32)(lc >> 32);
+					if (cm) {
+						u32 cc[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+						u32 k = (u32)lc;
+#pragma unroll
+						for (int q = 0; q < 8; ++q)
+							if ((cm >> q) & 1u)
+								cc[q] = W.leaf.res[k++];
+						a0 = make_uint4(cc[0], cc[1], cc[2], cc[3]);
+						a1 = make_uint4(cc[4], cc[5], cc[6], cc[7]);
+						cn4[0] = a0; // the commit writes the node from cnew
+						cn4[1] = a1;
+					}
+				}
 				const u32 c[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
 				if (a0.x == b0.x && a0.y == b0.y && a0.z == b0.z && a0.w == b0.w && a1.x == b1.x && a1.y == b1.y &&
 				    a1.z == b1.z && a1.w == b1.w) {
@@ -1037,11 +1109,16 @@ __global__ void __launch_bounds__(kBlock) k_commit(DevPool P, Workspace W, u32 l
 				break;
 			}
 			it.res[i] = r;
-			const u32 ps = it.parent[i];
-			if (ps == kNull)
-				W.ctr[kWsRoot] = r;
-			else
-				W.cnew[ps] = r;
+			if (Leaf) {
+				if (L == 1) // the root leaf
+					W.ctr[kWsRoot] = r;
+			} else {
+				const u32 ps = it.parent[i];
+				if (ps == kNull)
+					W.ctr[kWsRoot] = r;
+				else
+					W.cnew[ps] = r;
+			}
 		}
 		warp_count(&W.ctr[kWsIns + l], ins);
 		warp_count(&W.ctr[kWsInsWords + l], insw);
