@@ -521,7 +521,20 @@ static inline uint64_t mix64(uint64_t x) {
 struct Canon {
 	std::vector<uint64_t> counts, digests;
 	bool ok = true;
+	int bad_level = -1; // first level holding an invalid pointer
 };
+
+// A pointer names a node of `level` if it lies below its bucket's word count,
+// in a bucket of that level, on a page that exists.
+static bool valid_ptr(const Pool &pool, Word ptr, Word level) {
+	const Word wbb = pool.cfg.wbpp + pool.cfg.pbpb;
+	const uint64_t bucket = ptr >> wbb;
+	if (bucket < pool.bases[level] || bucket >= uint64_t(pool.bases[level]) + pool.cfg.buckets_at(level))
+		return false;
+	if ((ptr & ((Word(1) << wbb) - 1u)) >= pool.bucket_words[bucket])
+		return false;
+	return (ptr >> pool.cfg.wbpp) < pool.pages.size() && pool.pages[ptr >> pool.cfg.wbpp] != nullptr;
+}
 
 static Canon canonical(const Pool &pool, Word root) {
 	Word L = pool.cfg.node_levels();
@@ -530,6 +543,11 @@ static Canon canonical(const Pool &pool, Word root) {
 	c.digests.assign(L, 0);
 	if (root == kNull)
 		return c;
+	if (!valid_ptr(pool, root, 0)) {
+		c.ok = false;
+		c.bad_level = 0;
+		return c;
+	}
 	// reachable node pointers per level
 	std::vector<std::vector<Word>> lv(L);
 	lv[0].push_back(root);
@@ -538,9 +556,15 @@ static Canon canonical(const Pool &pool, Word root) {
 		for (Word p : lv[l]) {
 			const Word *n = pool.read_node(p);
 			Word k = std::popcount(n[0] & 0xFFu);
-			for (Word j = 0; j < k; ++j)
+			for (Word j = 0; j < k; ++j) {
+				if (!valid_ptr(pool, n[1 + j], l + 1)) {
+					c.ok = false;
+					c.bad_level = l + 1;
+					return c;
+				}
 				if (seen.insert(n[1 + j]).second)
 					lv[l + 1].push_back(n[1 + j]);
+			}
 		}
 	}
 	std::unordered_map<Word, Word> rank_below, rank_here;
@@ -842,6 +866,8 @@ void orc_pool_load(orc_pool *p, const uint32_t *bucket_words, const uint32_t *pa
 // is fully reduced (no duplicate node content on a level) and well formed.
 int orc_canonical(const orc_pool *p, uint32_t root, uint64_t *counts, uint64_t *digests) {
 	orc::Canon c = orc::canonical(p->pool, root);
+	if (c.bad_level >= 0)
+		counts[0] = ~0ull - uint64_t(c.bad_level); // marks where the walk stopped
 	for (size_t i = 0; i < c.counts.size(); ++i) {
 		counts[i] = c.counts[i];
 		digests[i] = c.digests[i];

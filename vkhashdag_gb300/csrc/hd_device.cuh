@@ -273,6 +273,7 @@ enum ItemState : u32 {
 	kStAlias = 4,     // result = res[link] (another item of the pass with equal content)
 	kStFail = 5,      // insertion failed (error recorded)
 	kStCand = 6,      // leaf candidate, dedup pending
+	kStDone = 7,      // level-(L-2) node resolved by the leaf kernel (result already in the parent's slot)
 };
 
 struct Items {
@@ -289,14 +290,14 @@ struct Items {
 };
 
 struct Workspace {
-	Items inner, leaf; // leaf: candidates (parent, res, state, link)
+	Items inner, leaf; // leaf: candidates (parent slot, res, state, link)
 	u32 *bchild;       // [inner.cap*8] children of the base node
 	u32 *cnew;         // [inner.cap*8] new children
 	u64 *leaf_new;     // [leaf.cap] bits of the leaf candidates
 	u32 *lists;        // edit lists
 	u64 list_cap;
 	u32 *long_q;       // per inner level: items with long edit lists (same index space as inner)
-	u64 *leafcand;     // [inner.cap] level-(L-2) items: first leaf candidate | child mask << 32
+	u32 *todo;         // [inner.cap] level-(L-2) items that still need the claiming probe
 	const hd_edit_desc *edits;
 	u32 n_edits;
 	u32 long_threshold; // lists longer than this are expanded by a block (inner) or a warp (level L-2)
@@ -321,6 +322,7 @@ enum WsCtr : u32 {
 	kWsMaxProbe = 68,   // longest index probe of the pass
 	kWsProbeSteps = 69, // index slots visited in the pass
 	kWsCasRetry = 70,   // failed bucket-count CAS attempts
+	kWsTodo = 71,       // entries in Workspace::todo
 	kWsCand = 96,
 	kWsCandWords = 128,
 	kWsIns = 160,

@@ -90,13 +90,13 @@ hd_status alloc_items(hd_ws_host &ws, Items &it, uint64_t cap) {
 	return HD_OK;
 }
 
-// Leaf candidates carry only result, state and link (bits in leaf_new); the
-// level-(L-2) node finds its candidates through Workspace::leafcand.
+// Leaf candidates carry parent slot, result, state and link (bits in leaf_new).
 hd_status alloc_leaf_candidates(hd_ws_host &ws, Items &it, uint64_t cap) {
 	it = Items{};
 	it.cap = cap;
 	hd_status s;
-	if ((s = ws_alloc(ws, &it.res, cap)) || (s = ws_alloc(ws, &it.state, cap)) || (s = ws_alloc(ws, &it.link, cap)))
+	if ((s = ws_alloc(ws, &it.parent, cap)) || (s = ws_alloc(ws, &it.res, cap)) || (s = ws_alloc(ws, &it.state, cap)) ||
+	    (s = ws_alloc(ws, &it.link, cap)))
 		return s;
 	return HD_OK;
 }
@@ -121,7 +121,7 @@ hd_status ws_reserve(hd_pool *pool, uint64_t inner_cap, uint64_t leaf_cap, uint6
 	if ((s = alloc_items(ws, d.inner, inner_cap)) || (s = alloc_leaf_candidates(ws, d.leaf, leaf_cap)) ||
 	    (s = ws_alloc(ws, &d.bchild, inner_cap * 8)) || (s = ws_alloc(ws, &d.cnew, inner_cap * 8)) ||
 	    (s = ws_alloc(ws, &d.leaf_new, leaf_cap)) || (s = ws_alloc(ws, &d.lists, list_cap)) ||
-	    (s = ws_alloc(ws, &d.long_q, inner_cap)) || (s = ws_alloc(ws, &d.leafcand, inner_cap)) ||
+	    (s = ws_alloc(ws, &d.long_q, inner_cap)) || (s = ws_alloc(ws, &d.todo, inner_cap)) ||
 	    (s = ws_alloc(ws, &d.ctr, (uint64_t)kWsCtrCount)) ||
 	    (s = ws_alloc(ws, &ws.edits, (uint64_t)edit_cap))) {
 		ws_free_all(ws);
@@ -267,17 +267,18 @@ hd_status launch_pass(hd_pool *pool, const hd_edit_desc *d_edits, uint32_t n, ui
 		}
 	}
 	mark();
-	k_probe<true><<<grid[L - 1], kBlock, 0, st>>>(P, W, L - 1);
+	k_probe<true><<<grid[L - 1], kBlock, 0, st>>>(P, W, L - 1, 0u);
 	dbg("probe_leaf", L - 1);
 	mark();
-	k_commit<true><<<grid[L - 1], kBlock, 0, st>>>(P, W, L - 1);
+	k_commit<true><<<grid[L - 1], kBlock, 0, st>>>(P, W, L - 1, 0u);
 	dbg("commit_leaf", L - 1);
 	mark();
 	for (uint32_t l = L - 1; l-- > 0;) {
-		k_probe<false><<<grid[l], kBlock, 0, st>>>(P, W, l);
+		const uint32_t todo = l + 2 == L ? 1u : 0u; // level L-2 runs over the unresolved nodes only
+		k_probe<false><<<grid[l], kBlock, 0, st>>>(P, W, l, todo);
 		dbg("probe", l);
 		mark();
-		k_commit<false><<<grid[l], kBlock, 0, st>>>(P, W, l);
+		k_commit<false><<<grid[l], kBlock, 0, st>>>(P, W, l, todo);
 		dbg("commit", l);
 		mark();
 	}
@@ -536,22 +537,21 @@ hd_status upsert_impl(hd_pool *pool, uint32_t level, const uint32_t *words, cons
 	ctr[kWsItems + level] = n;
 	HD_TRY(cudaStreamWaitEvent(st, pool->ws_free, 0));
 	HD_TRY(cudaMemcpyAsync(W.ctr, ctr.data(), kWsCtrCount * 8, cudaMemcpyHostToDevice, st));
-	if (!leaf)
-		HD_TRY(cudaMemcpyAsync(it.parent, parents.data(), n * 4ull, cudaMemcpyHostToDevice, st));
+	HD_TRY(cudaMemcpyAsync(it.parent, parents.data(), n * 4ull, cudaMemcpyHostToDevice, st));
+	HD_TRY(cudaMemcpyAsync(it.state, states.data(), n * 4ull, cudaMemcpyHostToDevice, st));
 	if (leaf) {
 		HD_TRY(cudaMemcpyAsync(W.leaf_new, leafbits.data(), n * 8ull, cudaMemcpyHostToDevice, st));
-		HD_TRY(cudaMemcpyAsync(it.state, states.data(), n * 4ull, cudaMemcpyHostToDevice, st));
 	} else {
 		HD_TRY(cudaMemcpyAsync(W.cnew, cnew.data(), n * 32ull, cudaMemcpyHostToDevice, st));
 		HD_TRY(cudaMemcpyAsync(W.bchild, bchild.data(), n * 32ull, cudaMemcpyHostToDevice, st));
 	}
 	const uint32_t grid = std::max(1u, std::min(ceil_div(n, kBlock), (uint32_t)pool->num_sms * 8u));
 	if (leaf) {
-		k_probe<true><<<grid, kBlock, 0, st>>>(pool->P, W, level);
-		k_commit<true><<<grid, kBlock, 0, st>>>(pool->P, W, level);
+		k_probe<true><<<grid, kBlock, 0, st>>>(pool->P, W, level, 0u);
+		k_commit<true><<<grid, kBlock, 0, st>>>(pool->P, W, level, 0u);
 	} else {
-		k_probe<false><<<grid, kBlock, 0, st>>>(pool->P, W, level);
-		k_commit<false><<<grid, kBlock, 0, st>>>(pool->P, W, level);
+		k_probe<false><<<grid, kBlock, 0, st>>>(pool->P, W, level, 0u);
+		k_commit<false><<<grid, kBlock, 0, st>>>(pool->P, W, level, 0u);
 	}
 	k_finish<<<1, 32, 0, st>>>(pool->P, W, nullptr);
 	pool->kernel_launches += 3;

@@ -508,6 +508,71 @@ __device__ __forceinline__ u32 lookup_leaf(const DevPool &P, u64 bits) {
 	return kNull;
 }
 
+// Read-only lookup of an inner node (packed words) at level l among the resident nodes.
+__device__ __forceinline__ u32 lookup_inner(const DevPool &P, u32 l, const u32 *w, u32 n, u32 h) {
+	const u32 bucket = P.cfg.bucket_base[l] + ((P.cfg.hasher == HD_HASHER_ZERO ? 0u : h) & ((1u << P.cfg.bucket_bits[l]) - 1u));
+	const u32 bucket_shift = P.cfg.wbpp + P.cfg.pbpb;
+	const u64 mask = P.index_mask;
+	const unsigned long long tag = h & 0x7FFFFFFFu;
+	u64 s = index_start(h, l, mask);
+	for (u32 probe = 0; probe < 32u; ++probe, s = (s + 1) & mask) {
+		const unsigned long long v = __ldg(&P.index[s]);
+		if (v == kSlotEmpty)
+			return kNull;
+		if ((v >> 63) || ((v >> 32) & 0x7FFFFFFFull) != tag)
+			continue;
+		const u32 val = (u32)v;
+		if ((val >> bucket_shift) != bucket)
+			continue;
+		const u32 *p = node_addr(P, val);
+		bool eq = true;
+		for (u32 k = 0; k < n; ++k)
+			eq = eq && p[k] == w[k];
+		if (eq)
+			return val;
+	}
+	return kNull;
+}
+
+// A level-(L-2) node whose 8 children are all known: unchanged, empty, or an
+// existing node found read-only.  Returns false if it needs the claiming probe.
+__device__ __forceinline__ bool resolve_node(const DevPool &P, u32 l, u32 base, const u32 old[8], const u32 res[8],
+                                             u32 *out) {
+	bool unchanged = true;
+	u32 mask = 0, w[9], k = 1;
+#pragma unroll
+	for (int c = 0; c < 8; ++c) {
+		unchanged = unchanged && res[c] == old[c];
+		if (res[c] != kNull) {
+			mask |= 1u << c;
+			w[k++] = res[c];
+		}
+	}
+	if (unchanged) {
+		*out = base;
+		return true;
+	}
+	if (!mask) {
+		*out = kNull;
+		return true;
+	}
+	w[0] = mask;
+	Murmur mm;
+	for (u32 q = 0; q < k; ++q)
+		mm.add(w[q]);
+	const u32 r = lookup_inner(P, l, w, k, mm.finish(k));
+	*out = r;
+	return r != kNull;
+}
+
+__device__ __forceinline__ void hand_to_parent(Workspace &W, u64 i, u32 r) {
+	const u32 ps = W.inner.parent[i];
+	if (ps == kNull)
+		W.ctr[kWsRoot] = r;
+	else
+		W.cnew[ps] = r;
+}
+
 // Thread per level-(L-2) node with a short edit list: computes its 8 leaves.
 __global__ void __launch_bounds__(kBlock, 3) k_leafparent_short(DevPool P, Workspace W) {
 	if (ws_failed(W))
@@ -553,8 +618,13 @@ __global__ void __launch_bounds__(kBlock, 3) k_leafparent_short(DevPool P, Works
 				res[c] = r;
 			}
 		}
+		// Every lane of the warp reaches both reservations below (lanes without
+		// a node of their own reserve 0).
+		u32 done = kNull;
+		const bool resolved = mine && !cand_mask && resolve_node(P, l, b, old, res, &done); // no dedup round trip
 		// the node's leaf candidates are contiguous, in child order
 		const u64 c0 = warp_reserve(&W.ctr[kWsItems + L - 1], __popc(cand_mask));
+		const u64 tq = warp_reserve(&W.ctr[kWsTodo], (mine && !resolved) ? 1u : 0u);
 		if (!mine)
 			continue;
 		u64 ci = c0;
@@ -564,13 +634,18 @@ __global__ void __launch_bounds__(kBlock, 3) k_leafparent_short(DevPool P, Works
 				continue;
 			if (ci < W.leaf.cap) {
 				W.leaf_new[ci] = cb[c];
+				W.leaf.parent[ci] = (u32)(i * 8u + c);
 				W.leaf.state[ci] = kStCand;
 			} else {
 				ws_error(W, kErrCapacity);
 			}
 			++ci;
 		}
-		W.leafcand[i] = c0 | ((u64)cand_mask << 32);
+		if (resolved) {
+			hand_to_parent(W, i, done);
+			continue;
+		}
+		W.todo[tq] = (u32)i;
 		uint4 *bc = reinterpret_cast<uint4 *>(W.bchild + i * 8u);
 		uint4 *cn = reinterpret_cast<uint4 *>(W.cnew + i * 8u);
 		bc[0] = make_uint4(old[0], old[1], old[2], old[3]);
@@ -658,6 +733,7 @@ __global__ void __launch_bounds__(kBlock) k_leafparent_long(DevPool P, Workspace
 				const u64 ci = c0 + __popc(cmask & ((1u << c) - 1u));
 				if (ci < W.leaf.cap) {
 					W.leaf_new[ci] = bits;
+					W.leaf.parent[ci] = (u32)(i * 8u + c);
 					W.leaf.state[ci] = kStCand;
 				} else {
 					ws_error(W, kErrCapacity);
@@ -667,7 +743,7 @@ __global__ void __launch_bounds__(kBlock) k_leafparent_long(DevPool P, Workspace
 			W.cnew[i * 8u + c] = cand ? kNull : r;
 		}
 		if (lane == 0)
-			W.leafcand[i] = c0 | ((u64)cmask << 32);
+			W.todo[atomicAdd(&W.ctr[kWsTodo], 1ull)] = (u32)i;
 	}
 }
 
@@ -716,9 +792,10 @@ __global__ void __launch_bounds__(kLongBlock) k_root(DevPool P, Workspace W, u32
 			bool cand;
 			const u32 r = leaf_result(P, bits, b0, root, &cand);
 			W.ctr[kWsRoot] = r;
-			if (cand) { // the root leaf is the only candidate; its commit reports the root
+			if (cand) { // the root leaf is the only candidate
 				W.ctr[kWsItems + 0] = 1;
 				W.leaf_new[0] = bits;
+				W.leaf.parent[0] = kNull;
 				W.leaf.state[0] = kStCand;
 			}
 		}
@@ -853,8 +930,23 @@ __device__ __forceinline__ void warp_count(unsigned long long *ctr, u32 v) {
 // shared-memory cache of leaf bits -> pointer for leaves found resident, so
 // repeated patterns are answered without touching the index.
 static constexpr u32 kLeafCache = 2048;
+// Item t of a level: the t-th entry of the todo list (level L-2) or of the level range.
+__device__ __forceinline__ u64 item_at(const Workspace &W, u32 use_todo, u64 begin, u64 t) {
+	return use_todo ? (u64)W.todo[t] : begin + t;
+}
+__device__ __forceinline__ void probe_range(const Workspace &W, u32 L, u32 l, u32 use_todo, u64 &begin, u64 &n) {
+	if (use_todo) {
+		begin = 0;
+		n = W.ctr[kWsTodo];
+		if (n > W.inner.cap)
+			n = W.inner.cap;
+		return;
+	}
+	level_range(W, L, l, begin, n);
+}
+
 template <bool Leaf>
-__global__ void __launch_bounds__(kBlock) k_probe(DevPool P, Workspace W, u32 l) {
+__global__ void __launch_bounds__(kBlock) k_probe(DevPool P, Workspace W, u32 l, u32 use_todo) {
 	if (ws_failed(W))
 		return;
 	__shared__ int s_skip;
@@ -871,7 +963,7 @@ __global__ void __launch_bounds__(kBlock) k_probe(DevPool P, Workspace W, u32 l)
 	const bool skip = s_skip != 0;
 	const u32 L = P.cfg.L;
 	u64 begin, n;
-	level_range(W, L, l, begin, n);
+	probe_range(W, L, l, use_todo, begin, n);
 	Items &it = Leaf ? W.leaf : W.inner;
 	const u32 nb_mask = (1u << P.cfg.bucket_bits[l]) - 1u;
 	const u32 bbase = P.cfg.bucket_base[l];
@@ -880,7 +972,7 @@ __global__ void __launch_bounds__(kBlock) k_probe(DevPool P, Workspace W, u32 l)
 	const u64 stride = (u64)gridDim.x * blockDim.x;
 	for (u64 w0 = (u64)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); w0 < n; w0 += stride) {
 		const u64 t = w0 + lane;
-		const u64 i = begin + t;
+		const u64 i = t < n ? item_at(W, use_todo, begin, t) : 0;
 		bool cand = false;
 		NodeWords nw;
 		nw.n = 0;
@@ -902,26 +994,10 @@ __global__ void __launch_bounds__(kBlock) k_probe(DevPool P, Workspace W, u32 l)
 				h = hash_leaf(bits);
 				cand = true;
 			} else {
-				uint4 *cn4 = reinterpret_cast<uint4 *>(W.cnew + i * 8u);
+				const uint4 *cn4 = reinterpret_cast<const uint4 *>(W.cnew + i * 8u);
 				const uint4 *bc4 = reinterpret_cast<const uint4 *>(W.bchild + i * 8u);
-				uint4 a0 = cn4[0], a1 = cn4[1];
+				const uint4 a0 = cn4[0], a1 = cn4[1];
 				const uint4 b0 = bc4[0], b1 = bc4[1];
-				if (l == L - 2) { // pick up the results of this node's leaf candidates
-					const u64 lc = W.leafcand[i];
-					const u32 cm = (u32)(lc >> 32);
-					if (cm) {
-						u32 cc[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-						u32 k = (u32)lc;
-#pragma unroll
-						for (int q = 0; q < 8; ++q)
-							if ((cm >> q) & 1u)
-								cc[q] = W.leaf.res[k++];
-						a0 = make_uint4(cc[0], cc[1], cc[2], cc[3]);
-						a1 = make_uint4(cc[4], cc[5], cc[6], cc[7]);
-						cn4[0] = a0; // the commit writes the node from cnew
-						cn4[1] = a1;
-					}
-				}
 				const u32 c[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
 				if (a0.x == b0.x && a0.y == b0.y && a0.z == b0.z && a0.w == b0.w && a1.x == b1.x && a1.y == b1.y &&
 				    a1.z == b1.z && a1.w == b1.w) {
@@ -1027,12 +1103,12 @@ __global__ void __launch_bounds__(kBlock) k_probe(DevPool P, Workspace W, u32 l)
 
 // ------------------------------------------------------------------ k_commit
 template <bool Leaf>
-__global__ void __launch_bounds__(kBlock) k_commit(DevPool P, Workspace W, u32 l) {
+__global__ void __launch_bounds__(kBlock) k_commit(DevPool P, Workspace W, u32 l, u32 use_todo) {
 	if (ws_failed(W))
 		return;
 	const u32 L = P.cfg.L;
 	u64 begin, n;
-	level_range(W, L, l, begin, n);
+	probe_range(W, L, l, use_todo, begin, n);
 	Items &it = Leaf ? W.leaf : W.inner;
 	const u32 wp = wpp(P.cfg);
 	const u32 bucket_shift = P.cfg.wbpp + P.cfg.pbpb;
@@ -1041,7 +1117,7 @@ __global__ void __launch_bounds__(kBlock) k_commit(DevPool P, Workspace W, u32 l
 		const u64 t = w0 + lane_id();
 		u32 ins = 0, insw = 0;
 		if (t < n) {
-			const u64 i = begin + t;
+			const u64 i = item_at(W, use_todo, begin, t);
 			const u32 st = it.state[i];
 			u32 r;
 			switch (st) {
@@ -1109,16 +1185,11 @@ __global__ void __launch_bounds__(kBlock) k_commit(DevPool P, Workspace W, u32 l
 				break;
 			}
 			it.res[i] = r;
-			if (Leaf) {
-				if (L == 1) // the root leaf
-					W.ctr[kWsRoot] = r;
-			} else {
-				const u32 ps = it.parent[i];
-				if (ps == kNull)
-					W.ctr[kWsRoot] = r;
-				else
-					W.cnew[ps] = r;
-			}
+			const u32 ps = it.parent[i];
+			if (ps == kNull)
+				W.ctr[kWsRoot] = r;
+			else
+				W.cnew[ps] = r;
 		}
 		warp_count(&W.ctr[kWsIns + l], ins);
 		warp_count(&W.ctr[kWsInsWords + l], insw);
