@@ -200,6 +200,25 @@ uint64_t hd_pool_kernel_launches(const hd_pool *pool);
 hd_status hd_upsert(hd_pool *pool, uint32_t level, const uint32_t *words, const uint32_t *lens, uint32_t n,
                     uint32_t *out_ptrs);
 
+/* Find-or-insert without any allocation (no counterpart in the reference).
+ * For callers that cannot call cudaMalloc when they insert nodes -- e.g. an
+ * application that gives all device memory to its own allocator up front, or
+ * an edit loop that must not take the device synchronisation a cudaMalloc /
+ * cudaFree can cause.  Same result as hd_upsert, but device inputs and
+ * outputs, stream-ordered, no host synchronisation, and the per-node scratch
+ * in a static device array of the library (about 5.5 MB, held by every GPU
+ * that loads the library until the process exits) instead of the pool's
+ * workspace.  d_nodes: n nodes on the device, 8 child pointers each (Null =
+ * 0xFFFFFFFF, child order) below the leaf level, 2 words each at the leaf
+ * level.  d_out_ptrs: n pointers (device).  At most 65536 nodes per call;
+ * larger n returns HD_ERR_INVALID_ARG without running anything.  Failures
+ * inside the kernels go to the pool's sticky error (hd_pool_get_error).  The
+ * first call on a device looks up the array's device address (make it before
+ * any stream capture).  All calls on a device share the one array: calls that
+ * overlap on the GPU race. */
+hd_status hd_upsert_noalloc(hd_pool *pool, uint32_t level, const uint32_t *d_nodes, uint32_t n, uint32_t *d_out_ptrs,
+                            void *stream);
+
 /* ---- host mirror (reference storage hooks) --------------------------------
  * GetBucketRefWords / ReadPage (include/hashdag/NodePool.hpp:22-29,
  * src/DAGNodePool.hpp:56-69).  Virtual page ids are the reference's page ids

@@ -97,6 +97,7 @@ def lib():
         "hd_pool_checkpoint": (I, [P]),
         "hd_pool_rollback": (I, [P, P]),
         "hd_upsert": (I, [P, U32, P, P, U32, P]),
+        "hd_upsert_noalloc": (I, [P, U32, P, U32, P, P]),
         "hd_edit_profile_begin": (I, [P, U32]),
         "hd_edit_profile_end": (I, [P, P, P]),
         "hd_pool_kernel_launches": (U64, [P]),

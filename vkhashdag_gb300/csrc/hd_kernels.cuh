@@ -194,7 +194,7 @@ __device__ __forceinline__ void write_child_list_thread(const Workspace &W, u32 
 // ------------------------------------------------------------------ k_expand_short
 // Thread per level-l inner node (l <= L-3) with an edit list of at most
 // long_threshold edits.  Children are inner items of level l+1.
-__global__ void __launch_bounds__(kBlock) k_expand_short(DevPool P, Workspace W, u32 l) {
+static __global__ void __launch_bounds__(kBlock) k_expand_short(DevPool P, Workspace W, u32 l) {
 	if (ws_failed(W)) // an earlier launch overflowed: some items were never written
 		return;
 	const u32 L = P.cfg.L;
@@ -402,7 +402,7 @@ __device__ void emit_child_block(Workspace &W, u32 cl, u64 child_begin, u32 pare
 
 // ------------------------------------------------------------------ k_expand_long
 // Block per (level-l node with a long edit list, child), l <= L-3.
-__global__ void __launch_bounds__(kLongBlock) k_expand_long(DevPool P, Workspace W, u32 l) {
+static __global__ void __launch_bounds__(kLongBlock) k_expand_long(DevPool P, Workspace W, u32 l) {
 	if (ws_failed(W))
 		return;
 	__shared__ u32 sm[40];
@@ -462,7 +462,7 @@ __device__ __forceinline__ u64 apply_edit_leaf(const hd_edit_desc &e, u32 lx, u3
 
 // New bits of one leaf after the edits of a list (kept out of line so the
 // caller keeps its 8 children in registers).
-__device__ __noinline__ u64 rebuild_leaf(const Workspace &W, u32 off, u32 len, u32 lx, u32 ly, u32 lz, u64 bits) {
+static __device__ __noinline__ u64 rebuild_leaf(const Workspace &W, u32 off, u32 len, u32 lx, u32 ly, u32 lz, u64 bits) {
 	for (u32 p = 0; p < len; ++p)
 		bits = apply_edit_leaf(W.edits[W.lists[off + p]], lx, ly, lz, bits);
 	return bits;
@@ -574,7 +574,7 @@ __device__ __forceinline__ void hand_to_parent(Workspace &W, u64 i, u32 r) {
 }
 
 // Thread per level-(L-2) node with a short edit list: computes its 8 leaves.
-__global__ void __launch_bounds__(kBlock, 3) k_leafparent_short(DevPool P, Workspace W) {
+static __global__ void __launch_bounds__(kBlock, 3) k_leafparent_short(DevPool P, Workspace W) {
 	if (ws_failed(W))
 		return;
 	const u32 L = P.cfg.L, l = L - 2;
@@ -658,7 +658,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_leafparent_short(DevPool P, Works
 // Warp per level-(L-2) node with a long edit list: lane = (leaf c = lane/4,
 // quarter q = lane%4) owns voxels 16q..16q+15 of leaf c and walks the whole
 // list in order.
-__global__ void __launch_bounds__(kBlock) k_leafparent_long(DevPool P, Workspace W) {
+static __global__ void __launch_bounds__(kBlock) k_leafparent_long(DevPool P, Workspace W) {
 	if (ws_failed(W))
 		return;
 	const u32 L = P.cfg.L, l = L - 2;
@@ -750,7 +750,7 @@ __global__ void __launch_bounds__(kBlock) k_leafparent_long(DevPool P, Workspace
 // ------------------------------------------------------------------ k_root
 // NodePool.hpp:405-414 edit_switch on the root for the whole list (one block).
 // With a single node level the root is a leaf and is rebuilt here directly.
-__global__ void __launch_bounds__(kLongBlock) k_root(DevPool P, Workspace W, u32 root_val, const u32 *root_ptr) {
+static __global__ void __launch_bounds__(kLongBlock) k_root(DevPool P, Workspace W, u32 root_val, const u32 *root_ptr) {
 	__shared__ u32 sm[40];
 	const u32 L = P.cfg.L;
 	const u32 root = root_ptr ? *root_ptr : root_val;
@@ -946,7 +946,7 @@ __device__ __forceinline__ void probe_range(const Workspace &W, u32 L, u32 l, u3
 }
 
 template <bool Leaf>
-__global__ void __launch_bounds__(kBlock) k_probe(DevPool P, Workspace W, u32 l, u32 use_todo) {
+static __global__ void __launch_bounds__(kBlock) k_probe(DevPool P, Workspace W, u32 l, u32 use_todo) {
 	if (ws_failed(W))
 		return;
 	__shared__ int s_skip;
@@ -1103,7 +1103,7 @@ __global__ void __launch_bounds__(kBlock) k_probe(DevPool P, Workspace W, u32 l,
 
 // ------------------------------------------------------------------ k_commit
 template <bool Leaf>
-__global__ void __launch_bounds__(kBlock) k_commit(DevPool P, Workspace W, u32 l, u32 use_todo) {
+static __global__ void __launch_bounds__(kBlock) k_commit(DevPool P, Workspace W, u32 l, u32 use_todo) {
 	if (ws_failed(W))
 		return;
 	const u32 L = P.cfg.L;
@@ -1197,7 +1197,7 @@ __global__ void __launch_bounds__(kBlock) k_commit(DevPool P, Workspace W, u32 l
 }
 
 // ------------------------------------------------------------------ k_finish
-__global__ void k_finish(DevPool P, Workspace W, u32 *out_root) {
+static __global__ void k_finish(DevPool P, Workspace W, u32 *out_root) {
 	if (threadIdx.x != 0)
 		return;
 	u64 ins = 0;
