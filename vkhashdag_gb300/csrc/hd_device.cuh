@@ -144,7 +144,24 @@ __device__ __forceinline__ u32 classify(const hd_edit_desc &e, u32 shift, u32 px
 		}
 		return out ? kClsNone : (in ? kClsFull : kClsPartial);
 	}
-	// SphereEditor::EditNode (src/main.cpp:77-106), same integer formulas
+	// SphereEditor::EditNode (src/main.cpp:77-106), same integer formulas.
+	// When every bound and the centre are <= 2^15, each distance is within
+	// +-2^15, each square <= 2^30 and each sum of three < 2^32, so 32-bit
+	// arithmetic is exact; clamping r2 to 2^32-1 keeps both comparisons exact.
+	if (((ub[0] | ub[1] | ub[2]) <= 0x8000u) && ((e.p0[0] | e.p0[1] | e.p0[2]) < 0x8000u)) {
+		const u32 r2c = e.r2 > 0xFFFFFFFFull ? 0xFFFFFFFFu : (u32)e.r2;
+		u32 mx32 = 0, mn32 = 0;
+#pragma unroll
+		for (int a = 0; a < 3; ++a) {
+			const int lbd = (int)lb[a] - (int)e.p0[a], ubd = (int)ub[a] - (int)e.p0[a];
+			const u32 l2 = (u32)(lbd * lbd), u2 = (u32)(ubd * ubd);
+			mx32 += l2 > u2 ? l2 : u2;
+			mn32 += (lbd > 0 ? l2 : 0u) + (ubd < 0 ? u2 : 0u);
+		}
+		if (mx32 <= r2c)
+			return kClsFull;
+		return mn32 > r2c ? kClsNone : kClsPartial;
+	}
 	u64 mx = 0, mn = 0;
 #pragma unroll
 	for (int a = 0; a < 3; ++a) {
