@@ -389,6 +389,199 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+# ---------------------------------------------------------------------- terrain + rays (configs 2 and 4)
+TERRAIN_RES = 16384
+TERRAIN_BITS = [10, 10, 10, 10, 10, 12, 14, 15, 16, 17, 18, 18, 16]
+
+
+def terrain_pool(hd, W, res, device):
+    from vkhashdag_gb300 import Config
+    cfg = Config(9, 2, list(TERRAIN_BITS)) if res == TERRAIN_RES else W.config_for_resolution(res, bottom_bits=16,
+                                                                                               top_levels=6)
+    pool = hd.NodePool(cfg, heap_pages=cfg.get_total_pages(), device=device)
+    cols = W.terrain_columns(res, 32, seed=0)
+    t0 = time.perf_counter()
+    root = pool.edit(hd.NULL, cols)  # one batched pass
+    t_build = time.perf_counter() - t0
+    return cfg, pool, cols, root, t_build
+
+
+def cameras(hd, W, res, n, seed=3, width=3840, height=2160, fov=np.pi / 3):
+    """Seeded pinhole cameras above the terrain (basis of Camera::GetLookSideUp)."""
+    cams = np.zeros(n, hd.CAMERA_DTYPE)
+    x = 0.1 + 0.8 * W.uniform(seed, 51, n)
+    z = 0.1 + 0.8 * W.uniform(seed, 52, n)
+    h = W.terrain_height(res, x * res, z * res, 0) / res
+    y = np.minimum(h + 0.05 + 0.15 * W.uniform(seed, 53, n), 0.99)
+    yaw = 2 * np.pi * W.uniform(seed, 54, n)
+    pitch = -(0.2 + 0.4 * W.uniform(seed, 55, n))
+    tg, aspect = np.tan(fov / 2), width / height
+    look = np.stack([np.cos(pitch) * np.sin(yaw), np.sin(pitch), np.cos(pitch) * np.cos(yaw)], 1)
+    side = np.stack([np.cos(yaw), np.zeros(n), -np.sin(yaw)], 1) * tg * aspect
+    up = np.cross(look, side)
+    up = up / np.linalg.norm(up, axis=1, keepdims=True) * tg
+    cams["position"] = np.stack([x, y, z], 1)
+    cams["look"], cams["side"], cams["up"] = look, side, up
+    return cams
+
+
+def host_rays(cams, width, height, rows):
+    """The pinhole rays of camera 0, pixel rows [0, rows), with the device's float32 operation order."""
+    c = cams[0]
+    px, py = np.meshgrid(np.arange(width, dtype=np.float32), np.arange(rows, dtype=np.float32))
+    u = ((px.ravel() + np.float32(0.5)) / np.float32(width)) * np.float32(2) - np.float32(1)
+    v = ((py.ravel() + np.float32(0.5)) / np.float32(height)) * np.float32(2) - np.float32(1)
+    dd = (c["look"][None, :] - c["side"][None, :] * u[:, None]) - c["up"][None, :] * v[:, None]
+    len2 = (dd[:, 0] * dd[:, 0] + dd[:, 1] * dd[:, 1]) + dd[:, 2] * dd[:, 2]
+    d = (dd * (np.float32(1) / np.sqrt(len2))[:, None]).astype(np.float32)
+    o = np.tile(c["position"], (len(u), 1)).astype(np.float32)
+    return o, d
+
+
+def run_rays(args):
+    import torch
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    build_if_needed()
+    import vkhashdag_gb300 as hd
+    from vkhashdag_gb300 import workloads as W
+    res, n_cams, width, height = args.resolution, args.cameras, args.width, args.height
+    cfg, pool, cols, root, t_build = terrain_pool(hd, W, res, local)
+    cams = cameras(hd, W, res, n_cams, width=width, height=height)
+    n_rays = n_cams * width * height
+    out = torch.empty(n_rays * 40, dtype=torch.uint8, device=f"cuda:{local}")
+    ctr = torch.zeros(3, dtype=torch.int64, device=f"cuda:{local}")
+    stream = torch.cuda.Stream(device=local)
+    sp = stream.cuda_stream
+    for _ in range(args.warmup):
+        pool.trace_pinhole_async(root, cams, width, height, out.data_ptr(), 0, sp)
+    torch.cuda.synchronize()
+    s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = pool.kernel_launches()
+    with ClockSampler(local) as clocks:
+        s0.record(stream)
+        for _ in range(args.steps):
+            pool.trace_pinhole_async(root, cams, width, height, out.data_ptr(), ctr.data_ptr(), sp)
+        s1.record(stream)
+        torch.cuda.synchronize()
+    ms = s0.elapsed_time(s1)
+    steps, reads, hits = (int(x) for x in ctr.cpu())
+    value = n_rays * args.steps / (ms / 1e3)
+    hbm, peak_kind = peaks()
+    alg = (reads * 4 + n_rays * args.steps * 40) / args.steps  # node words read + hit records written
+    achieved = alg / (ms / args.steps / 1e3) / 1e9
+    # e2e: host cameras in, hits back to pinned host memory
+    host = torch.empty(n_rays * 40, dtype=torch.uint8, pin_memory=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        pool.trace_pinhole_async(root, cams, width, height, out.data_ptr(), 0, sp)
+        with torch.cuda.stream(stream):
+            host.copy_(out, non_blocking=True)
+        stream.synchronize()
+    e2e = n_rays * args.steps / (time.perf_counter() - t0)
+    cpu = None
+    if not args.no_cpu:
+        import oracle
+        oracle.build()
+        bw, ids, pages = pool.download()
+        opool = oracle.OraclePool.from_config(cfg)
+        opool.load(bw, ids, pages, pool.filled_node_pointers())
+        o, d = host_rays(cams, width, height, args.cpu_rows)
+        threads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        ref = opool.trace(root, o, d, threads=threads)
+        t_cpu = time.perf_counter() - t0
+        got = out[: len(o) * 40].cpu().numpy().view(hd.HIT_DTYPE)
+        same = all(np.array_equal(got[f], ref[f]) for f in ("hit", "voxel", "size", "level"))
+        cpu = {"value": len(o) / t_cpu, "unit": "rays/s", "cores": threads, "kind": "port",
+               "sample": f"camera 0, pixel rows 0..{args.cpu_rows - 1} ({len(o)} rays), CPU traversal restatement",
+               "hits_equal_on_sample": bool(same)}
+    line = {
+        "metric": "rays/s primary-ray DAG traversal (first-hit voxel + level)", "value": value, "unit": "rays/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"{n_cams} pinhole cameras {width}x{height} on the {res}^3 terrain",
+                   "terrain_build_s": t_build, "column_edits": int(len(cols)), "node_levels": cfg.get_node_levels(),
+                   "l2": "output (40 B per ray) and pool far above L2; no flush"},
+        "e2e": {"value": e2e, "unit": "rays/s", "h2d_bytes_per_step": int(n_cams * 48),
+                "d2h_bytes_per_step": int(n_rays * 40)},
+        "roofline": {"bound": "hbm", "kernel": "k_trace_pinhole", "achieved": achieved, "peak": hbm,
+                     "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm, "traffic": None,
+                     "algorithmic_bytes_per_step": alg, "steps_per_ray": steps / (n_rays * args.steps),
+                     "node_words_per_ray": reads / (n_rays * args.steps)},
+        "hit_fraction": hits / (n_rays * args.steps), "cpu_baseline": cpu,
+        "gpu_launches": pool.kernel_launches() - launches0, "clocks": clocks.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_terrain(args):
+    """Config 2: plain one-edit-per-pass sphere edits on the 16384^3 terrain."""
+    import torch
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    build_if_needed()
+    import vkhashdag_gb300 as hd
+    from vkhashdag_gb300 import workloads as W
+    res = args.resolution
+    cfg, pool, cols, root0, t_build = terrain_pool(hd, W, res, local)
+    edits = W.surface_spheres(res, args.n_edits, seed=0, band=64, block=32)
+    ve = hd.count_voxel_edits(edits, res)
+    pool.checkpoint()
+    stream = torch.cuda.Stream(device=local)
+    sp = stream.cuda_stream
+    d_edits = torch.from_numpy(edits.view(np.uint8).copy()).to(f"cuda:{local}")
+    d_root = torch.zeros(1, dtype=torch.int32, device=f"cuda:{local}")
+    # size the workspace with the largest single edit, then warm up
+    for k in range(min(64, len(edits))):
+        pool.edit(root0, edits[k:k + 1])
+    pool.rollback(0)
+    torch.cuda.synchronize()
+    lat = []
+    with ClockSampler(local) as clocks:
+        t0 = time.perf_counter()
+        r = root0
+        for k in range(len(edits)):
+            t1 = time.perf_counter()
+            r = pool.edit(r, edits[k:k + 1])
+            lat.append(time.perf_counter() - t1)
+        wall = time.perf_counter() - t0
+    lat_ms = np.array(lat) * 1e3
+    final_plain = r
+    # the same edits as one batched pass, on the same scene
+    pool.rollback(0)
+    torch.cuda.synchronize()
+    s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    pool.edit(root0, edits)  # sizes the workspace
+    pool.rollback(0)
+    s0.record(stream)
+    pool.edit_async(root0, d_edits.data_ptr(), len(edits), d_root.data_ptr(), sp)
+    s1.record(stream)
+    torch.cuda.synchronize()
+    batched_ms = s0.elapsed_time(s1)
+    # both forms give the same DAG: re-running the plain chain finds every node
+    r = root0
+    for k in range(len(edits)):
+        r = pool.edit(r, edits[k:k + 1])
+    same = r == (int(d_root.item()) & 0xFFFFFFFF)
+    line = {
+        "metric": "voxel-edits/s per-edit (plain form) on the 16384^3 terrain; p99 edit latency",
+        "value": ve / wall, "unit": "voxel-edits/s", "n_gpus": world, "steps": len(edits), "warmup": 64,
+        "ms_per_step": float(lat_ms.mean()), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u32", "data": "synthetic",
+        "config": {"workload": f"{len(edits)} surface spheres r log-uniform [4,256], one pass each, {res}^3 terrain",
+                   "terrain_columns": int(len(cols)), "terrain_build_s": t_build,
+                   "node_levels": cfg.get_node_levels()},
+        "latency_ms": {"p50": float(np.percentile(lat_ms, 50)), "p99": float(np.percentile(lat_ms, 99)),
+                       "max": float(lat_ms.max())},
+        "batched_same_edits": {"ms": batched_ms, "voxel_edits_per_s": ve / (batched_ms / 1e3),
+                               "speedup_vs_plain": (wall * 1e3) / batched_ms, "same_dag_as_plain": bool(same)},
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -402,11 +595,26 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-step-seconds", type=float, default=6.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--mode", default="batched", choices=["batched", "terrain", "rays"])
+    ap.add_argument("--cameras", type=int, default=16)
+    ap.add_argument("--width", type=int, default=3840)
+    ap.add_argument("--height", type=int, default=2160)
+    ap.add_argument("--cpu-rows", type=int, default=64)
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.mode == "terrain":
+        if args.resolution == RES:
+            args.resolution = TERRAIN_RES
+        if args.n_edits == N_EDITS:
+            args.n_edits = 4096
+        run_terrain(args)
+    elif args.mode == "rays":
+        if args.resolution == RES:
+            args.resolution = TERRAIN_RES
+        run_rays(args)
     else:
         run_ours(args)
 

@@ -243,9 +243,10 @@ hd_status hd_trace(hd_pool *pool, uint32_t root, const float *origins, const flo
                    void *stream);
 /* Primary rays of n_cameras pinhole cameras at width x height, device output
  * (d_out = device pointer to n_cameras*width*height hits, camera-major,
- * row-major).  Async on stream. */
+ * row-major).  d_counters (device, 3 x u64, may be NULL) accumulates traversal
+ * loop iterations, node words read and hits.  Async on stream. */
 hd_status hd_trace_pinhole_async(hd_pool *pool, uint32_t root, const hd_camera *cameras, uint32_t n_cameras,
-                                 uint32_t width, uint32_t height, hd_hit *d_out, void *stream);
+                                 uint32_t width, uint32_t height, hd_hit *d_out, uint64_t *d_counters, void *stream);
 
 /* ---- workload helpers ------------------------------------------------------
  * Number of grid voxels inside each edit's shape clipped to [0,resolution)^3,

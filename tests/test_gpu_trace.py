@@ -61,8 +61,9 @@ def test_pinhole_cameras_match_host_rays(orc, hd):
     cams["up"] = [[0.0, 0.5, 0.3], [0.1, 0.5, 0.0]]
     w, h = 64, 48
     out = torch.empty(2 * w * h * 40, dtype=torch.uint8, device="cuda")
+    ctr = torch.zeros(3, dtype=torch.int64, device="cuda")
     st = hd.lib().hd_trace_pinhole_async(pool.handle, root, cams.ctypes.data_as(ctypes.c_void_p), 2, w, h,
-                                         ctypes.c_void_p(out.data_ptr()), None)
+                                         ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(ctr.data_ptr()), None)
     assert st == 0
     torch.cuda.synchronize()
     got = out.cpu().numpy().view(hd.HIT_DTYPE)
@@ -80,3 +81,5 @@ def test_pinhole_cameras_match_host_rays(orc, hd):
     for f in ("hit", "voxel", "size", "level"):
         assert np.array_equal(got[f], want[f]), f
     assert got["hit"].mean() > 0.3
+    steps, reads, hits = (int(x) for x in ctr.cpu())
+    assert hits == int(got["hit"].sum()) and steps >= 2 * w * h and reads > 0

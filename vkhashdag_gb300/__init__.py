@@ -107,7 +107,7 @@ def lib():
         "hd_pool_upload": (I, [P, P, P, U32, P, P]),
         "hd_query": (I, [P, U32, P, U32, P, P]),
         "hd_trace": (I, [P, U32, P, P, U32, P, P]),
-        "hd_trace_pinhole_async": (I, [P, U32, P, U32, U32, U32, P, P]),
+        "hd_trace_pinhole_async": (I, [P, U32, P, U32, U32, U32, P, P, P]),
         "hd_count_voxel_edits": (U64, [P, U32, U32]),
         "hd_status_string": (ctypes.c_char_p, [I]),
         "hd_device_available": (I, []),
@@ -426,6 +426,14 @@ class NodePool:
         out = np.zeros(len(pts), np.uint8)
         _check(lib().hd_query(self._h, root & 0xFFFFFFFF, _ptr(pts), len(pts), _ptr(out), None), "hd_query")
         return out
+
+    def trace_pinhole_async(self, root: int, cameras: np.ndarray, width: int, height: int, d_out: int,
+                            d_counters: int = 0, stream: int = 0):
+        """Primary rays of pinhole cameras (CAMERA_DTYPE array, host) into a device buffer of hits."""
+        cams = np.ascontiguousarray(cameras, dtype=CAMERA_DTYPE)
+        _check(lib().hd_trace_pinhole_async(self._h, root & 0xFFFFFFFF, _ptr(cams), len(cams), width, height,
+                                            ctypes.c_void_p(d_out), ctypes.c_void_p(d_counters or None),
+                                            ctypes.c_void_p(stream)), "hd_trace_pinhole_async")
 
     def traversal(self, root: int, origins, dirs) -> np.ndarray:
         o = np.ascontiguousarray(origins, dtype=np.float32).reshape(-1, 3)

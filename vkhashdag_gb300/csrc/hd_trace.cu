@@ -20,7 +20,10 @@ __device__ __forceinline__ float fmin_ref(float x, float y) { return (y < x) ? y
 __device__ __forceinline__ float fmax_ref(float x, float y) { return (x < y) ? y : x; } // glm::max
 __device__ __forceinline__ float abs_ref(float x) { return x >= 0.0f ? x : -x; }
 
-__device__ hd_hit trace_one(const DevPool &P, u32 root, float ox, float oy, float oz, float dx, float dy, float dz) {
+// steps: loop iterations; reads: node words fetched (mask words, child pointers, leaf words)
+__device__ hd_hit trace_one(const DevPool &P, u32 root, float ox, float oy, float oz, float dx, float dy, float dz,
+                            u32 *steps = nullptr, u32 *reads = nullptr) {
+	u32 n_steps = 0, n_reads = 0;
 	hd_hit out;
 	out.voxel[0] = out.voxel[1] = out.voxel[2] = 0;
 	out.size = 0;
@@ -74,10 +77,13 @@ __device__ hd_hit trace_one(const DevPool &P, u32 root, float ox, float oy, floa
 	const u32 leaf_level = P.cfg.L;
 	const int leaf_scale = kStack - (int)leaf_level;
 	for (int guard = 0; guard < (1 << 20); ++guard) { // a ray crosses at most a few thousand cells
+		++n_steps;
 		if (child_bits == 0u) {
-			if (scale > leaf_scale)
+			if (scale > leaf_scale) {
 				child_bits = node_addr(P, parent)[0];
-			else if (scale == leaf_scale) {
+				++n_reads;
+			} else if (scale == leaf_scale) {
+				n_reads += 2;
 				const u32 *p = node_addr(P, parent);
 				const u32 l0 = p[0], l1 = p[1];
 				child_bits = ((l0 & 0xFFu) ? 1u : 0u) | ((l0 & 0xFF00u) ? 2u : 0u) | ((l0 & 0xFF0000u) ? 4u : 0u) |
@@ -108,6 +114,7 @@ __device__ hd_hit trace_one(const DevPool &P, u32 root, float ox, float oy, floa
 				parent = node_addr(P, parent + 1u + __popc(child_bits & (child_mask - 1u)))[0];
 			else
 				parent = (node_addr(P, parent + (child_shift >> 2u))[0] >> ((child_shift & 3u) << 3u)) & 0xFFu;
+			++n_reads;
 			idx = 0;
 			--scale;
 			scale_exp2 = half;
@@ -154,6 +161,10 @@ __device__ hd_hit trace_one(const DevPool &P, u32 root, float ox, float oy, floa
 		}
 	}
 	const bool hit = scale < kStack && t_min <= t_max;
+	if (steps)
+		*steps = n_steps;
+	if (reads)
+		*reads = n_reads;
 	out.hit = hit ? 1u : 0u;
 	out.t = t_min;
 	const u32 voxel_level = leaf_level + 1u;
@@ -188,8 +199,11 @@ __global__ void k_trace(DevPool P, u32 root, const float *o, const float *d, u32
 }
 
 // Camera_GenRay (shader/src/trace.frag:366-370) at pixel centres, then the traversal.
-__global__ void k_trace_pinhole(DevPool P, u32 root, const hd_camera *cams, u32 n_cams, u32 w, u32 h, hd_hit *out) {
+// counters (optional): [0] += loop iterations, [1] += node words read, [2] += hits.
+__global__ void k_trace_pinhole(DevPool P, u32 root, const hd_camera *cams, u32 n_cams, u32 w, u32 h, hd_hit *out,
+                                unsigned long long *counters) {
 	const u64 per = (u64)w * h, total = per * n_cams;
+	u64 my_steps = 0, my_reads = 0, my_hits = 0;
 	for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (u64)gridDim.x * blockDim.x) {
 		const u32 c = (u32)(i / per);
 		const u32 px = (u32)(i % per % w), py = (u32)(i % per / w);
@@ -202,8 +216,25 @@ __global__ void k_trace_pinhole(DevPool P, u32 root, const hd_camera *cams, u32 
 			dd[a] = __fsub_rn(__fsub_rn(cam.look[a], __fmul_rn(cam.side[a], u)), __fmul_rn(cam.up[a], v));
 		const float len2 = __fadd_rn(__fadd_rn(__fmul_rn(dd[0], dd[0]), __fmul_rn(dd[1], dd[1])), __fmul_rn(dd[2], dd[2]));
 		const float inv = __fdiv_rn(1.0f, __fsqrt_rn(len2));
-		out[i] = trace_one(P, root, cam.position[0], cam.position[1], cam.position[2], __fmul_rn(dd[0], inv),
-		                   __fmul_rn(dd[1], inv), __fmul_rn(dd[2], inv));
+		u32 st_, rd_;
+		const hd_hit hh = trace_one(P, root, cam.position[0], cam.position[1], cam.position[2], __fmul_rn(dd[0], inv),
+		                            __fmul_rn(dd[1], inv), __fmul_rn(dd[2], inv), &st_, &rd_);
+		out[i] = hh;
+		my_steps += st_;
+		my_reads += rd_;
+		my_hits += hh.hit;
+	}
+	if (counters) { // one atomic per warp
+		for (int d = 16; d > 0; d >>= 1) {
+			my_steps += __shfl_down_sync(0xFFFFFFFFu, my_steps, d);
+			my_reads += __shfl_down_sync(0xFFFFFFFFu, my_reads, d);
+			my_hits += __shfl_down_sync(0xFFFFFFFFu, my_hits, d);
+		}
+		if ((threadIdx.x & 31u) == 0) {
+			atomicAdd(counters + 0, (unsigned long long)my_steps);
+			atomicAdd(counters + 1, (unsigned long long)my_reads);
+			atomicAdd(counters + 2, (unsigned long long)my_hits);
+		}
 	}
 }
 
@@ -246,7 +277,7 @@ hd_status hd_trace(hd_pool *pool, uint32_t root, const float *origins, const flo
 }
 
 hd_status hd_trace_pinhole_async(hd_pool *pool, uint32_t root, const hd_camera *cameras, uint32_t n_cameras,
-                                 uint32_t width, uint32_t height, hd_hit *d_out, void *stream) {
+                                 uint32_t width, uint32_t height, hd_hit *d_out, uint64_t *d_counters, void *stream) {
 	if (!pool || !cameras || !d_out || !n_cameras || !width || !height)
 		return HD_ERR_INVALID_ARG;
 	std::lock_guard<std::mutex> lk(pool->mtx);
@@ -263,7 +294,9 @@ hd_status hd_trace_pinhole_async(hd_pool *pool, uint32_t root, const hd_camera *
 	if (!s) {
 		const uint64_t total = (uint64_t)width * height * n_cameras;
 		const uint32_t grid = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((total + 255) / 256, pool->num_sms * 16ull));
-		k_trace_pinhole<<<grid, 256, 0, st>>>(pool->P, root, d_cams, n_cameras, width, height, d_out);
+		k_trace_pinhole<<<grid, 256, 0, st>>>(pool->P, root, d_cams, n_cameras, width, height, d_out,
+		                                      reinterpret_cast<unsigned long long *>(d_counters));
+		pool->kernel_launches++;
 		if (cudaGetLastError() != cudaSuccess)
 			s = HD_ERR_CUDA;
 	}
