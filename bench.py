@@ -582,6 +582,261 @@ def run_terrain(args):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------- serving (config 5)
+SERVE_RES = [4096, 4096, 8192, 8192, 16384, 16384, 32768, 65536]
+STATUS_NAME = {2: "bucket full", 3: "heap pages exhausted", 4: "index full"}
+SERVE_METRIC = ("serving: voxel-edits/s and rays/s of a 1000 req/s Poisson stream over 8 resident scenes "
+                "(80% edit batches, 20% ray batches); p50/p99 request latency")
+
+
+def _serving_requests(hd, W, n, seed, rate):
+    """The request stream: arrival time, kind, scene and payload of n requests."""
+    t = W.poisson_arrivals(seed, n, rate)
+    kind = W.uniform(seed, 72, n) < 0.8
+    scene = W.randint(seed, 73, n, 0, len(SERVE_RES) - 1)
+    n_edits = W.log_uniform_int(seed, 74, n, 1, 4096)
+    n_rays = W.log_uniform_int(seed, 75, n, 1 << 16, 1 << 22)
+    reqs = []
+    for k in range(n):
+        res = SERVE_RES[scene[k]]
+        if kind[k]:
+            e = W.mixed_batch(res, int(n_edits[k]), seed=seed * 100003 + k, r_max=512, side_max=1024)
+            reqs.append((float(t[k]), "edit", int(scene[k]), e))
+        else:
+            width = 1024
+            height = max(1, int(n_rays[k]) // width)
+            cams = cameras(hd, W, res, 1, seed=seed * 100003 + k, width=width, height=height)
+            reqs.append((float(t[k]), "cam", int(scene[k]), cams, width, height))
+    return reqs
+
+
+def _serve(srv, reqs, hd, torch, keep_every=0, keep_max_rays=1 << 20):
+    """Submits reqs at their arrival times; a collector thread takes the results
+    in order.  Returns results, kept hit buffers, submit wall time."""
+    import queue
+    q = queue.Queue()
+    results, kept = {}, {}
+
+    def collect():
+        while True:
+            item = q.get()
+            if item is None:
+                return
+            rid, buf, keep = item
+            results[rid] = srv.wait(rid)
+            if keep:
+                kept[rid] = buf
+    th = threading.Thread(target=collect, daemon=True)
+    th.start()
+    ids = []
+    n_cam = 0
+    t0 = time.perf_counter()
+    for r in reqs:
+        target = t0 + r[0]
+        while True:
+            dt = target - time.perf_counter()
+            if dt <= 0:
+                break
+            time.sleep(dt if dt > 0.002 else 0)
+        if r[1] == "edit":
+            rid = srv.submit_edits(r[2], r[3])
+            q.put((rid, None, False))
+        else:
+            n = len(r[3]) * r[4] * r[5]
+            buf = torch.empty(n * hd.HIT_DTYPE.itemsize, dtype=torch.uint8, pin_memory=True)
+            rid = srv.submit_camera(r[2], r[3], r[4], r[5], buf)
+            keep = keep_every > 0 and n_cam % keep_every == 0 and n <= keep_max_rays
+            n_cam += 1
+            q.put((rid, buf, keep))
+        ids.append(rid)
+    t_submit = time.perf_counter() - t0
+    q.put(None)
+    th.join()
+    return ids, results, kept, t_submit
+
+
+def run_serving(args):
+    import torch
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    build_if_needed()
+    import vkhashdag_gb300 as hd
+    from vkhashdag_gb300 import workloads as W
+    heap_pages = int(args.serve_heap_gb * (1 << 30)) >> 16  # 64 KB pages
+    pools, roots0, build_s = [], [], []
+    for res in SERVE_RES:
+        cfg = W.serving_config(res)
+        pool = hd.NodePool(cfg, heap_pages=min(heap_pages, cfg.get_total_pages()), device=local)
+        t0 = time.perf_counter()
+        roots0.append(pool.edit(hd.NULL, W.terrain_columns(res, res // 256, seed=0)))
+        build_s.append(time.perf_counter() - t0)
+        pools.append(pool)
+    used0 = [p.stats()["used_pages"] for p in pools]
+    n_req = int(args.serve_seconds * args.rate)
+    reqs = _serving_requests(hd, W, n_req, 17, args.rate)
+    warm = _serving_requests(hd, W, max(40, int(0.05 * n_req)), 901, args.rate)
+    ve = {k: hd.count_voxel_edits(r[3], SERVE_RES[r[2]]) for k, r in enumerate(reqs) if r[1] == "edit"}
+
+    srv = hd.Server(list(zip(pools, roots0)), max_pass_edits=args.max_pass_edits, ray_slots=args.ray_slots,
+                    max_rays_per_request=1 << 22)
+    # warm-up: grows the edit workspaces, the ray buffers and the pinned host cache
+    _serve(srv, warm, hd, torch)
+    srv.drain()
+    roots_w = [srv.scene_root(s) for s in range(len(pools))]
+    stats_w = srv.stats()
+    launches0 = sum(p.kernel_launches() for p in pools)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        ids, results, kept, t_submit = _serve(srv, reqs, hd, torch, keep_every=16)
+        srv.drain()
+    launches = sum(p.kernel_launches() for p in pools) - launches0
+    stats = srv.stats()
+    final_roots = [srv.scene_root(s) for s in range(len(pools))]
+    srv.close()
+
+    res_list = [results[i] for i in ids]
+    t_first = min(r["t_submit_ms"] for r in res_list)
+    t_last = max(r["t_done_ms"] for r in res_list)
+    wall_s = (t_last - t_first) / 1e3
+    ok_edit = [k for k, (q, r) in enumerate(zip(reqs, res_list)) if q[1] == "edit" and r["status"] == 0]
+    served_ve = float(sum(ve[k] for k in ok_edit))
+    rays = float(sum(r["rays"] for r in res_list if r["kind"] == 1 and r["status"] == 0))
+
+    def lat(kind=None, what="done"):
+        v = np.array([(r["t_done_ms"] if what == "done" else r["t_start_ms"]) - r["t_submit_ms"]
+                      for r in res_list if kind is None or r["kind"] == kind])
+        if not len(v):
+            return None
+        return {"p50": float(np.percentile(v, 50)), "p99": float(np.percentile(v, 99)), "max": float(v.max()),
+                "mean": float(v.mean()), "samples": int(len(v))}
+
+    passes = {}
+    for r in res_list:
+        if r["kind"] == 0 and r["admitted"]:
+            passes.setdefault((r["scene"], r["pass_id"]), r["pass_requests"])
+
+    # ---- checks: every result the same alone (replayed request by request on
+    # the same pool: the intermediate states of merged passes are new nodes, so
+    # a replay can run out of bucket room where the mix did not)
+    t_chk = time.perf_counter()
+    verified, notes, mismatches = 0, [], []
+    for s, pool in enumerate(pools):
+        mine = [(q, r) for q, r in zip(reqs, res_list) if q[2] == s and q[1] == "edit" and r["admitted"]]
+        root = roots_w[s]
+        complete = True
+        for k, (q, r) in enumerate(mine):
+            first = k == 0 or mine[k - 1][1]["pass_id"] != r["pass_id"]
+            last = k + 1 == len(mine) or mine[k + 1][1]["pass_id"] != r["pass_id"]
+            if first and r["root_in"] != root:
+                mismatches.append({"scene": s, "pass": r["pass_id"], "what": "root_in"})
+                root = r["root_in"]
+            try:
+                root = pool.edit(root, q[3]) if r["status"] == 0 else root
+            except hd.HashDagError as e:
+                notes.append(f"scene {s}: replay stopped at pass {r['pass_id']} of "
+                             f"{mine[-1][1]['pass_id']} ({STATUS_NAME.get(e.status, e.status)})")
+                complete = False
+                break
+            if last:
+                verified += 1
+                if root != r["root"]:
+                    mismatches.append({"scene": s, "pass": r["pass_id"], "requests": r["pass_requests"],
+                                       "edits": r["pass_edits"], "status": r["status"], "what": "root"})
+                    root = r["root"]  # carry on from the published state
+            if time.perf_counter() - t_chk > args.verify_seconds:
+                notes.append(f"time budget reached in scene {s}")
+                complete = False
+                break
+        if complete and root != final_roots[s]:
+            mismatches.append({"scene": s, "what": "final root"})
+        if time.perf_counter() - t_chk > args.verify_seconds:
+            break
+    edit_ok = not mismatches
+    verify_note = "; ".join(notes) if notes else "all passes"
+    n_passes_total = len(passes)
+    ray_ok, ray_checked = True, 0
+    for rid, buf in kept.items():
+        k = ids.index(rid)
+        q, r = reqs[k], results[rid]
+        n = len(q[3]) * q[4] * q[5]
+        d_out = torch.empty(n * 40, dtype=torch.uint8, device=f"cuda:{local}")
+        d_ctr = torch.zeros(4, dtype=torch.int64, device=f"cuda:{local}")
+        pools[q[2]].trace_pinhole_async(r["root"], q[3], q[4], q[5], d_out.data_ptr(), d_ctr.data_ptr(), 0)
+        torch.cuda.synchronize()
+        same = torch.equal(d_out.cpu(), buf) and d_ctr.cpu()[:3].tolist() == [r["steps"], r["node_words"], r["hits"]]
+        ray_ok = ray_ok and same
+        ray_checked += 1
+
+    # ---- CPU baseline: the reference's loop applies one request at a time with
+    # its threaded editor (src/main.cpp:280-296); the oracle restatement does the
+    # same for scene 0's requests on the host cores, for a bounded time
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        import oracle
+        oracle.build()
+        res0 = SERVE_RES[0]
+        ocfg = W.serving_config(res0)
+        opool = oracle.OraclePool.from_config(ocfg)
+        threads = os.cpu_count() or 1
+        mtl = max(0, ocfg.get_node_levels() - 4)
+        orr = opool.threaded_edit(oracle.NULL, W.terrain_columns(res0, res0 // 256, seed=0), mtl, threads)
+        lat_cpu, ve_cpu, t_cpu = [], 0, 0.0
+        for q in reqs:
+            if q[1] != "edit" or q[2] != 0:
+                continue
+            t0 = time.perf_counter()
+            orr = opool.threaded_edit(orr, q[3], mtl, threads)
+            dt = time.perf_counter() - t0
+            lat_cpu.append(dt * 1e3)
+            t_cpu += dt
+            ve_cpu += hd.count_voxel_edits(q[3], res0)
+            if t_cpu > args.cpu_seconds:
+                break
+        cpu = {"value": ve_cpu / t_cpu, "unit": "voxel-edits/s", "cores": threads, "kind": "port",
+               "sample": f"the first {len(lat_cpu)} edit requests of scene 0 ({res0}^3 terrain), one threaded "
+                         f"edit call per request in arrival order ({t_cpu:.1f} s)",
+               "latency_ms": {"p50": float(np.percentile(lat_cpu, 50)), "p99": float(np.percentile(lat_cpu, 99))}}
+        del opool
+
+    if rank != 0:
+        return
+    h2d = sum(40 * len(q[3]) if q[1] == "edit" else 48 * len(q[3]) for q in reqs)
+    d2h = sum(40 * r["rays"] for r in res_list if r["kind"] == 1)
+    line = {
+        "metric": SERVE_METRIC, "value": served_ve / wall_s, "unit": "voxel-edits/s", "n_gpus": 1,
+        "steps": len(reqs), "warmup": len(warm), "ms_per_step": 1e3 * wall_s / len(reqs), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": f"{len(SERVE_RES)} resident terrain scenes {SERVE_RES}, Poisson {args.rate:g} req/s "
+                               f"for {args.serve_seconds:g} s; edit batches 1..4096 mixed edits (spheres r<=512, "
+                               f"boxes <=1024), ray batches 2^16..2^22 rays (1024 wide)",
+                   "word_bits_per_page": 14, "page_bits_per_bucket": 2, "heap_pages_per_scene": heap_pages,
+                   "max_pass_edits": args.max_pass_edits, "ray_slots": args.ray_slots,
+                   "terrain_build_s": build_s, "l2": "pools far above L2; no flush"},
+        "rays_per_s": rays / wall_s,
+        "requests_per_s": len(reqs) / wall_s, "offered_rate": args.rate,
+        "submit_s": t_submit, "wall_s": wall_s,
+        "latency_ms": {"edit": lat(0), "camera": lat(1), "all": lat(), "queue_edit": lat(0, "start"),
+                       "queue_camera": lat(1, "start")},
+        "requests": {"edit": sum(1 for q in reqs if q[1] == "edit"), "camera": sum(1 for q in reqs if q[1] == "cam"),
+                     "refused": int(stats["refused"] - stats_w["refused"]),
+                     "failed": int(stats["failed"] - stats_w["failed"])},
+        "passes": {"count": len(passes), "mean_requests": float(np.mean(list(passes.values()))) if passes else 0,
+                   "max_requests": int(max(passes.values())) if passes else 0},
+        "pages": {"used_before": used0, "used_after": [p.stats()["used_pages"] for p in pools]},
+        "e2e": {"value": served_ve / wall_s, "unit": "voxel-edits/s", "h2d_bytes_per_step": h2d // len(reqs),
+                "d2h_bytes_per_step": d2h // len(reqs),
+                "note": "requests enter as host arrays and camera hits return to pinned host buffers"},
+        "gpu_launches": int(launches),
+        "clocks": clocks.summary(),
+        "cpu_baseline": cpu,
+        "checks": {"edits_same_alone": bool(edit_ok), "edit_passes_verified": verified,
+                   "edit_passes_total": n_passes_total, "edit_verify": verify_note,
+                   "edit_mismatches": mismatches[:8],
+                   "rays_same_alone": bool(ray_ok), "ray_requests_verified": ray_checked},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -595,7 +850,13 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-step-seconds", type=float, default=6.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--mode", default="batched", choices=["batched", "terrain", "rays"])
+    ap.add_argument("--mode", default="batched", choices=["batched", "terrain", "rays", "serving"])
+    ap.add_argument("--rate", type=float, default=1000.0)
+    ap.add_argument("--serve-seconds", type=float, default=5.0)
+    ap.add_argument("--serve-heap-gb", type=float, default=8.0)
+    ap.add_argument("--max-pass-edits", type=int, default=16384)
+    ap.add_argument("--ray-slots", type=int, default=4)
+    ap.add_argument("--verify-seconds", type=float, default=60.0)
     ap.add_argument("--cameras", type=int, default=16)
     ap.add_argument("--width", type=int, default=3840)
     ap.add_argument("--height", type=int, default=2160)
@@ -611,6 +872,8 @@ def main():
         if args.n_edits == N_EDITS:
             args.n_edits = 4096
         run_terrain(args)
+    elif args.mode == "serving":
+        run_serving(args)
     elif args.mode == "rays":
         if args.resolution == RES:
             args.resolution = TERRAIN_RES

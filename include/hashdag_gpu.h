@@ -248,6 +248,95 @@ hd_status hd_trace(hd_pool *pool, uint32_t root, const float *origins, const flo
 hd_status hd_trace_pinhole_async(hd_pool *pool, uint32_t root, const hd_camera *cameras, uint32_t n_cameras,
                                  uint32_t width, uint32_t height, hd_hit *d_out, uint64_t *d_counters, void *stream);
 
+/* ---- serving loop ------------------------------------------------------------
+ * Several resident scenes (one hd_pool each, all on one device) served from
+ * one request stream.  Generalises the reference application's edit loop
+ * (src/main.cpp:280-296: one edit at a time on a worker thread while frames
+ * trace the last finished root; an edit arriving while another runs is dropped
+ * there):
+ *   - edit requests of a scene queue in arrival order; whenever the scene's
+ *     previous pass has finished, everything queued (up to max_pass_edits
+ *     edits) is merged into ONE batched pass (continuous batching);
+ *   - admission by free pages: a request is taken into a pass only while the
+ *     pages its edits are expected to need (a running per-scene average of
+ *     pages per edit) fit into the scene's free heap pages; a request that
+ *     does not fit even alone is refused with HD_ERR_POOL_OOM, admitted = 0;
+ *   - camera (ray) requests run on ray_slots high-priority streams, each traced
+ *     against its scene's last finished root at the moment it starts, so ray
+ *     work overlaps the scenes' edit passes on the device;
+ *   - a merged pass that fails is re-run request by request from the pass's
+ *     input root, so every request gets the status it would get alone.
+ * Results: a merged pass's voxels equal applying its requests one after
+ * another (the batched-pass contract of hd_edit); a ray request's hits equal
+ * hd_trace_pinhole_async on the recorded root. */
+typedef struct hd_server hd_server;
+
+typedef struct hd_server_config {
+	uint32_t max_pass_edits;        /* edits merged into one pass at most (0 = 16384) */
+	uint32_t ray_slots;             /* concurrent ray requests (0 = 4) */
+	uint32_t max_rays_per_request;  /* larger camera requests are refused (0 = 1 << 24) */
+	uint32_t reserve_pages;         /* heap pages kept free by admission (0 = heap/64) */
+	double pages_per_edit_hint;     /* admission estimate before the first pass (0 = 1.0) */
+} hd_server_config;
+
+typedef enum hd_request_kind { HD_REQ_EDIT = 0, HD_REQ_CAMERA = 1 } hd_request_kind;
+
+typedef struct hd_request_result {
+	uint64_t id;
+	uint32_t kind;           /* hd_request_kind */
+	uint32_t scene;
+	int32_t status;          /* hd_status of this request */
+	uint32_t admitted;       /* 0: refused by admission control (nothing ran) */
+	uint32_t root_in;        /* edit: root the pass started from; camera: root traced */
+	uint32_t root;           /* edit: scene root after the pass carrying it; camera: root traced */
+	uint64_t pass_id;        /* edit: per-scene pass number (requests of one pass share it) */
+	uint32_t pass_requests;  /* edit: requests merged into that pass (1 = alone) */
+	uint32_t pass_edits;     /* edit: edits in that pass */
+	uint64_t rays;           /* camera: rays traced */
+	uint64_t hits, steps, node_words; /* camera: traversal counters */
+	double t_submit_ms, t_start_ms, t_done_ms; /* ms since hd_server_create */
+} hd_request_result;
+
+typedef struct hd_server_stats {
+	uint64_t edit_requests, camera_requests; /* completed */
+	uint64_t refused, failed;                /* refused by admission / finished with an error */
+	uint64_t edit_passes, edits_applied, rays_traced;
+	uint32_t max_pass_requests, queued;      /* largest merge; requests not finished yet */
+	double edit_p50_ms, edit_p99_ms, camera_p50_ms, camera_p99_ms; /* submit -> done */
+} hd_server_stats;
+
+/* pools[i] with its current root roots[i] (HD_NULL_PTR = empty) is scene i.
+ * The server does not own the pools; it must be destroyed before them, and
+ * nothing else may edit, roll back or upload to them while it runs. */
+hd_status hd_server_create(hd_pool *const *pools, const uint32_t *roots, uint32_t n_scenes,
+                           const hd_server_config *config, hd_server **out_server);
+/* Waits for every submitted request, stops the worker threads, frees the
+ * server's buffers.  Results not yet retrieved are dropped. */
+void hd_server_destroy(hd_server *server);
+/* Queues edits[0..n) (host array, copied) for scene; *out_id names the request. */
+hd_status hd_server_submit_edits(hd_server *server, uint32_t scene, const hd_edit_desc *edits, uint32_t n,
+                                 uint64_t *out_id);
+/* Queues n_cameras pinhole cameras at width x height for scene.  host_out
+ * (n_cameras*width*height hits, camera-major; pinned memory is fastest) receives
+ * the hits and must stay valid until the request is retrieved; NULL keeps
+ * them on the device (only the counters are returned). */
+hd_status hd_server_submit_camera(hd_server *server, uint32_t scene, const hd_camera *cameras, uint32_t n_cameras,
+                                  uint32_t width, uint32_t height, hd_hit *host_out, uint64_t *out_id);
+/* Waits up to timeout_ms (< 0: forever) for request id and hands out its
+ * result once (HD_ERR_TIMEOUT: not finished yet; HD_ERR_INVALID_ARG: unknown
+ * or already retrieved id). */
+hd_status hd_server_wait(hd_server *server, uint64_t id, double timeout_ms, hd_request_result *out);
+/* paused != 0: no new edit pass and no new ray request starts (running ones
+ * finish; submissions keep queueing), e.g. to take a consistent snapshot of
+ * the pools.  paused = 0 resumes; queued edits of a scene then merge. */
+hd_status hd_server_pause(hd_server *server, int paused);
+/* Waits until every request submitted so far has finished
+ * (HD_ERR_INVALID_ARG while paused with requests queued). */
+hd_status hd_server_drain(hd_server *server);
+/* Last finished root of a scene. */
+hd_status hd_server_scene_root(hd_server *server, uint32_t scene, uint32_t *out_root);
+hd_status hd_server_get_stats(hd_server *server, hd_server_stats *out);
+
 /* ---- workload helpers ------------------------------------------------------
  * Number of grid voxels inside each edit's shape clipped to [0,resolution)^3,
  * summed over the edits (the voxel-edits unit of the benchmark). */

@@ -88,3 +88,54 @@ def test_workloads_deterministic_and_in_range():
     assert 0.4 < (a["op"] == 1).mean() < 0.6
     t = W.terrain_columns(256, 8, seed=0)
     assert len(t) == 32 * 32 and t["p1"][:, 1].min() >= 1
+
+
+def test_struct_layouts_match_the_header(hd, tmp_path):
+    """sizeof/offsetof of every ABI struct, compiled from the header, equals the
+    Python mirrors (ctypes structures and numpy dtypes)."""
+    import shutil
+    import subprocess
+    if not shutil.which("gcc"):
+        pytest.skip("gcc not available")
+    structs = {
+        "hd_config": hd._Config, "hd_pool_stats": hd._Stats, "hd_server_config": hd._ServerConfig,
+        "hd_request_result": hd._RequestResult, "hd_server_stats": hd._ServerStats,
+    }
+    dtypes = {"hd_edit_desc": hd.EDIT_DTYPE, "hd_hit": hd.HIT_DTYPE, "hd_camera": hd.CAMERA_DTYPE}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "hashdag_gpu.h"', "int main(void) {"]
+    for name, cls in structs.items():
+        lines.append(f'printf("{name} %zu\\n", sizeof({name}));')
+        for field, _ in cls._fields_:
+            lines.append(f'printf("{name}.{field} %zu\\n", offsetof({name}, {field}));')
+    for name, dt in dtypes.items():
+        lines.append(f'printf("{name} %zu\\n", sizeof({name}));')
+        for field in dt.names:
+            lines.append(f'printf("{name}.{field} %zu\\n", offsetof({name}, {field}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = dict(l.split() for l in subprocess.run([str(exe)], check=True, capture_output=True,
+                                                   text=True).stdout.splitlines())
+    for name, cls in structs.items():
+        assert int(got[name]) == ctypes.sizeof(cls), name
+        for field, _ in cls._fields_:
+            assert int(got[f"{name}.{field}"]) == getattr(cls, field).offset, (name, field)
+    for name, dt in dtypes.items():
+        assert int(got[name]) == dt.itemsize, name
+        for field in dt.names:
+            assert int(got[f"{name}.{field}"]) == dt.fields[field][1], (name, field)
+
+
+def test_server_entry_points_reject_bad_arguments(hd):
+    lib = hd.lib()
+    out = ctypes.c_void_p()
+    assert lib.hd_server_create(None, None, 0, None, ctypes.byref(out)) == 1 and not out.value
+    rid = ctypes.c_uint64()
+    assert lib.hd_server_submit_edits(None, 0, None, 0, ctypes.byref(rid)) == 1
+    assert lib.hd_server_submit_camera(None, 0, None, 1, 1, 1, None, ctypes.byref(rid)) == 1
+    r = hd._RequestResult()
+    assert lib.hd_server_wait(None, 1, 0.0, ctypes.byref(r)) == 1
+    assert lib.hd_server_drain(None) == 1 and lib.hd_server_pause(None, 1) == 1
+    lib.hd_server_destroy(None)

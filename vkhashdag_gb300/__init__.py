@@ -24,7 +24,7 @@ import numpy as np
 __all__ = [
     "NULL", "Config", "DefaultConfig", "EditMode", "SphereEditor", "AABBEditor", "NodePool",
     "HashDagError", "EDIT_DTYPE", "HIT_DTYPE", "CAMERA_DTYPE", "edits_to_array", "lib", "library_path",
-    "count_voxel_edits", "device_available",
+    "count_voxel_edits", "device_available", "Server", "REQ_EDIT", "REQ_CAMERA",
 ]
 
 NULL = 0xFFFFFFFF
@@ -68,6 +68,30 @@ class _Stats(ctypes.Structure):
                 ("max_bucket_words", ctypes.c_uint32), ("words_per_bucket", ctypes.c_uint32)]
 
 
+class _ServerConfig(ctypes.Structure):
+    _fields_ = [("max_pass_edits", ctypes.c_uint32), ("ray_slots", ctypes.c_uint32),
+                ("max_rays_per_request", ctypes.c_uint32), ("reserve_pages", ctypes.c_uint32),
+                ("pages_per_edit_hint", ctypes.c_double)]
+
+
+class _RequestResult(ctypes.Structure):
+    _fields_ = [("id", ctypes.c_uint64), ("kind", ctypes.c_uint32), ("scene", ctypes.c_uint32),
+                ("status", ctypes.c_int32), ("admitted", ctypes.c_uint32), ("root_in", ctypes.c_uint32),
+                ("root", ctypes.c_uint32), ("pass_id", ctypes.c_uint64), ("pass_requests", ctypes.c_uint32),
+                ("pass_edits", ctypes.c_uint32), ("rays", ctypes.c_uint64), ("hits", ctypes.c_uint64),
+                ("steps", ctypes.c_uint64), ("node_words", ctypes.c_uint64), ("t_submit_ms", ctypes.c_double),
+                ("t_start_ms", ctypes.c_double), ("t_done_ms", ctypes.c_double)]
+
+
+class _ServerStats(ctypes.Structure):
+    _fields_ = [("edit_requests", ctypes.c_uint64), ("camera_requests", ctypes.c_uint64),
+                ("refused", ctypes.c_uint64), ("failed", ctypes.c_uint64), ("edit_passes", ctypes.c_uint64),
+                ("edits_applied", ctypes.c_uint64), ("rays_traced", ctypes.c_uint64),
+                ("max_pass_requests", ctypes.c_uint32), ("queued", ctypes.c_uint32),
+                ("edit_p50_ms", ctypes.c_double), ("edit_p99_ms", ctypes.c_double),
+                ("camera_p50_ms", ctypes.c_double), ("camera_p99_ms", ctypes.c_double)]
+
+
 _lib = None
 
 
@@ -108,6 +132,15 @@ def lib():
         "hd_query": (I, [P, U32, P, U32, P, P]),
         "hd_trace": (I, [P, U32, P, P, U32, P, P]),
         "hd_trace_pinhole_async": (I, [P, U32, P, U32, U32, U32, P, P, P]),
+        "hd_server_create": (I, [P, P, U32, ctypes.POINTER(_ServerConfig), ctypes.POINTER(P)]),
+        "hd_server_destroy": (None, [P]),
+        "hd_server_submit_edits": (I, [P, U32, P, U32, ctypes.POINTER(U64)]),
+        "hd_server_submit_camera": (I, [P, U32, P, U32, U32, U32, P, ctypes.POINTER(U64)]),
+        "hd_server_wait": (I, [P, U64, ctypes.c_double, ctypes.POINTER(_RequestResult)]),
+        "hd_server_drain": (I, [P]),
+        "hd_server_pause": (I, [P, I]),
+        "hd_server_scene_root": (I, [P, U32, ctypes.POINTER(U32)]),
+        "hd_server_get_stats": (I, [P, ctypes.POINTER(_ServerStats)]),
         "hd_count_voxel_edits": (U64, [P, U32, U32]),
         "hd_status_string": (ctypes.c_char_p, [I]),
         "hd_device_available": (I, []),
@@ -441,3 +474,105 @@ class NodePool:
         out = np.zeros(len(o), HIT_DTYPE)
         _check(lib().hd_trace(self._h, root & 0xFFFFFFFF, _ptr(o), _ptr(d), len(o), _ptr(out), None), "hd_trace")
         return out
+
+
+REQ_EDIT, REQ_CAMERA = 0, 1
+
+
+class Server:
+    """Serving loop over resident scenes (hd_server_* of the C ABI).
+
+    ``scenes`` is a list of (NodePool, root).  Edit requests of a scene are
+    merged into one batched pass whenever the scene's previous pass has
+    finished; camera requests are traced on their own streams against the
+    scene's last finished root.  ``wait`` returns a result dict once per id.
+    The pools must outlive the server and must not be edited around it while it
+    runs.
+    """
+
+    def __init__(self, scenes, max_pass_edits: int = 0, ray_slots: int = 0, max_rays_per_request: int = 0,
+                 reserve_pages: int = 0, pages_per_edit_hint: float = 0.0):
+        self._pools = [p for p, _ in scenes]  # keep the pools alive
+        handles = (ctypes.c_void_p * len(scenes))(*[p.handle for p, _ in scenes])
+        roots = np.array([r & 0xFFFFFFFF for _, r in scenes], np.uint32)
+        cfg = _ServerConfig(max_pass_edits, ray_slots, max_rays_per_request, reserve_pages, pages_per_edit_hint)
+        h = ctypes.c_void_p()
+        _check(lib().hd_server_create(handles, _ptr(roots), len(scenes), ctypes.byref(cfg), ctypes.byref(h)),
+               "hd_server_create")
+        self._h = h
+        self._keep = {}
+
+    def submit_edits(self, scene: int, edits: np.ndarray) -> int:
+        e = np.ascontiguousarray(edits, dtype=EDIT_DTYPE)
+        rid = ctypes.c_uint64()
+        _check(lib().hd_server_submit_edits(self._h, scene, _ptr(e), len(e), ctypes.byref(rid)),
+               "hd_server_submit_edits")
+        return rid.value
+
+    def submit_camera(self, scene: int, cameras: np.ndarray, width: int, height: int, out=None) -> int:
+        """out: None (hits stay on the device), a HIT_DTYPE numpy array, or an
+        object with data_ptr() (e.g. a pinned torch byte tensor) of
+        n_cameras*width*height*40 bytes; kept alive until the result is taken."""
+        cams = np.ascontiguousarray(cameras, dtype=CAMERA_DTYPE)
+        n = len(cams) * width * height
+        if out is None:
+            ptr = None
+        elif isinstance(out, np.ndarray):
+            if out.nbytes < n * HIT_DTYPE.itemsize or not out.flags.c_contiguous:
+                raise ValueError("output buffer too small or not contiguous")
+            ptr = out.ctypes.data
+        else:
+            if out.numel() * out.element_size() < n * HIT_DTYPE.itemsize:
+                raise ValueError("output buffer too small")
+            ptr = out.data_ptr()
+        rid = ctypes.c_uint64()
+        _check(lib().hd_server_submit_camera(self._h, scene, _ptr(cams), len(cams), width, height,
+                                             ctypes.c_void_p(ptr), ctypes.byref(rid)), "hd_server_submit_camera")
+        if out is not None:
+            self._keep[rid.value] = out
+        return rid.value
+
+    def wait(self, rid: int, timeout_ms: float = -1.0) -> Optional[dict]:
+        """Result of request rid as a dict, or None if timeout_ms ran out."""
+        r = _RequestResult()
+        st = lib().hd_server_wait(self._h, rid, float(timeout_ms), ctypes.byref(r))
+        if st == 7:
+            return None
+        _check(st, "hd_server_wait")
+        self._keep.pop(rid, None)
+        return {name: getattr(r, name) for name, _ in _RequestResult._fields_}
+
+    def drain(self):
+        _check(lib().hd_server_drain(self._h), "hd_server_drain")
+
+    def pause(self, paused: bool = True):
+        """While paused no new pass or ray request starts; submissions queue."""
+        _check(lib().hd_server_pause(self._h, 1 if paused else 0), "hd_server_pause")
+
+    def scene_root(self, scene: int) -> int:
+        r = ctypes.c_uint32()
+        _check(lib().hd_server_scene_root(self._h, scene, ctypes.byref(r)), "hd_server_scene_root")
+        return r.value
+
+    def stats(self) -> dict:
+        s = _ServerStats()
+        _check(lib().hd_server_get_stats(self._h, ctypes.byref(s)), "hd_server_get_stats")
+        return {name: getattr(s, name) for name, _ in _ServerStats._fields_}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().hd_server_destroy(self._h)
+            self._h = None
+            self._keep.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()

@@ -131,7 +131,11 @@ hd_status ws_reserve(hd_pool *pool, uint64_t inner_cap, uint64_t leaf_cap, uint6
 	d.long_threshold = 16;
 	ws.edit_cap = edit_cap;
 	ws.d = d;
-	return hd_check(cudaMemset(d.ctr, 0, kWsCtrCount * sizeof(unsigned long long)));
+	// cudaMemset runs on the legacy stream, which does not order against
+	// non-blocking streams: wait for it, or a pass already queued on another
+	// stream could see its counters zeroed half-way through
+	HD_TRY(cudaMemset(d.ctr, 0, kWsCtrCount * sizeof(unsigned long long)));
+	return hd_check(cudaDeviceSynchronize());
 }
 
 uint32_t ceil_div(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
@@ -772,6 +776,7 @@ hd_status hd_pool_get_error(const hd_pool *pool, uint32_t *out_error) {
 	if (!pool || !out_error)
 		return HD_ERR_INVALID_ARG;
 	HD_TRY(cudaSetDevice(pool->device));
+	HD_TRY(cudaEventSynchronize(pool->ws_free));
 	HD_TRY(cudaMemcpy(out_error, pool->P.counters + kCtrError, 4, cudaMemcpyDeviceToHost));
 	return HD_OK;
 }
@@ -780,14 +785,16 @@ hd_status hd_pool_clear_error(hd_pool *pool) {
 	if (!pool)
 		return HD_ERR_INVALID_ARG;
 	HD_TRY(cudaSetDevice(pool->device));
+	HD_TRY(cudaEventSynchronize(pool->ws_free));
 	HD_TRY(cudaMemset(pool->P.counters + kCtrError, 0, 4));
-	return HD_OK;
+	return hd_check(cudaDeviceSynchronize());
 }
 
 hd_status hd_pool_get_stats(const hd_pool *pool, hd_pool_stats *out) {
 	if (!pool || !out)
 		return HD_ERR_INVALID_ARG;
 	HD_TRY(cudaSetDevice(pool->device));
+	HD_TRY(cudaEventSynchronize(pool->ws_free));
 	uint32_t ctr[kCtrCount];
 	HD_TRY(cudaMemcpy(ctr, pool->P.counters, sizeof(ctr), cudaMemcpyDeviceToHost));
 	uint32_t *d_max = nullptr, mx = 0;
@@ -844,7 +851,8 @@ hd_status hd_edit_async(hd_pool *pool, uint32_t root, const hd_edit_desc *d_edit
 		return s;
 	k_error_from_ws<<<1, 32, 0, st>>>(pool->P, pool->ws.d);
 	pool->kernel_launches++;
-	return hd_check(cudaGetLastError());
+	HD_TRY(cudaGetLastError());
+	return hd_check(cudaEventRecord(pool->ws_free, st)); // hd_pool_get_error waits for this
 }
 
 hd_status hd_edit_async_droot(hd_pool *pool, const uint32_t *d_root, const hd_edit_desc *d_edits, uint32_t n,
@@ -859,7 +867,8 @@ hd_status hd_edit_async_droot(hd_pool *pool, const uint32_t *d_root, const hd_ed
 		return s;
 	k_error_from_ws<<<1, 32, 0, st>>>(pool->P, pool->ws.d);
 	pool->kernel_launches++;
-	return hd_check(cudaGetLastError());
+	HD_TRY(cudaGetLastError());
+	return hd_check(cudaEventRecord(pool->ws_free, st)); // hd_pool_get_error waits for this
 }
 
 hd_status hd_edit_profile_begin(hd_pool *pool, uint32_t max_passes) {
@@ -902,7 +911,7 @@ hd_status hd_edit_profile_end(hd_pool *pool, float *out_ms, uint32_t *out_passes
 	return HD_OK;
 }
 
-uint64_t hd_pool_kernel_launches(const hd_pool *pool) { return pool ? pool->kernel_launches : 0; }
+uint64_t hd_pool_kernel_launches(const hd_pool *pool) { return pool ? pool->kernel_launches.load() : 0; }
 
 hd_status hd_pool_checkpoint(hd_pool *pool) {
 	if (!pool)
@@ -930,6 +939,7 @@ hd_status hd_pool_checkpoint(hd_pool *pool) {
 	HD_TRY(cudaMemcpy(pool->ck_page_table, pool->P.page_table, pool->total_pages * 4, cudaMemcpyDeviceToDevice));
 	HD_TRY(cudaMemcpy(pool->ck_counters, pool->P.counters, kCtrCount * 4, cudaMemcpyDeviceToDevice));
 	HD_TRY(cudaMemcpy(pool->ck_index, pool->P.index, slots * 8, cudaMemcpyDeviceToDevice));
+	HD_TRY(cudaDeviceSynchronize()); // device-to-device copies return before they finish
 	for (uint32_t l = 0; l < pool->cfg.node_levels; ++l)
 		pool->ck_filled[l] = pool->P.cfg.filled[l];
 	pool->has_checkpoint = true;

@@ -3,6 +3,7 @@
 
 #include "hd_device.cuh"
 
+#include <atomic>
 #include <mutex>
 #include <vector>
 
@@ -26,7 +27,7 @@ struct hd_pool {
 	hd_ws_host ws;
 	std::mutex mtx;
 	uint64_t last_items[HD_MAX_LEVELS] = {}, last_cand[HD_MAX_LEVELS] = {}, last_ins[HD_MAX_LEVELS] = {};
-	uint64_t kernel_launches = 0; // kernels launched by this pool since creation
+	std::atomic<uint64_t> kernel_launches{0}; // kernels launched by this pool since creation (any thread)
 	// phase timing: one set of events per profiled pass
 	std::vector<cudaEvent_t> prof_events;
 	uint32_t prof_passes = 0, prof_max_passes = 0;
@@ -43,4 +44,9 @@ inline uint32_t hd_prof_events_per_pass(uint32_t L) { return 3u + 2u * L + 1u; }
 
 // hd_engine.cu
 hd_status hd_check(cudaError_t e);
+// hd_trace.cu (no wait for edit passes on other streams; the caller orders)
+hd_status hd_launch_pinhole(hd_pool *pool, uint32_t root, const hd_camera *d_cams, uint32_t n_cameras, uint32_t width,
+                            uint32_t height, hd_hit *d_out, uint64_t *d_counters, cudaStream_t st);
+hd_status hd_launch_rays(hd_pool *pool, uint32_t root, const float *d_o, const float *d_d, uint32_t n, hd_hit *d_out,
+                         cudaStream_t st);
 void hd_grid_for_levels(const hd_pool *pool, const hd_edit_desc *host_edits, uint32_t n, uint32_t *grid_per_level);

@@ -1137,8 +1137,9 @@ static __global__ void __launch_bounds__(kBlock) k_commit(DevPool P, Workspace W
 				r = it.res[i];
 				const u32 slot = it.link[i];
 				const u32 phys = P.page_table[r >> P.cfg.wbpp];
-				if (page_lost(P, phys)) {
+				if (page_lost(P, phys)) { // its page could not be allocated: the pass fails
 					P.index[slot] = kSlotTomb;
+					set_error(&P.counters[kCtrError], kErrOom);
 					r = kNull;
 					break;
 				}

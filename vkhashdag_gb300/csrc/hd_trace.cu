@@ -284,24 +284,38 @@ hd_status hd_trace_pinhole_async(hd_pool *pool, uint32_t root, const hd_camera *
 	if (cudaSetDevice(pool->device) != cudaSuccess)
 		return HD_ERR_CUDA;
 	cudaStream_t st = (cudaStream_t)stream;
+	if (cudaStreamWaitEvent(st, pool->ws_free, 0) != cudaSuccess)
+		return HD_ERR_CUDA;
 	hd_camera *d_cams = nullptr;
 	if (cudaMallocAsync((void **)&d_cams, n_cameras * sizeof(hd_camera), st) != cudaSuccess)
 		return HD_ERR_CUDA;
 	hd_status s = HD_OK;
-	if (cudaStreamWaitEvent(st, pool->ws_free, 0) != cudaSuccess ||
-	    cudaMemcpyAsync(d_cams, cameras, n_cameras * sizeof(hd_camera), cudaMemcpyHostToDevice, st) != cudaSuccess)
+	if (cudaMemcpyAsync(d_cams, cameras, n_cameras * sizeof(hd_camera), cudaMemcpyHostToDevice, st) != cudaSuccess)
 		s = HD_ERR_CUDA;
-	if (!s) {
-		const uint64_t total = (uint64_t)width * height * n_cameras;
-		const uint32_t grid = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((total + 255) / 256, pool->num_sms * 16ull));
-		k_trace_pinhole<<<grid, 256, 0, st>>>(pool->P, root, d_cams, n_cameras, width, height, d_out,
-		                                      reinterpret_cast<unsigned long long *>(d_counters));
-		pool->kernel_launches++;
-		if (cudaGetLastError() != cudaSuccess)
-			s = HD_ERR_CUDA;
-	}
+	if (!s)
+		s = hd_launch_pinhole(pool, root, d_cams, n_cameras, width, height, d_out, d_counters, st);
 	cudaFreeAsync(d_cams, st);
 	return s;
 }
 
 } // extern "C"
+
+// Launchers shared with the serving loop: stream-ordered, no wait for edit
+// passes of other streams (the caller traces a root whose pass has completed).
+hd_status hd_launch_pinhole(hd_pool *pool, uint32_t root, const hd_camera *d_cams, uint32_t n_cameras, uint32_t width,
+                            uint32_t height, hd_hit *d_out, uint64_t *d_counters, cudaStream_t st) {
+	const uint64_t total = (uint64_t)width * height * n_cameras;
+	const uint32_t grid = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((total + 255) / 256, pool->num_sms * 16ull));
+	k_trace_pinhole<<<grid, 256, 0, st>>>(pool->P, root, d_cams, n_cameras, width, height, d_out,
+	                                      reinterpret_cast<unsigned long long *>(d_counters));
+	pool->kernel_launches++;
+	return cudaGetLastError() == cudaSuccess ? HD_OK : HD_ERR_CUDA;
+}
+
+hd_status hd_launch_rays(hd_pool *pool, uint32_t root, const float *d_o, const float *d_d, uint32_t n, hd_hit *d_out,
+                         cudaStream_t st) {
+	const uint32_t grid = std::max(1u, std::min((n + 255u) / 256u, (uint32_t)pool->num_sms * 16u));
+	k_trace<<<grid, 256, 0, st>>>(pool->P, root, d_o, d_d, n, d_out);
+	pool->kernel_launches++;
+	return cudaGetLastError() == cudaSuccess ? HD_OK : HD_ERR_CUDA;
+}

@@ -180,3 +180,37 @@ def config_for_resolution(resolution: int, top_bits: int = 10, bottom_bits: int 
     return DefaultConfig(level_count=level_count, top_level_count=top_levels, word_bits_per_page=word_bits_per_page,
                          page_bits_per_bucket=page_bits_per_bucket, bucket_bits_per_top_level=top_bits,
                          bucket_bits_per_bottom_level=bottom_bits)()
+
+
+# bucket bits of the six bottom node levels, top to bottom (leaf level last):
+# the levels just above the leaves hold most of the words an edit inserts
+SERVING_BOTTOM_BITS = (11, 12, 13, 14, 14, 10)
+
+
+def serving_upper_bits(level: int) -> int:
+    """Bucket bits of an upper level of a serving scene.  Every pass writes a
+    new copy of each ancestor it touches (up to 8^l at level l) and nothing is
+    collected, so the upper levels get room for thousands of passes: 8, 64 and
+    512 buckets on levels 0-2, 1024 below."""
+    return min(3 * level + 3, 10)
+
+
+def serving_config(resolution: int, bottom_bits=SERVING_BOTTOM_BITS):
+    """Config of a resident serving scene: 64 KB pages (word_bits_per_page 14),
+    4 pages per bucket, serving_upper_bits() on the upper levels and
+    `bottom_bits` on the six lowest; at most 55k buckets (3.6e9 words) up to
+    2^16 voxels per side, so pointers stay 32-bit."""
+    from . import Config
+    level_count = resolution.bit_length() - 1
+    assert 1 << level_count == resolution and level_count >= 2
+    L = level_count - 1
+    bits = [serving_upper_bits(l) for l in range(L)]
+    nb = min(len(bottom_bits), L)
+    bits[L - nb:] = list(bottom_bits)[len(bottom_bits) - nb:]
+    return Config(14, 2, bits)
+
+
+def poisson_arrivals(seed: int, n: int, rate: float) -> np.ndarray:
+    """Arrival times (s) of a Poisson stream of `rate` requests/s."""
+    u = uniform(seed, 71, n)
+    return np.cumsum(-np.log1p(-u) / rate)
