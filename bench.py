@@ -256,6 +256,7 @@ def run_ours(args):
     if err:
         raise RuntimeError(f"device error {err} in the timed region")
     counters = pool.last_counters_full()
+    probe_stats = pool.last_probe_stats()
     # self-check: re-running the last batch on the same pool finds every node it
     # inserted, so the synchronous path must return the very same root
     last_root = int(d_out[n_batches - 1].item()) & 0xFFFFFFFF
@@ -379,6 +380,7 @@ def run_ours(args):
                      "dedup_ms_per_step": per_step_dedup_ms},
         "phases_ms_per_step": phase_ms,
         "counters_last_step": {k: [int(x) for x in v] for k, v in counters.items()},
+        "probe_stats_last_step": probe_stats,
         "cpu_baseline": cpu,
         "gpu_launches": int(launches),
         "clocks": clk,

@@ -175,6 +175,10 @@ hd_status hd_edit_reserve(hd_pool *pool, uint64_t max_items, uint64_t max_list_e
  * appended to buckets and their words. */
 hd_status hd_edit_last_counters(hd_pool *pool, uint64_t *items, uint64_t *candidates, uint64_t *candidate_words,
                                 uint64_t *inserted, uint64_t *inserted_words);
+/* Dedup-index statistics of the last edit pass (any may be NULL): index slots
+ * visited by all find-or-insert probes, the longest single probe, and failed
+ * compare-and-swap attempts on bucket word counts (contention). */
+hd_status hd_edit_last_probe_stats(hd_pool *pool, uint64_t *probe_steps, uint64_t *max_probe, uint64_t *cas_retries);
 /* Checkpoint / rollback of the whole pool state (bucket word counts, page
  * table, heap and index counters, dedup index), kept in device memory.
  * Rollback (stream-ordered) forgets every node inserted after the checkpoint;

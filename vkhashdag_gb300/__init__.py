@@ -118,6 +118,7 @@ def lib():
         "hd_edit_async_droot": (I, [P, P, P, U32, P, P]),
         "hd_edit_reserve": (I, [P, U64, U64, U32]),
         "hd_edit_last_counters": (I, [P, P, P, P, P, P]),
+        "hd_edit_last_probe_stats": (I, [P, P, P, P]),
         "hd_pool_checkpoint": (I, [P]),
         "hd_pool_rollback": (I, [P, P]),
         "hd_upsert": (I, [P, U32, P, P, U32, P]),
@@ -381,6 +382,13 @@ class NodePool:
         arrs = {k: np.zeros(n, np.uint64) for k in names}
         _check(lib().hd_edit_last_counters(self._h, *[_ptr(arrs[k]) for k in names]), "hd_edit_last_counters")
         return arrs
+
+    def last_probe_stats(self) -> dict:
+        """Index slots visited by the last pass's probes, longest probe, bucket CAS retries."""
+        v = np.zeros(3, np.uint64)
+        _check(lib().hd_edit_last_probe_stats(self._h, _ptr(v[0:1]), _ptr(v[1:2]), _ptr(v[2:3])),
+               "hd_edit_last_probe_stats")
+        return {"probe_steps": int(v[0]), "max_probe": int(v[1]), "cas_retries": int(v[2])}
 
     def checkpoint(self):
         _check(lib().hd_pool_checkpoint(self._h), "hd_pool_checkpoint")

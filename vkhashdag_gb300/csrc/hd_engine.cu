@@ -724,7 +724,7 @@ hd_status hd_pool_create(const hd_config *config, uint64_t heap_pages, uint32_t 
 	const uint64_t heap_words = heap_pages << c.wbpp;
 	uint64_t slots = 1;
 	if (index_log2)
-		slots = 1ull << std::min<uint32_t>(index_log2, 40);
+		slots = 1ull << std::min<uint32_t>(index_log2, 31); // slot numbers are carried as u32
 	else
 		while (slots < std::max<uint64_t>(heap_words / 2, 1024))
 			slots <<= 1;
@@ -987,6 +987,23 @@ hd_status hd_edit_last_counters(hd_pool *pool, uint64_t *items, uint64_t *candid
 		if (inserted_words)
 			inserted_words[l] = c[kWsInsWords + l];
 	}
+	return HD_OK;
+}
+
+hd_status hd_edit_last_probe_stats(hd_pool *pool, uint64_t *probe_steps, uint64_t *max_probe, uint64_t *cas_retries) {
+	if (!pool)
+		return HD_ERR_INVALID_ARG;
+	std::lock_guard<std::mutex> lk(pool->mtx);
+	HD_TRY(cudaSetDevice(pool->device));
+	HD_TRY(cudaEventSynchronize(pool->ws_free));
+	std::vector<unsigned long long> c(kWsCtrCount);
+	HD_TRY(cudaMemcpy(c.data(), pool->ws.d.ctr, kWsCtrCount * 8, cudaMemcpyDeviceToHost));
+	if (probe_steps)
+		*probe_steps = c[kWsProbeSteps];
+	if (max_probe)
+		*max_probe = c[kWsMaxProbe];
+	if (cas_retries)
+		*cas_retries = c[kWsCasRetry];
 	return HD_OK;
 }
 

@@ -831,7 +831,7 @@ __device__ __forceinline__ bool equal_resident(const DevPool &P, u32 ptr, const 
 
 // Reserve space for a node of w words in bucket b (NodePool.hpp:134-157 on an
 // atomic word count).  Returns false when the bucket is full.
-__device__ __forceinline__ bool reserve(const DevPool &P, Workspace &W, u32 b, u32 w, u32 *ptr_out, u32 *pad_out) {
+__device__ __forceinline__ bool reserve(const DevPool &P, u32 b, u32 w, u32 *ptr_out, u32 *pad_out, u32 *retries) {
 	const u32 wp = wpp(P.cfg), wpb = 1u << (P.cfg.wbpp + P.cfg.pbpb);
 	u32 old = *(volatile u32 *)&P.bucket_words[b];
 	u32 off, nw;
@@ -849,7 +849,7 @@ __device__ __forceinline__ bool reserve(const DevPool &P, Workspace &W, u32 b, u
 		const u32 prev = atomicCAS(&P.bucket_words[b], old, nw);
 		if (prev == old)
 			break;
-		atomicAdd(&W.ctr[kWsCasRetry], 1ull);
+		++*retries;
 		old = prev;
 	}
 	*pad_out = off != old ? old : kNull;
@@ -873,31 +873,30 @@ __device__ __forceinline__ bool reserve(const DevPool &P, Workspace &W, u32 b, u
 // few dozen); longer walks are reported as a full index instead of scanned.
 static constexpr u64 kMaxProbe = 1u << 16;
 template <typename CmpPending>
-__device__ __forceinline__ Outcome find_or_claim(const DevPool &P, Workspace &W, u64 i, u32 level, u32 h, u32 bucket,
-                                                 const NodeWords &nw, u32 *probes, CmpPending &&cmp_pending) {
+__device__ __forceinline__ Outcome find_or_claim(const DevPool &P, u64 i, u32 level, u32 h, u32 bucket,
+                                                 const NodeWords &nw, u32 *probes, u32 *retries,
+                                                 CmpPending &&cmp_pending) {
 	const u64 mask = P.index_mask;
 	const unsigned long long tag = (unsigned long long)(h & 0x7FFFFFFFu) << 32;
 	const u32 bucket_shift = P.cfg.wbpp + P.cfg.pbpb;
 	const u64 limit = mask < kMaxProbe ? mask + 1 : kMaxProbe;
 	u64 s = index_start(h, level, mask);
+	const unsigned long long claim = (1ull << 63) | tag | (unsigned long long)i;
 	Outcome out = {kStFail, kNull, kNull, kNull};
 	u64 probe = 0;
 	for (; probe < limit; ++probe, s = (s + 1) & mask) {
-		unsigned long long v = *(volatile unsigned long long *)&P.index[s];
+		// claim-or-read in one atomic: an empty slot is claimed at once (no
+		// separate load first), an occupied one returns its entry
+		const unsigned long long v = atomicCAS(&P.index[s], kSlotEmpty, claim);
 		if (v == kSlotEmpty) {
-			const unsigned long long claim = (1ull << 63) | tag | (unsigned long long)i;
-			const unsigned long long prev = atomicCAS(&P.index[s], kSlotEmpty, claim);
-			if (prev == kSlotEmpty) {
-				u32 ptr, pad;
-				if (reserve(P, W, bucket, nw.n, &ptr, &pad))
-					out = {kStRep, ptr, (u32)s, pad};
-				else {
-					set_error(&P.counters[kCtrError], kErrBucketFull);
-					out = {kStFail, kNull, (u32)s, kNull};
-				}
-				break;
+			u32 ptr, pad;
+			if (reserve(P, bucket, nw.n, &ptr, &pad, retries))
+				out = {kStRep, ptr, (u32)s, pad};
+			else {
+				set_error(&P.counters[kCtrError], kErrBucketFull);
+				out = {kStFail, kNull, (u32)s, kNull};
 			}
-			v = prev;
+			break;
 		}
 		if (v == kSlotTomb || ((v >> 32) & 0x7FFFFFFFull) != (tag >> 32))
 			continue;
@@ -918,10 +917,37 @@ __device__ __forceinline__ Outcome find_or_claim(const DevPool &P, Workspace &W,
 	return out;
 }
 
-__device__ __forceinline__ void warp_count(unsigned long long *ctr, u32 v) {
-	v = __reduce_add_sync(kFullMask, v);
-	if (lane_id() == 0 && v)
-		atomicAdd(ctr, (unsigned long long)v);
+// Per-thread statistics summed (or maxed) over the block, then one global
+// atomic per counter and block instead of one per warp and iteration.  s_acc
+// holds N shared slots zeroed before the block's first __syncthreads; every
+// thread of the block calls this once, after its loop.
+template <int N>
+__device__ __forceinline__ void flush_block_stats(const unsigned long long (&v)[N], unsigned long long *const (&dst)[N],
+                                                  const bool (&is_max)[N], unsigned long long *s_acc) {
+#pragma unroll
+	for (int k = 0; k < N; ++k) {
+		unsigned long long x = v[k];
+#pragma unroll
+		for (int d = 16; d > 0; d >>= 1) {
+			const unsigned long long y = __shfl_down_sync(kFullMask, x, d);
+			x = is_max[k] ? (x > y ? x : y) : x + y;
+		}
+		if (lane_id() == 0 && x) {
+			if (is_max[k])
+				atomicMax(&s_acc[k], x);
+			else
+				atomicAdd(&s_acc[k], x);
+		}
+	}
+	__syncthreads();
+#pragma unroll
+	for (int k = 0; k < N; ++k)
+		if (threadIdx.x == (unsigned)k && s_acc[k]) {
+			if (is_max[k])
+				atomicMax(dst[k], s_acc[k]);
+			else
+				atomicAdd(dst[k], s_acc[k]);
+		}
 }
 
 // ------------------------------------------------------------------ k_probe
@@ -957,10 +983,14 @@ static __global__ void __launch_bounds__(kBlock) k_probe(DevPool P, Workspace W,
 			s_key[e] = 0ull; // no leaf candidate is all-empty
 			s_val[e] = kNull;
 		}
+	__shared__ unsigned long long s_acc[5];
+	if (threadIdx.x < 5)
+		s_acc[threadIdx.x] = 0ull;
 	if (threadIdx.x == 0)
 		s_skip = pool_failed(P) ? 1 : 0;
 	__syncthreads();
 	const bool skip = s_skip != 0;
+	u32 a_cand = 0, a_words = 0, a_steps = 0, a_retry = 0, a_max = 0; // per-thread sums (saturating)
 	const u32 L = P.cfg.L;
 	u64 begin, n;
 	probe_range(W, L, l, use_todo, begin, n);
@@ -1050,16 +1080,17 @@ static __global__ void __launch_bounds__(kBlock) k_probe(DevPool P, Workspace W,
 		}
 		const bool follower = eq;
 		Outcome o = {kStFail, kNull, kNull, kNull};
-		u32 probes = 0;
+		u32 probes = 0, retries = 0;
 		if (probe_me && !follower) {
 			const u32 bucket = bbase + ((zero_hash ? 0u : h) & nb_mask);
 			if (Leaf) {
 				const u64 mine = W.leaf_new[i];
-				o = find_or_claim(P, W, i, l, h, bucket, nw, &probes, [&](u32 j) { return W.leaf_new[j] == mine; });
+				o = find_or_claim(P, i, l, h, bucket, nw, &probes, &retries,
+				                  [&](u32 j) { return W.leaf_new[j] == mine; });
 			} else {
 				const uint4 *cn4 = reinterpret_cast<const uint4 *>(W.cnew + i * 8u);
 				const uint4 a0 = cn4[0], a1 = cn4[1];
-				o = find_or_claim(P, W, i, l, h, bucket, nw, &probes, [&](u32 j) {
+				o = find_or_claim(P, i, l, h, bucket, nw, &probes, &retries, [&](u32 j) {
 					const uint4 *o4 = reinterpret_cast<const uint4 *>(W.cnew + (u64)j * 8u);
 					const uint4 c0 = o4[0], c1 = o4[1];
 					return c0.x == a0.x && c0.y == a0.y && c0.z == a0.z && c0.w == a0.w && c1.x == a1.x &&
@@ -1092,13 +1123,17 @@ static __global__ void __launch_bounds__(kBlock) k_probe(DevPool P, Workspace W,
 			if (!Leaf)
 				it.pad[i] = o.pad;
 		}
-		warp_count(&W.ctr[kWsCand + l], cand ? 1u : 0u);
-		warp_count(&W.ctr[kWsCandWords + l], cand ? nw.n : 0u);
-		warp_count(&W.ctr[kWsProbeSteps], probes);
-		const u32 pmax = __reduce_max_sync(kFullMask, probes);
-		if (lane == 0 && pmax)
-			atomicMax(&W.ctr[kWsMaxProbe], (unsigned long long)pmax);
+		a_cand += cand ? 1u : 0u;
+		a_words += cand ? nw.n : 0u;
+		a_steps = a_steps + probes < a_steps ? 0xFFFFFFFFu : a_steps + probes;
+		a_retry = a_retry + retries < a_retry ? 0xFFFFFFFFu : a_retry + retries;
+		a_max = a_max > probes ? a_max : probes;
 	}
+	const unsigned long long v[5] = {a_cand, a_words, a_steps, a_retry, a_max};
+	unsigned long long *const dst[5] = {&W.ctr[kWsCand + l], &W.ctr[kWsCandWords + l], &W.ctr[kWsProbeSteps],
+	                                    &W.ctr[kWsCasRetry], &W.ctr[kWsMaxProbe]};
+	const bool is_max[5] = {false, false, false, false, true};
+	flush_block_stats(v, dst, is_max, s_acc);
 }
 
 // ------------------------------------------------------------------ k_commit
@@ -1106,6 +1141,11 @@ template <bool Leaf>
 static __global__ void __launch_bounds__(kBlock) k_commit(DevPool P, Workspace W, u32 l, u32 use_todo) {
 	if (ws_failed(W))
 		return;
+	__shared__ unsigned long long s_acc[2];
+	if (threadIdx.x < 2)
+		s_acc[threadIdx.x] = 0ull;
+	__syncthreads();
+	u32 a_ins = 0, a_insw = 0;
 	const u32 L = P.cfg.L;
 	u64 begin, n;
 	probe_range(W, L, l, use_todo, begin, n);
@@ -1136,7 +1176,8 @@ static __global__ void __launch_bounds__(kBlock) k_commit(DevPool P, Workspace W
 			case kStRep: {
 				r = it.res[i];
 				const u32 slot = it.link[i];
-				const u32 phys = P.page_table[r >> P.cfg.wbpp];
+				// identity heap: virtual page = physical page, no table read
+				const u32 phys = P.identity ? (r >> P.cfg.wbpp) : P.page_table[r >> P.cfg.wbpp];
 				if (page_lost(P, phys)) { // its page could not be allocated: the pass fails
 					P.index[slot] = kSlotTomb;
 					set_error(&P.counters[kCtrError], kErrOom);
@@ -1144,28 +1185,37 @@ static __global__ void __launch_bounds__(kBlock) k_commit(DevPool P, Workspace W
 					break;
 				}
 				u32 *dst = P.heap + ((u64)phys << P.cfg.wbpp) + (r & (wp - 1u));
+				u32 h;
 				if (Leaf) {
 					const u64 bits = W.leaf_new[i];
 					dst[0] = (u32)bits;
 					dst[1] = (u32)(bits >> 32);
 					insw = 2;
+					h = hash_leaf(bits);
 				} else {
 					const uint4 *cn4 = reinterpret_cast<const uint4 *>(W.cnew + i * 8u);
 					const uint4 a0 = cn4[0], a1 = cn4[1];
 					const u32 c[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-					u32 mask = 0, k = 1;
+					u32 mask = 0;
+#pragma unroll
+					for (int q = 0; q < 8; ++q)
+						mask |= c[q] != kNull ? 1u << q : 0u;
+					Murmur mm;
+					mm.add(mask);
+					u32 k = 1;
 #pragma unroll
 					for (int q = 0; q < 8; ++q)
 						if (c[q] != kNull) {
-							mask |= 1u << q;
 							dst[k++] = c[q];
+							mm.add(c[q]);
 						}
 					dst[0] = mask;
 					insw = k;
+					h = mm.finish(k);
 					const u32 pad = it.pad[i];
 					if (pad != kNull) {
 						const u32 vp = ((r >> bucket_shift) << P.cfg.pbpb) | (pad >> P.cfg.wbpp);
-						const u32 zp = P.page_table[vp];
+						const u32 zp = P.identity ? vp : P.page_table[vp];
 						if (zp != kUnallocPage && !page_lost(P, zp)) {
 							u32 *z = P.heap + ((u64)zp << P.cfg.wbpp);
 							for (u32 q = pad & (wp - 1u); q < wp; ++q)
@@ -1174,9 +1224,9 @@ static __global__ void __launch_bounds__(kBlock) k_commit(DevPool P, Workspace W
 					}
 				}
 				ins = 1;
-				__threadfence();
-				const unsigned long long pend = P.index[slot];
-				P.index[slot] = (((pend >> 32) & 0x7FFFFFFFull) << 32) | r;
+				// publish: the claim's tag is the content hash, recomputed here
+				// instead of read back; readers of the entry run in later launches
+				P.index[slot] = ((unsigned long long)(h & 0x7FFFFFFFu) << 32) | r;
 				break;
 			}
 			default: // kStFail
@@ -1192,9 +1242,13 @@ static __global__ void __launch_bounds__(kBlock) k_commit(DevPool P, Workspace W
 			else
 				W.cnew[ps] = r;
 		}
-		warp_count(&W.ctr[kWsIns + l], ins);
-		warp_count(&W.ctr[kWsInsWords + l], insw);
+		a_ins += ins;
+		a_insw += insw;
 	}
+	const unsigned long long v[2] = {a_ins, a_insw};
+	unsigned long long *const dst[2] = {&W.ctr[kWsIns + l], &W.ctr[kWsInsWords + l]};
+	const bool is_max[2] = {false, false};
+	flush_block_stats(v, dst, is_max, s_acc);
 }
 
 // ------------------------------------------------------------------ k_finish
