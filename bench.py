@@ -839,6 +839,78 @@ def run_serving(args):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------- garbage collection
+def _gc_workload(hd, W, res, n_batches, n_edits, device, heap_pages):
+    """Seeded scene plus n_batches batches applied one after another (no
+    rollback): every batch leaves the nodes it replaced behind."""
+    from vkhashdag_gb300 import Config
+    cfg = bench_config() if res == RES else W.config_for_resolution(res, bottom_bits=16, top_levels=6)
+    pool = hd.NodePool(cfg, heap_pages=min(cfg.get_total_pages(), heap_pages), device=device)
+    root = pool.edit(hd.NULL, W.sphere_scene(res, 64, seed=0))
+    for k in range(n_batches):
+        root = pool.edit(root, W.mixed_batch(res, n_edits, seed=2000 + k))
+    return cfg, pool, root
+
+
+def run_gc(args):
+    import torch
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    build_if_needed()
+    import vkhashdag_gb300 as hd
+    from vkhashdag_gb300 import workloads as W
+    res = args.resolution
+    cfg, pool, root = _gc_workload(hd, W, res, args.gc_batches, args.n_edits, local, args.heap_pages)
+    q = W.point_queries(res, 1 << 16, seed=7)
+    occ = pool.query(root, q)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        t0 = time.perf_counter()
+        (new_root,), st = pool.gc([root])
+        t_gc = time.perf_counter() - t0
+    same = bool(np.array_equal(pool.query(new_root, q), occ))
+    moved = 4.0 * 2 * st["words_after"]  # live words read once and written once
+    # CPU: the oracle's collector (the reference's algorithm, one thread) on a
+    # smaller pool of the same workload; the device collects the same pool, and
+    # both results must be word-identical
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        import oracle
+        oracle.build()
+        cres = args.gc_cpu_resolution
+        ccfg, cpool, croot = _gc_workload(hd, W, cres, args.gc_batches, max(1, args.n_edits // 8), local, 1 << 22)
+        bw, ids, pages = cpool.download()
+        opool = oracle.OraclePool.from_config(ccfg)
+        opool.load(bw, ids, pages, cpool.filled_node_pointers())
+        tc = time.perf_counter()
+        (oroot,) = opool.gc([croot])
+        t_cpu = time.perf_counter() - tc
+        tg = time.perf_counter()
+        (groot,), cst = cpool.gc([croot])
+        t_dev_small = time.perf_counter() - tg
+        wb, pb = ccfg.word_bits_per_page, ccfg.page_bits_per_bucket
+        identical = (oroot == groot and oracle.pool_words_digest(*opool.dump(), wb, pb) ==
+                     oracle.pool_words_digest(*cpool.download(), wb, pb))
+        cpu = {"value": cst["live_nodes"] / t_cpu, "unit": "live nodes/s", "cores": 1, "kind": "port",
+               "sample": f"{cres}^3 pool of the same workload ({cst['live_nodes']} live nodes, "
+                         f"{cst['words_before']} words before): oracle collector {t_cpu:.2f} s vs device "
+                         f"{t_dev_small * 1e3:.1f} ms",
+               "device_value_same_pool": cst["live_nodes"] / t_dev_small, "word_identical": bool(identical)}
+    if rank != 0:
+        return
+    line = {
+        "metric": "garbage collection: live nodes/s (mark + compact + index rebuild, one call)",
+        "value": st["live_nodes"] / t_gc, "unit": "live nodes/s", "n_gpus": 1, "steps": 1, "warmup": 0,
+        "ms_per_step": 1e3 * t_gc, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u32", "data": "synthetic",
+        "config": {"workload": f"{res}^3 sphere scene + {args.gc_batches} x {args.n_edits} mixed edits, "
+                               f"collect keeping the last root", "node_levels": cfg.get_node_levels()},
+        "gc": st, "live_bytes_moved_gbs": moved / t_gc / 1e9, "queries_equal_after": same,
+        "cpu_baseline": cpu, "clocks": clocks.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -852,7 +924,9 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-step-seconds", type=float, default=6.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--mode", default="batched", choices=["batched", "terrain", "rays", "serving"])
+    ap.add_argument("--mode", default="batched", choices=["batched", "terrain", "rays", "serving", "gc"])
+    ap.add_argument("--gc-batches", type=int, default=2)
+    ap.add_argument("--gc-cpu-resolution", type=int, default=4096)
     ap.add_argument("--rate", type=float, default=1000.0)
     ap.add_argument("--serve-seconds", type=float, default=5.0)
     ap.add_argument("--serve-heap-gb", type=float, default=8.0)
@@ -876,6 +950,8 @@ def main():
         run_terrain(args)
     elif args.mode == "serving":
         run_serving(args)
+    elif args.mode == "gc":
+        run_gc(args)
     elif args.mode == "rays":
         if args.resolution == RES:
             args.resolution = TERRAIN_RES

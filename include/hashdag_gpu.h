@@ -238,6 +238,27 @@ hd_status hd_pool_read_pages(const hd_pool *pool, const uint32_t *page_ids, uint
 hd_status hd_pool_upload(hd_pool *pool, const uint32_t *bucket_words, const uint32_t *page_ids, uint32_t n_pages,
                          const uint32_t *page_words, const uint32_t *filled_levels);
 
+/* ---- garbage collection -----------------------------------------------------
+ * NodePoolThreadedGC::ThreadedGC (include/hashdag/NodePoolThreadedGC.hpp:29-403):
+ * keeps the nodes reachable from roots[0..n_roots) and from the filled nodes,
+ * compacts every level into the layout the reference's collector writes with
+ * one worker (buckets re-filled in old-pointer order, inner nodes re-hashed
+ * into their new buckets), frees every page it no longer needs, rebuilds the
+ * dedup index and re-finds the filled nodes.  roots are remapped in place
+ * (HD_NULL_PTR stays).  Every root made before the call and not passed in
+ * becomes invalid.  Nothing is changed when it fails (a root that is not a
+ * level-0 node: HD_ERR_INVALID_ARG; a bucket that cannot hold the nodes that
+ * hash to it after compaction: HD_ERR_BUCKET_FULL; not enough device memory
+ * for the collection's scratch: HD_ERR_POOL_OOM).  stats may be NULL. */
+typedef struct hd_gc_stats {
+	uint64_t live_nodes;     /* nodes kept */
+	uint64_t words_before;   /* sum of bucket word counts before / after */
+	uint64_t words_after;
+	uint64_t pages_before;   /* heap pages in use before / after */
+	uint64_t pages_after;
+} hd_gc_stats;
+hd_status hd_gc(hd_pool *pool, uint32_t *roots, uint32_t n_roots, hd_gc_stats *stats);
+
 /* ---- read path --------------------------------------------------------------
  * Point occupancy: out[i] = voxel (xyz[3i], xyz[3i+1], xyz[3i+2]) set under root. */
 hd_status hd_query(hd_pool *pool, uint32_t root, const uint32_t *xyz, uint32_t n, uint8_t *out, void *stream);
@@ -269,7 +290,10 @@ hd_status hd_trace_pinhole_async(hd_pool *pool, uint32_t root, const hd_camera *
  *     against its scene's last finished root at the moment it starts, so ray
  *     work overlaps the scenes' edit passes on the device;
  *   - a merged pass that fails is re-run request by request from the pass's
- *     input root, so every request gets the status it would get alone.
+ *     input root, so every request gets the status it would get alone;
+ *   - with gc_free_fraction set, a scene whose heap runs low is collected
+ *     between two of its passes (its ray requests wait meanwhile), so memory
+ *     frees up and later requests are admitted again.
  * Results: a merged pass's voxels equal applying its requests one after
  * another (the batched-pass contract of hd_edit); a ray request's hits equal
  * hd_trace_pinhole_async on the recorded root. */
@@ -281,6 +305,9 @@ typedef struct hd_server_config {
 	uint32_t max_rays_per_request;  /* larger camera requests are refused (0 = 1 << 24) */
 	uint32_t reserve_pages;         /* heap pages kept free by admission (0 = heap/64) */
 	double pages_per_edit_hint;     /* admission estimate before the first pass (0 = 1.0) */
+	double gc_free_fraction;        /* collect a scene (hd_gc, its current root kept) after a pass
+	                                   that leaves fewer than this fraction of its heap pages free;
+	                                   0 = never */
 } hd_server_config;
 
 typedef enum hd_request_kind { HD_REQ_EDIT = 0, HD_REQ_CAMERA = 1 } hd_request_kind;
@@ -299,6 +326,8 @@ typedef struct hd_request_result {
 	uint64_t rays;           /* camera: rays traced */
 	uint64_t hits, steps, node_words; /* camera: traversal counters */
 	double t_submit_ms, t_start_ms, t_done_ms; /* ms since hd_server_create */
+	uint64_t gc_epoch;       /* collections of the scene before root_in / root were taken: roots
+	                            of an older epoch are no longer valid */
 } hd_request_result;
 
 typedef struct hd_server_stats {
@@ -307,6 +336,8 @@ typedef struct hd_server_stats {
 	uint64_t edit_passes, edits_applied, rays_traced;
 	uint32_t max_pass_requests, queued;      /* largest merge; requests not finished yet */
 	double edit_p50_ms, edit_p99_ms, camera_p50_ms, camera_p99_ms; /* submit -> done */
+	uint64_t gc_runs;                        /* collections run by the server */
+	double gc_ms;                            /* their total wall time */
 } hd_server_stats;
 
 /* pools[i] with its current root roots[i] (HD_NULL_PTR = empty) is scene i.

@@ -92,6 +92,7 @@ def lib():
             "orc_dense": (None, [P, U32, P]),
             "orc_trace": (None, [P, U32, P, P, U32, P]),
             "orc_trace_threads": (None, [P, U32, P, P, U32, P, I]),
+            "orc_gc": (None, [P, P, U32]),
             "orc_hash_inner": (U32, [P, U32]),
             "orc_hash_leaf": (U32, [U32, U32]),
         }
@@ -177,6 +178,12 @@ class OraclePool:
         fl = None if filled is None else np.ascontiguousarray(filled, np.uint32)
         lib().orc_pool_load(self._h, _p(bw), _p(ids), len(ids), _p(pg), None if fl is None else _p(fl))
 
+    def gc(self, roots):
+        """NodePoolThreadedGC::ThreadedGC (one-worker order); returns the remapped roots."""
+        r = np.ascontiguousarray(roots, np.uint32).copy()
+        lib().orc_gc(self._h, _p(r), len(r))
+        return [int(x) for x in r]
+
     def canonical(self, root):
         """(ok, per-level unique node counts, per-level digests) of the reachable DAG."""
         c = np.zeros(self.L, np.uint64)
@@ -217,11 +224,11 @@ def hash_leaf(w0, w1) -> int:
 
 
 # ---------------------------------------------------------------------- reference driver
-MODE_EDIT, MODE_THREADED, MODE_UPSERT, MODE_TRACE = 0, 1, 2, 3
+MODE_EDIT, MODE_THREADED, MODE_UPSERT, MODE_TRACE, MODE_GC = 0, 1, 2, 3, 4
 
 
 def run_reference(mode, word_bits_per_page, page_bits_per_bucket, bucket_bits, edits=None, hasher=0, threads=1,
-                  max_task_level=0xFFFFFFFF, upserts=None, rays=None):
+                  max_task_level=0xFFFFFFFF, upserts=None, rays=None, keep=None):
     """Run the reference headers through oracle/_ref/ref_driver.  Returns a dict
     with root, filled, bucket_words, page_ids, pages, elapsed_ns, and ptrs
     (upsert mode) or hits (trace mode: hit flags and positions)."""
@@ -237,6 +244,8 @@ def run_reference(mode, word_bits_per_page, page_bits_per_bucket, bucket_bits, e
         req += struct.pack("<I", len(upserts))
         for level, words in upserts:
             req += struct.pack(f"<{2 + len(words)}I", level, len(words), *words)
+    if mode == MODE_GC:
+        req += struct.pack(f"<{1 + len(keep)}I", len(keep), *keep)
     if mode == MODE_TRACE:
         o, d = rays
         o = np.ascontiguousarray(o, np.float32).reshape(-1, 3)
@@ -272,6 +281,13 @@ def run_reference(mode, word_bits_per_page, page_bits_per_bucket, bucket_bits, e
         pages[i] = np.frombuffer(data, np.uint32, wpp, off)
         off += 4 * wpp
     out = dict(root=root, filled=filled, bucket_words=bw, page_ids=ids, pages=pages, elapsed_ns=ns)
+    if mode == MODE_GC:
+        (n,) = struct.unpack_from("<I", data, off)
+        off += 4
+        out["roots_before"] = list(struct.unpack_from(f"<{n}I", data, off))
+        off += 4 * n
+        out["roots_after"] = list(struct.unpack_from(f"<{n}I", data, off))
+        off += 4 * n
     if mode == MODE_UPSERT:
         (n,) = struct.unpack_from("<I", data, off)
         off += 4
@@ -282,3 +298,22 @@ def run_reference(mode, word_bits_per_page, page_bits_per_bucket, bucket_bits, e
         rec = np.frombuffer(data, np.dtype([("hit", "<u4"), ("pos", "<f4", (3,))]), n, off)
         out["hits"] = rec.copy()
     return out
+
+
+def pool_words_digest(bucket_words, page_ids, pages, word_bits_per_page, page_bits_per_bucket) -> str:
+    """sha256 over every bucket's word count and its words [0, count) in bucket
+    order: the pool's meaningful content (words past a bucket's count, e.g. in
+    pages a collection left behind, are not part of it)."""
+    import hashlib
+    wpp = 1 << word_bits_per_page
+    where = {int(i): k for k, i in enumerate(page_ids)}
+    h = hashlib.sha256()
+    bw = np.asarray(bucket_words, np.uint32)
+    h.update(bw.tobytes())
+    for b in np.nonzero(bw)[0]:
+        n = int(bw[b])
+        first = int(b) << page_bits_per_bucket
+        for k in range((n + wpp - 1) // wpp):
+            m = min(wpp, n - k * wpp)
+            h.update(np.ascontiguousarray(pages[where[first + k]][:m], np.uint32).tobytes())
+    return h.hexdigest()

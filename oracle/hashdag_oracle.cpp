@@ -325,6 +325,104 @@ struct Pool {
 		}
 	}
 
+	// NodePoolThreadedGC.hpp:29-403 (ThreadedGC) in the order the reference runs
+	// it with one worker: mark level by level from the roots (the filled root
+	// first, :357-369), every bucket's node list sorted and unique (:36-37);
+	// then bottom-up, leaves re-appended in place to their own bucket
+	// (:223-265), inner nodes re-written with remapped children, re-hashed and
+	// appended to their new bucket's cache in old-bucket / old-pointer order
+	// (:105-171) and the caches flushed as the level's new bucket contents
+	// (:189-213); roots remapped at level 0 (:323-328); filled pointers made
+	// again (:378-381).  A bucket cache that outgrows its bucket clears `ok`
+	// (the reference would write past the bucket there).
+	void gc(Word *roots, Word n_roots, bool *ok) {
+		const Word L = cfg.node_levels(), wbpb = cfg.wbpp + cfg.pbpb, wpp = cfg.words_per_page();
+		std::vector<std::vector<Word>> bucket_nodes(cfg.total_buckets());
+		if (!filled.empty() && filled[0] != kNull)
+			bucket_nodes[filled[0] >> wbpb].push_back(filled[0]);
+		for (Word i = 0; i < n_roots; ++i)
+			if (roots[i] != kNull)
+				bucket_nodes[roots[i] >> wbpb].push_back(roots[i]);
+		for (Word l = 0; l < L; ++l) {
+			const bool leaf = l == L - 1;
+			for (Word b = bases[l]; b < bases[l] + cfg.buckets_at(l); ++b) {
+				std::vector<Word> &v = bucket_nodes[b];
+				std::sort(v.begin(), v.end());
+				v.erase(std::unique(v.begin(), v.end()), v.end());
+				if (leaf)
+					continue;
+				for (Word node : v) {
+					const Word *pn = read_node(node);
+					const Word *child = pn + 1;
+					for (Word m = pn[0]; m; m &= m - 1) {
+						const Word c = *(child++);
+						bucket_nodes[c >> wbpb].push_back(c);
+					}
+				}
+			}
+		}
+		std::unordered_map<Word, Word> child_map, cur_map;
+		for (Word l = L - 1; l != Word(-1); --l) {
+			cur_map.clear();
+			if (l == L - 1) {
+				for (Word b = bases[l]; b < bases[l] + cfg.buckets_at(l); ++b) {
+					Word nbw = 0;
+					for (Word node : bucket_nodes[b]) {
+						const Word w[2] = {read_node(node)[0], read_node(node)[1]};
+						auto [np, nb] = append_node(b, nbw, w, 2);
+						if (np == kNull) {
+							if (ok)
+								*ok = false;
+							break;
+						}
+						cur_map[node] = np;
+						nbw = nb;
+					}
+					bucket_words[b] = nbw;
+				}
+			} else {
+				std::vector<std::vector<Word>> caches(cfg.buckets_at(l));
+				for (Word b = bases[l]; b < bases[l] + cfg.buckets_at(l); ++b)
+					for (Word node : bucket_nodes[b]) {
+						const Word *pn = read_node(node);
+						Word w[9];
+						const Word len = inner_node_words(pn);
+						std::copy(pn, pn + len, w);
+						for (Word i = 1; i < len; ++i)
+							w[i] = child_map.at(w[i]);
+						const Word nb = bases[l] + (node_hash(false, w, len) & (cfg.buckets_at(l) - 1u));
+						std::vector<Word> &cache = caches[nb - bases[l]];
+						Word off = Word(cache.size());
+						if ((off & (wpp - 1u)) + len > wpp)
+							off = ((off >> cfg.wbpp) + 1u) << cfg.wbpp;
+						cache.resize(off + len, 0u);
+						std::copy(w, w + len, cache.begin() + off);
+						cur_map[node] = (nb << wbpb) | off;
+					}
+				for (Word k = 0; k < cfg.buckets_at(l); ++k) {
+					const Word b = bases[l] + k;
+					const std::vector<Word> &cache = caches[k];
+					if (cache.size() > cfg.words_per_bucket()) {
+						if (ok)
+							*ok = false;
+						continue;
+					}
+					for (Word off = 0; off < cache.size(); off += wpp)
+						write_page((b << cfg.pbpb) | (off >> cfg.wbpp), 0, cache.data() + off,
+						           std::min<Word>(wpp, Word(cache.size()) - off));
+					bucket_words[b] = Word(cache.size());
+				}
+			}
+			if (l == 0)
+				for (Word i = 0; i < n_roots; ++i)
+					if (roots[i] != kNull)
+						roots[i] = cur_map.at(roots[i]);
+			std::swap(child_map, cur_map);
+		}
+		filled.clear();
+		make_filled(ok);
+	}
+
 	// NodePool.hpp:278-309
 	std::array<Word, 9> unpack(Word ptr) const {
 		std::array<Word, 9> u;
@@ -902,6 +1000,8 @@ void orc_trace_threads(const orc_pool *p, uint32_t root, const float *o, const f
 	for (int64_t i = 0; i < int64_t(n); ++i)
 		out[i] = orc::trace_ray(p->pool, root, o + 3 * size_t(i), d + 3 * size_t(i));
 }
+
+void orc_gc(orc_pool *p, uint32_t *roots, uint32_t n_roots) { p->pool.gc(roots, n_roots, &p->ok); }
 
 uint32_t orc_hash_inner(const uint32_t *w, uint32_t n) { return orc::murmur_words(w, n); }
 uint32_t orc_hash_leaf(uint32_t w0, uint32_t w1) { return orc::murmur_leaf(w0, w1); }

@@ -4,8 +4,8 @@
 // reference headers (include/hashdag/*.hpp, dep/libfork, dep/glm) where the
 // reference tree is present, into oracle/_ref/.  It executes the reference's
 // NodePoolBase::Edit, NodePoolThreadedEdit::ThreadedEdit,
-// NodePoolBase::upsert_inner_node / upsert_leaf and
-// NodePoolTraversal::Traversal on a vector-backed pool whose storage hooks
+// NodePoolBase::upsert_inner_node / upsert_leaf, NodePoolThreadedGC::ThreadedGC
+// and NodePoolTraversal::Traversal on a vector-backed pool whose storage hooks
 // follow src/DAGNodePool.hpp:56-69, and dumps the resulting pool, so the
 // oracle restatement can be pinned against the reference and golden fixtures
 // can be generated.  The editors restate the stateless SphereEditor<kFill/kDig>
@@ -13,20 +13,27 @@
 // library) plus an AABB dig by symmetry.
 //
 // Protocol (all little-endian uint32 unless noted), input file:
-//   magic 'HDRQ', mode (0 edit, 1 threaded edit, 2 upsert, 3 trace-after-edit),
+//   magic 'HDRQ', mode (0 edit, 1 threaded edit, 2 upsert, 3 trace-after-edit,
+//   4 edit then garbage-collect),
 //   wbpp, pbpb, node_levels, hasher, bucket_bits[node_levels],
 //   threads, max_task_level, n_edits, edits[n_edits] (40 bytes each),
 //   mode 2: n_ops, then per op: level, len, words[len]
 //   mode 3: n_rays, then origins[3n] and dirs[3n] (float)
+//   mode 4: n_keep, keep[n_keep] (keep the root after edit keep[i]; the roots
+//           are the GC roots, collected by ThreadedGC on a one-worker pool)
 // output file:
 //   magic 'HDRS', root, ok, elapsed_ns (uint64), filled[node_levels],
 //   total_buckets, bucket_words[total_buckets], n_pages, then per page: id, words[wpp]
 //   mode 2: n_ops, ptrs[n_ops] (after the pool dump)
 //   mode 3: n_rays, per ray: hit, pos[3] (float)
+//   mode 4: the dump is the pool after GC; then n_keep, roots before[n_keep],
+//           roots after[n_keep]
 
 #include <hashdag/NodePool.hpp>
 #include <hashdag/NodePoolThreadedEdit.hpp>
+#include <hashdag/NodePoolThreadedGC.hpp>
 #include <hashdag/NodePoolTraversal.hpp>
+#include <parallel_hashmap/phmap.h>
 
 #include <chrono>
 #include <cstdio>
@@ -41,9 +48,14 @@ struct ZeroHasher {
 	inline uint32_t operator()(auto &&) const { return 0; }
 };
 
+// the map/set types the application instantiates the GC with (src/DAGNodePool.hpp:26-29)
+template <typename K, typename V> using GcMap = phmap::flat_hash_map<K, V>;
+template <typename K> using GcSet = phmap::flat_hash_set<K>;
+
 template <typename HasherT>
 struct RefPool final : public hashdag::NodePoolBase<RefPool<HasherT>, uint32_t>,
                        public hashdag::NodePoolThreadedEdit<RefPool<HasherT>, uint32_t>,
+                       public hashdag::NodePoolThreadedGC<RefPool<HasherT>, uint32_t, GcMap, GcSet>,
                        public hashdag::NodePoolTraversal<RefPool<HasherT>, uint32_t> {
 	using WordSpanHasher = HasherT;
 	using Base = hashdag::NodePoolBase<RefPool<HasherT>, uint32_t>;
@@ -70,6 +82,7 @@ struct RefPool final : public hashdag::NodePoolBase<RefPool<HasherT>, uint32_t>,
 	void WritePage(uint32_t p, uint32_t off, std::span<const uint32_t> s) {
 		std::copy(s.begin(), s.end(), page(p) + off);
 	}
+	void FreePage(uint32_t p) { pages[p].reset(); }
 };
 
 // Stateless editors (src/main.cpp:32-150) for one hd_edit_desc.
@@ -144,8 +157,30 @@ template <typename HasherT> static int run(FILE *in, FILE *out, uint32_t mode, c
 	hashdag::NodePointer<uint32_t> root{};
 	std::vector<uint32_t> upsert_ptrs;
 	std::vector<float> rays;
+	std::vector<uint32_t> keep_at;
+	std::vector<hashdag::NodePointer<uint32_t>> kept;
+	std::vector<uint32_t> kept_before;
+	if (mode == 4) {
+		uint32_t n_keep = rd(in);
+		keep_at.resize(n_keep);
+		for (auto &k : keep_at)
+			k = rd(in);
+		kept.resize(n_keep);
+	}
 	auto t0 = std::chrono::steady_clock::now();
-	if (mode == 0 || mode == 3) {
+	if (mode == 4) {
+		for (uint32_t i = 0; i < n_edits; ++i) {
+			root = pool->Edit(root, hashdag::StatelessEditorWrapper<uint32_t, DescEditor>{.editor = DescEditor{edits[i]}});
+			for (size_t k = 0; k < keep_at.size(); ++k)
+				if (keep_at[k] == i)
+					kept[k] = root;
+		}
+		for (auto &r : kept)
+			kept_before.push_back(*r);
+		lf::busy_pool busy(1);
+		kept = pool->ThreadedGC(&busy, kept);
+		root = kept.empty() ? hashdag::NodePointer<uint32_t>{} : kept.back();
+	} else if (mode == 0 || mode == 3) {
 		for (auto &e : edits)
 			root = pool->Edit(root, hashdag::StatelessEditorWrapper<uint32_t, DescEditor>{.editor = DescEditor{e}});
 	} else if (mode == 1) {
@@ -190,6 +225,13 @@ template <typename HasherT> static int run(FILE *in, FILE *out, uint32_t mode, c
 			wr(out, i);
 			fwrite(pool->pages[i].get(), 4, config.GetWordsPerPage(), out);
 		}
+	if (mode == 4) {
+		wr(out, (uint32_t)kept.size());
+		for (uint32_t v : kept_before)
+			wr(out, v);
+		for (auto &r : kept)
+			wr(out, *r);
+	}
 	if (mode == 2) {
 		wr(out, (uint32_t)upsert_ptrs.size());
 		fwrite(upsert_ptrs.data(), 4, upsert_ptrs.size(), out);

@@ -51,6 +51,8 @@ def scenario_edits(spec):
                                                  a["r_lo"], a["r_hi"])])
     if kind == "explicit":
         return np.array([tuple(x) for x in spec["edits"]], dtype=EDIT_DTYPE)
+    if kind == "concat":
+        return np.concatenate([scenario_edits(p) for p in spec["parts"]])
     raise ValueError(kind)
 
 
@@ -155,6 +157,42 @@ def upsert_kats():
     return kat, full
 
 
+# NodePoolThreadedGC (ThreadedGC on a one-worker busy pool): edits applied one
+# by one, the roots after the edits listed in `keep` are the GC roots.
+GC_CASES = [
+    dict(name="gc_mixed256", res=256, kind="concat", keep=[10, 40, -1], parts=[
+        dict(kind="sphere_scene", args=dict(resolution=256, n_digs=16, seed=0)),
+        dict(kind="mixed_batch", args=dict(resolution=256, n=60, seed=3, r_max=30, side_max=60))]),
+    dict(name="gc_only_filled", res=256, kind="concat", keep=[], parts=[
+        dict(kind="sphere_scene", args=dict(resolution=256, n_digs=16, seed=0)),
+        dict(kind="mixed_batch", args=dict(resolution=256, n=20, seed=3, r_max=30, side_max=60))]),
+    dict(name="gc_tiny_pages64", res=64, kind="concat", wbpp=4, pbpb=6, keep=[5, -1], parts=[
+        dict(kind="sphere_scene", args=dict(resolution=64, n_digs=8, seed=9)),
+        dict(kind="mixed_batch", args=dict(resolution=64, n=40, seed=5, r_max=8, side_max=16))]),
+    dict(name="gc_zero16", res=16, kind="concat", hasher=1, wbpp=9, pbpb=4, keep=[-1], parts=[
+        dict(kind="sphere_scene", args=dict(resolution=16, n_digs=4, seed=2)),
+        dict(kind="mixed_batch", args=dict(resolution=16, n=20, seed=6, r_max=4, side_max=6))]),
+]
+
+
+def gc_golden(s):
+    cfg = config_of(s)
+    edits = scenario_edits(s)
+    keep = [k if k >= 0 else len(edits) - 1 for k in s["keep"]]
+    wb, pb = cfg.word_bits_per_page, cfg.page_bits_per_bucket
+    pre = oracle.run_reference(oracle.MODE_EDIT, wb, pb, cfg.bucket_bits_each_level, edits, hasher=cfg.hasher)
+    post = oracle.run_reference(oracle.MODE_GC, wb, pb, cfg.bucket_bits_each_level, edits, hasher=cfg.hasher,
+                                keep=keep)
+    rec = dict(s)
+    rec.update(config=cfg_dict(cfg), edits_sha=sha(edits), n_edits=int(len(edits)), keep_after=keep,
+               pre_root=pre["root"], pre_filled=pre["filled"],
+               pre_digest=oracle.pool_words_digest(pre["bucket_words"], pre["page_ids"], pre["pages"], wb, pb),
+               roots_before=post["roots_before"], roots_after=post["roots_after"], filled_after=post["filled"],
+               post_words=int(post["bucket_words"].sum()),
+               post_digest=oracle.pool_words_digest(post["bucket_words"], post["page_ids"], post["pages"], wb, pb))
+    return rec
+
+
 def rays_for(res, n, seed):
     o = W.uniform(seed, 41, 3 * n).reshape(n, 3).astype(np.float32)
     # half the rays start outside the cube
@@ -187,6 +225,7 @@ def main():
     by = {s["name"]: s for s in SCENARIOS}
     g["traversal"] = [traversal_golden(by["scene256"]), traversal_golden(by["mixed256"], n=384, seed=12),
                       traversal_golden(by["full_then_dig"], n=256, seed=13)]
+    g["gc"] = [gc_golden(s) for s in GC_CASES]
     with open(OUT, "w") as f:
         json.dump(g, f, indent=1)
     print("wrote", OUT, os.path.getsize(OUT), "bytes")

@@ -32,6 +32,8 @@ def scenario_edits(spec):
                                                  a["r_lo"], a["r_hi"])])
     if kind == "explicit":
         return np.array([(s, o, tuple(p0), tuple(p1), r2) for s, o, p0, p1, r2 in spec["edits"]], dtype=EDIT_DTYPE)
+    if kind == "concat":
+        return np.concatenate([scenario_edits(p) for p in spec["parts"]])
     raise ValueError(kind)
 
 

@@ -206,3 +206,51 @@ def test_serving_pause_drain_and_ids(hd):
             srv.wait(i)  # a result is handed out once
         z = srv.wait(srv.submit_edits(0, np.zeros(0, hd.EDIT_DTYPE)))
         assert z["status"] == 0 and z["root"] == r["root"]
+
+
+def test_serving_collects_when_memory_runs_low(orc, hd):
+    """With gc_free_fraction set the server collects a scene whose heap runs
+    low, so memory frees up and requests keep being admitted; the scene ends
+    with the same DAG as applying every request alone, in order."""
+    from vkhashdag_gb300 import workloads as W
+    res = 256
+    # few, deep buckets (16 pages of 512 words each): pages fill up, so the
+    # replaced history, not one page per touched bucket, decides the heap size
+    cfg = hd.Config(9, 4, [3, 3, 4, 5, 7, 7, 4])
+    reqs = [W.mixed_batch(res, 40, seed=500 + k, r_max=30, side_max=60) for k in range(80)]
+    # sizes: every request alone on a roomy pool
+    big = hd.NodePool(cfg, heap_pages=1 << 14)
+    r = big.edit(hd.NULL, W.sphere_scene(res, 16, seed=0))
+    used, grow = [big.stats()["used_pages"]], []
+    for e in reqs:
+        r = big.edit(r, e)
+        used.append(big.stats()["used_pages"])
+        grow.append(used[-1] - used[-2])
+    (r_final,), st = big.gc([r])
+    heap = st["pages_after"] + 4 * max(grow) + 16
+    assert heap < used[-1]  # without collection the history does not fit
+    ref = orc.OraclePool.from_config(cfg)
+    rr = ref.edit(orc.NULL, W.sphere_scene(res, 16, seed=0))
+    for e in reqs:
+        rr = ref.edit(rr, e)
+    want = [str(x) for x in ref.canonical(rr)[2]]
+
+    def serve(gc_fraction):
+        pool = hd.NodePool(cfg, heap_pages=heap)
+        r0 = pool.edit(hd.NULL, W.sphere_scene(res, 16, seed=0))
+        with hd.Server([(pool, r0)], reserve_pages=1, pages_per_edit_hint=0.01,
+                       gc_free_fraction=gc_fraction) as srv:
+            ids = [srv.submit_edits(0, e) for e in reqs]
+            results = [srv.wait(i) for i in ids]
+            stats = srv.stats()
+            final = srv.scene_root(0)
+        return pool, final, results, stats
+
+    pool, final, results, stats = serve(0.0)
+    assert stats["refused"] + stats["failed"] > 0 and stats["gc_runs"] == 0
+    pool, final, results, stats = serve(0.3)
+    assert stats["refused"] == 0 and stats["failed"] == 0 and stats["gc_runs"] > 0
+    assert all(x["status"] == 0 for x in results)
+    assert max(x["gc_epoch"] for x in results) > 0
+    ok, counts, dig, _ = canonical_of_device(orc, pool, final)
+    assert ok and dig == want

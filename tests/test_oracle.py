@@ -131,3 +131,40 @@ def test_live_reference_when_present(orc):
     root = pool.edit(orc.NULL, e)
     bw, ids, pages = pool.dump()
     assert root == r["root"] and np.array_equal(pages, r["pages"]) and np.array_equal(bw, r["bucket_words"])
+
+
+def gc_case(golden, name):
+    return next(g for g in golden["gc"] if g["name"] == name)
+
+
+def oracle_pool_with_roots(orc, g):
+    """The case's edits applied one by one; the roots kept after edits keep_after."""
+    cfg = config_from(g["config"])
+    pool = orc.OraclePool.from_config(cfg)
+    edits = scenario_edits(g)
+    assert sha(edits) == g["edits_sha"]
+    root, kept = orc.NULL, {}
+    for i in range(len(edits)):
+        root = pool.edit(root, edits[i:i + 1])
+        kept[i] = root
+    return cfg, pool, root, [kept[k] for k in g["keep_after"]]
+
+
+@pytest.mark.parametrize("name", ["gc_mixed256", "gc_only_filled", "gc_tiny_pages64", "gc_zero16"])
+def test_gc_matches_reference(golden, orc, name):
+    """NodePoolThreadedGC::ThreadedGC restated (one-worker order): same remapped
+    roots, same pool words, same filled pointers as the reference's collector."""
+    g = gc_case(golden, name)
+    cfg, pool, root, roots = oracle_pool_with_roots(orc, g)
+    wb, pb = cfg.word_bits_per_page, cfg.page_bits_per_bucket
+    assert root == g["pre_root"] and roots == g["roots_before"]
+    assert orc.pool_words_digest(*pool.dump(), wb, pb) == g["pre_digest"]
+    before = [pool.canonical(r)[2] for r in roots]
+    new = pool.gc(roots)
+    assert pool.ok
+    assert new == g["roots_after"]
+    bw, ids, pages = pool.dump()
+    assert int(bw.sum()) == g["post_words"]
+    assert orc.pool_words_digest(bw, ids, pages, wb, pb) == g["post_digest"]
+    assert pool.make_filled() == g["filled_after"]
+    assert [pool.canonical(r)[2] for r in new] == before  # same DAGs under the new pointers

@@ -68,10 +68,15 @@ class _Stats(ctypes.Structure):
                 ("max_bucket_words", ctypes.c_uint32), ("words_per_bucket", ctypes.c_uint32)]
 
 
+class _GcStats(ctypes.Structure):
+    _fields_ = [("live_nodes", ctypes.c_uint64), ("words_before", ctypes.c_uint64), ("words_after", ctypes.c_uint64),
+                ("pages_before", ctypes.c_uint64), ("pages_after", ctypes.c_uint64)]
+
+
 class _ServerConfig(ctypes.Structure):
     _fields_ = [("max_pass_edits", ctypes.c_uint32), ("ray_slots", ctypes.c_uint32),
                 ("max_rays_per_request", ctypes.c_uint32), ("reserve_pages", ctypes.c_uint32),
-                ("pages_per_edit_hint", ctypes.c_double)]
+                ("pages_per_edit_hint", ctypes.c_double), ("gc_free_fraction", ctypes.c_double)]
 
 
 class _RequestResult(ctypes.Structure):
@@ -80,7 +85,7 @@ class _RequestResult(ctypes.Structure):
                 ("root", ctypes.c_uint32), ("pass_id", ctypes.c_uint64), ("pass_requests", ctypes.c_uint32),
                 ("pass_edits", ctypes.c_uint32), ("rays", ctypes.c_uint64), ("hits", ctypes.c_uint64),
                 ("steps", ctypes.c_uint64), ("node_words", ctypes.c_uint64), ("t_submit_ms", ctypes.c_double),
-                ("t_start_ms", ctypes.c_double), ("t_done_ms", ctypes.c_double)]
+                ("t_start_ms", ctypes.c_double), ("t_done_ms", ctypes.c_double), ("gc_epoch", ctypes.c_uint64)]
 
 
 class _ServerStats(ctypes.Structure):
@@ -89,7 +94,8 @@ class _ServerStats(ctypes.Structure):
                 ("edits_applied", ctypes.c_uint64), ("rays_traced", ctypes.c_uint64),
                 ("max_pass_requests", ctypes.c_uint32), ("queued", ctypes.c_uint32),
                 ("edit_p50_ms", ctypes.c_double), ("edit_p99_ms", ctypes.c_double),
-                ("camera_p50_ms", ctypes.c_double), ("camera_p99_ms", ctypes.c_double)]
+                ("camera_p50_ms", ctypes.c_double), ("camera_p99_ms", ctypes.c_double),
+                ("gc_runs", ctypes.c_uint64), ("gc_ms", ctypes.c_double)]
 
 
 _lib = None
@@ -123,6 +129,7 @@ def lib():
         "hd_pool_rollback": (I, [P, P]),
         "hd_upsert": (I, [P, U32, P, P, U32, P]),
         "hd_upsert_noalloc": (I, [P, U32, P, U32, P, P]),
+        "hd_gc": (I, [P, P, U32, ctypes.POINTER(_GcStats)]),
         "hd_edit_profile_begin": (I, [P, U32]),
         "hd_edit_profile_end": (I, [P, P, P]),
         "hd_pool_kernel_launches": (U64, [P]),
@@ -390,6 +397,14 @@ class NodePool:
                "hd_edit_last_probe_stats")
         return {"probe_steps": int(v[0]), "max_probe": int(v[1]), "cas_retries": int(v[2])}
 
+    def gc(self, roots) -> tuple:
+        """NodePoolThreadedGC::ThreadedGC: keeps what `roots` (and the filled nodes)
+        reach, compacts the pool; returns (remapped roots, statistics)."""
+        r = np.ascontiguousarray([int(x) & 0xFFFFFFFF for x in roots], np.uint32)
+        st = _GcStats()
+        _check(lib().hd_gc(self._h, _ptr(r) if len(r) else None, len(r), ctypes.byref(st)), "hd_gc")
+        return [int(x) for x in r], {name: int(getattr(st, name)) for name, _ in _GcStats._fields_}
+
     def checkpoint(self):
         _check(lib().hd_pool_checkpoint(self._h), "hd_pool_checkpoint")
 
@@ -499,11 +514,12 @@ class Server:
     """
 
     def __init__(self, scenes, max_pass_edits: int = 0, ray_slots: int = 0, max_rays_per_request: int = 0,
-                 reserve_pages: int = 0, pages_per_edit_hint: float = 0.0):
+                 reserve_pages: int = 0, pages_per_edit_hint: float = 0.0, gc_free_fraction: float = 0.0):
         self._pools = [p for p, _ in scenes]  # keep the pools alive
         handles = (ctypes.c_void_p * len(scenes))(*[p.handle for p, _ in scenes])
         roots = np.array([r & 0xFFFFFFFF for _, r in scenes], np.uint32)
-        cfg = _ServerConfig(max_pass_edits, ray_slots, max_rays_per_request, reserve_pages, pages_per_edit_hint)
+        cfg = _ServerConfig(max_pass_edits, ray_slots, max_rays_per_request, reserve_pages, pages_per_edit_hint,
+                            gc_free_fraction)
         h = ctypes.c_void_p()
         _check(lib().hd_server_create(handles, _ptr(roots), len(scenes), ctypes.byref(cfg), ctypes.byref(h)),
                "hd_server_create")

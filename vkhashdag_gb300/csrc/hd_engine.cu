@@ -637,6 +637,22 @@ uint64_t sphere_count(int64_t cx, int64_t cy, int64_t cz, uint64_t r2, int64_t r
 
 } // namespace
 
+// Internal entry points shared with the other translation units (device
+// current, pool lock held, no pass in flight).
+hd_status hd_rebuild_index(hd_pool *pool, cudaStream_t st) {
+	HD_TRY(cudaMemsetAsync(pool->P.index, 0xFF, (pool->P.index_mask + 1) * 8, st));
+	HD_TRY(cudaMemsetAsync(pool->P.counters + kCtrError, 0, 8, st)); // error word and index usage
+	k_index_rebuild<<<std::max(1u, std::min(ceil_div(pool->total_buckets, 256), 8192u)), 256, 0, st>>>(
+	    pool->P, (uint32_t)pool->total_buckets);
+	HD_TRY(cudaGetLastError());
+	HD_TRY(cudaMemcpyAsync(pool->h_small, pool->P.counters + kCtrError, 4, cudaMemcpyDeviceToHost, st));
+	HD_TRY(cudaStreamSynchronize(st));
+	const uint32_t err = pool->h_small[0];
+	return err ? status_of(err) : HD_OK;
+}
+
+hd_status hd_remake_filled(hd_pool *pool) { return make_filled(pool); }
+
 // ====================================================================== C ABI
 extern "C" {
 
@@ -1102,15 +1118,9 @@ hd_status hd_pool_upload(hd_pool *pool, const uint32_t *bucket_words, const uint
 	HD_TRY(cudaDeviceSynchronize());
 	uint32_t ctr0[kCtrCount] = {n_pages + 1u, 0u, 0u, 0u};
 	HD_TRY(cudaMemcpy(pool->P.counters, ctr0, sizeof(ctr0), cudaMemcpyHostToDevice));
-	HD_TRY(cudaMemset(pool->P.index, 0xFF, (pool->P.index_mask + 1) * 8));
-	k_index_rebuild<<<std::max(1u, std::min(ceil_div(pool->total_buckets, 256), 8192u)), 256>>>(
-	    pool->P, (uint32_t)pool->total_buckets);
-	HD_TRY(cudaGetLastError());
-	HD_TRY(cudaDeviceSynchronize());
-	uint32_t err = 0;
-	HD_TRY(cudaMemcpy(&err, pool->P.counters + kCtrError, 4, cudaMemcpyDeviceToHost));
-	if (err)
-		return status_of(err);
+	hd_status s = hd_rebuild_index(pool, nullptr);
+	if (s)
+		return s;
 	if (filled) {
 		for (uint32_t l = 0; l < pool->cfg.node_levels; ++l)
 			pool->P.cfg.filled[l] = filled[l];

@@ -44,6 +44,8 @@ inline uint32_t hd_prof_events_per_pass(uint32_t L) { return 3u + 2u * L + 1u; }
 
 // hd_engine.cu
 hd_status hd_check(cudaError_t e);
+hd_status hd_rebuild_index(hd_pool *pool, cudaStream_t st); // dedup index from the bucket contents (synchronous)
+hd_status hd_remake_filled(hd_pool *pool); // filled-node pointers found or inserted again
 // hd_trace.cu (no wait for edit passes on other streams; the caller orders)
 hd_status hd_launch_pinhole(hd_pool *pool, uint32_t root, const hd_camera *d_cams, uint32_t n_cameras, uint32_t width,
                             uint32_t height, hd_hit *d_out, uint64_t *d_counters, cudaStream_t st);

@@ -60,6 +60,9 @@ struct Scene {
 	uint64_t used_pages = 0, heap_pages = 0;
 	double pages_per_edit = 1.0;
 	uint64_t passes = 0;
+	bool gc_busy = false;        // a collection runs: no ray request of the scene starts (server mutex)
+	uint32_t rays_in_flight = 0; // ray requests of the scene on the device (server mutex)
+	uint64_t gc_epoch = 0;       // collections so far (server mutex)
 };
 
 struct RaySlot {
@@ -90,7 +93,7 @@ struct hd_server {
 	int device = 0;
 	Clock::time_point t0;
 	std::mutex mu;
-	std::condition_variable cv_ray, cv_done;
+	std::condition_variable cv_ray, cv_done, cv_gc;
 	std::vector<std::unique_ptr<Scene>> scenes;
 	std::vector<std::unique_ptr<RaySlot>> slots;
 	std::deque<std::unique_ptr<Request>> ray_queue;
@@ -101,8 +104,9 @@ struct hd_server {
 	bool paused = false; // no new pass or ray request starts while set
 	// statistics
 	std::vector<double> lat_edit, lat_cam;
-	uint64_t refused = 0, failed = 0, edit_passes = 0, edits_applied = 0, rays_traced = 0;
+	uint64_t refused = 0, failed = 0, edit_passes = 0, edits_applied = 0, rays_traced = 0, gc_runs = 0;
 	uint32_t max_pass_requests = 0;
+	double gc_ms = 0.0;
 
 	double now_ms() const { return std::chrono::duration<double, std::milli>(Clock::now() - t0).count(); }
 
@@ -125,6 +129,7 @@ struct hd_server {
 
 	void edit_loop(Scene &sc, uint32_t scene_idx);
 	void ray_loop(RaySlot &slot);
+	hd_status collect(Scene &sc, std::vector<uint32_t> &roots);
 };
 
 namespace {
@@ -176,6 +181,7 @@ void hd_server::edit_loop(Scene &sc, uint32_t scene_idx) {
 					r.status = HD_ERR_POOL_OOM;
 					r.admitted = 0;
 					r.root_in = r.root = sc.root;
+					r.gc_epoch = sc.gc_epoch;
 					r.t_start_ms = now_ms();
 					publish(r);
 					sc.queue.pop_front();
@@ -259,20 +265,72 @@ void hd_server::edit_loop(Scene &sc, uint32_t scene_idx) {
 			sc.pages_per_edit = sc.passes == 1 ? std::max(per, 1e-3) : 0.75 * sc.pages_per_edit + 0.25 * per;
 			sc.pages_per_edit = std::max(sc.pages_per_edit, 1e-3);
 		}
+		// collect before publishing, so every root a client receives stays
+		// valid until the scene's next pass (the pass's input and output roots
+		// are kept and remapped)
+		const uint64_t free_pages = sc.heap_pages - 1 - std::min(sc.used_pages, sc.heap_pages - 1);
+		bool collected = false;
+		if (cfg.gc_free_fraction > 0.0 && double(free_pages) < cfg.gc_free_fraction * double(sc.heap_pages)) {
+			collected = true;
+			std::vector<uint32_t> keep;
+			keep.reserve(2 * res.size() + 1);
+			keep.push_back(root);
+			for (auto &r : res) {
+				keep.push_back(r.root_in);
+				keep.push_back(r.root);
+			}
+			if (collect(sc, keep) == HD_OK) {
+				root = keep[0];
+				for (size_t i = 0; i < res.size(); ++i) {
+					res[i].root_in = keep[1 + 2 * i];
+					res[i].root = keep[2 + 2 * i];
+				}
+			}
+		}
 		{
 			std::lock_guard<std::mutex> lk(mu);
 			sc.root = root;
+			sc.gc_busy = false; // ray requests see the remapped root from here on
 			++edit_passes;
 			max_pass_requests = std::max<uint32_t>(max_pass_requests, (uint32_t)take.size());
 			for (size_t i = 0; i < take.size(); ++i) {
 				if (res[i].status == HD_OK)
 					edits_applied += take[i]->edits.size();
+				res[i].gc_epoch = sc.gc_epoch;
 				publish(res[i]);
 			}
 		}
 		cv_done.notify_all();
+		if (collected)
+			cv_ray.notify_all();
 		(void)scene_idx;
 	}
+}
+
+// Collects a scene between two of its passes (the edit thread runs this, so
+// its queued edits wait and merge into the next pass): waits until none of
+// its ray requests is on the device, keeps the nodes `roots` reach and
+// remaps them in place.
+hd_status hd_server::collect(Scene &sc, std::vector<uint32_t> &roots) {
+	{
+		std::unique_lock<std::mutex> lk(mu);
+		sc.gc_busy = true;
+		cv_gc.wait(lk, [&] { return sc.rays_in_flight == 0; });
+	}
+	const double t0 = now_ms();
+	const hd_status st = hd_gc(sc.pool, roots.data(), (uint32_t)roots.size(), nullptr);
+	if (st)
+		fprintf(stderr, "hashdag_gb300: server collection failed: %s\n", hd_status_string(st));
+	cudaSetDevice(device);
+	read_used_pages(sc);
+	{
+		std::lock_guard<std::mutex> lk(mu);
+		if (!st)
+			++sc.gc_epoch;
+		++gc_runs;
+		gc_ms += now_ms() - t0;
+	}
+	return st; // gc_busy stays set until the caller has published the remapped root
 }
 
 void hd_server::ray_loop(RaySlot &slot) {
@@ -281,6 +339,7 @@ void hd_server::ray_loop(RaySlot &slot) {
 		std::unique_ptr<Request> q;
 		uint32_t root;
 		hd_pool *pool;
+		uint64_t epoch;
 		{
 			std::unique_lock<std::mutex> lk(mu);
 			cv_ray.wait(lk, [&] { return stop || (!paused && !ray_queue.empty()); });
@@ -288,8 +347,12 @@ void hd_server::ray_loop(RaySlot &slot) {
 				return;
 			q = std::move(ray_queue.front());
 			ray_queue.pop_front();
-			root = scenes[q->scene]->root; // snapshot: last finished pass
-			pool = scenes[q->scene]->pool;
+			Scene &s = *scenes[q->scene];
+			cv_ray.wait(lk, [&] { return !s.gc_busy; }); // its pool is being rewritten
+			root = s.root; // snapshot: last finished pass
+			pool = s.pool;
+			epoch = s.gc_epoch;
+			++s.rays_in_flight;
 		}
 		hd_request_result r = base_result(*q);
 		r.t_start_ms = now_ms();
@@ -346,13 +409,16 @@ void hd_server::ray_loop(RaySlot &slot) {
 			}
 		}
 		r.status = st;
+		r.gc_epoch = epoch;
 		{
 			std::lock_guard<std::mutex> lk(mu);
 			if (!st)
 				rays_traced += rays;
+			--scenes[r.scene]->rays_in_flight;
 			publish(r);
 		}
 		cv_done.notify_all();
+		cv_gc.notify_all();
 	}
 }
 
@@ -500,6 +566,7 @@ hd_status hd_server_submit_edits(hd_server *server, uint32_t scene, const hd_edi
 		if (n == 0) { // nothing to apply: finished at once with the current root
 			hd_request_result r = base_result(*q);
 			r.root_in = r.root = sc.root;
+			r.gc_epoch = sc.gc_epoch;
 			r.t_start_ms = q->t_submit;
 			server->publish(r);
 			server->cv_done.notify_all();
@@ -606,6 +673,8 @@ hd_status hd_server_get_stats(hd_server *server, hd_server_stats *out) {
 	out->edit_p99_ms = percentile(server->lat_edit, 0.99);
 	out->camera_p50_ms = percentile(server->lat_cam, 0.50);
 	out->camera_p99_ms = percentile(server->lat_cam, 0.99);
+	out->gc_runs = server->gc_runs;
+	out->gc_ms = server->gc_ms;
 	return HD_OK;
 }
 
