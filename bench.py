@@ -487,6 +487,28 @@ def run_rays(args):
             host.copy_(out, non_blocking=True)
         stream.synchronize()
     e2e = n_rays * args.steps / (time.perf_counter() - t0)
+    # the renderer's form: level of detail (trace.frag:148), alone and with the
+    # 8x8 beam prepass (beam.frag), same cameras, projection factors of a 60 deg
+    # vertical field of view (src/rg/TracePass.cpp:114-118, BeamPass.cpp:90-94)
+    fov = np.pi / 3
+    lod = {}
+    lout = torch.empty_like(out)  # keeps `out` for the CPU check of the plain traversal below
+    for name, bproj in (("lod", 0.0), ("lod_beam", hd.projection_factor(fov, height, 8))):
+        proj = hd.projection_factor(fov, height, 1)
+        for _ in range(args.warmup):
+            pool.trace_pinhole_lod_async(root, cams, width, height, proj, bproj, lout.data_ptr(), 0, sp)
+        ctr.zero_()
+        torch.cuda.synchronize()
+        s0.record(stream)
+        for _ in range(args.steps):
+            pool.trace_pinhole_lod_async(root, cams, width, height, proj, bproj, lout.data_ptr(), ctr.data_ptr(), sp)
+        s1.record(stream)
+        torch.cuda.synchronize()
+        lms = s0.elapsed_time(s1)
+        lsteps, lreads, lhits = (int(x) for x in ctr.cpu())
+        lod[name] = {"rays_per_s": n_rays * args.steps / (lms / 1e3), "ms_per_step": lms / args.steps,
+                     "steps_per_ray": lsteps / (n_rays * args.steps), "hit_fraction": lhits / (n_rays * args.steps),
+                     "projection_factor": proj, "beam_projection_factor": bproj}
     cpu = None
     if not args.no_cpu:
         import oracle
@@ -494,6 +516,16 @@ def run_rays(args):
         bw, ids, pages = pool.download()
         opool = oracle.OraclePool.from_config(cfg)
         opool.load(bw, ids, pages, pool.filled_node_pointers())
+        # level of detail + beam on the device equals the CPU restatement, bit for
+        # bit, on the same cameras at 1/10 of the size in each direction
+        sw, sh = max(8, width // 10), max(8, height // 10)
+        sproj, sbproj = hd.projection_factor(fov, sh, 1), hd.projection_factor(fov, sh, 8)
+        small = torch.empty(n_cams * sw * sh * 40, dtype=torch.uint8, device=f"cuda:{local}")
+        pool.trace_pinhole_lod_async(root, cams, sw, sh, sproj, sbproj, small.data_ptr(), 0, sp)
+        torch.cuda.synchronize()
+        lod["lod_beam_equal_to_cpu"] = bool(small.cpu().numpy().tobytes() == opool.trace_pinhole_lod(
+            root, cams, sw, sh, sproj, sbproj).tobytes())
+        lod["cpu_check"] = f"{n_cams} cameras at {sw}x{sh}"
         o, d = host_rays(cams, width, height, args.cpu_rows)
         threads = os.cpu_count() or 1
         t0 = time.perf_counter()
@@ -522,7 +554,7 @@ def run_rays(args):
                              "the hit output",
                      "algorithmic_bytes_per_step": alg, "steps_per_ray": steps / (n_rays * args.steps),
                      "node_words_per_ray": reads / (n_rays * args.steps)},
-        "hit_fraction": hits / (n_rays * args.steps), "cpu_baseline": cpu,
+        "hit_fraction": hits / (n_rays * args.steps), "lod": lod, "cpu_baseline": cpu,
         "gpu_launches": pool.kernel_launches() - launches0, "clocks": clocks.summary(),
     }
     print(json.dumps(line), flush=True)

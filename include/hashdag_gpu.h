@@ -372,6 +372,23 @@ hd_status hd_server_drain(hd_server *server);
 hd_status hd_server_scene_root(hd_server *server, uint32_t scene, uint32_t *out_root);
 hd_status hd_server_get_stats(hd_server *server, hd_server_stats *out);
 
+/* Level of detail and the beam prepass of the renderer (shader/src/trace.frag
+ * with BEAM_OPTIMIZATION, shader/src/beam.frag, src/rg/BeamPass.cpp):
+ *   - descent stops at a cube whose size times proj_factor is below its entry t
+ *     (trace.frag:148), so distant geometry is hit at coarser voxels (hd_hit.size);
+ *   - beam_proj_factor > 0 first traces one ray per 8x8 pixel block with that
+ *     factor and stores t - cube size (+inf on a miss); each pixel then starts at
+ *     o + b * d with b = 0.98 * the minimum of the 2x2 block values around it
+ *     (the linear MIN-reduction sampler of src/rg/TracePass.cpp:37-54) and uses b
+ *     as projection bias; a pixel whose b is +inf is a miss without tracing.
+ * proj_factor / beam_proj_factor: hd_projection_factor(fov_y, height, 1 or 8). */
+hd_status hd_trace_pinhole_lod_async(hd_pool *pool, uint32_t root, const hd_camera *cameras, uint32_t n_cameras,
+                                     uint32_t width, uint32_t height, float proj_factor, float beam_proj_factor,
+                                     hd_hit *d_out, uint64_t *d_counters, void *stream);
+/* inv_2tan_half_fov / screen_tolerance of src/rg/TracePass.cpp:114-118 (divisor 1)
+ * and src/rg/BeamPass.cpp:90-94 (divisor 8), in float like the reference. */
+float hd_projection_factor(float fov_y, uint32_t height, uint32_t divisor);
+
 /* ---- workload helpers ------------------------------------------------------
  * Number of grid voxels inside each edit's shape clipped to [0,resolution)^3,
  * summed over the edits (the voxel-edits unit of the benchmark). */

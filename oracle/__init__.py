@@ -93,6 +93,7 @@ def lib():
             "orc_trace": (None, [P, U32, P, P, U32, P]),
             "orc_trace_threads": (None, [P, U32, P, P, U32, P, I]),
             "orc_gc": (None, [P, P, U32]),
+            "orc_trace_pinhole_lod": (None, [P, U32, P, U32, U32, U32, ctypes.c_float, ctypes.c_float, P, I]),
             "orc_hash_inner": (U32, [P, U32]),
             "orc_hash_leaf": (U32, [U32, U32]),
         }
@@ -177,6 +178,17 @@ class OraclePool:
         pg = np.ascontiguousarray(pages, np.uint32)
         fl = None if filled is None else np.ascontiguousarray(filled, np.uint32)
         lib().orc_pool_load(self._h, _p(bw), _p(ids), len(ids), _p(pg), None if fl is None else _p(fl))
+
+    def trace_pinhole_lod(self, root, cameras, width, height, proj_factor, beam_proj_factor=0.0, threads=0):
+        """trace.frag main with level of detail (and the beam.frag prepass when
+        beam_proj_factor > 0) for CAMERA_DTYPE cameras; HIT_DTYPE records."""
+        from vkhashdag_gb300 import CAMERA_DTYPE, HIT_DTYPE
+        cams = np.ascontiguousarray(cameras, CAMERA_DTYPE)
+        out = np.zeros(len(cams) * width * height, HIT_DTYPE)
+        t = threads or lib().orc_max_threads()
+        lib().orc_trace_pinhole_lod(self._h, root, _p(cams), len(cams), width, height, float(proj_factor),
+                                    float(beam_proj_factor), _p(out), t)
+        return out
 
     def gc(self, roots):
         """NodePoolThreadedGC::ThreadedGC (one-worker order); returns the remapped roots."""

@@ -733,7 +733,11 @@ static inline int find_msb(Word x) { return x ? 31 - std::countl_zero(x) : -1; }
 // glm::abs for float (x >= 0 ? x : -x)
 static inline float abs_ref(float x) { return x >= 0.0f ? x : -x; }
 
-static hd_hit trace_ray(const Pool &pool, Word root, const float o_in[3], const float d_in[3]) {
+// Lod: the level-of-detail cut of shader/src/trace.frag:148 / beam.frag:128;
+// *scale_out = size of the cube the ray stopped in (beam.frag:203).
+template <bool Lod>
+static hd_hit trace_ray_core(const Pool &pool, Word root, const float o_in[3], const float d_in[3], float proj_factor,
+                             float proj_bias, float *scale_out) {
 	hd_hit out{};
 	out.hit = 0;
 	if (root == kNull)
@@ -791,7 +795,7 @@ static hd_hit trace_ray(const Pool &pool, Word root, const float o_in[3], const 
 		if ((child_bits & child_mask) != 0 && t_min <= t_max) {
 			float half = scale_exp2 * 0.5f;
 			float tcen[3] = {half * tc[0] + tcorner[0], half * tc[1] + tcorner[1], half * tc[2] + tcorner[2]};
-			if (scale < leaf_scale)
+			if (scale < leaf_scale || (Lod && scale_exp2 * proj_factor < tc_max + proj_bias))
 				break;
 			if (tc_max < h)
 				stack[scale] = parent;
@@ -838,6 +842,8 @@ static hd_hit trace_ray(const Pool &pool, Word root, const float o_in[3], const 
 		}
 	}
 	bool hit = scale < kStack && t_min <= t_max;
+	if (scale_out)
+		*scale_out = scale_exp2;
 	out.hit = hit ? 1u : 0u;
 	out.t = t_min;
 	const Word voxel_level = leaf_level + 1u;
@@ -862,6 +868,72 @@ static hd_hit trace_ray(const Pool &pool, Word root, const float o_in[3], const 
 		}
 	}
 	return out;
+}
+
+static hd_hit trace_ray(const Pool &pool, Word root, const float o_in[3], const float d_in[3]) {
+	return trace_ray_core<false>(pool, root, o_in, d_in, 0.0f, 0.0f, nullptr);
+}
+
+// Camera_GenRay (shader/src/trace.frag:366-370) at the centre of pixel (px, py) of a w x h image.
+static void pinhole_dir(const hd_camera &cam, Word px, Word py, Word w, Word h, float d[3]) {
+	const float u = ((float(px) + 0.5f) / float(w)) * 2.0f - 1.0f;
+	const float v = ((float(py) + 0.5f) / float(h)) * 2.0f - 1.0f;
+	float dd[3];
+	for (int a = 0; a < 3; ++a)
+		dd[a] = (cam.look[a] - cam.side[a] * u) - cam.up[a] * v;
+	const float len2 = (dd[0] * dd[0] + dd[1] * dd[1]) + dd[2] * dd[2];
+	const float inv = 1.0f / std::sqrt(len2);
+	for (int a = 0; a < 3; ++a)
+		d[a] = dd[a] * inv;
+}
+
+static int floor_div(long long a, long long b) { return int(a >= 0 ? a / b : -((-a + b - 1) / b)); }
+
+// beam.frag main over every 8x8 block, then trace.frag main with
+// BEAM_OPTIMIZATION (beam_proj <= 0: without the prepass).  Pixels are
+// camera-major, row-major, like the device.
+static void trace_pinhole_lod(const Pool &pool, Word root, const hd_camera *cams, Word n_cams, Word w, Word h,
+                              float proj, float beam_proj, hd_hit *out, int threads) {
+	const Word bw = (w + 7) / 8, bh = (h + 7) / 8;
+	const bool use_beam = beam_proj > 0.0f;
+	std::vector<float> beam(use_beam ? size_t(n_cams) * bw * bh : 0);
+	const float inf = w2f(0x7F800000u);
+	if (use_beam) {
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 256)
+		for (int64_t i = 0; i < int64_t(beam.size()); ++i) {
+			const Word c = Word(i / (int64_t(bw) * bh)), r = Word(i % (int64_t(bw) * bh));
+			float d[3];
+			pinhole_dir(cams[c], r % bw, r / bw, bw, bh, d);
+			float sexp = 0.0f;
+			const hd_hit hh = trace_ray_core<true>(pool, root, cams[c].position, d, beam_proj, 0.0f, &sexp);
+			beam[size_t(i)] = hh.hit ? std::max(hh.t - sexp, 0.0f) : inf;
+		}
+	}
+	const int64_t per = int64_t(w) * h, total = per * n_cams;
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 4096)
+	for (int64_t i = 0; i < total; ++i) {
+		const Word c = Word(i / per), px = Word(i % per % w), py = Word(i % per / w);
+		float d[3], o[3] = {cams[c].position[0], cams[c].position[1], cams[c].position[2]};
+		pinhole_dir(cams[c], px, py, w, h, d);
+		float bias = 0.0f;
+		if (use_beam) {
+			const float *b = beam.data() + size_t(c) * bw * bh;
+			const int i0 = floor_div((2ll * px + 1) * bw - w, 2ll * w), j0 = floor_div((2ll * py + 1) * bh - h, 2ll * h);
+			const int xs[2] = {std::clamp(i0, 0, int(bw) - 1), std::clamp(i0 + 1, 0, int(bw) - 1)};
+			const int ys[2] = {std::clamp(j0, 0, int(bh) - 1), std::clamp(j0 + 1, 0, int(bh) - 1)};
+			float m = b[size_t(ys[0]) * bw + xs[0]];
+			for (int k = 1; k < 4; ++k)
+				m = std::min(m, b[size_t(ys[k >> 1]) * bw + xs[k & 1]]);
+			bias = m * 0.98f;
+			if (f2w(bias) == 0x7F800000u) { // the block's ray missed
+				out[i] = hd_hit{};
+				continue;
+			}
+			for (int a = 0; a < 3; ++a)
+				o[a] = o[a] + bias * d[a];
+		}
+		out[i] = trace_ray_core<true>(pool, root, o, d, proj, bias, nullptr);
+	}
 }
 
 } // namespace orc
@@ -999,6 +1071,11 @@ void orc_trace_threads(const orc_pool *p, uint32_t root, const float *o, const f
 #pragma omp parallel for num_threads(threads) schedule(dynamic, 4096)
 	for (int64_t i = 0; i < int64_t(n); ++i)
 		out[i] = orc::trace_ray(p->pool, root, o + 3 * size_t(i), d + 3 * size_t(i));
+}
+
+void orc_trace_pinhole_lod(const orc_pool *p, uint32_t root, const hd_camera *cams, uint32_t n_cams, uint32_t w,
+                           uint32_t h, float proj, float beam_proj, hd_hit *out, int threads) {
+	orc::trace_pinhole_lod(p->pool, root, cams, n_cams, w, h, proj, beam_proj, out, threads);
 }
 
 void orc_gc(orc_pool *p, uint32_t *roots, uint32_t n_roots) { p->pool.gc(roots, n_roots, &p->ok); }

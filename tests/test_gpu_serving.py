@@ -238,7 +238,9 @@ def test_serving_collects_when_memory_runs_low(orc, hd):
     def serve(gc_fraction):
         pool = hd.NodePool(cfg, heap_pages=heap)
         r0 = pool.edit(hd.NULL, W.sphere_scene(res, 16, seed=0))
-        with hd.Server([(pool, r0)], reserve_pages=1, pages_per_edit_hint=0.01,
+        # passes of at most 4 requests: a pass never needs more than the heap
+        # keeps free after a collection (4 x the largest growth of one request)
+        with hd.Server([(pool, r0)], reserve_pages=1, pages_per_edit_hint=max(grow) / 40.0, max_pass_edits=160,
                        gc_free_fraction=gc_fraction) as srv:
             ids = [srv.submit_edits(0, e) for e in reqs]
             results = [srv.wait(i) for i in ids]

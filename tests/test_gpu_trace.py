@@ -83,3 +83,58 @@ def test_pinhole_cameras_match_host_rays(orc, hd):
     assert got["hit"].mean() > 0.3
     steps, reads, hits = (int(x) for x in ctr.cpu())
     assert hits == int(got["hit"].sum()) and steps >= 2 * w * h and reads > 0
+
+
+def _terrain_and_cameras(hd, orc, res=512):
+    from vkhashdag_gb300 import workloads as W
+    cfg = W.config_for_resolution(res)
+    pool = hd.NodePool(cfg, heap_pages=1 << 13)
+    edits = np.concatenate([W.terrain_columns(res, 8, 1), W.surface_spheres(res, 100, 1, 16, 8, 2, 20)])
+    root = pool.edit(hd.NULL, edits)
+    ref = orc.OraclePool.from_config(cfg)
+    rr = ref.edit(orc.NULL, edits)
+    cams = np.zeros(2, hd.CAMERA_DTYPE)
+    cams["position"] = [[0.2, 0.9, 0.3], [0.7, 0.95, 0.6]]
+    cams["look"] = [[0.3, -0.5, 0.8], [-0.4, -0.6, -0.7]]
+    cams["look"] /= np.linalg.norm(cams["look"], axis=1, keepdims=True)
+    cams["side"] = [[0.5, 0.0, -0.2], [0.4, 0.0, -0.3]]
+    cams["up"] = [[0.0, 0.5, 0.3], [0.1, 0.5, 0.0]]
+    return pool, root, ref, rr, cams
+
+
+def _lod_on_device(hd, pool, root, cams, w, h, proj, beam_proj):
+    import torch
+    out = torch.empty(len(cams) * w * h * 40, dtype=torch.uint8, device="cuda")
+    ctr = torch.zeros(4, dtype=torch.int64, device="cuda")
+    pool.trace_pinhole_lod_async(root, cams, w, h, proj, beam_proj, out.data_ptr(), ctr.data_ptr(), 0)
+    torch.cuda.synchronize()
+    return out.cpu().numpy().view(hd.HIT_DTYPE), [int(x) for x in ctr.cpu()[:3]]
+
+
+@pytest.mark.parametrize("beam", [False, True])
+@pytest.mark.parametrize("size", [(96, 64), (100, 58)])
+def test_lod_and_beam_bit_identical_to_oracle(orc, hd, beam, size):
+    """Level-of-detail traversal (trace.frag:148) with and without the 8x8 beam
+    prepass (beam.frag): every hit record equals the CPU restatement bit for
+    bit (image sizes that are and are not multiples of the block)."""
+    pool, root, ref, rr, cams = _terrain_and_cameras(hd, orc)
+    w, h = size
+    fov = np.pi / 3
+    proj = hd.projection_factor(fov, h, 1)
+    bproj = hd.projection_factor(fov, h, 8) if beam else 0.0
+    got, ctr = _lod_on_device(hd, pool, root, cams, w, h, proj, bproj)
+    want = ref.trace_pinhole_lod(rr, cams, w, h, proj, bproj)
+    assert got.tobytes() == want.tobytes()
+    assert got["hit"].mean() > 0.3 and ctr[2] == int(got["hit"].sum())
+    assert (got["size"][got["hit"] == 1] > 1).any()  # distant geometry is hit at coarser voxels
+
+
+def test_lod_with_unbounded_projection_equals_plain_traversal(orc, hd):
+    import torch
+    pool, root, ref, rr, cams = _terrain_and_cameras(hd, orc)
+    w, h = 64, 48
+    got, _ = _lod_on_device(hd, pool, root, cams, w, h, float("inf"), 0.0)
+    plain = torch.empty(2 * w * h * 40, dtype=torch.uint8, device="cuda")
+    pool.trace_pinhole_async(root, cams, w, h, plain.data_ptr(), 0, 0)
+    torch.cuda.synchronize()
+    assert got.tobytes() == plain.cpu().numpy().tobytes()

@@ -168,3 +168,34 @@ def test_gc_matches_reference(golden, orc, name):
     assert orc.pool_words_digest(bw, ids, pages, wb, pb) == g["post_digest"]
     assert pool.make_filled() == g["filled_after"]
     assert [pool.canonical(r)[2] for r in new] == before  # same DAGs under the new pointers
+
+
+def test_lod_oracle_without_cut_equals_plain_traversal(orc):
+    """The level-of-detail restatement with an unbounded projection factor is
+    the plain traversal (pinned against the reference above) on the same rays."""
+    import vkhashdag_gb300 as hd
+    from vkhashdag_gb300 import workloads as W
+    cfg = W.config_for_resolution(128)
+    pool = orc.OraclePool.from_config(cfg)
+    root = pool.edit(orc.NULL, W.sphere_scene(128, 8, seed=3))
+    cams = np.zeros(1, hd.CAMERA_DTYPE)
+    cams["position"] = [[0.1, 0.8, 0.2]]
+    look = np.array([0.5, -0.5, 0.6]); look /= np.linalg.norm(look)
+    cams["look"], cams["side"], cams["up"] = look, [0.5, 0.0, -0.3], [0.0, 0.5, 0.2]
+    w, h = 40, 24
+    lod = pool.trace_pinhole_lod(root, cams, w, h, float("inf"))
+    px, py = np.meshgrid(np.arange(w, dtype=np.float32), np.arange(h, dtype=np.float32))
+    u = ((px.ravel() + np.float32(0.5)) / np.float32(w)) * np.float32(2) - np.float32(1)
+    v = ((py.ravel() + np.float32(0.5)) / np.float32(h)) * np.float32(2) - np.float32(1)
+    c = cams[0]
+    dd = (c["look"][None, :] - c["side"][None, :] * u[:, None]) - c["up"][None, :] * v[:, None]
+    len2 = (dd[:, 0] * dd[:, 0] + dd[:, 1] * dd[:, 1]) + dd[:, 2] * dd[:, 2]
+    d = (dd * (np.float32(1) / np.sqrt(len2))[:, None]).astype(np.float32)
+    o = np.tile(c["position"], (len(u), 1)).astype(np.float32)
+    plain = pool.trace(root, o, d)
+    assert lod.tobytes() == plain.tobytes()
+    assert lod["hit"].mean() > 0.2
+    # a finite projection factor cuts the descent: coarser voxels, fewer or equal levels
+    coarse = pool.trace_pinhole_lod(root, cams, w, h, hd.projection_factor(np.pi / 3, h, 8))
+    hit = coarse["hit"] == 1
+    assert (coarse["size"][hit] >= 1).all() and (coarse["size"][hit] > 1).any()

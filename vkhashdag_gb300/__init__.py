@@ -24,7 +24,7 @@ import numpy as np
 __all__ = [
     "NULL", "Config", "DefaultConfig", "EditMode", "SphereEditor", "AABBEditor", "NodePool",
     "HashDagError", "EDIT_DTYPE", "HIT_DTYPE", "CAMERA_DTYPE", "edits_to_array", "lib", "library_path",
-    "count_voxel_edits", "device_available", "Server", "REQ_EDIT", "REQ_CAMERA",
+    "count_voxel_edits", "device_available", "Server", "REQ_EDIT", "REQ_CAMERA", "projection_factor",
 ]
 
 NULL = 0xFFFFFFFF
@@ -140,6 +140,8 @@ def lib():
         "hd_query": (I, [P, U32, P, U32, P, P]),
         "hd_trace": (I, [P, U32, P, P, U32, P, P]),
         "hd_trace_pinhole_async": (I, [P, U32, P, U32, U32, U32, P, P, P]),
+        "hd_trace_pinhole_lod_async": (I, [P, U32, P, U32, U32, U32, ctypes.c_float, ctypes.c_float, P, P, P]),
+        "hd_projection_factor": (ctypes.c_float, [ctypes.c_float, U32, U32]),
         "hd_server_create": (I, [P, P, U32, ctypes.POINTER(_ServerConfig), ctypes.POINTER(P)]),
         "hd_server_destroy": (None, [P]),
         "hd_server_submit_edits": (I, [P, U32, P, U32, ctypes.POINTER(U64)]),
@@ -287,6 +289,12 @@ class AABBEditor:
 def edits_to_array(editors: Iterable) -> np.ndarray:
     items = [e.desc() for e in editors]
     return np.array(items, dtype=EDIT_DTYPE)
+
+
+def projection_factor(fov_y: float, height: int, divisor: int = 1) -> float:
+    """Pixel-tolerance projection factor of the renderer (src/rg/TracePass.cpp:114-118,
+    divisor 1; src/rg/BeamPass.cpp:90-94, divisor 8)."""
+    return float(lib().hd_projection_factor(float(fov_y), int(height), int(divisor)))
 
 
 def count_voxel_edits(edits: np.ndarray, resolution: int) -> int:
@@ -490,6 +498,16 @@ class NodePool:
         _check(lib().hd_trace_pinhole_async(self._h, root & 0xFFFFFFFF, _ptr(cams), len(cams), width, height,
                                             ctypes.c_void_p(d_out), ctypes.c_void_p(d_counters or None),
                                             ctypes.c_void_p(stream)), "hd_trace_pinhole_async")
+
+    def trace_pinhole_lod_async(self, root: int, cameras: np.ndarray, width: int, height: int, proj_factor: float,
+                                beam_proj_factor: float, d_out: int, d_counters: int = 0, stream: int = 0):
+        """Renderer traversal with level of detail (trace.frag) and, when
+        beam_proj_factor > 0, the 8x8 beam prepass (beam.frag) into device hits."""
+        cams = np.ascontiguousarray(cameras, dtype=CAMERA_DTYPE)
+        _check(lib().hd_trace_pinhole_lod_async(self._h, root & 0xFFFFFFFF, _ptr(cams), len(cams), width, height,
+                                                float(proj_factor), float(beam_proj_factor), ctypes.c_void_p(d_out),
+                                                ctypes.c_void_p(d_counters or None), ctypes.c_void_p(stream)),
+               "hd_trace_pinhole_lod_async")
 
     def traversal(self, root: int, origins, dirs) -> np.ndarray:
         o = np.ascontiguousarray(origins, dtype=np.float32).reshape(-1, 3)

@@ -217,9 +217,10 @@ void hd_server::edit_loop(Scene &sc, uint32_t scene_idx) {
 			res.back().t_start_ms = t_start;
 			res.back().root_in = root_in;
 		}
-		const uint64_t used_before = sc.used_pages;
+		uint64_t used_before = sc.used_pages;
 		uint32_t root = root_in;
 		hd_status st = HD_OK;
+		bool gc_held = false; // a collection ran: ray requests of the scene wait until the publish below
 		if (!sc.staging) {
 			st = HD_ERR_POOL_OOM; // no pinned staging memory: host allocation failed
 		} else {
@@ -229,6 +230,20 @@ void hd_server::edit_loop(Scene &sc, uint32_t scene_idx) {
 				off += q->edits.size();
 			}
 			st = hd_edit(sc.pool, root_in, sc.staging, (uint32_t)n_edits, &root, sc.stream);
+			if (st == HD_ERR_POOL_OOM && cfg.gc_free_fraction > 0.0) {
+				// the heap ran out during the pass: collect (the failed pass's words
+				// and lost pages go with the garbage) and run the pass once more
+				std::vector<uint32_t> keep{root_in};
+				if (collect(sc, keep) == HD_OK) {
+					root_in = keep[0];
+					for (auto &r : res)
+						r.root_in = root_in;
+					used_before = sc.used_pages;
+					root = root_in;
+					st = hd_edit(sc.pool, root_in, sc.staging, (uint32_t)n_edits, &root, sc.stream);
+				}
+				gc_held = true;
+			}
 		}
 		const uint64_t pass_id = ++sc.passes;
 		if (st == HD_OK || take.size() == 1) {
@@ -269,9 +284,8 @@ void hd_server::edit_loop(Scene &sc, uint32_t scene_idx) {
 		// valid until the scene's next pass (the pass's input and output roots
 		// are kept and remapped)
 		const uint64_t free_pages = sc.heap_pages - 1 - std::min(sc.used_pages, sc.heap_pages - 1);
-		bool collected = false;
 		if (cfg.gc_free_fraction > 0.0 && double(free_pages) < cfg.gc_free_fraction * double(sc.heap_pages)) {
-			collected = true;
+			gc_held = true;
 			std::vector<uint32_t> keep;
 			keep.reserve(2 * res.size() + 1);
 			keep.push_back(root);
@@ -301,7 +315,7 @@ void hd_server::edit_loop(Scene &sc, uint32_t scene_idx) {
 			}
 		}
 		cv_done.notify_all();
-		if (collected)
+		if (gc_held)
 			cv_ray.notify_all();
 		(void)scene_idx;
 	}

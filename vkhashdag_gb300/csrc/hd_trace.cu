@@ -9,6 +9,8 @@
 // with -ffp-contract=off.
 #include "hd_internal.h"
 
+#include <cmath>
+
 #include <algorithm>
 #include <cstdio>
 
@@ -16,13 +18,19 @@ using namespace hd;
 
 namespace {
 
+constexpr uint32_t kBeamBlock = 8; // src/rg/BeamPass.cpp:11 kBlockSize
+
 __device__ __forceinline__ float fmin_ref(float x, float y) { return (y < x) ? y : x; } // glm::min
 __device__ __forceinline__ float fmax_ref(float x, float y) { return (x < y) ? y : x; } // glm::max
 __device__ __forceinline__ float abs_ref(float x) { return x >= 0.0f ? x : -x; }
 
-// steps: loop iterations; reads: node words fetched (mask words, child pointers, leaf words)
-__device__ hd_hit trace_one(const DevPool &P, u32 root, float ox, float oy, float oz, float dx, float dy, float dz,
-                            u32 *steps = nullptr, u32 *reads = nullptr) {
+// steps: loop iterations; reads: node words fetched (mask words, child pointers, leaf words).
+// Lod: the level-of-detail cut of shader/src/trace.frag:148 and beam.frag:128 --
+// descent stops at a cube whose size times proj_factor is below its entry t plus
+// proj_bias; *scale_out receives the size of the cube the ray stopped in.
+template <bool Lod>
+__device__ hd_hit trace_core(const DevPool &P, u32 root, float ox, float oy, float oz, float dx, float dy, float dz,
+                             float proj_factor, float proj_bias, u32 *steps, u32 *reads, float *scale_out) {
 	u32 n_steps = 0, n_reads = 0;
 	hd_hit out;
 	out.voxel[0] = out.voxel[1] = out.voxel[2] = 0;
@@ -105,7 +113,7 @@ __device__ hd_hit trace_one(const DevPool &P, u32 root, float ox, float oy, floa
 #pragma unroll
 			for (int a = 0; a < 3; ++a)
 				tcen[a] = __fadd_rn(__fmul_rn(half, tc[a]), tcor[a]);
-			if (scale < leaf_scale)
+			if (scale < leaf_scale || (Lod && __fmul_rn(scale_exp2, proj_factor) < __fadd_rn(tc_max, proj_bias)))
 				break;
 			if (tc_max < h)
 				stack[scale] = parent;
@@ -165,6 +173,8 @@ __device__ hd_hit trace_one(const DevPool &P, u32 root, float ox, float oy, floa
 		*steps = n_steps;
 	if (reads)
 		*reads = n_reads;
+	if (scale_out)
+		*scale_out = scale_exp2;
 	out.hit = hit ? 1u : 0u;
 	out.t = t_min;
 	const u32 voxel_level = leaf_level + 1u;
@@ -193,6 +203,118 @@ __device__ hd_hit trace_one(const DevPool &P, u32 root, float ox, float oy, floa
 	return out;
 }
 
+__device__ __forceinline__ hd_hit trace_one(const DevPool &P, u32 root, float ox, float oy, float oz, float dx,
+                                            float dy, float dz, u32 *steps = nullptr, u32 *reads = nullptr) {
+	return trace_core<false>(P, root, ox, oy, oz, dx, dy, dz, 0.0f, 0.0f, steps, reads, nullptr);
+}
+
+// Camera_GenRay (shader/src/trace.frag:366-370) at the centre of pixel (px, py)
+// of a w x h image, normalised with the same float operations as the host.
+__device__ __forceinline__ void pinhole_dir(const hd_camera &cam, u32 px, u32 py, u32 w, u32 h, float d[3]) {
+	const float u = __fsub_rn(__fmul_rn(__fdiv_rn(__fadd_rn((float)px, 0.5f), (float)w), 2.0f), 1.0f);
+	const float v = __fsub_rn(__fmul_rn(__fdiv_rn(__fadd_rn((float)py, 0.5f), (float)h), 2.0f), 1.0f);
+	float dd[3];
+#pragma unroll
+	for (int a = 0; a < 3; ++a)
+		dd[a] = __fsub_rn(__fsub_rn(cam.look[a], __fmul_rn(cam.side[a], u)), __fmul_rn(cam.up[a], v));
+	const float len2 = __fadd_rn(__fadd_rn(__fmul_rn(dd[0], dd[0]), __fmul_rn(dd[1], dd[1])), __fmul_rn(dd[2], dd[2]));
+	const float inv = __fdiv_rn(1.0f, __fsqrt_rn(len2));
+#pragma unroll
+	for (int a = 0; a < 3; ++a)
+		d[a] = __fmul_rn(dd[a], inv);
+}
+
+__device__ __forceinline__ void warp_add_counters(unsigned long long *counters, u64 a, u64 b, u64 c) {
+	for (int k = 16; k > 0; k >>= 1) {
+		a += __shfl_down_sync(0xFFFFFFFFu, a, k);
+		b += __shfl_down_sync(0xFFFFFFFFu, b, k);
+		c += __shfl_down_sync(0xFFFFFFFFu, c, k);
+	}
+	if ((threadIdx.x & 31u) == 0) {
+		atomicAdd(counters + 0, (unsigned long long)a);
+		atomicAdd(counters + 1, (unsigned long long)b);
+		atomicAdd(counters + 2, (unsigned long long)c);
+	}
+}
+
+// beam.frag main: one ray per block of the beam image (bw x bh per camera),
+// t = max(t_hit - size of the stopping cube, 0), +inf where the ray misses.
+__global__ void k_beam(DevPool P, u32 root, const hd_camera *cams, u32 n_cams, u32 bw, u32 bh, float proj_factor,
+                       float *beam, unsigned long long *counters) {
+	const u64 per = (u64)bw * bh, total = per * n_cams;
+	u64 my_steps = 0, my_reads = 0;
+	for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (u64)gridDim.x * blockDim.x) {
+		const u32 c = (u32)(i / per);
+		const u32 px = (u32)(i % per % bw), py = (u32)(i % per / bw);
+		const hd_camera cam = cams[c];
+		float d[3];
+		pinhole_dir(cam, px, py, bw, bh, d);
+		u32 st_, rd_;
+		float sexp = 0.0f;
+		const hd_hit hh = trace_core<true>(P, root, cam.position[0], cam.position[1], cam.position[2], d[0], d[1], d[2],
+		                                   proj_factor, 0.0f, &st_, &rd_, &sexp);
+		beam[i] = hh.hit ? fmax_ref(__fsub_rn(hh.t, sexp), 0.0f) : __uint_as_float(0x7F800000u);
+		my_steps += st_;
+		my_reads += rd_;
+	}
+	if (counters)
+		warp_add_counters(counters, my_steps, my_reads, 0);
+}
+
+// Beam value of pixel (px, py): textureLod(uBeam, coord, 0) with a linear
+// sampler in MIN reduction mode and clamp-to-edge (src/rg/TracePass.cpp:37-54),
+// i.e. the minimum of the 2x2 texels around x = coord * size - 0.5, the
+// footprint taken with exact rational arithmetic; times 0.98 (trace.frag:385).
+__device__ __forceinline__ int floor_div(long long a, long long b) {
+	return (int)(a >= 0 ? a / b : -((-a + b - 1) / b));
+}
+__device__ __forceinline__ float beam_at(const float *beam, u32 px, u32 py, u32 w, u32 h, u32 bw, u32 bh) {
+	const int i0 = floor_div((2ll * px + 1) * bw - w, 2ll * w), j0 = floor_div((2ll * py + 1) * bh - h, 2ll * h);
+	const int xs[2] = {max(0, min(i0, (int)bw - 1)), max(0, min(i0 + 1, (int)bw - 1))};
+	const int ys[2] = {max(0, min(j0, (int)bh - 1)), max(0, min(j0 + 1, (int)bh - 1))};
+	float m = beam[(u64)ys[0] * bw + xs[0]];
+#pragma unroll
+	for (int k = 1; k < 4; ++k)
+		m = fmin_ref(m, beam[(u64)ys[k >> 1] * bw + xs[k & 1]]);
+	return __fmul_rn(m, 0.98f);
+}
+
+// trace.frag main with BEAM_OPTIMIZATION (beam != nullptr) or without it:
+// the level-of-detail traversal from the camera, or from o + beam * d with the
+// beam value as projection bias.
+__global__ void k_trace_pinhole_lod(DevPool P, u32 root, const hd_camera *cams, u32 n_cams, u32 w, u32 h,
+                                    float proj_factor, const float *beam, u32 bw, u32 bh, hd_hit *out,
+                                    unsigned long long *counters) {
+	const u64 per = (u64)w * h, total = per * n_cams;
+	u64 my_steps = 0, my_reads = 0, my_hits = 0;
+	for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (u64)gridDim.x * blockDim.x) {
+		const u32 c = (u32)(i / per);
+		const u32 px = (u32)(i % per % w), py = (u32)(i % per / w);
+		const hd_camera cam = cams[c];
+		float d[3], o[3] = {cam.position[0], cam.position[1], cam.position[2]};
+		pinhole_dir(cam, px, py, w, h, d);
+		float bias = 0.0f;
+		bool traced = true;
+		if (beam) {
+			bias = beam_at(beam + (u64)c * bw * bh, px, py, w, h, bw, bh);
+			traced = __float_as_uint(bias) != 0x7F800000u; // isinf: the block's ray missed
+#pragma unroll
+			for (int a = 0; a < 3; ++a)
+				o[a] = __fadd_rn(o[a], __fmul_rn(bias, d[a]));
+		}
+		hd_hit hh{};
+		u32 st_ = 0, rd_ = 0;
+		if (traced)
+			hh = trace_core<true>(P, root, o[0], o[1], o[2], d[0], d[1], d[2], proj_factor, bias, &st_, &rd_, nullptr);
+		out[i] = hh;
+		my_steps += st_;
+		my_reads += rd_;
+		my_hits += hh.hit;
+	}
+	if (counters)
+		warp_add_counters(counters, my_steps, my_reads, my_hits);
+}
+
 __global__ void k_trace(DevPool P, u32 root, const float *o, const float *d, u32 n, hd_hit *out) {
 	for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (u64)gridDim.x * blockDim.x)
 		out[i] = trace_one(P, root, o[3 * i], o[3 * i + 1], o[3 * i + 2], d[3 * i], d[3 * i + 1], d[3 * i + 2]);
@@ -208,34 +330,17 @@ __global__ void k_trace_pinhole(DevPool P, u32 root, const hd_camera *cams, u32 
 		const u32 c = (u32)(i / per);
 		const u32 px = (u32)(i % per % w), py = (u32)(i % per / w);
 		const hd_camera cam = cams[c];
-		const float u = __fsub_rn(__fmul_rn(__fdiv_rn(__fadd_rn((float)px, 0.5f), (float)w), 2.0f), 1.0f);
-		const float v = __fsub_rn(__fmul_rn(__fdiv_rn(__fadd_rn((float)py, 0.5f), (float)h), 2.0f), 1.0f);
-		float dd[3];
-#pragma unroll
-		for (int a = 0; a < 3; ++a)
-			dd[a] = __fsub_rn(__fsub_rn(cam.look[a], __fmul_rn(cam.side[a], u)), __fmul_rn(cam.up[a], v));
-		const float len2 = __fadd_rn(__fadd_rn(__fmul_rn(dd[0], dd[0]), __fmul_rn(dd[1], dd[1])), __fmul_rn(dd[2], dd[2]));
-		const float inv = __fdiv_rn(1.0f, __fsqrt_rn(len2));
+		float d[3];
+		pinhole_dir(cam, px, py, w, h, d);
 		u32 st_, rd_;
-		const hd_hit hh = trace_one(P, root, cam.position[0], cam.position[1], cam.position[2], __fmul_rn(dd[0], inv),
-		                            __fmul_rn(dd[1], inv), __fmul_rn(dd[2], inv), &st_, &rd_);
+		const hd_hit hh = trace_one(P, root, cam.position[0], cam.position[1], cam.position[2], d[0], d[1], d[2], &st_, &rd_);
 		out[i] = hh;
 		my_steps += st_;
 		my_reads += rd_;
 		my_hits += hh.hit;
 	}
-	if (counters) { // one atomic per warp
-		for (int d = 16; d > 0; d >>= 1) {
-			my_steps += __shfl_down_sync(0xFFFFFFFFu, my_steps, d);
-			my_reads += __shfl_down_sync(0xFFFFFFFFu, my_reads, d);
-			my_hits += __shfl_down_sync(0xFFFFFFFFu, my_hits, d);
-		}
-		if ((threadIdx.x & 31u) == 0) {
-			atomicAdd(counters + 0, (unsigned long long)my_steps);
-			atomicAdd(counters + 1, (unsigned long long)my_reads);
-			atomicAdd(counters + 2, (unsigned long long)my_hits);
-		}
-	}
+	if (counters) // one atomic per warp and counter
+		warp_add_counters(counters, my_steps, my_reads, my_hits);
 }
 
 } // namespace
@@ -294,6 +399,57 @@ hd_status hd_trace_pinhole_async(hd_pool *pool, uint32_t root, const hd_camera *
 		s = HD_ERR_CUDA;
 	if (!s)
 		s = hd_launch_pinhole(pool, root, d_cams, n_cameras, width, height, d_out, d_counters, st);
+	cudaFreeAsync(d_cams, st);
+	return s;
+}
+
+float hd_projection_factor(float fov_y, uint32_t height, uint32_t divisor) {
+	// src/rg/TracePass.cpp:114-118 (divisor 1), src/rg/BeamPass.cpp:90-94 (divisor 8)
+	const float inv_2tan_half_fov = 1.0f / (2.0f * std::tan(0.5f * fov_y));
+	const float screen_tolerance = 1.0f / (float(height) / float(divisor));
+	return inv_2tan_half_fov / screen_tolerance;
+}
+
+hd_status hd_trace_pinhole_lod_async(hd_pool *pool, uint32_t root, const hd_camera *cameras, uint32_t n_cameras,
+                                     uint32_t width, uint32_t height, float proj_factor, float beam_proj_factor,
+                                     hd_hit *d_out, uint64_t *d_counters, void *stream) {
+	if (!pool || !cameras || !d_out || !n_cameras || !width || !height || !(proj_factor > 0.0f))
+		return HD_ERR_INVALID_ARG;
+	std::lock_guard<std::mutex> lk(pool->mtx);
+	if (cudaSetDevice(pool->device) != cudaSuccess)
+		return HD_ERR_CUDA;
+	cudaStream_t st = (cudaStream_t)stream;
+	if (cudaStreamWaitEvent(st, pool->ws_free, 0) != cudaSuccess)
+		return HD_ERR_CUDA;
+	const bool use_beam = beam_proj_factor > 0.0f;
+	const uint32_t bw = (width + kBeamBlock - 1) / kBeamBlock, bh = (height + kBeamBlock - 1) / kBeamBlock;
+	hd_camera *d_cams = nullptr;
+	float *d_beam = nullptr;
+	if (cudaMallocAsync((void **)&d_cams, n_cameras * sizeof(hd_camera), st) != cudaSuccess)
+		return HD_ERR_CUDA;
+	hd_status s = HD_OK;
+	if (use_beam && cudaMallocAsync((void **)&d_beam, (uint64_t)n_cameras * bw * bh * 4, st) != cudaSuccess)
+		s = HD_ERR_CUDA;
+	if (!s && cudaMemcpyAsync(d_cams, cameras, n_cameras * sizeof(hd_camera), cudaMemcpyHostToDevice, st) != cudaSuccess)
+		s = HD_ERR_CUDA;
+	unsigned long long *ctr = reinterpret_cast<unsigned long long *>(d_counters);
+	if (!s && use_beam) {
+		const uint64_t nb = (uint64_t)n_cameras * bw * bh;
+		const uint32_t grid = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((nb + 255) / 256, pool->num_sms * 16ull));
+		k_beam<<<grid, 256, 0, st>>>(pool->P, root, d_cams, n_cameras, bw, bh, beam_proj_factor, d_beam, ctr);
+		pool->kernel_launches++;
+	}
+	if (!s) {
+		const uint64_t total = (uint64_t)width * height * n_cameras;
+		const uint32_t grid = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((total + 255) / 256, pool->num_sms * 16ull));
+		k_trace_pinhole_lod<<<grid, 256, 0, st>>>(pool->P, root, d_cams, n_cameras, width, height, proj_factor, d_beam,
+		                                          bw, bh, d_out, ctr);
+		pool->kernel_launches++;
+		if (cudaGetLastError() != cudaSuccess)
+			s = HD_ERR_CUDA;
+	}
+	if (d_beam)
+		cudaFreeAsync(d_beam, st);
 	cudaFreeAsync(d_cams, st);
 	return s;
 }
