@@ -255,3 +255,36 @@ def test_identity_and_paged_heaps_agree(golden, orc, hd):
     ident2.upload(bw, ids, pages, paged.filled_node_pointers())
     bw2, ids2, pages2 = ident2.download()
     assert np.array_equal(bw, bw2) and np.array_equal(ids, ids2) and np.array_equal(pages, pages2)
+
+
+def test_one_cta_pass_equals_the_multi_kernel_pass(orc, hd):
+    """A small pass through hd_edit runs as one CTA (one launch); the same edit
+    through hd_edit_async (no host bounding box: the multi-kernel pass) on the
+    same pool finds every node the first one stored: the same root."""
+    import torch
+    from vkhashdag_gb300 import workloads as W
+    res = 1024
+    cfg = W.config_for_resolution(res)
+    pool = hd.NodePool(cfg, heap_pages=1 << 15)
+    ref = orc.OraclePool.from_config(cfg)
+    root = pool.edit(hd.NULL, W.sphere_scene(res, 16, seed=2))
+    rr = ref.edit(orc.NULL, W.sphere_scene(res, 16, seed=2))
+    edits = W.mixed_batch(res, 60, seed=77, r_max=12, side_max=20)
+    pool.reserve(1 << 20, 1 << 20, 16)
+    d_out = torch.zeros(1, dtype=torch.int32, device="cuda")
+    one_launch = 0
+    for k in range(len(edits)):
+        e = edits[k:k + 1]
+        n0 = pool.kernel_launches()
+        r_small = pool.edit(root, e)
+        one_launch += pool.kernel_launches() - n0 == 1
+        d_e = torch.from_numpy(e.view(np.uint8).copy()).cuda()
+        pool.edit_async(root, d_e.data_ptr(), 1, d_out.data_ptr(), 0)
+        torch.cuda.synchronize()
+        assert pool.error() == 0
+        assert (int(d_out.item()) & 0xFFFFFFFF) == r_small, k
+        root = r_small
+        rr = ref.edit(rr, e)
+    assert one_launch >= len(edits) // 2  # most of these small edits took the one-CTA pass
+    ok, counts, dig, _ = canonical_of_device(orc, pool, root)
+    assert ok and dig == [str(x) for x in ref.canonical(rr)[2]]

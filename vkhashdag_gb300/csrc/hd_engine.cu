@@ -206,6 +206,10 @@ void hd_grid_for_levels(const hd_pool *pool, const hd_edit_desc *edits, uint32_t
 
 namespace {
 
+// One-CTA passes: at most this many blocks' worth of level-(L-2) nodes
+// (2048) and of nodes at any level (8192) by the bounding-box estimate.
+constexpr uint32_t kSmallPassLeafGrid = 8, kSmallPassGrid = 32;
+
 // Launch sequence of one pass.  edits = device array of n edits; root from
 // root_ptr (device) when non-null, else root_val.  host_edits (optional) sizes
 // the grids.
@@ -219,6 +223,22 @@ hd_status launch_pass(hd_pool *pool, const hd_edit_desc *d_edits, uint32_t n, ui
 	uint32_t grid[HD_MAX_LEVELS];
 	hd_grid_for_levels(pool, host_edits, n, grid);
 	const uint32_t long_grid = (uint32_t)pool->num_sms * 4u;
+	// a pass that is small (grids sized from the edits' bounding boxes) and has
+	// no long lists runs as one CTA: one launch instead of 3L+1
+	if (host_edits && n <= W.long_threshold && pool->prof_passes >= pool->prof_max_passes && L >= 2) {
+		bool small = grid[L - 2] <= kSmallPassLeafGrid;
+		for (uint32_t l = 0; l < L; ++l)
+			small = small && grid[l] <= kSmallPassGrid;
+		if (small) {
+			HD_TRY(cudaStreamWaitEvent(st, pool->ws_free, 0));
+			HD_TRY(cudaMemsetAsync(W.ctr, 0, kWsCtrCount * sizeof(unsigned long long), st));
+			k_small_pass<<<1, kBlock, 0, st>>>(P, W, root_val, root_ptr, d_out);
+			pool->kernel_launches += 1;
+			HD_TRY(cudaGetLastError());
+			HD_TRY(cudaEventRecord(pool->ws_free, st));
+			return HD_OK;
+		}
+	}
 	static const bool debug_sync = getenv("HD_DEBUG_SYNC") != nullptr;
 	cudaEvent_t *ev = nullptr;
 	if (pool->prof_passes < pool->prof_max_passes)

@@ -194,7 +194,7 @@ __device__ __forceinline__ void write_child_list_thread(const Workspace &W, u32 
 // ------------------------------------------------------------------ k_expand_short
 // Thread per level-l inner node (l <= L-3) with an edit list of at most
 // long_threshold edits.  Children are inner items of level l+1.
-static __global__ void __launch_bounds__(kBlock) k_expand_short(DevPool P, Workspace W, u32 l) {
+__device__ __forceinline__ void expand_short_phase(const DevPool &P, Workspace &W, u32 l, u64 tbase, u64 tstride) {
 	if (ws_failed(W)) // an earlier launch overflowed: some items were never written
 		return;
 	const u32 L = P.cfg.L;
@@ -205,8 +205,8 @@ static __global__ void __launch_bounds__(kBlock) k_expand_short(DevPool P, Works
 	const u32 shift = L + 1u - cl; // child bounds at voxel level
 	const u32 filled_c = P.cfg.filled[cl];
 	const u32 T = W.long_threshold;
-	const u64 stride = (u64)gridDim.x * blockDim.x;
-	for (u64 w0 = (u64)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); w0 < n; w0 += stride) {
+	const u64 stride = tstride;
+	for (u64 w0 = tbase + (threadIdx.x & ~31u); w0 < n; w0 += stride) {
 		const u64 t = w0 + lane_id();
 		const bool valid = t < n;
 		const u64 i = begin + t;
@@ -278,6 +278,9 @@ static __global__ void __launch_bounds__(kBlock) k_expand_short(DevPool P, Works
 		cn[0] = make_uint4(res[0], res[1], res[2], res[3]);
 		cn[1] = make_uint4(res[4], res[5], res[6], res[7]);
 	}
+}
+static __global__ void __launch_bounds__(kBlock) k_expand_short(DevPool P, Workspace W, u32 l) {
+	expand_short_phase(P, W, l, (u64)blockIdx.x * blockDim.x, (u64)gridDim.x * blockDim.x);
 }
 
 // ------------------------------------------------------------------ block planning (long lists)
@@ -574,15 +577,15 @@ __device__ __forceinline__ void hand_to_parent(Workspace &W, u64 i, u32 r) {
 }
 
 // Thread per level-(L-2) node with a short edit list: computes its 8 leaves.
-static __global__ void __launch_bounds__(kBlock, 3) k_leafparent_short(DevPool P, Workspace W) {
+__device__ __forceinline__ void leafparent_short_phase(const DevPool &P, Workspace &W, u64 tbase, u64 tstride) {
 	if (ws_failed(W))
 		return;
 	const u32 L = P.cfg.L, l = L - 2;
 	u64 begin, n;
 	level_range(W, L, l, begin, n);
 	const u32 T = W.long_threshold;
-	const u64 stride = (u64)gridDim.x * blockDim.x;
-	for (u64 w0 = (u64)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); w0 < n; w0 += stride) {
+	const u64 stride = tstride;
+	for (u64 w0 = tbase + (threadIdx.x & ~31u); w0 < n; w0 += stride) {
 		const u64 t = w0 + lane_id();
 		const u64 i = begin + t;
 		const bool valid = t < n;
@@ -653,6 +656,9 @@ static __global__ void __launch_bounds__(kBlock, 3) k_leafparent_short(DevPool P
 		cn[0] = make_uint4(res[0], res[1], res[2], res[3]);
 		cn[1] = make_uint4(res[4], res[5], res[6], res[7]);
 	}
+}
+static __global__ void __launch_bounds__(kBlock, 3) k_leafparent_short(DevPool P, Workspace W) {
+	leafparent_short_phase(P, W, (u64)blockIdx.x * blockDim.x, (u64)gridDim.x * blockDim.x);
 }
 
 // Warp per level-(L-2) node with a long edit list: lane = (leaf c = lane/4,
@@ -750,7 +756,7 @@ static __global__ void __launch_bounds__(kBlock) k_leafparent_long(DevPool P, Wo
 // ------------------------------------------------------------------ k_root
 // NodePool.hpp:405-414 edit_switch on the root for the whole list (one block).
 // With a single node level the root is a leaf and is rebuilt here directly.
-static __global__ void __launch_bounds__(kLongBlock) k_root(DevPool P, Workspace W, u32 root_val, const u32 *root_ptr) {
+__device__ __forceinline__ void root_phase(const DevPool &P, Workspace &W, u32 root_val, const u32 *root_ptr) {
 	__shared__ u32 sm[40];
 	const u32 L = P.cfg.L;
 	const u32 root = root_ptr ? *root_ptr : root_val;
@@ -809,6 +815,9 @@ static __global__ void __launch_bounds__(kLongBlock) k_root(DevPool P, Workspace
 		return;
 	}
 	emit_child_block<true>(W, 0, 0, kNull, 0, W.n_edits, L + 1u, 0, 0, 0, b, f, cnt, sm);
+}
+static __global__ void __launch_bounds__(kLongBlock) k_root(DevPool P, Workspace W, u32 root_val, const u32 *root_ptr) {
+	root_phase(P, W, root_val, root_ptr);
 }
 
 // ------------------------------------------------------------------ dedup: find or claim
@@ -972,7 +981,8 @@ __device__ __forceinline__ void probe_range(const Workspace &W, u32 L, u32 l, u3
 }
 
 template <bool Leaf>
-static __global__ void __launch_bounds__(kBlock) k_probe(DevPool P, Workspace W, u32 l, u32 use_todo) {
+__device__ __forceinline__ void probe_phase(const DevPool &P, Workspace &W, u32 l, u32 use_todo, u64 tbase,
+                                            u64 tstride) {
 	if (ws_failed(W))
 		return;
 	__shared__ int s_skip;
@@ -999,8 +1009,8 @@ static __global__ void __launch_bounds__(kBlock) k_probe(DevPool P, Workspace W,
 	const u32 bbase = P.cfg.bucket_base[l];
 	const bool zero_hash = P.cfg.hasher == HD_HASHER_ZERO;
 	const u32 lane = lane_id();
-	const u64 stride = (u64)gridDim.x * blockDim.x;
-	for (u64 w0 = (u64)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); w0 < n; w0 += stride) {
+	const u64 stride = tstride;
+	for (u64 w0 = tbase + (threadIdx.x & ~31u); w0 < n; w0 += stride) {
 		const u64 t = w0 + lane;
 		const u64 i = t < n ? item_at(W, use_todo, begin, t) : 0;
 		bool cand = false;
@@ -1135,10 +1145,15 @@ static __global__ void __launch_bounds__(kBlock) k_probe(DevPool P, Workspace W,
 	const bool is_max[5] = {false, false, false, false, true};
 	flush_block_stats(v, dst, is_max, s_acc);
 }
+template <bool Leaf>
+static __global__ void __launch_bounds__(kBlock) k_probe(DevPool P, Workspace W, u32 l, u32 use_todo) {
+	probe_phase<Leaf>(P, W, l, use_todo, (u64)blockIdx.x * blockDim.x, (u64)gridDim.x * blockDim.x);
+}
 
 // ------------------------------------------------------------------ k_commit
 template <bool Leaf>
-static __global__ void __launch_bounds__(kBlock) k_commit(DevPool P, Workspace W, u32 l, u32 use_todo) {
+__device__ __forceinline__ void commit_phase(const DevPool &P, Workspace &W, u32 l, u32 use_todo, u64 tbase,
+                                             u64 tstride) {
 	if (ws_failed(W))
 		return;
 	__shared__ unsigned long long s_acc[2];
@@ -1152,8 +1167,8 @@ static __global__ void __launch_bounds__(kBlock) k_commit(DevPool P, Workspace W
 	Items &it = Leaf ? W.leaf : W.inner;
 	const u32 wp = wpp(P.cfg);
 	const u32 bucket_shift = P.cfg.wbpp + P.cfg.pbpb;
-	const u64 stride = (u64)gridDim.x * blockDim.x;
-	for (u64 w0 = (u64)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); w0 < n; w0 += stride) {
+	const u64 stride = tstride;
+	for (u64 w0 = tbase + (threadIdx.x & ~31u); w0 < n; w0 += stride) {
 		const u64 t = w0 + lane_id();
 		u32 ins = 0, insw = 0;
 		if (t < n) {
@@ -1250,9 +1265,13 @@ static __global__ void __launch_bounds__(kBlock) k_commit(DevPool P, Workspace W
 	const bool is_max[2] = {false, false};
 	flush_block_stats(v, dst, is_max, s_acc);
 }
+template <bool Leaf>
+static __global__ void __launch_bounds__(kBlock) k_commit(DevPool P, Workspace W, u32 l, u32 use_todo) {
+	commit_phase<Leaf>(P, W, l, use_todo, (u64)blockIdx.x * blockDim.x, (u64)gridDim.x * blockDim.x);
+}
 
 // ------------------------------------------------------------------ k_finish
-static __global__ void k_finish(DevPool P, Workspace W, u32 *out_root) {
+__device__ __forceinline__ void finish_phase(const DevPool &P, Workspace &W, u32 *out_root) {
 	if (threadIdx.x != 0)
 		return;
 	u64 ins = 0;
@@ -1264,6 +1283,43 @@ static __global__ void k_finish(DevPool P, Workspace W, u32 *out_root) {
 	W.ctr[kWsRoot] = r;
 	if (out_root)
 		*out_root = r;
+}
+static __global__ void k_finish(DevPool P, Workspace W, u32 *out_root) { finish_phase(P, W, out_root); }
+
+// ------------------------------------------------------------------ one-CTA pass
+// A whole pass in one block, the phases separated by block barriers instead of
+// kernel boundaries: the plain one-edit form (and other small passes) costs one
+// launch.  Only for passes without long edit lists (n_edits <= long_threshold),
+// whose every list is handled by the short phases.  Between phases a thread
+// reads what other threads of the block wrote before the barrier; the
+// read-only loads (index lookups in the leaf phase, page-table reads) never
+// touch words written earlier in the same pass.
+static __global__ void __launch_bounds__(kBlock) k_small_pass(DevPool P, Workspace W, u32 root_val, const u32 *root_ptr,
+                                                              u32 *out_root) {
+	const u32 L = P.cfg.L;
+	const u64 tb = 0, ts = blockDim.x;
+	root_phase(P, W, root_val, root_ptr);
+	__syncthreads();
+	for (u32 l = 0; l + 2 < L; ++l) {
+		expand_short_phase(P, W, l, tb, ts);
+		__syncthreads();
+	}
+	if (L >= 2) {
+		leafparent_short_phase(P, W, tb, ts);
+		__syncthreads();
+	}
+	probe_phase<true>(P, W, L - 1, 0u, tb, ts);
+	__syncthreads();
+	commit_phase<true>(P, W, L - 1, 0u, tb, ts);
+	__syncthreads();
+	for (u32 l = L - 1; l-- > 0;) {
+		const u32 todo = l + 2 == L ? 1u : 0u; // level L-2 runs over the unresolved nodes only
+		probe_phase<false>(P, W, l, todo, tb, ts);
+		__syncthreads();
+		commit_phase<false>(P, W, l, todo, tb, ts);
+		__syncthreads();
+	}
+	finish_phase(P, W, out_root);
 }
 
 } // namespace hd
