@@ -224,6 +224,14 @@ def run_ours(args):
     sp = stream.cuda_stream
     pool = hd.NodePool(cfg, heap_pages=heap_pages, device=local)
     root0 = pool.edit(hd.NULL, base)
+    # launch shape from the autotuner, on the first warm-up batch (the pool ends
+    # unchanged); the timed batches are different ones
+    tuning = None
+    if not args.no_tune:
+        try:
+            tuning = pool.autotune(root0, batches[0])
+        except hd.HashDagError as e:
+            tuning = {"error": str(e)}
     pool.checkpoint()
     d_batches = [torch.from_numpy(b.view(np.uint8).copy()).to(f"cuda:{local}") for b in batches]
     d_out = torch.zeros(n_batches, dtype=torch.int32, device=f"cuda:{local}")
@@ -383,6 +391,7 @@ def run_ours(args):
                      "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "algorithmic_bytes_per_step": dedup_bytes,
                      "dedup_ms_per_step": per_step_dedup_ms},
+        "tuning": tuning,
         "phases_ms_per_step": phase_ms,
         "counters_last_step": {k: [int(x) for x in v] for k, v in counters.items()},
         "probe_stats_last_step": probe_stats,
@@ -966,6 +975,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-step-seconds", type=float, default=6.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--mode", default="batched", choices=["batched", "terrain", "rays", "serving", "gc"])
     ap.add_argument("--gc-batches", type=int, default=2)
     ap.add_argument("--gc-cpu-resolution", type=int, default=4096)

@@ -179,6 +179,26 @@ hd_status hd_edit_last_counters(hd_pool *pool, uint64_t *items, uint64_t *candid
  * visited by all find-or-insert probes, the longest single probe, and failed
  * compare-and-swap attempts on bucket word counts (contention). */
 hd_status hd_edit_last_probe_stats(hd_pool *pool, uint64_t *probe_steps, uint64_t *max_probe, uint64_t *cas_retries);
+/* Launch shape of the batched pass: grid caps in blocks per SM for each kernel
+ * family and the edit-list length above which a node is expanded by a block
+ * (level L-2: a warp) instead of a thread.  Results never depend on them. */
+typedef struct hd_tuning {
+	uint32_t expand_blocks_per_sm;     /* k_expand_short (default 8) */
+	uint32_t leaf_blocks_per_sm;       /* k_leafparent_short (default 12) */
+	uint32_t dedup_blocks_per_sm;      /* k_probe / k_commit (default 32) */
+	uint32_t long_blocks_per_sm;       /* k_expand_long / k_leafparent_long (default 4) */
+	uint32_t long_threshold;           /* default 16, at least 1 */
+} hd_tuning;
+hd_status hd_edit_get_tuning(const hd_pool *pool, hd_tuning *out);
+hd_status hd_edit_set_tuning(hd_pool *pool, const hd_tuning *tuning);
+/* Autotuner: times the batched pass of edits[0..n) on root (the pool is rolled
+ * back after every trial, so it ends unchanged) for candidate launch shapes,
+ * one parameter at a time, keeps the fastest and installs it.  out (may be
+ * NULL) receives the chosen shape; ms_before / ms_after (may be NULL) the
+ * device time of the pass with the shape before and after. */
+hd_status hd_edit_autotune(hd_pool *pool, uint32_t root, const hd_edit_desc *edits, uint32_t n, hd_tuning *out,
+                           float *ms_before, float *ms_after);
+
 /* Checkpoint / rollback of the whole pool state (bucket word counts, page
  * table, heap and index counters, dedup index), kept in device memory.
  * Rollback (stream-ordered) forgets every node inserted after the checkpoint;

@@ -139,3 +139,11 @@ def test_server_entry_points_reject_bad_arguments(hd):
     assert lib.hd_server_wait(None, 1, 0.0, ctypes.byref(r)) == 1
     assert lib.hd_server_drain(None) == 1 and lib.hd_server_pause(None, 1) == 1
     lib.hd_server_destroy(None)
+
+
+def test_tuning_entry_points_reject_bad_arguments(hd):
+    lib = hd.lib()
+    t = hd._Tuning(8, 8, 8, 4, 16)
+    assert lib.hd_edit_set_tuning(None, ctypes.byref(t)) == 1
+    assert lib.hd_edit_get_tuning(None, ctypes.byref(t)) == 1
+    assert lib.hd_edit_autotune(None, 0, None, 0, None, None, None) == 1

@@ -288,3 +288,31 @@ def test_one_cta_pass_equals_the_multi_kernel_pass(orc, hd):
     assert one_launch >= len(edits) // 2  # most of these small edits took the one-CTA pass
     ok, counts, dig, _ = canonical_of_device(orc, pool, root)
     assert ok and dig == [str(x) for x in ref.canonical(rr)[2]]
+
+
+def test_launch_shape_never_changes_results(orc, hd):
+    """Every launch shape (grid caps, long-list threshold) gives the same DAG;
+    the autotuner leaves the pool as it found it."""
+    from vkhashdag_gb300 import workloads as W
+    res = 1024
+    cfg = W.config_for_resolution(res)
+    pool = hd.NodePool(cfg, heap_pages=1 << 15)
+    root = pool.edit(hd.NULL, W.sphere_scene(res, 16, seed=4))
+    batch = W.mixed_batch(res, 3000, seed=12, r_max=64, side_max=128)
+    want = pool.edit(root, batch)
+    shapes = [dict(long_threshold=1, expand_blocks_per_sm=1, leaf_blocks_per_sm=1, dedup_blocks_per_sm=1,
+                   long_blocks_per_sm=1),
+              dict(long_threshold=64, expand_blocks_per_sm=32, leaf_blocks_per_sm=24, dedup_blocks_per_sm=32,
+                   long_blocks_per_sm=8),
+              dict(long_threshold=4, expand_blocks_per_sm=2, leaf_blocks_per_sm=3, dedup_blocks_per_sm=4,
+                   long_blocks_per_sm=2)]
+    for sh in shapes:
+        pool.set_tuning(**sh)
+        assert pool.edit(root, batch) == want, sh
+    used = pool.stats()["used_pages"]
+    t = pool.autotune(root, batch)
+    assert t["ms_after"] <= t["ms_before"] and t["long_threshold"] >= 1
+    assert pool.stats()["used_pages"] == used  # rolled back to where it started
+    assert pool.edit(root, batch) == want
+    with pytest.raises(hd.HashDagError):
+        pool.set_tuning(long_threshold=0)

@@ -68,6 +68,12 @@ class _Stats(ctypes.Structure):
                 ("max_bucket_words", ctypes.c_uint32), ("words_per_bucket", ctypes.c_uint32)]
 
 
+class _Tuning(ctypes.Structure):
+    _fields_ = [("expand_blocks_per_sm", ctypes.c_uint32), ("leaf_blocks_per_sm", ctypes.c_uint32),
+                ("dedup_blocks_per_sm", ctypes.c_uint32), ("long_blocks_per_sm", ctypes.c_uint32),
+                ("long_threshold", ctypes.c_uint32)]
+
+
 class _GcStats(ctypes.Structure):
     _fields_ = [("live_nodes", ctypes.c_uint64), ("words_before", ctypes.c_uint64), ("words_after", ctypes.c_uint64),
                 ("pages_before", ctypes.c_uint64), ("pages_after", ctypes.c_uint64)]
@@ -130,6 +136,9 @@ def lib():
         "hd_upsert": (I, [P, U32, P, P, U32, P]),
         "hd_upsert_noalloc": (I, [P, U32, P, U32, P, P]),
         "hd_gc": (I, [P, P, U32, ctypes.POINTER(_GcStats)]),
+        "hd_edit_get_tuning": (I, [P, ctypes.POINTER(_Tuning)]),
+        "hd_edit_set_tuning": (I, [P, ctypes.POINTER(_Tuning)]),
+        "hd_edit_autotune": (I, [P, U32, P, U32, ctypes.POINTER(_Tuning), P, P]),
         "hd_edit_profile_begin": (I, [P, U32]),
         "hd_edit_profile_end": (I, [P, P, P]),
         "hd_pool_kernel_launches": (U64, [P]),
@@ -412,6 +421,30 @@ class NodePool:
         st = _GcStats()
         _check(lib().hd_gc(self._h, _ptr(r) if len(r) else None, len(r), ctypes.byref(st)), "hd_gc")
         return [int(x) for x in r], {name: int(getattr(st, name)) for name, _ in _GcStats._fields_}
+
+    def tuning(self) -> dict:
+        t = _Tuning()
+        _check(lib().hd_edit_get_tuning(self._h, ctypes.byref(t)), "hd_edit_get_tuning")
+        return {name: getattr(t, name) for name, _ in _Tuning._fields_}
+
+    def set_tuning(self, **kw):
+        cur = self.tuning()
+        cur.update(kw)
+        t = _Tuning(**cur)
+        _check(lib().hd_edit_set_tuning(self._h, ctypes.byref(t)), "hd_edit_set_tuning")
+
+    def autotune(self, root: int, edits: np.ndarray) -> dict:
+        """Times the batched pass of `edits` on `root` for candidate launch shapes
+        (the pool ends unchanged; its checkpoint slot is reused) and installs the
+        fastest; returns the shape and the pass times before / after."""
+        e = np.ascontiguousarray(edits, dtype=EDIT_DTYPE)
+        t = _Tuning()
+        before, after = ctypes.c_float(), ctypes.c_float()
+        _check(lib().hd_edit_autotune(self._h, root & 0xFFFFFFFF, _ptr(e), len(e), ctypes.byref(t),
+                                      ctypes.byref(before), ctypes.byref(after)), "hd_edit_autotune")
+        out = {name: getattr(t, name) for name, _ in _Tuning._fields_}
+        out["ms_before"], out["ms_after"] = before.value, after.value
+        return out
 
     def checkpoint(self):
         _check(lib().hd_pool_checkpoint(self._h), "hd_pool_checkpoint")

@@ -178,7 +178,7 @@ bool edit_bbox(const hd_edit_desc &e, uint32_t res, uint32_t lo[3], uint32_t hi[
 // small grids.
 void hd_grid_for_levels(const hd_pool *pool, const hd_edit_desc *edits, uint32_t n, uint32_t *grid) {
 	const uint32_t L = pool->cfg.node_levels, VL = L + 1, res = 1u << VL;
-	const uint32_t max_grid = (uint32_t)pool->num_sms * 8u;
+	const uint32_t max_grid = (uint32_t)pool->num_sms * 64u; // the launch sites cap per kernel family
 	std::vector<double> bound(L, 0.0);
 	if (!edits) {
 		for (uint32_t l = 0; l < L; ++l)
@@ -219,10 +219,13 @@ hd_status launch_pass(hd_pool *pool, const hd_edit_desc *d_edits, uint32_t n, ui
 	Workspace W = pool->ws.d;
 	W.edits = d_edits;
 	W.n_edits = n;
+	W.long_threshold = std::max(1u, pool->tune.long_threshold);
 	const DevPool &P = pool->P;
 	uint32_t grid[HD_MAX_LEVELS];
 	hd_grid_for_levels(pool, host_edits, n, grid);
-	const uint32_t long_grid = (uint32_t)pool->num_sms * 4u;
+	const uint32_t sms = (uint32_t)pool->num_sms;
+	const uint32_t long_grid = sms * std::max(1u, pool->tune.long_blocks_per_sm);
+	const auto cap = [&](uint32_t g, uint32_t per_sm) { return std::max(1u, std::min(g, sms * std::max(1u, per_sm))); };
 	// a pass that is small (grids sized from the edits' bounding boxes) and has
 	// no long lists runs as one CTA: one launch instead of 3L+1
 	if (host_edits && n <= W.long_threshold && pool->prof_passes >= pool->prof_max_passes && L >= 2) {
@@ -270,7 +273,7 @@ hd_status launch_pass(hd_pool *pool, const hd_edit_desc *d_edits, uint32_t n, ui
 	uint64_t launches = 1;
 	const bool longs = n > W.long_threshold; // no list can be longer than the batch
 	for (uint32_t l = 0; l + 2 < L; ++l) {
-		k_expand_short<<<grid[l], kBlock, 0, st>>>(P, W, l);
+		k_expand_short<<<cap(grid[l], pool->tune.expand_blocks_per_sm), kBlock, 0, st>>>(P, W, l);
 		dbg("expand_short", l + 1);
 		++launches;
 		if (longs) {
@@ -281,7 +284,7 @@ hd_status launch_pass(hd_pool *pool, const hd_edit_desc *d_edits, uint32_t n, ui
 	}
 	mark();
 	if (L >= 2) {
-		k_leafparent_short<<<grid[L - 2], kBlock, 0, st>>>(P, W);
+		k_leafparent_short<<<cap(grid[L - 2], pool->tune.leaf_blocks_per_sm), kBlock, 0, st>>>(P, W);
 		dbg("leafparent_short", L - 1);
 		++launches;
 		if (longs) {
@@ -291,18 +294,19 @@ hd_status launch_pass(hd_pool *pool, const hd_edit_desc *d_edits, uint32_t n, ui
 		}
 	}
 	mark();
-	k_probe<true><<<grid[L - 1], kBlock, 0, st>>>(P, W, L - 1, 0u);
+	const uint32_t dq = pool->tune.dedup_blocks_per_sm;
+	k_probe<true><<<cap(grid[L - 1], dq), kBlock, 0, st>>>(P, W, L - 1, 0u);
 	dbg("probe_leaf", L - 1);
 	mark();
-	k_commit<true><<<grid[L - 1], kBlock, 0, st>>>(P, W, L - 1, 0u);
+	k_commit<true><<<cap(grid[L - 1], dq), kBlock, 0, st>>>(P, W, L - 1, 0u);
 	dbg("commit_leaf", L - 1);
 	mark();
 	for (uint32_t l = L - 1; l-- > 0;) {
 		const uint32_t todo = l + 2 == L ? 1u : 0u; // level L-2 runs over the unresolved nodes only
-		k_probe<false><<<grid[l], kBlock, 0, st>>>(P, W, l, todo);
+		k_probe<false><<<cap(grid[l], dq), kBlock, 0, st>>>(P, W, l, todo);
 		dbg("probe", l);
 		mark();
-		k_commit<false><<<grid[l], kBlock, 0, st>>>(P, W, l, todo);
+		k_commit<false><<<cap(grid[l], dq), kBlock, 0, st>>>(P, W, l, todo);
 		dbg("commit", l);
 		mark();
 	}
@@ -905,6 +909,143 @@ hd_status hd_edit_async_droot(hd_pool *pool, const uint32_t *d_root, const hd_ed
 	pool->kernel_launches++;
 	HD_TRY(cudaGetLastError());
 	return hd_check(cudaEventRecord(pool->ws_free, st)); // hd_pool_get_error waits for this
+}
+
+hd_status hd_edit_get_tuning(const hd_pool *pool, hd_tuning *out) {
+	if (!pool || !out)
+		return HD_ERR_INVALID_ARG;
+	*out = pool->tune;
+	return HD_OK;
+}
+
+hd_status hd_edit_set_tuning(hd_pool *pool, const hd_tuning *t) {
+	if (!pool || !t || !t->expand_blocks_per_sm || !t->leaf_blocks_per_sm || !t->dedup_blocks_per_sm ||
+	    !t->long_blocks_per_sm || !t->long_threshold || t->expand_blocks_per_sm > 64 || t->leaf_blocks_per_sm > 64 ||
+	    t->dedup_blocks_per_sm > 64 || t->long_blocks_per_sm > 64)
+		return HD_ERR_INVALID_ARG;
+	std::lock_guard<std::mutex> lk(pool->mtx);
+	pool->tune = *t;
+	return HD_OK;
+}
+
+// Coordinate descent over the launch shape, one parameter at a time, each
+// candidate timed (CUDA events, best of two) on the same pass from the same
+// pool state (checkpoint before, rollback after every trial).
+hd_status hd_edit_autotune(hd_pool *pool, uint32_t root, const hd_edit_desc *edits, uint32_t n, hd_tuning *out,
+                           float *ms_before, float *ms_after) {
+	if (!pool || !edits || !n)
+		return HD_ERR_INVALID_ARG;
+	hd_status s = hd_pool_checkpoint(pool);
+	if (s)
+		return s;
+	uint32_t sized_root = kNull;
+	s = hd_edit(pool, root, edits, n, &sized_root, nullptr); // sizes the workspace for this pass
+	if (s)
+		return s;
+	HD_TRY(cudaSetDevice(pool->device));
+	cudaStream_t st = nullptr;
+	cudaEvent_t e0 = nullptr, e1 = nullptr;
+	hd_edit_desc *d_edits = nullptr;
+	uint32_t *d_root = nullptr;
+	auto cleanup = [&]() {
+		if (d_edits)
+			cudaFree(d_edits);
+		if (d_root)
+			cudaFree(d_root);
+		if (e0)
+			cudaEventDestroy(e0);
+		if (e1)
+			cudaEventDestroy(e1);
+		if (st)
+			cudaStreamDestroy(st);
+	};
+	if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess || cudaEventCreate(&e0) != cudaSuccess ||
+	    cudaEventCreate(&e1) != cudaSuccess || cudaMalloc(&d_edits, n * sizeof(hd_edit_desc)) != cudaSuccess ||
+	    cudaMalloc(&d_root, 4) != cudaSuccess ||
+	    cudaMemcpy(d_edits, edits, n * sizeof(hd_edit_desc), cudaMemcpyHostToDevice) != cudaSuccess) {
+		cudaGetLastError();
+		cleanup();
+		return HD_ERR_CUDA;
+	}
+	auto trial = [&](const hd_tuning &t, float *ms) -> hd_status {
+		float best = 1e30f;
+		for (int rep = 0; rep < 2; ++rep) {
+			hd_status r = hd_pool_rollback(pool, st);
+			if (r)
+				return r;
+			{
+				std::lock_guard<std::mutex> lk(pool->mtx);
+				pool->tune = t;
+			}
+			if (cudaEventRecord(e0, st) != cudaSuccess)
+				return HD_ERR_CUDA;
+			r = hd_edit_async(pool, root, d_edits, n, d_root, st);
+			if (r)
+				return r;
+			if (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess)
+				return HD_ERR_CUDA;
+			uint32_t err = 0;
+			if ((r = hd_pool_get_error(pool, &err)))
+				return r;
+			if (err) { // a pass that failed does not count (and must not happen: same pass as the sizing run)
+				hd_pool_clear_error(pool);
+				return HD_ERR_INTERNAL;
+			}
+			float ms_r = 0.0f;
+			cudaEventElapsedTime(&ms_r, e0, e1);
+			best = std::min(best, ms_r);
+		}
+		*ms = best;
+		return HD_OK;
+	};
+	hd_tuning cur = pool->tune;
+	float cur_ms = 0.0f;
+	s = trial(cur, &cur_ms);
+	const float start_ms = cur_ms;
+	struct Knob {
+		uint32_t hd_tuning::*field;
+		std::vector<uint32_t> values;
+	};
+	const std::vector<Knob> knobs = {{&hd_tuning::long_threshold, {8, 16, 32, 64}},
+	                                 {&hd_tuning::leaf_blocks_per_sm, {3, 6, 12, 24}},
+	                                 {&hd_tuning::dedup_blocks_per_sm, {4, 8, 16, 32}},
+	                                 {&hd_tuning::expand_blocks_per_sm, {4, 8, 16, 32}},
+	                                 {&hd_tuning::long_blocks_per_sm, {2, 4, 8}}};
+	for (const Knob &k : knobs) {
+		if (s)
+			break;
+		for (uint32_t v : k.values) {
+			if (v == cur.*(k.field))
+				continue;
+			hd_tuning t = cur;
+			t.*(k.field) = v;
+			float ms = 0.0f;
+			if ((s = trial(t, &ms)))
+				break;
+			if (ms < cur_ms * 0.98f) { // keep a change only when it is clearly faster
+				cur = t;
+				cur_ms = ms;
+			}
+		}
+	}
+	{
+		std::lock_guard<std::mutex> lk(pool->mtx);
+		pool->tune = cur;
+	}
+	const hd_status rb = hd_pool_rollback(pool, st);
+	if (!s)
+		s = rb;
+	cudaStreamSynchronize(st);
+	cleanup();
+	if (s)
+		return s;
+	if (out)
+		*out = cur;
+	if (ms_before)
+		*ms_before = start_ms;
+	if (ms_after)
+		*ms_after = cur_ms;
+	return HD_OK;
 }
 
 hd_status hd_edit_profile_begin(hd_pool *pool, uint32_t max_passes) {

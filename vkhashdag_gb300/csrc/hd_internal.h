@@ -28,6 +28,7 @@ struct hd_pool {
 	std::mutex mtx;
 	uint64_t last_items[HD_MAX_LEVELS] = {}, last_cand[HD_MAX_LEVELS] = {}, last_ins[HD_MAX_LEVELS] = {};
 	std::atomic<uint64_t> kernel_launches{0}; // kernels launched by this pool since creation (any thread)
+	hd_tuning tune{8, 12, 32, 4, 16};         // launch shape of the batched pass (the autotuner's pick on the benchmark)
 	// phase timing: one set of events per profiled pass
 	std::vector<cudaEvent_t> prof_events;
 	uint32_t prof_passes = 0, prof_max_passes = 0;
