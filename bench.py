@@ -720,6 +720,9 @@ def run_serving(args):
     for res in SERVE_RES:
         cfg = W.serving_config(res)
         pool = hd.NodePool(cfg, heap_pages=min(heap_pages, cfg.get_total_pages()), device=local)
+        if args.serve_shape:
+            e, lf, dd = (int(x) for x in args.serve_shape.split(","))
+            pool.set_tuning(expand_blocks_per_sm=e, leaf_blocks_per_sm=lf, dedup_blocks_per_sm=dd)
         t0 = time.perf_counter()
         roots0.append(pool.edit(hd.NULL, W.terrain_columns(res, res // 256, seed=0)))
         build_s.append(time.perf_counter() - t0)
@@ -864,6 +867,7 @@ def run_serving(args):
                                f"boxes <=1024), ray batches 2^16..2^22 rays (1024 wide)",
                    "word_bits_per_page": 14, "page_bits_per_bucket": 2, "heap_pages_per_scene": heap_pages,
                    "max_pass_edits": args.max_pass_edits, "ray_slots": args.ray_slots,
+                   "launch_shape": pools[0].tuning(),
                    "terrain_build_s": build_s, "l2": "pools far above L2; no flush"},
         "rays_per_s": rays / wall_s,
         "requests_per_s": len(reqs) / wall_s, "offered_rate": args.rate,
@@ -985,6 +989,7 @@ def main():
     ap.add_argument("--max-pass-edits", type=int, default=16384)
     ap.add_argument("--ray-slots", type=int, default=4)
     ap.add_argument("--verify-seconds", type=float, default=60.0)
+    ap.add_argument("--serve-shape", default="", help="expand,leaf,dedup blocks per SM of the serving pools")
     ap.add_argument("--cameras", type=int, default=16)
     ap.add_argument("--width", type=int, default=3840)
     ap.add_argument("--height", type=int, default=2160)

@@ -316,3 +316,34 @@ def test_launch_shape_never_changes_results(orc, hd):
     assert pool.edit(root, batch) == want
     with pytest.raises(hd.HashDagError):
         pool.set_tuning(long_threshold=0)
+
+
+def test_graph_replayed_pass_equals_direct_pass(orc, hd):
+    """hd_edit replays a captured CUDA graph for passes of 4096+ edits (captured on
+    first use, recaptured when the workspace or launch shape changes): the same
+    roots as the directly launched pass, and the oracle's DAG."""
+    import torch
+    from vkhashdag_gb300 import workloads as W
+    res = 512
+    cfg = W.config_for_resolution(res)
+    pool = hd.NodePool(cfg, heap_pages=1 << 15)
+    ref = orc.OraclePool.from_config(cfg)
+    root = pool.edit(hd.NULL, W.sphere_scene(res, 16, seed=8))
+    rr = ref.edit(orc.NULL, W.sphere_scene(res, 16, seed=8))
+    d_out = torch.zeros(1, dtype=torch.int32, device="cuda")
+    for k, n in enumerate((5000, 4096, 6000)):
+        batch = W.mixed_batch(res, n, seed=300 + k, r_max=24, side_max=48)
+        r_graph = pool.edit(root, batch)  # may grow the workspace and retry (a recapture each time)
+        n0 = pool.kernel_launches()
+        assert pool.edit(root, batch) == r_graph  # replay
+        assert pool.kernel_launches() - n0 == 4 * cfg.get_node_levels()  # every kernel of the graph
+        d_e = torch.from_numpy(batch.view(np.uint8).copy()).cuda()
+        pool.edit_async(root, d_e.data_ptr(), n, d_out.data_ptr(), 0)
+        torch.cuda.synchronize()
+        assert pool.error() == 0 and (int(d_out.item()) & 0xFFFFFFFF) == r_graph
+        if k == 1:
+            pool.set_tuning(dedup_blocks_per_sm=4)  # recapture with another shape
+        root = r_graph
+        rr = ref.edit(rr, batch)
+    ok, counts, dig, _ = canonical_of_device(orc, pool, root)
+    assert ok and dig == [str(x) for x in ref.canonical(rr)[2]]

@@ -318,6 +318,10 @@ struct Workspace {
 	const hd_edit_desc *edits;
 	u32 n_edits;
 	u32 long_threshold; // lists longer than this are expanded by a block (inner) or a warp (level L-2)
+	// non-null for passes replayed from a CUDA graph: [0] = number of edits,
+	// [1] = input root, written before each replay (the graph's kernels keep
+	// the parameters they were captured with)
+	const u32 *pass_desc;
 	// device counters (u64 so that overflow counts stay exact):
 	//   [0..L-1)     items per inner level, [L-1] leaf candidates
 	//   [32..)       long items per level

@@ -116,6 +116,7 @@ hd_status ws_reserve(hd_pool *pool, uint64_t inner_cap, uint64_t leaf_cap, uint6
 	edit_cap = std::max<uint32_t>(edit_cap, ws.edit_cap);
 	cudaDeviceSynchronize();
 	ws_free_all(ws);
+	++pool->shape_gen; // a captured pass graph holds the old workspace pointers
 	Workspace d{};
 	hd_status s;
 	if ((s = alloc_items(ws, d.inner, inner_cap)) || (s = alloc_leaf_candidates(ws, d.leaf, leaf_cap)) ||
@@ -206,20 +207,47 @@ void hd_grid_for_levels(const hd_pool *pool, const hd_edit_desc *edits, uint32_t
 
 namespace {
 
+// hd_edit passes of at least this many edits replay the captured pass graph.
+constexpr uint32_t kGraphMinEdits = 4096;
+
+// Word offset of the pass descriptor (edit count, input root) in the pool's
+// 16-word device scratch (d_out_root) and its pinned host mirror (h_small).
+constexpr uint32_t kPassDescWord = 4;
+
 // One-CTA passes: at most this many blocks' worth of level-(L-2) nodes
 // (2048) and of nodes at any level (8192) by the bounding-box estimate.
 constexpr uint32_t kSmallPassLeafGrid = 8, kSmallPassGrid = 32;
 
+// Whether a pass with these host edits runs as one CTA (bounding-box grids).
+bool small_pass_grids(const hd_pool *pool, const hd_edit_desc *host_edits, uint32_t n, const uint32_t *grid) {
+	const uint32_t L = pool->cfg.node_levels;
+	if (!host_edits || n > std::max(1u, pool->tune.long_threshold) || L < 2)
+		return false;
+	bool small = grid[L - 2] <= kSmallPassLeafGrid;
+	for (uint32_t l = 0; l < L; ++l)
+		small = small && grid[l] <= kSmallPassGrid;
+	return small;
+}
+
 // Launch sequence of one pass.  edits = device array of n edits; root from
 // root_ptr (device) when non-null, else root_val.  host_edits (optional) sizes
 // the grids.
+// capture: enqueue for a CUDA graph (edit count and root from the pass
+// descriptor, grids at their caps, long-list kernels always present, no waits,
+// events or records).
 hd_status launch_pass(hd_pool *pool, const hd_edit_desc *d_edits, uint32_t n, uint32_t root_val,
-                      const uint32_t *root_ptr, uint32_t *d_out, cudaStream_t st, const hd_edit_desc *host_edits) {
+                      const uint32_t *root_ptr, uint32_t *d_out, cudaStream_t st, const hd_edit_desc *host_edits,
+                      bool capture = false) {
 	const uint32_t L = pool->cfg.node_levels;
 	Workspace W = pool->ws.d;
 	W.edits = d_edits;
 	W.n_edits = n;
 	W.long_threshold = std::max(1u, pool->tune.long_threshold);
+	if (capture) {
+		W.pass_desc = pool->d_out_root + kPassDescWord;
+		root_ptr = W.pass_desc + 1;
+		host_edits = nullptr;
+	}
 	const DevPool &P = pool->P;
 	uint32_t grid[HD_MAX_LEVELS];
 	hd_grid_for_levels(pool, host_edits, n, grid);
@@ -228,11 +256,8 @@ hd_status launch_pass(hd_pool *pool, const hd_edit_desc *d_edits, uint32_t n, ui
 	const auto cap = [&](uint32_t g, uint32_t per_sm) { return std::max(1u, std::min(g, sms * std::max(1u, per_sm))); };
 	// a pass that is small (grids sized from the edits' bounding boxes) and has
 	// no long lists runs as one CTA: one launch instead of 3L+1
-	if (host_edits && n <= W.long_threshold && pool->prof_passes >= pool->prof_max_passes && L >= 2) {
-		bool small = grid[L - 2] <= kSmallPassLeafGrid;
-		for (uint32_t l = 0; l < L; ++l)
-			small = small && grid[l] <= kSmallPassGrid;
-		if (small) {
+	if (!capture && pool->prof_passes >= pool->prof_max_passes && small_pass_grids(pool, host_edits, n, grid)) {
+		{
 			HD_TRY(cudaStreamWaitEvent(st, pool->ws_free, 0));
 			HD_TRY(cudaMemsetAsync(W.ctr, 0, kWsCtrCount * sizeof(unsigned long long), st));
 			k_small_pass<<<1, kBlock, 0, st>>>(P, W, root_val, root_ptr, d_out);
@@ -242,9 +267,10 @@ hd_status launch_pass(hd_pool *pool, const hd_edit_desc *d_edits, uint32_t n, ui
 			return HD_OK;
 		}
 	}
-	static const bool debug_sync = getenv("HD_DEBUG_SYNC") != nullptr;
+	static const bool debug_env = getenv("HD_DEBUG_SYNC") != nullptr;
+	const bool debug_sync = debug_env && !capture;
 	cudaEvent_t *ev = nullptr;
-	if (pool->prof_passes < pool->prof_max_passes)
+	if (!capture && pool->prof_passes < pool->prof_max_passes)
 		ev = pool->prof_events.data() + (uint64_t)pool->prof_passes++ * hd_prof_events_per_pass(L);
 	uint32_t e = 0;
 	auto mark = [&]() {
@@ -265,13 +291,14 @@ hd_status launch_pass(hd_pool *pool, const hd_edit_desc *d_edits, uint32_t n, ui
 		        what, l, cudaGetErrorString(err), c[kWsError], perr, l < HD_MAX_LEVELS ? c[kWsItems + l] : 0ull,
 		        c[kWsList], l < HD_MAX_LEVELS ? c[kWsLong + l] : 0ull, c[kWsMaxProbe], c[kWsProbeSteps], c[kWsCasRetry]);
 	};
-	HD_TRY(cudaStreamWaitEvent(st, pool->ws_free, 0));
+	if (!capture)
+		HD_TRY(cudaStreamWaitEvent(st, pool->ws_free, 0));
 	mark();
 	HD_TRY(cudaMemsetAsync(W.ctr, 0, kWsCtrCount * sizeof(unsigned long long), st));
 	k_root<<<1, kLongBlock, 0, st>>>(P, W, root_val, root_ptr);
 	dbg("root", 0);
 	uint64_t launches = 1;
-	const bool longs = n > W.long_threshold; // no list can be longer than the batch
+	const bool longs = capture || n > W.long_threshold; // no list can be longer than the batch
 	for (uint32_t l = 0; l + 2 < L; ++l) {
 		k_expand_short<<<cap(grid[l], pool->tune.expand_blocks_per_sm), kBlock, 0, st>>>(P, W, l);
 		dbg("expand_short", l + 1);
@@ -313,9 +340,62 @@ hd_status launch_pass(hd_pool *pool, const hd_edit_desc *d_edits, uint32_t n, ui
 	k_finish<<<1, 32, 0, st>>>(P, W, d_out);
 	mark();
 	launches += 1 + 2ull * L;
-	pool->kernel_launches += launches;
 	HD_TRY(cudaGetLastError());
+	if (capture) {
+		pool->pass_graph_kernels = (uint32_t)launches;
+		return HD_OK;
+	}
+	pool->kernel_launches += launches;
 	HD_TRY(cudaEventRecord(pool->ws_free, st));
+	return HD_OK;
+}
+
+// The multi-kernel pass of hd_edit as a CUDA graph: captured once per
+// workspace allocation and launch shape on a private stream, replayed with the
+// edit count and root written into the pinned pass descriptor first.  Nodes:
+// descriptor upload, error-word clear, the pass's kernels, counter and error
+// downloads into the pinned buffers run_pass_sync reads.
+hd_status pass_graph(hd_pool *pool, cudaGraphExec_t *out) {
+	if (pool->pass_graph && pool->graph_gen == pool->shape_gen) {
+		*out = pool->pass_graph;
+		return HD_OK;
+	}
+	if (pool->pass_graph) {
+		cudaGraphExecDestroy(pool->pass_graph);
+		pool->pass_graph = nullptr;
+	}
+	if (!pool->capture_stream)
+		HD_TRY(cudaStreamCreateWithFlags(&pool->capture_stream, cudaStreamNonBlocking));
+	cudaStream_t cs = pool->capture_stream;
+	HD_TRY(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+	hd_status s = HD_OK;
+	if (cudaMemcpyAsync(pool->d_out_root + kPassDescWord, pool->h_small + kPassDescWord, 8, cudaMemcpyHostToDevice,
+	                    cs) != cudaSuccess ||
+	    cudaMemsetAsync(pool->P.counters + kCtrError, 0, 4, cs) != cudaSuccess)
+		s = HD_ERR_CUDA;
+	if (!s)
+		s = launch_pass(pool, pool->ws.edits, 0, kNull, nullptr, pool->d_out_root, cs, nullptr, true);
+	if (!s && (cudaMemcpyAsync(pool->ws.ctr_host, pool->ws.d.ctr, kWsCtrCount * sizeof(unsigned long long),
+	                           cudaMemcpyDeviceToHost, cs) != cudaSuccess ||
+	           cudaMemcpyAsync(pool->h_small, pool->P.counters + kCtrError, 4, cudaMemcpyDeviceToHost, cs) !=
+	               cudaSuccess))
+		s = HD_ERR_CUDA;
+	cudaGraph_t g = nullptr;
+	const cudaError_t ec = cudaStreamEndCapture(cs, &g);
+	if (!s && ec != cudaSuccess)
+		s = HD_ERR_CUDA;
+	cudaGraphExec_t exec = nullptr;
+	if (!s && cudaGraphInstantiate(&exec, g, 0) != cudaSuccess)
+		s = HD_ERR_CUDA;
+	if (g)
+		cudaGraphDestroy(g);
+	if (s) {
+		cudaGetLastError();
+		return s;
+	}
+	pool->pass_graph = exec;
+	pool->graph_gen = pool->shape_gen;
+	*out = exec;
 	return HD_OK;
 }
 
@@ -352,16 +432,33 @@ hd_status status_of(uint32_t err) {
 hd_status run_pass_sync(hd_pool *pool, const hd_edit_desc *h_edits, uint32_t n, uint32_t root, uint32_t *out_root,
                         cudaStream_t st) {
 	const uint32_t L = pool->cfg.node_levels;
+	static const bool debug_env = getenv("HD_DEBUG_SYNC") != nullptr;
 	for (int attempt = 0; attempt < 24; ++attempt) {
+		// large passes replay the captured multi-kernel graph (its grids are the
+		// caps, which large passes reach anyway); smaller ones launch with grids
+		// sized from the edits' bounding boxes, which a graph cannot follow
+		cudaGraphExec_t graph = nullptr;
+		if (n >= kGraphMinEdits && pool->prof_passes >= pool->prof_max_passes && !debug_env &&
+		    pass_graph(pool, &graph) != HD_OK)
+			graph = nullptr;
 		HD_TRY(cudaStreamWaitEvent(st, pool->ws_free, 0));
-		HD_TRY(cudaMemsetAsync(pool->P.counters + kCtrError, 0, 4, st));
-		HD_TRY(cudaMemcpyAsync(pool->ws.edits, h_edits, n * sizeof(hd_edit_desc), cudaMemcpyHostToDevice, st));
-		hd_status s = launch_pass(pool, pool->ws.edits, n, root, nullptr, pool->d_out_root, st, h_edits);
-		if (s)
-			return s;
-		HD_TRY(cudaMemcpyAsync(pool->ws.ctr_host, pool->ws.d.ctr, kWsCtrCount * sizeof(unsigned long long),
-		                       cudaMemcpyDeviceToHost, st));
-		HD_TRY(cudaMemcpyAsync(pool->h_small, pool->P.counters + kCtrError, 4, cudaMemcpyDeviceToHost, st));
+		if (graph) {
+			pool->h_small[kPassDescWord] = n;
+			pool->h_small[kPassDescWord + 1] = root;
+			HD_TRY(cudaMemcpyAsync(pool->ws.edits, h_edits, n * sizeof(hd_edit_desc), cudaMemcpyHostToDevice, st));
+			HD_TRY(cudaGraphLaunch(graph, st));
+			pool->kernel_launches += pool->pass_graph_kernels;
+			HD_TRY(cudaEventRecord(pool->ws_free, st));
+		} else {
+			HD_TRY(cudaMemsetAsync(pool->P.counters + kCtrError, 0, 4, st));
+			HD_TRY(cudaMemcpyAsync(pool->ws.edits, h_edits, n * sizeof(hd_edit_desc), cudaMemcpyHostToDevice, st));
+			hd_status s = launch_pass(pool, pool->ws.edits, n, root, nullptr, pool->d_out_root, st, h_edits);
+			if (s)
+				return s;
+			HD_TRY(cudaMemcpyAsync(pool->ws.ctr_host, pool->ws.d.ctr, kWsCtrCount * sizeof(unsigned long long),
+			                       cudaMemcpyDeviceToHost, st));
+			HD_TRY(cudaMemcpyAsync(pool->h_small, pool->P.counters + kCtrError, 4, cudaMemcpyDeviceToHost, st));
+		}
 		HD_TRY(cudaStreamSynchronize(st));
 		const unsigned long long *c = pool->ws.ctr_host;
 		for (uint32_t l = 0; l < L; ++l) {
@@ -593,6 +690,7 @@ hd_status upsert_impl(hd_pool *pool, uint32_t level, const uint32_t *words, cons
 
 hd_status make_filled(hd_pool *pool) {
 	const uint32_t L = pool->cfg.node_levels;
+	++pool->shape_gen; // the filled pointers are kernel parameters of a captured pass graph
 	uint32_t leaf[2] = {kNull, kNull}, two = 2, nine = 9, r;
 	hd_status s = upsert_impl(pool, L - 1, leaf, &two, 1, &r);
 	if (s)
@@ -626,6 +724,10 @@ void pool_free(hd_pool *p) {
 		cudaFreeHost(p->ws.ctr_host);
 	if (p->ws_free)
 		cudaEventDestroy(p->ws_free);
+	if (p->pass_graph)
+		cudaGraphExecDestroy(p->pass_graph);
+	if (p->capture_stream)
+		cudaStreamDestroy(p->capture_stream);
 	for (cudaEvent_t e : p->prof_events)
 		cudaEventDestroy(e);
 	cudaFree(p->ck_bucket_words);
@@ -925,6 +1027,7 @@ hd_status hd_edit_set_tuning(hd_pool *pool, const hd_tuning *t) {
 		return HD_ERR_INVALID_ARG;
 	std::lock_guard<std::mutex> lk(pool->mtx);
 	pool->tune = *t;
+	++pool->shape_gen;
 	return HD_OK;
 }
 
@@ -976,6 +1079,7 @@ hd_status hd_edit_autotune(hd_pool *pool, uint32_t root, const hd_edit_desc *edi
 			{
 				std::lock_guard<std::mutex> lk(pool->mtx);
 				pool->tune = t;
+				++pool->shape_gen;
 			}
 			if (cudaEventRecord(e0, st) != cudaSuccess)
 				return HD_ERR_CUDA;
@@ -1031,6 +1135,7 @@ hd_status hd_edit_autotune(hd_pool *pool, uint32_t root, const hd_edit_desc *edi
 	{
 		std::lock_guard<std::mutex> lk(pool->mtx);
 		pool->tune = cur;
+		++pool->shape_gen;
 	}
 	const hd_status rb = hd_pool_rollback(pool, st);
 	if (!s)
@@ -1139,6 +1244,7 @@ hd_status hd_pool_rollback(hd_pool *pool, void *stream) {
 	HD_TRY(cudaMemcpyAsync(pool->P.index, pool->ck_index, (pool->P.index_mask + 1) * 8, cudaMemcpyDeviceToDevice, st));
 	for (uint32_t l = 0; l < pool->cfg.node_levels; ++l)
 		pool->P.cfg.filled[l] = pool->ck_filled[l];
+	++pool->shape_gen;
 	HD_TRY(cudaEventRecord(pool->ws_free, st));
 	return HD_OK;
 }
@@ -1285,6 +1391,7 @@ hd_status hd_pool_upload(hd_pool *pool, const uint32_t *bucket_words, const uint
 	if (filled) {
 		for (uint32_t l = 0; l < pool->cfg.node_levels; ++l)
 			pool->P.cfg.filled[l] = filled[l];
+		++pool->shape_gen;
 		return HD_OK;
 	}
 	return make_filled(pool);

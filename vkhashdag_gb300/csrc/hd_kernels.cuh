@@ -40,6 +40,12 @@ static constexpr int kLongBlock = 256;
 
 __device__ __forceinline__ u32 lane_id() { return threadIdx.x & 31u; }
 
+// Kernels replayed from a CUDA graph read the pass's edit count from device memory.
+__device__ __forceinline__ void apply_pass_desc(Workspace &W) {
+	if (W.pass_desc)
+		W.n_edits = W.pass_desc[0];
+}
+
 // Exclusive offset of this lane's `count` within a warp-wide reservation on *ctr.
 // All 32 lanes must call it.
 __device__ __forceinline__ u64 warp_reserve(unsigned long long *ctr, u32 count) {
@@ -280,6 +286,7 @@ __device__ __forceinline__ void expand_short_phase(const DevPool &P, Workspace &
 	}
 }
 static __global__ void __launch_bounds__(kBlock) k_expand_short(DevPool P, Workspace W, u32 l) {
+	apply_pass_desc(W);
 	expand_short_phase(P, W, l, (u64)blockIdx.x * blockDim.x, (u64)gridDim.x * blockDim.x);
 }
 
@@ -406,6 +413,7 @@ __device__ void emit_child_block(Workspace &W, u32 cl, u64 child_begin, u32 pare
 // ------------------------------------------------------------------ k_expand_long
 // Block per (level-l node with a long edit list, child), l <= L-3.
 static __global__ void __launch_bounds__(kLongBlock) k_expand_long(DevPool P, Workspace W, u32 l) {
+	apply_pass_desc(W);
 	if (ws_failed(W))
 		return;
 	__shared__ u32 sm[40];
@@ -658,6 +666,7 @@ __device__ __forceinline__ void leafparent_short_phase(const DevPool &P, Workspa
 	}
 }
 static __global__ void __launch_bounds__(kBlock, 3) k_leafparent_short(DevPool P, Workspace W) {
+	apply_pass_desc(W);
 	leafparent_short_phase(P, W, (u64)blockIdx.x * blockDim.x, (u64)gridDim.x * blockDim.x);
 }
 
@@ -665,6 +674,7 @@ static __global__ void __launch_bounds__(kBlock, 3) k_leafparent_short(DevPool P
 // quarter q = lane%4) owns voxels 16q..16q+15 of leaf c and walks the whole
 // list in order.
 static __global__ void __launch_bounds__(kBlock) k_leafparent_long(DevPool P, Workspace W) {
+	apply_pass_desc(W);
 	if (ws_failed(W))
 		return;
 	const u32 L = P.cfg.L, l = L - 2;
@@ -817,6 +827,7 @@ __device__ __forceinline__ void root_phase(const DevPool &P, Workspace &W, u32 r
 	emit_child_block<true>(W, 0, 0, kNull, 0, W.n_edits, L + 1u, 0, 0, 0, b, f, cnt, sm);
 }
 static __global__ void __launch_bounds__(kLongBlock) k_root(DevPool P, Workspace W, u32 root_val, const u32 *root_ptr) {
+	apply_pass_desc(W);
 	root_phase(P, W, root_val, root_ptr);
 }
 
@@ -1147,6 +1158,7 @@ __device__ __forceinline__ void probe_phase(const DevPool &P, Workspace &W, u32 
 }
 template <bool Leaf>
 static __global__ void __launch_bounds__(kBlock) k_probe(DevPool P, Workspace W, u32 l, u32 use_todo) {
+	apply_pass_desc(W);
 	probe_phase<Leaf>(P, W, l, use_todo, (u64)blockIdx.x * blockDim.x, (u64)gridDim.x * blockDim.x);
 }
 
@@ -1267,6 +1279,7 @@ __device__ __forceinline__ void commit_phase(const DevPool &P, Workspace &W, u32
 }
 template <bool Leaf>
 static __global__ void __launch_bounds__(kBlock) k_commit(DevPool P, Workspace W, u32 l, u32 use_todo) {
+	apply_pass_desc(W);
 	commit_phase<Leaf>(P, W, l, use_todo, (u64)blockIdx.x * blockDim.x, (u64)gridDim.x * blockDim.x);
 }
 
