@@ -14,7 +14,7 @@ voxel-edits = sum over its edits of the grid voxels inside the shape.
   e2e        the public C-ABI call hd_edit() with host edits (H2D copy of the
              edit array and D2H of root/status inside the timed region)
   per_edit   the plain form on the same edit list: one pass per edit
-  roofline   the dedup pass (k_probe + k_commit over all levels) against the
+  roofline   the dedup pass (k_dedup over all levels) against the
              measured HBM copy bandwidth
   cpu_baseline  the CPU restatement of the reference's threaded edit
              (oracle, OpenMP on all host cores) on a bounded sample
@@ -334,15 +334,14 @@ def run_ours(args):
 
     # ---------------- roofline of the dedup pass
     hbm, peak_kind = peaks()
-    per_step_dedup_ms = float(sum(phases[2:2 + 2 * L])) / max(1, npass)
+    per_step_dedup_ms = float(sum(phases[2:2 + L])) / max(1, npass)
     cw, c, iw = counters["candidate_words"], counters["candidates"], counters["inserted_words"]
     dedup_bytes = float(8 * cw.sum() + 8 * c.sum() + 4 * iw.sum())
     achieved = dedup_bytes / (per_step_dedup_ms / 1e3) / 1e9
     phase_ms = {"root+expand": float(phases[0]) / npass, "leaf_voxels": float(phases[1]) / npass}
     for k in range(L):
         lvl = L - 1 - k
-        phase_ms[f"probe_l{lvl}"] = float(phases[2 + 2 * k]) / npass
-        phase_ms[f"commit_l{lvl}"] = float(phases[3 + 2 * k]) / npass
+        phase_ms[f"dedup_l{lvl}"] = float(phases[2 + k]) / npass
     phase_ms["finish"] = float(phases[-1]) / npass
     # DRAM bytes of the dedup pass per step, from the committed ncu summary of a
     # smaller case scaled to this workload (only meaningful for the default one)
@@ -387,7 +386,7 @@ def run_ours(args):
                      "mean_ms": float(lat_ms.mean()), "device_ms_per_edit": plain_dev_ms / len(plain),
                      "same_root_as_sync": bool(plain_same)},
         "batched_vs_per_edit": {"e2e": e2e_value / plain_rate, "device": value / plain_dev_rate},
-        "roofline": {"bound": "hbm", "kernel": "dedup pass (k_probe+k_commit, all levels)", "achieved": achieved,
+        "roofline": {"bound": "hbm", "kernel": "dedup pass (k_dedup, all levels)", "achieved": achieved,
                      "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "algorithmic_bytes_per_step": dedup_bytes,
                      "dedup_ms_per_step": per_step_dedup_ms},

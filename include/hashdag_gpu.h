@@ -209,8 +209,8 @@ hd_status hd_pool_rollback(hd_pool *pool, void *stream);
 /* Phase timing of edit passes with CUDA events recorded on the pass's own
  * stream: after hd_edit_profile_begin, the next max_passes passes record
  * events; hd_edit_profile_end waits for them and writes, summed over those
- * passes, node_levels*2+3 phase durations in ms: [0] root+expand (all levels),
- * [1] leaf voxels, then for level L-1 down to 0: probe, commit; [last] finish. */
+ * passes, node_levels+3 phase durations in ms: [0] root+expand (all levels),
+ * [1] leaf voxels, then the dedup launch of level L-1 down to 0; [last] finish. */
 hd_status hd_edit_profile_begin(hd_pool *pool, uint32_t max_passes);
 hd_status hd_edit_profile_end(hd_pool *pool, float *out_ms, uint32_t *out_passes);
 /* Kernels this pool has launched since creation. */

@@ -457,9 +457,9 @@ class NodePool:
 
     def profile_end(self):
         """(phase times in ms summed over the profiled passes, number of passes).
-        Phases: [0] root+expand, [1] leaf voxels, then probe/commit for level
-        L-1 down to 0, [last] finish."""
-        n = 2 * self.config.get_node_levels() + 3
+        Phases: [0] root+expand, [1] leaf voxels, then the dedup launch of
+        level L-1 down to 0, [last] finish."""
+        n = self.config.get_node_levels() + 3
         out = np.zeros(n, np.float32)
         passes = ctypes.c_uint32(0)
         _check(lib().hd_edit_profile_end(self._h, _ptr(out), ctypes.byref(passes)), "hd_edit_profile_end")

@@ -282,32 +282,18 @@ __device__ __forceinline__ u32 pos_z(u64 p) { return (u32)((p >> 42) & 0x1FFFFFu
 // leaf level has no items: the kernel of level L-2 computes the 8 child leaves
 // of each node itself and emits only the changed leaves as candidates
 // (Workspace::leaf, with their bits in leaf_new).
-enum ItemState : u32 {
-	kStUnchanged = 0, // result = base pointer
-	kStEmpty = 1,     // result = Null
-	kStFound = 2,     // result = existing node res[]
-	kStRep = 3,       // result = node inserted by this item (res[]); link = index slot
-	kStAlias = 4,     // result = res[link] (another item of the pass with equal content)
-	kStFail = 5,      // insertion failed (error recorded)
-	kStCand = 6,      // leaf candidate, dedup pending
-	kStDone = 7,      // level-(L-2) node resolved by the leaf kernel (result already in the parent's slot)
-};
-
 struct Items {
 	u64 *pos;     // packed node coordinate (inner items)
 	u32 *base;    // node the edit list applies to (original node, filled node or Null) (inner items)
 	u32 *parent;  // child slot of the parent (inner index*8 + child) or kNull for the root
 	u32 *lst_off; // edit list [lst_off, lst_off+lst_len) in Workspace::lists (inner items)
 	u32 *lst_len;
-	u32 *res;     // result pointer
-	u32 *state;   // ItemState
-	u32 *link;    // index slot (kStRep) or representative item (kStAlias)
-	u32 *pad;     // bucket word offset where zero padding starts (kStRep), or kNull (inner items)
+	u32 *res;     // result pointer of items without a parent (the root item, upsert calls)
 	u64 cap;
 };
 
 struct Workspace {
-	Items inner, leaf; // leaf: candidates (parent slot, res, state, link)
+	Items inner, leaf; // leaf: candidates (parent slot, res)
 	u32 *bchild;       // [inner.cap*8] children of the base node
 	u32 *cnew;         // [inner.cap*8] new children
 	u64 *leaf_new;     // [leaf.cap] bits of the leaf candidates

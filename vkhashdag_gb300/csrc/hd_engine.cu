@@ -84,19 +84,17 @@ hd_status alloc_items(hd_ws_host &ws, Items &it, uint64_t cap) {
 	it.cap = cap;
 	hd_status s;
 	if ((s = ws_alloc(ws, &it.pos, cap)) || (s = ws_alloc(ws, &it.base, cap)) || (s = ws_alloc(ws, &it.parent, cap)) ||
-	    (s = ws_alloc(ws, &it.lst_off, cap)) || (s = ws_alloc(ws, &it.lst_len, cap)) || (s = ws_alloc(ws, &it.res, cap)) ||
-	    (s = ws_alloc(ws, &it.state, cap)) || (s = ws_alloc(ws, &it.link, cap)) || (s = ws_alloc(ws, &it.pad, cap)))
+	    (s = ws_alloc(ws, &it.lst_off, cap)) || (s = ws_alloc(ws, &it.lst_len, cap)) || (s = ws_alloc(ws, &it.res, cap)))
 		return s;
 	return HD_OK;
 }
 
-// Leaf candidates carry parent slot, result, state and link (bits in leaf_new).
+// Leaf candidates carry parent slot and result (bits in leaf_new).
 hd_status alloc_leaf_candidates(hd_ws_host &ws, Items &it, uint64_t cap) {
 	it = Items{};
 	it.cap = cap;
 	hd_status s;
-	if ((s = ws_alloc(ws, &it.parent, cap)) || (s = ws_alloc(ws, &it.res, cap)) || (s = ws_alloc(ws, &it.state, cap)) ||
-	    (s = ws_alloc(ws, &it.link, cap)))
+	if ((s = ws_alloc(ws, &it.parent, cap)) || (s = ws_alloc(ws, &it.res, cap)))
 		return s;
 	return HD_OK;
 }
@@ -322,24 +320,18 @@ hd_status launch_pass(hd_pool *pool, const hd_edit_desc *d_edits, uint32_t n, ui
 	}
 	mark();
 	const uint32_t dq = pool->tune.dedup_blocks_per_sm;
-	k_probe<true><<<cap(grid[L - 1], dq), kBlock, 0, st>>>(P, W, L - 1, 0u);
-	dbg("probe_leaf", L - 1);
-	mark();
-	k_commit<true><<<cap(grid[L - 1], dq), kBlock, 0, st>>>(P, W, L - 1, 0u);
-	dbg("commit_leaf", L - 1);
+	k_dedup<true><<<cap(grid[L - 1], dq), kBlock, 0, st>>>(P, W, L - 1, 0u);
+	dbg("dedup_leaf", L - 1);
 	mark();
 	for (uint32_t l = L - 1; l-- > 0;) {
 		const uint32_t todo = l + 2 == L ? 1u : 0u; // level L-2 runs over the unresolved nodes only
-		k_probe<false><<<cap(grid[l], dq), kBlock, 0, st>>>(P, W, l, todo);
-		dbg("probe", l);
-		mark();
-		k_commit<false><<<cap(grid[l], dq), kBlock, 0, st>>>(P, W, l, todo);
-		dbg("commit", l);
+		k_dedup<false><<<cap(grid[l], dq), kBlock, 0, st>>>(P, W, l, todo);
+		dbg("dedup", l);
 		mark();
 	}
 	k_finish<<<1, 32, 0, st>>>(P, W, d_out);
 	mark();
-	launches += 1 + 2ull * L;
+	launches += 1 + (uint64_t)L;
 	HD_TRY(cudaGetLastError());
 	if (capture) {
 		pool->pass_graph_kernels = (uint32_t)launches;
@@ -657,13 +649,12 @@ hd_status upsert_impl(hd_pool *pool, uint32_t level, const uint32_t *words, cons
 	Workspace W = pool->ws.d;
 	Items &it = leaf ? W.leaf : W.inner;
 	cudaStream_t st = 0;
-	std::vector<uint32_t> parents(n, kNull), states(n, kStCand);
+	std::vector<uint32_t> parents(n, kNull);
 	std::vector<unsigned long long> ctr(kWsCtrCount, 0ull);
 	ctr[kWsItems + level] = n;
 	HD_TRY(cudaStreamWaitEvent(st, pool->ws_free, 0));
 	HD_TRY(cudaMemcpyAsync(W.ctr, ctr.data(), kWsCtrCount * 8, cudaMemcpyHostToDevice, st));
 	HD_TRY(cudaMemcpyAsync(it.parent, parents.data(), n * 4ull, cudaMemcpyHostToDevice, st));
-	HD_TRY(cudaMemcpyAsync(it.state, states.data(), n * 4ull, cudaMemcpyHostToDevice, st));
 	if (leaf) {
 		HD_TRY(cudaMemcpyAsync(W.leaf_new, leafbits.data(), n * 8ull, cudaMemcpyHostToDevice, st));
 	} else {
@@ -671,15 +662,12 @@ hd_status upsert_impl(hd_pool *pool, uint32_t level, const uint32_t *words, cons
 		HD_TRY(cudaMemcpyAsync(W.bchild, bchild.data(), n * 32ull, cudaMemcpyHostToDevice, st));
 	}
 	const uint32_t grid = std::max(1u, std::min(ceil_div(n, kBlock), (uint32_t)pool->num_sms * 8u));
-	if (leaf) {
-		k_probe<true><<<grid, kBlock, 0, st>>>(pool->P, W, level, 0u);
-		k_commit<true><<<grid, kBlock, 0, st>>>(pool->P, W, level, 0u);
-	} else {
-		k_probe<false><<<grid, kBlock, 0, st>>>(pool->P, W, level, 0u);
-		k_commit<false><<<grid, kBlock, 0, st>>>(pool->P, W, level, 0u);
-	}
+	if (leaf)
+		k_dedup<true><<<grid, kBlock, 0, st>>>(pool->P, W, level, 0u);
+	else
+		k_dedup<false><<<grid, kBlock, 0, st>>>(pool->P, W, level, 0u);
 	k_finish<<<1, 32, 0, st>>>(pool->P, W, nullptr);
-	pool->kernel_launches += 3;
+	pool->kernel_launches += 2;
 	HD_TRY(cudaGetLastError());
 	HD_TRY(cudaEventRecord(pool->ws_free, st));
 	HD_TRY(cudaMemcpyAsync(out, it.res, n * 4ull, cudaMemcpyDeviceToHost, st));

@@ -47,7 +47,7 @@ struct hd_pool {
 
 // events per profiled pass: start, after expand, after leaf, after probe/commit of
 // every level (2 per level), after finish
-inline uint32_t hd_prof_events_per_pass(uint32_t L) { return 3u + 2u * L + 1u; }
+inline uint32_t hd_prof_events_per_pass(uint32_t L) { return 3u + L + 1u; }
 
 // hd_engine.cu
 hd_status hd_check(cudaError_t e);

@@ -16,13 +16,13 @@
 //                     the node's edit list to the 64 voxels of each of its 8
 //                     child leaves (NodePool.hpp:319-343) and emit the changed
 //                     leaves as dedup candidates
-//   k_probe(l)        hash each candidate (Hasher.hpp:21-48), merge equal
-//                     candidates of a warp (__match_any_sync), find-or-claim
-//                     it in the dedup index; claimed nodes reserve words in
-//                     their bucket (page padding rule of NodePool.hpp:134-157)
-//                     and open pages from the heap
-//   k_commit(l)       write claimed nodes, publish them in the index, hand
-//                     every node's pointer to its parent's child slot
+//   k_dedup(l)        hash each candidate (Hasher.hpp:21-48), merge equal
+//                     candidates of a warp (__match_any_sync), find or insert
+//                     it through the dedup index: a claimed node reserves
+//                     words in its bucket (page padding rule of
+//                     NodePool.hpp:134-157), opens pages from the heap, is
+//                     written and published; every node's pointer goes to its
+//                     parent's child slot
 //   k_finish          report the root
 //
 // Per voxel the result equals applying the edits one after another: the last
@@ -646,7 +646,6 @@ __device__ __forceinline__ void leafparent_short_phase(const DevPool &P, Workspa
 			if (ci < W.leaf.cap) {
 				W.leaf_new[ci] = cb[c];
 				W.leaf.parent[ci] = (u32)(i * 8u + c);
-				W.leaf.state[ci] = kStCand;
 			} else {
 				ws_error(W, kErrCapacity);
 			}
@@ -750,7 +749,6 @@ static __global__ void __launch_bounds__(kBlock) k_leafparent_long(DevPool P, Wo
 				if (ci < W.leaf.cap) {
 					W.leaf_new[ci] = bits;
 					W.leaf.parent[ci] = (u32)(i * 8u + c);
-					W.leaf.state[ci] = kStCand;
 				} else {
 					ws_error(W, kErrCapacity);
 				}
@@ -812,7 +810,6 @@ __device__ __forceinline__ void root_phase(const DevPool &P, Workspace &W, u32 r
 				W.ctr[kWsItems + 0] = 1;
 				W.leaf_new[0] = bits;
 				W.leaf.parent[0] = kNull;
-				W.leaf.state[0] = kStCand;
 			}
 		}
 		return;
@@ -831,26 +828,97 @@ static __global__ void __launch_bounds__(kLongBlock) k_root(DevPool P, Workspace
 	root_phase(P, W, root_val, root_ptr);
 }
 
-// ------------------------------------------------------------------ dedup: find or claim
+// ------------------------------------------------------------------ dedup: find or insert
+// One launch per level.  Every candidate is hashed, merged with the equal
+// candidates of its warp, and found or inserted in the dedup index; a new node
+// is written and published by the thread that claimed it, in the same launch,
+// and every result goes straight into the parent's child slot.
+//
+// Index protocol inside a launch (later launches see only final entries and
+// tombstones):
+//   * a claim CAS turns an empty slot into a pending entry (bit 63, the content
+//     hash tag, the claiming item);
+//   * the claimer reserves its words in the bucket, writes the node, and
+//     publishes the final entry with a release store -- or a tombstone when the
+//     bucket is full or the heap ran out;
+//   * a candidate that meets a pending entry with its tag compares its words
+//     with the claiming item's words in the workspace (written by earlier
+//     launches); when equal it waits for the publication and takes the pointer
+//     without reading the heap;
+//   * a candidate that meets a final entry with its tag has read it with an
+//     acquiring CAS and compares the node through L2 (no L1 copies), so a node
+//     published earlier in the same launch is seen complete.
 struct NodeWords {
 	u32 w[9];
 	u32 n;
 };
 
-struct Outcome {
-	u32 state, res, link, pad;
-};
+// Bounded waits: a wait that runs out records HD_ERR_TIMEOUT and fails the
+// candidate instead of spinning on.
+static constexpr u32 kSpinLimit = 1u << 20;
 
+__device__ __forceinline__ unsigned long long cas_acquire(unsigned long long *p, unsigned long long cmp,
+                                                          unsigned long long val) {
+	unsigned long long old;
+	asm volatile("atom.acquire.gpu.global.cas.b64 %0, [%1], %2, %3;" : "=l"(old) : "l"(p), "l"(cmp), "l"(val) : "memory");
+	return old;
+}
+__device__ __forceinline__ unsigned long long load_acquire(const unsigned long long *p) {
+	unsigned long long v;
+	asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+	return v;
+}
+__device__ __forceinline__ u32 load_acquire(const u32 *p) {
+	u32 v;
+	asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+	return v;
+}
+__device__ __forceinline__ void store_release(unsigned long long *p, unsigned long long v) {
+	asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ void store_release(u32 *p, u32 v) {
+	asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Physical page of virtual page vp, for a node written in this launch.  The
+// thread whose reservation opened the page maps it right after its
+// bucket-count CAS, so another thread that reserved words in that page in the
+// same launch can find it unmapped for a moment: wait for the mapping.
+__device__ __forceinline__ u32 mapped_page(const DevPool &P, u32 vp) {
+	if (P.identity)
+		return vp;
+	u32 phys = load_acquire(P.page_table + vp);
+	for (u32 spin = 0; phys == kUnallocPage; ++spin) {
+		if (spin > kSpinLimit) {
+			set_error(&P.counters[kCtrError], kErrTimeout);
+			return kZeroPage;
+		}
+		__nanosleep(64);
+		phys = load_acquire(P.page_table + vp);
+	}
+	return phys;
+}
+
+// A resident node equal to nw?  Loads through L2: the node may have been
+// written earlier in this launch by another SM.
 __device__ __forceinline__ bool equal_resident(const DevPool &P, u32 ptr, const NodeWords &nw) {
-	const u32 *p = node_addr(P, ptr);
+	const u32 *p;
+	if (P.identity) {
+		p = P.heap + ptr;
+	} else {
+		const u32 phys = __ldcg(P.page_table + (ptr >> P.cfg.wbpp));
+		p = P.heap + ((u64)phys << P.cfg.wbpp) + (ptr & (wpp(P.cfg) - 1u));
+	}
 	for (u32 k = 0; k < nw.n; ++k)
-		if (p[k] != nw.w[k])
+		if (__ldcg(p + k) != nw.w[k])
 			return false;
 	return true;
 }
 
 // Reserve space for a node of w words in bucket b (NodePool.hpp:134-157 on an
-// atomic word count).  Returns false when the bucket is full.
+// atomic word count).  Returns false when the bucket is full.  *pad_out is the
+// old word count when the node skips the rest of a page (that tail must be
+// zeroed), else kNull.
 __device__ __forceinline__ bool reserve(const DevPool &P, u32 b, u32 w, u32 *ptr_out, u32 *pad_out, u32 *retries) {
 	const u32 wp = wpp(P.cfg), wpb = 1u << (P.cfg.wbpp + P.cfg.pbpb);
 	u32 old = *(volatile u32 *)&P.bucket_words[b];
@@ -882,59 +950,111 @@ __device__ __forceinline__ bool reserve(const DevPool &P, u32 b, u32 w, u32 *ptr
 			phys = kZeroPage;
 			set_error(&P.counters[kCtrError], kErrOom);
 		}
-		P.page_table[vpage] = phys;
+		if (!P.identity)
+			store_release(P.page_table + vpage, phys);
+		else
+			P.page_table[vpage] = phys;
 	}
 	*ptr_out = (b << (P.cfg.wbpp + P.cfg.pbpb)) | off;
 	return true;
 }
 
-// Find-or-claim of one candidate.  cmp_pending(j) tests equality with pending item j.
-// The probe walks at most kMaxProbe slots (a table at its load limit needs a
-// few dozen); longer walks are reported as a full index instead of scanned.
+// Writes a reserved node, and zeroes the page tail its reservation skipped
+// (NodePool.hpp:145-150).  False if its page could not be allocated.
+__device__ __forceinline__ bool write_node(const DevPool &P, u32 ptr, u32 pad, const NodeWords &nw) {
+	const u32 wp = wpp(P.cfg);
+	const u32 phys = mapped_page(P, ptr >> P.cfg.wbpp);
+	if (page_lost(P, phys))
+		return false;
+	u32 *dst = P.heap + ((u64)phys << P.cfg.wbpp) + (ptr & (wp - 1u));
+	for (u32 k = 0; k < nw.n; ++k)
+		dst[k] = nw.w[k];
+	if (pad != kNull) {
+		const u32 vp = ((ptr >> (P.cfg.wbpp + P.cfg.pbpb)) << P.cfg.pbpb) | (pad >> P.cfg.wbpp);
+		const u32 zp = mapped_page(P, vp);
+		if (!page_lost(P, zp)) {
+			u32 *z = P.heap + ((u64)zp << P.cfg.wbpp);
+			for (u32 q = pad & (wp - 1u); q < wp; ++q)
+				z[q] = 0u;
+		}
+	}
+	return true;
+}
+
+// Pointer published in slot s by the thread that claimed it in this launch,
+// or kNull when that insertion failed (its error is already recorded).
+__device__ __forceinline__ u32 await_publication(const DevPool &P, u64 s) {
+	for (u32 spin = 0;; ++spin) {
+		const unsigned long long v = load_acquire(&P.index[s]);
+		if (v == kSlotTomb)
+			return kNull;
+		if (!(v >> 63))
+			return (u32)v;
+		if (spin > kSpinLimit) {
+			set_error(&P.counters[kCtrError], kErrTimeout);
+			return kNull;
+		}
+		__nanosleep(32);
+	}
+}
+
+// Find-or-insert of one candidate (NodePool.hpp:159-212 upsert_node with the
+// linear bucket scan replaced by the index).  cmp_pending(j) tests equality
+// with the words of item j of this level.  The probe walks at most kMaxProbe
+// slots (a table at its load limit needs a few dozen); a longer walk is
+// reported as a full index instead of scanned.  Returns the node's pointer, or
+// kNull when the insertion failed (error recorded).
 static constexpr u64 kMaxProbe = 1u << 16;
 template <typename CmpPending>
-__device__ __forceinline__ Outcome find_or_claim(const DevPool &P, u64 i, u32 level, u32 h, u32 bucket,
-                                                 const NodeWords &nw, u32 *probes, u32 *retries,
-                                                 CmpPending &&cmp_pending) {
+__device__ __forceinline__ u32 find_or_insert(const DevPool &P, u64 i, u32 level, u32 h, u32 bucket,
+                                              const NodeWords &nw, u32 *probes, u32 *retries, bool *inserted,
+                                              CmpPending &&cmp_pending) {
 	const u64 mask = P.index_mask;
 	const unsigned long long tag = (unsigned long long)(h & 0x7FFFFFFFu) << 32;
 	const u32 bucket_shift = P.cfg.wbpp + P.cfg.pbpb;
 	const u64 limit = mask < kMaxProbe ? mask + 1 : kMaxProbe;
 	u64 s = index_start(h, level, mask);
 	const unsigned long long claim = (1ull << 63) | tag | (unsigned long long)i;
-	Outcome out = {kStFail, kNull, kNull, kNull};
+	u32 r = kNull;
+	*inserted = false;
 	u64 probe = 0;
 	for (; probe < limit; ++probe, s = (s + 1) & mask) {
-		// claim-or-read in one atomic: an empty slot is claimed at once (no
-		// separate load first), an occupied one returns its entry
-		const unsigned long long v = atomicCAS(&P.index[s], kSlotEmpty, claim);
+		// claim-or-read in one atomic: an empty slot is claimed at once, an
+		// occupied one returns its entry
+		const unsigned long long v = cas_acquire(&P.index[s], kSlotEmpty, claim);
 		if (v == kSlotEmpty) {
 			u32 ptr, pad;
-			if (reserve(P, bucket, nw.n, &ptr, &pad, retries))
-				out = {kStRep, ptr, (u32)s, pad};
-			else {
+			if (!reserve(P, bucket, nw.n, &ptr, &pad, retries)) {
 				set_error(&P.counters[kCtrError], kErrBucketFull);
-				out = {kStFail, kNull, (u32)s, kNull};
+				store_release(&P.index[s], kSlotTomb);
+			} else if (!write_node(P, ptr, pad, nw)) {
+				set_error(&P.counters[kCtrError], kErrOom);
+				store_release(&P.index[s], kSlotTomb);
+			} else {
+				store_release(&P.index[s], tag | ptr);
+				r = ptr;
+				*inserted = true;
 			}
 			break;
 		}
-		if (v == kSlotTomb || ((v >> 32) & 0x7FFFFFFFull) != (tag >> 32))
+		if (v == kSlotTomb || (v & (0x7FFFFFFFull << 32)) != tag)
 			continue;
+		if (v >> 63) { // claimed in this launch by item (u32)v
+			if (!cmp_pending((u32)v))
+				continue;
+			r = await_publication(P, s);
+			break;
+		}
 		const u32 val = (u32)v;
-		if (v >> 63) { // pending in this pass
-			if (cmp_pending(val)) {
-				out = {kStAlias, kNull, val, kNull};
-				break;
-			}
-		} else if ((val >> bucket_shift) == bucket && equal_resident(P, val, nw)) {
-			out = {kStFound, val, kNull, kNull};
+		if ((val >> bucket_shift) == bucket && equal_resident(P, val, nw)) {
+			r = val;
 			break;
 		}
 	}
 	if (probe == limit)
 		set_error(&P.counters[kCtrError], kErrIndexFull);
 	*probes = (u32)probe + 1u;
-	return out;
+	return r;
 }
 
 // Per-thread statistics summed (or maxed) over the block, then one global
@@ -970,7 +1090,7 @@ __device__ __forceinline__ void flush_block_stats(const unsigned long long (&v)[
 		}
 }
 
-// ------------------------------------------------------------------ k_probe
+// ------------------------------------------------------------------ k_dedup
 // Leaf: the leaf candidates.  Inner: the level-l items, rebuilt from cnew.
 // Leaves repeat a few patterns many times: each block keeps a direct-mapped
 // shared-memory cache of leaf bits -> pointer for leaves found resident, so
@@ -980,7 +1100,7 @@ static constexpr u32 kLeafCache = 2048;
 __device__ __forceinline__ u64 item_at(const Workspace &W, u32 use_todo, u64 begin, u64 t) {
 	return use_todo ? (u64)W.todo[t] : begin + t;
 }
-__device__ __forceinline__ void probe_range(const Workspace &W, u32 L, u32 l, u32 use_todo, u64 &begin, u64 &n) {
+__device__ __forceinline__ void dedup_range(const Workspace &W, u32 L, u32 l, u32 use_todo, u64 &begin, u64 &n) {
 	if (use_todo) {
 		begin = 0;
 		n = W.ctr[kWsTodo];
@@ -990,9 +1110,10 @@ __device__ __forceinline__ void probe_range(const Workspace &W, u32 L, u32 l, u3
 	}
 	level_range(W, L, l, begin, n);
 }
+__device__ __forceinline__ u32 sat_add(u32 a, u32 b) { return a + b < a ? 0xFFFFFFFFu : a + b; }
 
 template <bool Leaf>
-__device__ __forceinline__ void probe_phase(const DevPool &P, Workspace &W, u32 l, u32 use_todo, u64 tbase,
+__device__ __forceinline__ void dedup_phase(const DevPool &P, Workspace &W, u32 l, u32 use_todo, u64 tbase,
                                             u64 tstride) {
 	if (ws_failed(W))
 		return;
@@ -1004,17 +1125,18 @@ __device__ __forceinline__ void probe_phase(const DevPool &P, Workspace &W, u32 
 			s_key[e] = 0ull; // no leaf candidate is all-empty
 			s_val[e] = kNull;
 		}
-	__shared__ unsigned long long s_acc[5];
-	if (threadIdx.x < 5)
+	__shared__ unsigned long long s_acc[7];
+	if (threadIdx.x < 7)
 		s_acc[threadIdx.x] = 0ull;
 	if (threadIdx.x == 0)
 		s_skip = pool_failed(P) ? 1 : 0;
 	__syncthreads();
-	const bool skip = s_skip != 0;
-	u32 a_cand = 0, a_words = 0, a_steps = 0, a_retry = 0, a_max = 0; // per-thread sums (saturating)
+	const bool skip = s_skip != 0; // an earlier level failed: insert nothing more, hand Null up
+	// per-thread sums (saturating)
+	u32 a_cand = 0, a_words = 0, a_steps = 0, a_retry = 0, a_max = 0, a_ins = 0, a_insw = 0;
 	const u32 L = P.cfg.L;
 	u64 begin, n;
-	probe_range(W, L, l, use_todo, begin, n);
+	dedup_range(W, L, l, use_todo, begin, n);
 	Items &it = Leaf ? W.leaf : W.inner;
 	const u32 nb_mask = (1u << P.cfg.bucket_bits[l]) - 1u;
 	const u32 bbase = P.cfg.bucket_base[l];
@@ -1023,21 +1145,18 @@ __device__ __forceinline__ void probe_phase(const DevPool &P, Workspace &W, u32 
 	const u64 stride = tstride;
 	for (u64 w0 = tbase + (threadIdx.x & ~31u); w0 < n; w0 += stride) {
 		const u64 t = w0 + lane;
-		const u64 i = t < n ? item_at(W, use_todo, begin, t) : 0;
+		const bool valid = t < n;
+		const u64 i = valid ? item_at(W, use_todo, begin, t) : 0;
 		bool cand = false;
+		u32 r = kNull;
 		NodeWords nw;
 		nw.n = 0;
 #pragma unroll
 		for (int k = 0; k < 9; ++k)
 			nw.w[k] = 0;
 		u32 h = 0;
-		if (t < n) {
-			if (skip) { // an earlier level failed: insert nothing more
-				if (!Leaf || it.state[i] == kStCand) {
-					it.state[i] = kStFail;
-					it.link[i] = kNull;
-				}
-			} else if (Leaf) {
+		if (valid && !skip) {
+			if (Leaf) {
 				const u64 bits = W.leaf_new[i];
 				nw.w[0] = (u32)bits;
 				nw.w[1] = (u32)(bits >> 32);
@@ -1052,7 +1171,7 @@ __device__ __forceinline__ void probe_phase(const DevPool &P, Workspace &W, u32 
 				const u32 c[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
 				if (a0.x == b0.x && a0.y == b0.y && a0.z == b0.z && a0.w == b0.w && a1.x == b1.x && a1.y == b1.y &&
 				    a1.z == b1.z && a1.w == b1.w) {
-					it.state[i] = kStUnchanged;
+					r = it.base[i]; // no child changed
 				} else {
 					u32 mask = 0, k = 1;
 #pragma unroll
@@ -1061,9 +1180,7 @@ __device__ __forceinline__ void probe_phase(const DevPool &P, Workspace &W, u32 
 							mask |= 1u << q;
 							nw.w[k++] = c[q];
 						}
-					if (!mask) {
-						it.state[i] = kStEmpty;
-					} else {
+					if (mask) { // else every child is gone: Null
 						nw.w[0] = mask;
 						nw.n = k;
 						Murmur mm;
@@ -1077,13 +1194,16 @@ __device__ __forceinline__ void probe_phase(const DevPool &P, Workspace &W, u32 
 		}
 		// cached leaf: found without a probe
 		bool hit = false;
-		u32 hit_ptr = kNull, slot_e = 0;
+		u32 slot_e = 0;
 		if (Leaf && cand) {
 			const u64 bits = (u64)nw.w[0] | ((u64)nw.w[1] << 32);
 			slot_e = (h ^ (h >> 13)) & (kLeafCache - 1u);
 			if (s_key[slot_e] == bits) {
-				hit_ptr = *(volatile u32 *)&s_val[slot_e];
-				hit = hit_ptr != kNull;
+				const u32 hp = *(volatile u32 *)&s_val[slot_e];
+				if (hp != kNull) {
+					hit = true;
+					r = hp;
+				}
 			}
 		}
 		const bool probe_me = cand && !hit;
@@ -1100,187 +1220,68 @@ __device__ __forceinline__ void probe_phase(const DevPool &P, Workspace &W, u32 
 			eq = eq && lw == nw.w[k];
 		}
 		const bool follower = eq;
-		Outcome o = {kStFail, kNull, kNull, kNull};
-		u32 probes = 0, retries = 0;
+		u32 probes = 0, retries = 0, mine = kNull;
+		bool ins = false;
 		if (probe_me && !follower) {
 			const u32 bucket = bbase + ((zero_hash ? 0u : h) & nb_mask);
 			if (Leaf) {
-				const u64 mine = W.leaf_new[i];
-				o = find_or_claim(P, i, l, h, bucket, nw, &probes, &retries,
-				                  [&](u32 j) { return W.leaf_new[j] == mine; });
+				const u64 bits = (u64)nw.w[0] | ((u64)nw.w[1] << 32);
+				mine = find_or_insert(P, i, l, h, bucket, nw, &probes, &retries, &ins,
+				                      [&](u32 j) { return W.leaf_new[j] == bits; });
 			} else {
-				const uint4 *cn4 = reinterpret_cast<const uint4 *>(W.cnew + i * 8u);
-				const uint4 a0 = cn4[0], a1 = cn4[1];
-				o = find_or_claim(P, i, l, h, bucket, nw, &probes, &retries, [&](u32 j) {
+				mine = find_or_insert(P, i, l, h, bucket, nw, &probes, &retries, &ins, [&](u32 j) {
 					const uint4 *o4 = reinterpret_cast<const uint4 *>(W.cnew + (u64)j * 8u);
 					const uint4 c0 = o4[0], c1 = o4[1];
-					return c0.x == a0.x && c0.y == a0.y && c0.z == a0.z && c0.w == a0.w && c1.x == a1.x &&
-					       c1.y == a1.y && c1.z == a1.z && c1.w == a1.w;
-				});
-			}
-		}
-		const u32 lst = __shfl_sync(kFullMask, o.state, leader), lres = __shfl_sync(kFullMask, o.res, leader),
-		          llink = __shfl_sync(kFullMask, o.link, leader);
-		const u64 litem = __shfl_sync(kFullMask, i, leader);
-		if (follower) {
-			if (lst == kStRep)
-				o = {kStAlias, kNull, (u32)litem, kNull};
-			else if (lst == kStFail)
-				o = {kStFail, kNull, kNull, kNull};
-			else
-				o = {lst, lres, llink, kNull};
-		}
-		if (hit)
-			o = {kStFound, hit_ptr, kNull, kNull};
-		else if (Leaf && probe_me && !follower && o.state == kStFound) {
-			const u64 bits = (u64)nw.w[0] | ((u64)nw.w[1] << 32);
-			if (s_key[slot_e] == 0ull && atomicCAS(&s_key[slot_e], 0ull, (unsigned long long)bits) == 0ull)
-				*(volatile u32 *)&s_val[slot_e] = o.res;
-		}
-		if (cand) {
-			it.state[i] = o.state;
-			it.res[i] = o.res;
-			it.link[i] = o.link;
-			if (!Leaf)
-				it.pad[i] = o.pad;
-		}
-		a_cand += cand ? 1u : 0u;
-		a_words += cand ? nw.n : 0u;
-		a_steps = a_steps + probes < a_steps ? 0xFFFFFFFFu : a_steps + probes;
-		a_retry = a_retry + retries < a_retry ? 0xFFFFFFFFu : a_retry + retries;
-		a_max = a_max > probes ? a_max : probes;
-	}
-	const unsigned long long v[5] = {a_cand, a_words, a_steps, a_retry, a_max};
-	unsigned long long *const dst[5] = {&W.ctr[kWsCand + l], &W.ctr[kWsCandWords + l], &W.ctr[kWsProbeSteps],
-	                                    &W.ctr[kWsCasRetry], &W.ctr[kWsMaxProbe]};
-	const bool is_max[5] = {false, false, false, false, true};
-	flush_block_stats(v, dst, is_max, s_acc);
-}
-template <bool Leaf>
-static __global__ void __launch_bounds__(kBlock) k_probe(DevPool P, Workspace W, u32 l, u32 use_todo) {
-	apply_pass_desc(W);
-	probe_phase<Leaf>(P, W, l, use_todo, (u64)blockIdx.x * blockDim.x, (u64)gridDim.x * blockDim.x);
-}
-
-// ------------------------------------------------------------------ k_commit
-template <bool Leaf>
-__device__ __forceinline__ void commit_phase(const DevPool &P, Workspace &W, u32 l, u32 use_todo, u64 tbase,
-                                             u64 tstride) {
-	if (ws_failed(W))
-		return;
-	__shared__ unsigned long long s_acc[2];
-	if (threadIdx.x < 2)
-		s_acc[threadIdx.x] = 0ull;
-	__syncthreads();
-	u32 a_ins = 0, a_insw = 0;
-	const u32 L = P.cfg.L;
-	u64 begin, n;
-	probe_range(W, L, l, use_todo, begin, n);
-	Items &it = Leaf ? W.leaf : W.inner;
-	const u32 wp = wpp(P.cfg);
-	const u32 bucket_shift = P.cfg.wbpp + P.cfg.pbpb;
-	const u64 stride = tstride;
-	for (u64 w0 = tbase + (threadIdx.x & ~31u); w0 < n; w0 += stride) {
-		const u64 t = w0 + lane_id();
-		u32 ins = 0, insw = 0;
-		if (t < n) {
-			const u64 i = item_at(W, use_todo, begin, t);
-			const u32 st = it.state[i];
-			u32 r;
-			switch (st) {
-			case kStUnchanged:
-				r = it.base[i];
-				break;
-			case kStEmpty:
-				r = kNull;
-				break;
-			case kStFound:
-				r = it.res[i];
-				break;
-			case kStAlias:
-				r = it.res[it.link[i]];
-				break;
-			case kStRep: {
-				r = it.res[i];
-				const u32 slot = it.link[i];
-				// identity heap: virtual page = physical page, no table read
-				const u32 phys = P.identity ? (r >> P.cfg.wbpp) : P.page_table[r >> P.cfg.wbpp];
-				if (page_lost(P, phys)) { // its page could not be allocated: the pass fails
-					P.index[slot] = kSlotTomb;
-					set_error(&P.counters[kCtrError], kErrOom);
-					r = kNull;
-					break;
-				}
-				u32 *dst = P.heap + ((u64)phys << P.cfg.wbpp) + (r & (wp - 1u));
-				u32 h;
-				if (Leaf) {
-					const u64 bits = W.leaf_new[i];
-					dst[0] = (u32)bits;
-					dst[1] = (u32)(bits >> 32);
-					insw = 2;
-					h = hash_leaf(bits);
-				} else {
-					const uint4 *cn4 = reinterpret_cast<const uint4 *>(W.cnew + i * 8u);
-					const uint4 a0 = cn4[0], a1 = cn4[1];
-					const u32 c[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-					u32 mask = 0;
-#pragma unroll
-					for (int q = 0; q < 8; ++q)
-						mask |= c[q] != kNull ? 1u << q : 0u;
-					Murmur mm;
-					mm.add(mask);
-					u32 k = 1;
+					u32 m = 0, k = 1;
+					const u32 c[8] = {c0.x, c0.y, c0.z, c0.w, c1.x, c1.y, c1.z, c1.w};
+					bool same_words = true;
 #pragma unroll
 					for (int q = 0; q < 8; ++q)
 						if (c[q] != kNull) {
-							dst[k++] = c[q];
-							mm.add(c[q]);
+							m |= 1u << q;
+							same_words = same_words && k < nw.n && c[q] == nw.w[k];
+							++k;
 						}
-					dst[0] = mask;
-					insw = k;
-					h = mm.finish(k);
-					const u32 pad = it.pad[i];
-					if (pad != kNull) {
-						const u32 vp = ((r >> bucket_shift) << P.cfg.pbpb) | (pad >> P.cfg.wbpp);
-						const u32 zp = P.identity ? vp : P.page_table[vp];
-						if (zp != kUnallocPage && !page_lost(P, zp)) {
-							u32 *z = P.heap + ((u64)zp << P.cfg.wbpp);
-							for (u32 q = pad & (wp - 1u); q < wp; ++q)
-								z[q] = 0u;
-						}
-					}
-				}
-				ins = 1;
-				// publish: the claim's tag is the content hash, recomputed here
-				// instead of read back; readers of the entry run in later launches
-				P.index[slot] = ((unsigned long long)(h & 0x7FFFFFFFu) << 32) | r;
-				break;
+					return same_words && m == nw.w[0] && k == nw.n;
+				});
 			}
-			default: // kStFail
-				if (it.link[i] != kNull)
-					P.index[it.link[i]] = kSlotTomb;
-				r = kNull;
-				break;
-			}
-			it.res[i] = r;
-			const u32 ps = it.parent[i];
-			if (ps == kNull)
-				W.ctr[kWsRoot] = r;
-			else
-				W.cnew[ps] = r;
 		}
-		a_ins += ins;
-		a_insw += insw;
+		const u32 lres = __shfl_sync(kFullMask, mine, leader);
+		if (probe_me)
+			r = follower ? lres : mine;
+		if (Leaf && probe_me && !follower && !ins && r != kNull) { // found resident: remember it in the block
+			const u64 bits = (u64)nw.w[0] | ((u64)nw.w[1] << 32);
+			if (s_key[slot_e] == 0ull && atomicCAS(&s_key[slot_e], 0ull, (unsigned long long)bits) == 0ull)
+				*(volatile u32 *)&s_val[slot_e] = r;
+		}
+		if (valid) {
+			const u32 ps = it.parent[i];
+			if (ps == kNull) { // the pass's root item, or a node of an upsert call
+				W.ctr[kWsRoot] = r;
+				it.res[i] = r;
+			} else {
+				W.cnew[ps] = r;
+			}
+		}
+		a_cand += cand ? 1u : 0u;
+		a_words += cand ? nw.n : 0u;
+		a_ins += ins ? 1u : 0u;
+		a_insw += ins ? nw.n : 0u;
+		a_steps = sat_add(a_steps, probes);
+		a_retry = sat_add(a_retry, retries);
+		a_max = a_max > probes ? a_max : probes;
 	}
-	const unsigned long long v[2] = {a_ins, a_insw};
-	unsigned long long *const dst[2] = {&W.ctr[kWsIns + l], &W.ctr[kWsInsWords + l]};
-	const bool is_max[2] = {false, false};
+	const unsigned long long v[7] = {a_cand, a_words, a_steps, a_retry, a_max, a_ins, a_insw};
+	unsigned long long *const dst[7] = {&W.ctr[kWsCand + l], &W.ctr[kWsCandWords + l], &W.ctr[kWsProbeSteps],
+	                                    &W.ctr[kWsCasRetry],  &W.ctr[kWsMaxProbe],     &W.ctr[kWsIns + l],
+	                                    &W.ctr[kWsInsWords + l]};
+	const bool is_max[7] = {false, false, false, false, true, false, false};
 	flush_block_stats(v, dst, is_max, s_acc);
 }
 template <bool Leaf>
-static __global__ void __launch_bounds__(kBlock) k_commit(DevPool P, Workspace W, u32 l, u32 use_todo) {
+static __global__ void __launch_bounds__(kBlock) k_dedup(DevPool P, Workspace W, u32 l, u32 use_todo) {
 	apply_pass_desc(W);
-	commit_phase<Leaf>(P, W, l, use_todo, (u64)blockIdx.x * blockDim.x, (u64)gridDim.x * blockDim.x);
+	dedup_phase<Leaf>(P, W, l, use_todo, (u64)blockIdx.x * blockDim.x, (u64)gridDim.x * blockDim.x);
 }
 
 // ------------------------------------------------------------------ k_finish
@@ -1321,15 +1322,11 @@ static __global__ void __launch_bounds__(kBlock) k_small_pass(DevPool P, Workspa
 		leafparent_short_phase(P, W, tb, ts);
 		__syncthreads();
 	}
-	probe_phase<true>(P, W, L - 1, 0u, tb, ts);
-	__syncthreads();
-	commit_phase<true>(P, W, L - 1, 0u, tb, ts);
+	dedup_phase<true>(P, W, L - 1, 0u, tb, ts);
 	__syncthreads();
 	for (u32 l = L - 1; l-- > 0;) {
 		const u32 todo = l + 2 == L ? 1u : 0u; // level L-2 runs over the unresolved nodes only
-		probe_phase<false>(P, W, l, todo, tb, ts);
-		__syncthreads();
-		commit_phase<false>(P, W, l, todo, tb, ts);
+		dedup_phase<false>(P, W, l, todo, tb, ts);
 		__syncthreads();
 	}
 	finish_phase(P, W, out_root);

@@ -5,8 +5,8 @@
 // allocator up front (as the reference renderer does with its sparse Vulkan
 // buffers), or latency-bound edit loops that must not take the implicit device
 // synchronisation a cudaMalloc/cudaFree can cause.  hd_upsert_noalloc serves
-// them: it runs the same dedup kernels as hd_upsert (k_probe / k_commit), but
-// the per-node scratch those kernels need lives in the file-scope device array
+// them: it runs the same dedup kernel as hd_upsert (k_dedup), but the
+// per-node scratch that kernel needs lives in the file-scope device array
 // g_upsert_scratch below instead of the pool's cudaMalloc'ed workspace.
 //
 // Limits and sharing:
@@ -33,8 +33,8 @@ namespace {
 
 constexpr uint32_t kNoAllocMaxNodes = 65536;
 constexpr uint32_t kCtrWords = kWsCtrCount;
-// per node: state, res, link, pad, parent (5 words) + cnew and bchild (16 words)
-constexpr size_t kNodeScratchWords = 21;
+// per node: res, parent (2 words) + cnew and bchild (16 words)
+constexpr size_t kNodeScratchWords = 18;
 constexpr size_t kScratchBytes =
     kCtrWords * sizeof(unsigned long long) + (size_t)kNoAllocMaxNodes * kNodeScratchWords * sizeof(uint32_t);
 
@@ -69,12 +69,9 @@ Workspace scratch_workspace(unsigned char *base, uint32_t n, bool leaf) {
 	uint32_t *w = reinterpret_cast<uint32_t *>(base + kCtrWords * sizeof(unsigned long long));
 	Items it{};
 	it.cap = n;
-	it.state = w;
-	it.res = w + kNoAllocMaxNodes;
-	it.link = w + 2 * (size_t)kNoAllocMaxNodes;
-	it.pad = w + 3 * (size_t)kNoAllocMaxNodes;
-	it.parent = w + 4 * (size_t)kNoAllocMaxNodes;
-	uint32_t *tail = w + 5 * (size_t)kNoAllocMaxNodes; // 16 words per node, 256-byte aligned offset
+	it.res = w;
+	it.parent = w + (size_t)kNoAllocMaxNodes;
+	uint32_t *tail = w + 2 * (size_t)kNoAllocMaxNodes; // 16 words per node, 256-byte aligned offset
 	if (leaf) {
 		W.leaf = it;
 		W.leaf_new = reinterpret_cast<u64 *>(tail);
@@ -98,14 +95,12 @@ __global__ void k_noalloc_load(Workspace W, const uint32_t *nodes, uint32_t n, u
 		return;
 	if (leaf) {
 		W.leaf_new[i] = (u64)nodes[2 * i] | ((u64)nodes[2 * i + 1] << 32);
-		W.leaf.state[i] = kStCand;
 		W.leaf.parent[i] = kNull;
 	} else {
 		for (int c = 0; c < 8; ++c) {
 			W.cnew[i * 8 + c] = nodes[i * 8 + c];
 			W.bchild[i * 8 + c] = 0xFFFFFFFEu; // never equal to a child: the node is always looked up
 		}
-		W.inner.state[i] = kStCand;
 		W.inner.parent[i] = kNull;
 	}
 }
@@ -144,17 +139,14 @@ extern "C" hd_status hd_upsert_noalloc(hd_pool *pool, uint32_t level, const uint
 	    cudaMemsetAsync(W.ctr, 0, kCtrWords * sizeof(unsigned long long), st) != cudaSuccess)
 		return HD_ERR_CUDA;
 	k_noalloc_load<<<grid, kBlock, 0, st>>>(W, d_nodes, n, level, leaf ? 1u : 0u);
-	if (leaf) {
-		k_probe<true><<<grid, kBlock, 0, st>>>(pool->P, W, level, 0u);
-		k_commit<true><<<grid, kBlock, 0, st>>>(pool->P, W, level, 0u);
-	} else {
-		k_probe<false><<<grid, kBlock, 0, st>>>(pool->P, W, level, 0u);
-		k_commit<false><<<grid, kBlock, 0, st>>>(pool->P, W, level, 0u);
-	}
+	if (leaf)
+		k_dedup<true><<<grid, kBlock, 0, st>>>(pool->P, W, level, 0u);
+	else
+		k_dedup<false><<<grid, kBlock, 0, st>>>(pool->P, W, level, 0u);
 	k_finish<<<1, 32, 0, st>>>(pool->P, W, nullptr);
 	k_noalloc_store<<<grid, kBlock, 0, st>>>(W, n, leaf ? 1u : 0u, d_out_ptrs);
 	if (cudaGetLastError() != cudaSuccess || cudaEventRecord(pool->ws_free, st) != cudaSuccess)
 		return HD_ERR_CUDA;
-	pool->kernel_launches += 6;
+	pool->kernel_launches += 4;
 	return HD_OK;
 }
