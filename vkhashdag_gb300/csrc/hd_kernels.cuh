@@ -1057,13 +1057,16 @@ __device__ __forceinline__ u32 find_or_insert(const DevPool &P, u64 i, u32 level
 	return r;
 }
 
-// Per-thread statistics summed (or maxed) over the block, then one global
-// atomic per counter and block instead of one per warp and iteration.  s_acc
-// holds N shared slots zeroed before the block's first __syncthreads; every
-// thread of the block calls this once, after its loop.
+// Per-thread statistics summed (or maxed) over the warp and added to the
+// block's shared accumulators; the block's last warp to get here adds them to
+// the global counters (one global atomic per counter and block instead of one
+// per warp and iteration).  No block barrier: warps that finish early leave at
+// once instead of waiting for the block's slowest warp.  s_acc (N slots) and
+// *s_done are zeroed before the block's first __syncthreads; every warp of the
+// block calls this once, with all its lanes, after its loop.
 template <int N>
 __device__ __forceinline__ void flush_block_stats(const unsigned long long (&v)[N], unsigned long long *const (&dst)[N],
-                                                  const bool (&is_max)[N], unsigned long long *s_acc) {
+                                                  const bool (&is_max)[N], unsigned long long *s_acc, u32 *s_done) {
 #pragma unroll
 	for (int k = 0; k < N; ++k) {
 		unsigned long long x = v[k];
@@ -1079,15 +1082,24 @@ __device__ __forceinline__ void flush_block_stats(const unsigned long long (&v)[
 				atomicAdd(&s_acc[k], x);
 		}
 	}
-	__syncthreads();
-#pragma unroll
-	for (int k = 0; k < N; ++k)
-		if (threadIdx.x == (unsigned)k && s_acc[k]) {
+	u32 last = 0;
+	if (lane_id() == 0) {
+		__threadfence_block();
+		last = atomicAdd(s_done, 1u) == (blockDim.x >> 5) - 1u ? 1u : 0u;
+	}
+	if (!__shfl_sync(kFullMask, last, 0))
+		return;
+	__threadfence_block();
+	if (lane_id() < (u32)N) {
+		const u32 k = lane_id();
+		const unsigned long long x = atomicAdd(&s_acc[k], 0ull); // read after every warp's update
+		if (x) {
 			if (is_max[k])
-				atomicMax(dst[k], s_acc[k]);
+				atomicMax(dst[k], x);
 			else
-				atomicAdd(dst[k], s_acc[k]);
+				atomicAdd(dst[k], x);
 		}
+	}
 }
 
 // ------------------------------------------------------------------ k_dedup
@@ -1126,10 +1138,13 @@ __device__ __forceinline__ void dedup_phase(const DevPool &P, Workspace &W, u32 
 			s_val[e] = kNull;
 		}
 	__shared__ unsigned long long s_acc[7];
+	__shared__ u32 s_done;
 	if (threadIdx.x < 7)
 		s_acc[threadIdx.x] = 0ull;
-	if (threadIdx.x == 0)
+	if (threadIdx.x == 0) {
 		s_skip = pool_failed(P) ? 1 : 0;
+		s_done = 0u;
+	}
 	__syncthreads();
 	const bool skip = s_skip != 0; // an earlier level failed: insert nothing more, hand Null up
 	// per-thread sums (saturating)
@@ -1276,7 +1291,7 @@ __device__ __forceinline__ void dedup_phase(const DevPool &P, Workspace &W, u32 
 	                                    &W.ctr[kWsCasRetry],  &W.ctr[kWsMaxProbe],     &W.ctr[kWsIns + l],
 	                                    &W.ctr[kWsInsWords + l]};
 	const bool is_max[7] = {false, false, false, false, true, false, false};
-	flush_block_stats(v, dst, is_max, s_acc);
+	flush_block_stats(v, dst, is_max, s_acc, &s_done);
 }
 template <bool Leaf>
 static __global__ void __launch_bounds__(kBlock) k_dedup(DevPool P, Workspace W, u32 l, u32 use_todo) {
