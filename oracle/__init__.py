@@ -94,6 +94,12 @@ def lib():
             "orc_trace_threads": (None, [P, U32, P, P, U32, P, I]),
             "orc_gc": (None, [P, P, U32]),
             "orc_trace_pinhole_lod": (None, [P, U32, P, U32, U32, U32, ctypes.c_float, ctypes.c_float, P, I]),
+            "orc_color_pool_create": (P, [U32, I]),
+            "orc_color_pool_destroy": (None, [P]),
+            "orc_color_nodes": (U64, [P, P]),
+            "orc_color_leaves": (U64, [P, P]),
+            "orc_vbr_edit": (None, [P, P, U32, U32, P, U32, U32, U32, U32, P, P]),
+            "orc_color_fetch": (None, [P, P, U32, P, U32, P]),
             "orc_hash_inner": (U32, [P, U32]),
             "orc_hash_leaf": (U32, [U32, U32]),
         }
@@ -107,6 +113,32 @@ def lib():
 
 def _p(a):
     return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class OracleColorPool:
+    """Colour octree of the application's DAGColorPool (restated)."""
+
+    NULL = 3 << 30
+
+    def __init__(self, leaf_level, keep_history=False):
+        self._h = lib().orc_color_pool_create(leaf_level, int(keep_history))
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            lib().orc_color_pool_destroy(self._h)
+            self._h = None
+
+    def nodes(self):
+        n = lib().orc_color_nodes(self._h, None)
+        out = np.zeros((n, 8), np.uint32)
+        lib().orc_color_nodes(self._h, _p(out))
+        return out
+
+    def leaves(self):
+        n = lib().orc_color_leaves(self._h, None)
+        out = np.zeros(n, np.uint32)
+        lib().orc_color_leaves(self._h, _p(out))
+        return out
 
 
 class OraclePool:
@@ -190,6 +222,22 @@ class OraclePool:
                                     float(beam_proj_factor), _p(out), t)
         return out
 
+    def vbr_edit(self, root, color_pool, color_root, edit, kind, colors, weight=0, bpw=0):
+        """One colour edit through VBREditorWrapper (kind 1 fill, 2 paint) with
+        the old root for the colour rules; returns (root, colour root)."""
+        e = np.ascontiguousarray(np.asarray(edit, EDIT_DTYPE).reshape(1))
+        r, c = ctypes.c_uint32(0), ctypes.c_uint32(0)
+        lib().orc_vbr_edit(self._h, color_pool._h, root, color_root, _p(e), kind, colors, weight, bpw, ctypes.byref(r),
+                           ctypes.byref(c))
+        return int(r.value), int(c.value)
+
+    def color_fetch(self, color_pool, color_root, xyz):
+        """trace.frag Color_Fetch of voxels (n,3): COLOR_DTYPE records."""
+        q = np.ascontiguousarray(xyz, np.uint32).reshape(-1, 3)
+        out = np.zeros(len(q), COLOR_DTYPE)
+        lib().orc_color_fetch(self._h, color_pool._h, color_root, _p(q), len(q), _p(out))
+        return out
+
     def gc(self, roots):
         """NodePoolThreadedGC::ThreadedGC (one-worker order); returns the remapped roots."""
         r = np.ascontiguousarray(roots, np.uint32).copy()
@@ -236,14 +284,21 @@ def hash_leaf(w0, w1) -> int:
 
 
 # ---------------------------------------------------------------------- reference driver
-MODE_EDIT, MODE_THREADED, MODE_UPSERT, MODE_TRACE, MODE_GC = 0, 1, 2, 3, 4
+MODE_EDIT, MODE_THREADED, MODE_UPSERT, MODE_TRACE, MODE_GC, MODE_VBR = 0, 1, 2, 3, 4, 5
+# colour of one voxel: VBRColor fields and VBRColor::Get() (VBRColor.hpp:18-43)
+COLOR_DTYPE = np.dtype([("has_value", "<u4"), ("colors", "<u4"), ("weight", "<u4"), ("bpw", "<u4"),
+                        ("rgb", "<f4", (3,))])
 
 
 def run_reference(mode, word_bits_per_page, page_bits_per_bucket, bucket_bits, edits=None, hasher=0, threads=1,
-                  max_task_level=0xFFFFFFFF, upserts=None, rays=None, keep=None):
+                  max_task_level=0xFFFFFFFF, upserts=None, rays=None, keep=None, vbr=None):
     """Run the reference headers through oracle/_ref/ref_driver.  Returns a dict
     with root, filled, bucket_words, page_ids, pages, elapsed_ns, and ptrs
-    (upsert mode) or hits (trace mode: hit flags and positions)."""
+    (upsert mode) or hits (trace mode: hit flags and positions).  Colour mode:
+    vbr = dict(leaf_level, keep_history, ops=[(kind, colors, weight, bpw)] per
+    edit, queries=(n,3) voxel coordinates); adds color_root, color_nodes
+    (n,8), color_leaves and colors (per query: has_value, colors, weight,
+    bpw, rgb)."""
     if not reference_available():
         raise RuntimeError("oracle/_ref/ref_driver is not built (reference tree absent)")
     edits = np.zeros(0, EDIT_DTYPE) if edits is None else np.ascontiguousarray(edits, EDIT_DTYPE)
@@ -258,6 +313,12 @@ def run_reference(mode, word_bits_per_page, page_bits_per_bucket, bucket_bits, e
             req += struct.pack(f"<{2 + len(words)}I", level, len(words), *words)
     if mode == MODE_GC:
         req += struct.pack(f"<{1 + len(keep)}I", len(keep), *keep)
+    if mode == MODE_VBR:
+        q = np.ascontiguousarray(vbr["queries"], np.uint32).reshape(-1, 3)
+        req += struct.pack("<2I", vbr["leaf_level"], int(vbr.get("keep_history", False)))
+        for op in vbr["ops"]:
+            req += struct.pack("<4I", *op)
+        req += struct.pack("<I", len(q)) + q.tobytes()
     if mode == MODE_TRACE:
         o, d = rays
         o = np.ascontiguousarray(o, np.float32).reshape(-1, 3)
@@ -300,6 +361,18 @@ def run_reference(mode, word_bits_per_page, page_bits_per_bucket, bucket_bits, e
         off += 4 * n
         out["roots_after"] = list(struct.unpack_from(f"<{n}I", data, off))
         off += 4 * n
+    if mode == MODE_VBR:
+        (out["color_root"], nn) = struct.unpack_from("<2I", data, off)
+        off += 8
+        out["color_nodes"] = np.frombuffer(data, np.uint32, 8 * nn, off).reshape(nn, 8).copy()
+        off += 32 * nn
+        (nl,) = struct.unpack_from("<I", data, off)
+        off += 4
+        out["color_leaves"] = np.frombuffer(data, np.uint32, nl, off).copy()
+        off += 4 * nl
+        nq = len(np.asarray(vbr["queries"]).reshape(-1, 3))
+        out["colors"] = np.frombuffer(data, COLOR_DTYPE, nq, off).copy()
+        off += COLOR_DTYPE.itemsize * nq
     if mode == MODE_UPSERT:
         (n,) = struct.unpack_from("<I", data, off)
         off += 4

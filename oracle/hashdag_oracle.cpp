@@ -936,6 +936,318 @@ static void trace_pinhole_lod(const Pool &pool, Word root, const hd_camera *cams
 	}
 }
 
+// ---------------------------------------------------------------- VBR colour
+// Colour editing through VBREditorWrapper (include/hashdag/VBREditor.hpp:26-107)
+// into the application's colour octree (src/DAGColorPool.hpp:20-218) with VBR
+// leaf chunks (include/hashdag/VBRColor.hpp:222-491), and the colour lookup of
+// trace.frag:272-356.
+//
+// Octree pointers: 2-bit tag (0 node, 1 colour, 2 leaf, 3 null) above 30 bits
+// of data (node index, RGB8 colour, leaf word index).  Nodes are 8 pointers,
+// appended in JoinNode (post) order.  A leaf block in the word vector is
+// [block size][macro count M][block count B][weight word count W]
+// [M macro blocks: first block, weight start][B block headers: colours,
+// voxel offset:14 | bits per weight:2 | weight offset:16][W weight words].
+//
+// A colour leaf covers the 8^(voxel_level - leaf_level) voxels under an octree
+// node at leaf_level, in Morton order (bit 3k = x_k, 3k+1 = y_k, 3k+2 = z_k,
+// finest first; the order in which the edit recursion visits children and
+// leaf voxels, NodeCoord.hpp:18-43).  The chunk the reference's VBRChunkWriter
+// produces depends only on the per-voxel sequence of (colours, bits per
+// weight, weight): a block starts at every voxel whose (colours, bits per
+// weight) differ from the previous voxel's and at every macro block start
+// (every 2^14 voxels); the weight bits are the voxels' weights back to back.
+// The colour rules of the editors (src/main.cpp:48-69,107-148) under the
+// wrapper give every voxel of an edited leaf its colour:
+//   walking from the colour leaf down through the old DAG, the first node that
+//   the edit covers (kFill) or that is empty gives the edit's colour to its
+//   whole subtree; the first node the edit does not touch keeps the old
+//   colours of its subtree; at a voxel, the edit's colour if the voxel is in
+//   the shape or was empty, else its old colour.
+// Fill and paint editors follow the same colour rules (paint only keeps the
+// geometry).
+static constexpr Word kTagNode = 0, kTagColor = 1, kTagLeaf = 2, kTagNull = 3;
+static constexpr Word kColorNull = kTagNull << 30;
+static constexpr Word kMacroBits = 14; // VBRInfo::kVoxelBitsPerMacroBlock
+static inline Word cptr(Word tag, Word data) { return (tag << 30) | data; }
+static inline Word ctag(Word p) { return p >> 30; }
+static inline Word cdata(Word p) { return p & 0x3FFFFFFFu; }
+
+struct VColor { // VBRColor (VBRColor.hpp:18-43)
+	Word colors = 0, weight = 0, bpw = 0, has = 0;
+	bool operator==(const VColor &o) const {
+		return colors == o.colors && weight == o.weight && bpw == o.bpw && has == o.has;
+	}
+};
+
+// VBRColor::Get (VBRColor.hpp:31-36) with RGB8Color/R5G6B5Color::Get
+// (Color.hpp:24,42-45) and glm::mix = x * (1 - a) + y * a, in float.
+static inline void vcolor_rgb(const VColor &c, float rgb[3]) {
+	if (c.bpw == 0) {
+		for (int k = 0; k < 3; ++k)
+			rgb[k] = float((c.colors >> (8 * k)) & 0xFFu) / 255.0f;
+		return;
+	}
+	const Word lo = c.colors & 0xFFFFu, hi = c.colors >> 16;
+	const float x[3] = {float(lo & 0x1Fu) / 31.0f, float((lo >> 5) & 0x3Fu) / 63.0f, float((lo >> 11) & 0x1Fu) / 31.0f};
+	const float y[3] = {float(hi & 0x1Fu) / 31.0f, float((hi >> 5) & 0x3Fu) / 63.0f, float((hi >> 11) & 0x1Fu) / 31.0f};
+	const float a = float(c.weight) / float((1u << c.bpw) - 1u);
+	for (int k = 0; k < 3; ++k) {
+		const float p = x[k] * (1.0f - a), q = y[k] * a;
+		rgb[k] = p + q;
+	}
+}
+// DAGColorPool::FillNode (src/DAGColorPool.hpp:167-169): RGB8Color{color.Get()}
+static inline Word vcolor_rgb8(const VColor &c) {
+	float rgb[3];
+	vcolor_rgb(c, rgb);
+	Word out = 0;
+	for (int k = 0; k < 3; ++k)
+		out |= Word(uint8_t(rgb[k] * 255.0f)) << (8 * k);
+	return out;
+}
+// DAGColorPool::GetFill (src/DAGColorPool.hpp:147-149)
+static inline VColor fill_of(Word p) { return ctag(p) == kTagColor ? VColor{cdata(p), 0, 0, 1} : VColor{}; }
+
+struct ColorPool {
+	Word leaf_level = 0;
+	bool keep_history = false;
+	std::vector<Word> nodes;  // 8 pointers per node
+	std::vector<Word> leaves; // leaf blocks
+
+	// DAGColorPool::GetChild (src/DAGColorPool.hpp:142-146)
+	Word child(Word p, Word c) const {
+		return ctag(p) == kTagNode ? nodes[size_t(cdata(p)) * 8 + c] : (ctag(p) == kTagColor ? p : kColorNull);
+	}
+	// DAGColorPool::SetNode (src/DAGColorPool.hpp:150-165)
+	Word set_node(Word p, const Word ch[8]) {
+		bool all_null = true, all_same_color = ctag(ch[0]) == kTagColor;
+		for (int c = 0; c < 8; ++c) {
+			all_null = all_null && ctag(ch[c]) == kTagNull;
+			all_same_color = all_same_color && ch[c] == ch[0];
+		}
+		if (all_null)
+			return kColorNull;
+		if (all_same_color)
+			return ch[0];
+		if (ctag(p) == kTagNode && std::equal(ch, ch + 8, nodes.begin() + size_t(cdata(p)) * 8))
+			return p;
+		const Word idx = Word(nodes.size() / 8);
+		nodes.insert(nodes.end(), ch, ch + 8);
+		return cptr(kTagNode, idx);
+	}
+	// DAGColorPool::SetLeaf (src/DAGColorPool.hpp:176-207); chunk = [M, B, W, ...]
+	Word set_leaf(Word p, const std::vector<Word> &chunk) {
+		const size_t data_size = chunk.size() + 1;
+		size_t append_size = (data_size & 1) ? data_size + 1 : data_size;
+		if (!keep_history && ctag(p) == kTagLeaf) {
+			const size_t idx = cdata(p), block_size = leaves[idx];
+			if (data_size <= block_size) {
+				std::copy(chunk.begin(), chunk.end(), leaves.begin() + idx + 1);
+				return p;
+			}
+			append_size = std::max(block_size << 1, append_size);
+		}
+		const size_t idx = leaves.size();
+		leaves.resize(idx + append_size, 0u);
+		leaves[idx] = Word(append_size);
+		std::copy(chunk.begin(), chunk.end(), leaves.begin() + idx + 1);
+		return cptr(kTagLeaf, Word(idx));
+	}
+};
+
+struct VStream { // per-voxel colours of one colour leaf, Morton order
+	std::vector<Word> colors;
+	std::vector<uint8_t> bpw, weight;
+	explicit VStream(size_t n) : colors(n), bpw(n), weight(n) {}
+	void set(size_t m, const VColor &c) {
+		colors[m] = c.colors;
+		bpw[m] = uint8_t(c.bpw);
+		weight[m] = uint8_t(c.weight);
+	}
+	VColor get(size_t m) const { return VColor{colors[m], weight[m], bpw[m], 1}; }
+};
+
+// Voxel colours of the chunk of leaf pointer p (VBRChunkIterator, VBRColor.hpp:286-365),
+// or the octree node's fill colour everywhere (VBRChunkWriter::Copy/Edit of an empty source).
+static VStream decode_leaf(const ColorPool &cp, Word p, size_t n) {
+	VStream s(n);
+	if (ctag(p) != kTagLeaf) {
+		const VColor f = fill_of(p);
+		for (size_t m = 0; m < n; ++m)
+			s.set(m, f);
+		return s;
+	}
+	const Word *w = cp.leaves.data() + cdata(p);
+	const Word M = w[1], B = w[2];
+	const Word *macro = w + 4, *hdr = macro + 2 * M, *bits = hdr + 2 * B;
+	for (Word k = 0; k < M; ++k) {
+		const Word first = macro[2 * k], end = k + 1 < M ? macro[2 * k + 2] : B, wstart = macro[2 * k + 1];
+		for (Word b = first; b < end; ++b) {
+			const Word v0 = hdr[2 * b + 1] >> 18, bpw = (hdr[2 * b + 1] >> 16) & 3u, woff = hdr[2 * b + 1] & 0xFFFFu;
+			Word v1 = b + 1 < end ? hdr[2 * (b + 1) + 1] >> 18 : (1u << kMacroBits);
+			for (Word v = v0; v < v1; ++v) {
+				const size_t m = (size_t(k) << kMacroBits) + v;
+				if (m >= n)
+					break;
+				Word wt = 0;
+				if (bpw) {
+					const size_t bit = size_t(wstart) + woff + size_t(v - v0) * bpw;
+					const uint64_t two = uint64_t(bits[bit >> 5]) | (((bit >> 5) + 1 < w[3]) ? uint64_t(bits[(bit >> 5) + 1]) << 32 : 0);
+					wt = Word(two >> (bit & 31)) & ((1u << bpw) - 1u);
+				}
+				s.set(m, VColor{hdr[2 * b], wt, bpw, 1});
+			}
+		}
+	}
+	return s;
+}
+
+// VBRChunkWriter (VBRColor.hpp:367-488) output for a per-voxel colour sequence:
+// [M, B, W, macro blocks, block headers, weight words].
+static std::vector<Word> encode_leaf(const VStream &s) {
+	const size_t n = s.colors.size();
+	const size_t M = (n + (size_t(1) << kMacroBits) - 1) >> kMacroBits;
+	std::vector<Word> macros, hdrs, wbits;
+	uint64_t bit = 0, macro_wstart = 0;
+	for (size_t m = 0; m < n; ++m) {
+		const bool macro_start = (m & ((size_t(1) << kMacroBits) - 1)) == 0;
+		if (macro_start) {
+			macro_wstart = bit;
+			macros.push_back(Word(hdrs.size() / 2));
+			macros.push_back(Word(bit));
+		}
+		if (macro_start || s.colors[m] != s.colors[m - 1] || s.bpw[m] != s.bpw[m - 1]) {
+			hdrs.push_back(s.colors[m]);
+			hdrs.push_back(Word((m & ((size_t(1) << kMacroBits) - 1)) << 18) | (Word(s.bpw[m]) << 16) |
+			               Word(bit - macro_wstart));
+		}
+		for (Word b = 0; b < s.bpw[m]; ++b, ++bit) {
+			if ((bit & 31) == 0)
+				wbits.push_back(0u);
+			wbits.back() |= Word((s.weight[m] >> b) & 1u) << (bit & 31);
+		}
+	}
+	std::vector<Word> out = {Word(M), Word(hdrs.size() / 2), Word(wbits.size())};
+	out.insert(out.end(), macros.begin(), macros.end());
+	out.insert(out.end(), hdrs.begin(), hdrs.end());
+	out.insert(out.end(), wbits.begin(), wbits.end());
+	return out;
+}
+
+// New colours of the voxels [m0, m0 + 8^(V - level)) of a colour leaf being
+// edited: VBREditorWrapper::EditNode/EditVoxel below the leaf level
+// (VBREditor.hpp:61-80,82-90) with the editors' colour rules.
+static void vbr_region(const Pool &dag, const hd_edit_desc &g, const VColor &C, Word level, const Word pos[3],
+                       Word dptr, Word leaf_level, size_t m0, const VStream &src, VStream &dst) {
+	const Word V = dag.cfg.voxel_level(), L = dag.cfg.node_levels();
+	const size_t count = size_t(1) << (3 * (V - level));
+	if (level > leaf_level) {
+		const EditType t = edit_node_type(g, V, level, pos);
+		if (t == kFill || dptr == kNull) {
+			for (size_t k = 0; k < count; ++k)
+				dst.set(m0 + k, C);
+			return;
+		}
+		if (t == kNotAffected) {
+			for (size_t k = 0; k < count; ++k)
+				dst.set(m0 + k, src.get(m0 + k));
+			return;
+		}
+	}
+	if (level == L - 1) {
+		const Word *p = dag.read_node(dptr);
+		for (Word i = 0; i < 64; ++i) {
+			const Word vp[3] = {(pos[0] << 2) | ((i >> 2) & 2u) | (i & 1u), (pos[1] << 2) | ((i >> 3) & 2u) | ((i >> 1) & 1u),
+			                    (pos[2] << 2) | ((i >> 4) & 2u) | ((i >> 2) & 1u)};
+			const bool old = (p[i >> 5] >> (i & 31)) & 1u;
+			dst.set(m0 + i, (voxel_in_shape(g, vp) || !old) ? C : src.get(m0 + i));
+		}
+		return;
+	}
+	const std::array<Word, 9> u = dag.unpack(dptr);
+	for (Word c = 0; c < 8; ++c) {
+		Word cp[3];
+		Pool::child_pos(pos, c, cp);
+		vbr_region(dag, g, C, level + 1, cp, u[1 + c], leaf_level, m0 + c * (count >> 3), src, dst);
+	}
+}
+
+// The colour octree part of one VBR edit at or above the colour leaf level:
+// VBREditorWrapper::EditNode/JoinNode (VBREditor.hpp:40-80,92-107) with
+// FillNode/ClearNode/SetNode/SetLeaf.  Returns the node's new pointer.
+static Word vbr_walk(ColorPool &cp, const Pool &dag, const hd_edit_desc &g, const VColor &C, Word level,
+                     const Word pos[3], Word optr, Word dptr) {
+	const Word V = dag.cfg.voxel_level();
+	const EditType t = edit_node_type(g, V, level, pos);
+	if (t == kFill || dptr == kNull || fill_of(optr) == C)
+		return cptr(kTagColor, vcolor_rgb8(C));
+	if (t == kNotAffected)
+		return optr;
+	if (level == cp.leaf_level) {
+		const size_t n = size_t(1) << (3 * (V - level));
+		const VStream src = decode_leaf(cp, optr, n);
+		VStream dst(n);
+		vbr_region(dag, g, C, level, pos, dptr, cp.leaf_level, 0, src, dst);
+		return cp.set_leaf(optr, encode_leaf(dst));
+	}
+	const std::array<Word, 9> u = dag.unpack(dptr);
+	Word ch[8];
+	for (Word c = 0; c < 8; ++c) {
+		Word cpos[3];
+		Pool::child_pos(pos, c, cpos);
+		ch[c] = vbr_walk(cp, dag, g, C, level + 1, cpos, cp.child(optr, c), u[1 + c]);
+	}
+	return cp.set_node(optr, ch);
+}
+
+// Colour of one voxel: Color_Fetch / Color_GetLeafColor (trace.frag:303-356).
+static VColor color_fetch(const ColorPool &cp, Word root, Word voxel_level, const Word v[3]) {
+	Word p = root;
+	for (Word l = 0; l < cp.leaf_level && ctag(p) == kTagNode; ++l) {
+		const Word s = voxel_level - 1u - l;
+		p = cp.nodes[size_t(cdata(p)) * 8 + (((v[0] >> s) & 1u) | (((v[1] >> s) & 1u) << 1) | (((v[2] >> s) & 1u) << 2))];
+	}
+	if (ctag(p) != kTagLeaf)
+		return ctag(p) == kTagColor ? fill_of(p) : VColor{};
+	const Word bits = voxel_level - cp.leaf_level;
+	Word vox = 0;
+	for (Word b = 0; b < bits; ++b)
+		vox |= (((v[0] >> b) & 1u) << (3 * b)) | (((v[1] >> b) & 1u) << (3 * b + 1)) | (((v[2] >> b) & 1u) << (3 * b + 2));
+	const Word *w = cp.leaves.data() + cdata(p);
+	const Word M = w[1];
+	Word nb = w[2];
+	const Word *macro = w + 4, *hdr = macro + 2 * M, *wb = hdr + 2 * nb;
+	const Word mid = vox >> kMacroBits;
+	if (mid >= M)
+		return VColor{0, 0, 0, 1};
+	const Word first = macro[2 * mid], wstart = macro[2 * mid + 1];
+	Word cnt = mid + 1 < M ? macro[2 * mid + 2] - first : nb - first;
+	const Word *b = hdr + 2 * first;
+	vox &= (1u << kMacroBits) - 1u;
+	if (cnt == 0)
+		return VColor{0, 0, 0, 1};
+	for (Word it = 0; it <= 14u && cnt != 0; ++it) { // first block whose voxel offset is > vox
+		const Word step = cnt >> 1;
+		if ((b[2 * step + 1] >> 18) <= vox) {
+			cnt -= step + 1;
+			b += 2 * (step + 1);
+		} else
+			cnt = step;
+	}
+	b -= 2;
+	const Word bpw = (b[1] >> 16) & 3u;
+	if (bpw == 0)
+		return VColor{b[0], 0, 0, 1};
+	const Word bit = wstart + (b[1] & 0xFFFFu) + (vox - (b[1] >> 18)) * bpw, off = bit & 31u;
+	Word wt = wb[bit >> 5] >> off;
+	if (off + bpw <= 32)
+		wt &= (1u << bpw) - 1u;
+	else
+		wt |= (wb[(bit >> 5) + 1] & ((1u << (off + bpw - 32u)) - 1u)) << (32u - off);
+	return VColor{b[0], wt, bpw, 1};
+}
+
 } // namespace orc
 
 // ---------------------------------------------------------------- C ABI
@@ -1079,6 +1391,56 @@ void orc_trace_pinhole_lod(const orc_pool *p, uint32_t root, const hd_camera *ca
 }
 
 void orc_gc(orc_pool *p, uint32_t *roots, uint32_t n_roots) { p->pool.gc(roots, n_roots, &p->ok); }
+
+// ---- VBR colour (test infrastructure)
+struct orc_color_pool {
+	orc::ColorPool cp;
+};
+orc_color_pool *orc_color_pool_create(uint32_t leaf_level, int keep_history) {
+	auto *c = new orc_color_pool;
+	c->cp.leaf_level = leaf_level;
+	c->cp.keep_history = keep_history != 0;
+	return c;
+}
+void orc_color_pool_destroy(orc_color_pool *c) { delete c; }
+uint64_t orc_color_nodes(const orc_color_pool *c, uint32_t *out) {
+	if (out)
+		std::copy(c->cp.nodes.begin(), c->cp.nodes.end(), out);
+	return c->cp.nodes.size() / 8;
+}
+uint64_t orc_color_leaves(const orc_color_pool *c, uint32_t *out) {
+	if (out)
+		std::copy(c->cp.leaves.begin(), c->cp.leaves.end(), out);
+	return c->cp.leaves.size();
+}
+// One VBR edit (kind 1 fill, 2 paint; colour = colors/weight/bpw): the colour
+// octree from the old DAG root, then the geometry (fill only).
+void orc_vbr_edit(orc_pool *p, orc_color_pool *c, uint32_t root, uint32_t color_root, const hd_edit_desc *e,
+                  uint32_t kind, uint32_t colors, uint32_t weight, uint32_t bpw, uint32_t *out_root,
+                  uint32_t *out_color_root) {
+	hd_edit_desc g = *e;
+	g.op = HD_OP_FILL;
+	p->pool.make_filled(&p->ok);
+	const orc::VColor C{colors, weight, bpw, 1};
+	const orc::Word zero[3] = {0, 0, 0};
+	*out_color_root = orc::vbr_walk(c->cp, p->pool, g, C, 0, zero, color_root, root);
+	*out_root = kind == 2 ? root : p->pool.edit(root, g, &p->ok);
+}
+// Colour of voxels (x,y,z triples): has_value, colors, weight, bpw, rgb[3] (float bits).
+void orc_color_fetch(const orc_pool *p, const orc_color_pool *c, uint32_t color_root, const uint32_t *xyz, uint32_t n,
+                     uint32_t *out) {
+	for (uint32_t i = 0; i < n; ++i) {
+		const orc::VColor v = orc::color_fetch(c->cp, color_root, p->pool.cfg.voxel_level(), xyz + 3 * i);
+		float rgb[3];
+		orc::vcolor_rgb(v, rgb);
+		uint32_t *o = out + 7 * size_t(i);
+		o[0] = v.has;
+		o[1] = v.colors;
+		o[2] = v.weight;
+		o[3] = v.bpw;
+		std::memcpy(o + 4, rgb, 12);
+	}
+}
 
 uint32_t orc_hash_inner(const uint32_t *w, uint32_t n) { return orc::murmur_words(w, n); }
 uint32_t orc_hash_leaf(uint32_t w0, uint32_t w1) { return orc::murmur_leaf(w0, w1); }

@@ -21,6 +21,10 @@
 //   mode 3: n_rays, then origins[3n] and dirs[3n] (float)
 //   mode 4: n_keep, keep[n_keep] (keep the root after edit keep[i]; the roots
 //           are the GC roots, collected by ThreadedGC on a one-worker pool)
+//   mode 5 (colour edits through VBREditorWrapper): color_leaf_level,
+//           keep_history, per edit: kind (0 stateless, 1 VBR fill, 2 VBR
+//           paint), colors, weight, bits_per_weight; then n_queries and
+//           queries[3n] (voxel coordinates) for colour lookups
 // output file:
 //   magic 'HDRS', root, ok, elapsed_ns (uint64), filled[node_levels],
 //   total_buckets, bucket_words[total_buckets], n_pages, then per page: id, words[wpp]
@@ -28,11 +32,15 @@
 //   mode 3: n_rays, per ray: hit, pos[3] (float)
 //   mode 4: the dump is the pool after GC; then n_keep, roots before[n_keep],
 //           roots after[n_keep]
+//   mode 5: colour root, n_nodes, nodes[8 n_nodes], n_leaf_words,
+//           leaf_words[n], then per query: has_value, colors, weight,
+//           bits_per_weight, rgb[3] (float, VBRColor::Get())
 
 #include <hashdag/NodePool.hpp>
 #include <hashdag/NodePoolThreadedEdit.hpp>
 #include <hashdag/NodePoolThreadedGC.hpp>
 #include <hashdag/NodePoolTraversal.hpp>
+#include <hashdag/VBREditor.hpp>
 #include <parallel_hashmap/phmap.h>
 
 #include <chrono>
@@ -138,6 +146,165 @@ struct DescEditor {
 	}
 };
 
+// Colour octree with the behaviour of the application's DAGColorPool
+// (src/DAGColorPool.hpp:20-218) on plain vectors instead of Vulkan paged
+// buffers: tagged 32-bit pointers (2-bit tag: node, colour, leaf, null; 30-bit
+// data), nodes of 8 child pointers appended in JoinNode order, VBR leaf chunks
+// in one word vector ([block size][macro count][block count][weight words]
+// [macro blocks][block headers][weight words]), rewritten in place when
+// keep_history is off and the new chunk fits, else appended with doubled room.
+struct RefColorPool {
+	struct Pointer {
+		static constexpr uint32_t kDataBits = 30u;
+		enum class Tag { kNode = 0, kColor, kLeaf, kNull };
+		uint32_t pointer;
+		Pointer() : Pointer(Tag::kNull, 0u) {}
+		Pointer(Tag tag, uint32_t data) : pointer{(static_cast<uint32_t>(tag) << kDataBits) | data} {}
+		Tag GetTag() const { return static_cast<Tag>(pointer >> kDataBits); }
+		uint32_t GetData() const { return pointer & ((1u << kDataBits) - 1u); }
+		bool operator==(const Pointer &r) const { return pointer == r.pointer; }
+	};
+	using Node = std::array<Pointer, 8>;
+	using Chunk = hashdag::VBRChunk<uint32_t, hashdag::VBRWriterContainer>;
+	std::vector<Node> nodes;
+	std::vector<uint32_t> leaves;
+	uint32_t leaf_level = 0;
+	bool keep_history = false;
+
+	Pointer GetChild(Pointer ptr, auto idx) const {
+		return ptr.GetTag() == Pointer::Tag::kNode ? nodes[ptr.GetData()][idx]
+		                                           : (ptr.GetTag() == Pointer::Tag::kColor ? ptr : Pointer{});
+	}
+	static hashdag::VBRColor GetFill(Pointer ptr) {
+		return ptr.GetTag() == Pointer::Tag::kColor ? hashdag::VBRColor{hashdag::RGB8Color{ptr.GetData()}}
+		                                            : hashdag::VBRColor{};
+	}
+	Pointer SetNode(Pointer ptr, std::span<const Pointer, 8> ch) {
+		if (std::ranges::all_of(ch, [](Pointer p) { return p.GetTag() == Pointer::Tag::kNull; }))
+			return {};
+		if (Pointer c = ch[0];
+		    c.GetTag() == Pointer::Tag::kColor && std::ranges::all_of(ch.subspan(1), [c](Pointer p) { return p == c; }))
+			return c;
+		if (ptr.GetTag() == Pointer::Tag::kNode && std::ranges::equal(nodes[ptr.GetData()], ch))
+			return ptr;
+		Node n;
+		std::ranges::copy(ch, n.begin());
+		nodes.push_back(n);
+		return Pointer{Pointer::Tag::kNode, (uint32_t)(nodes.size() - 1)};
+	}
+	static Pointer ClearNode(Pointer) { return Pointer{}; }
+	static Pointer FillNode(Pointer, hashdag::VBRColor color) {
+		return Pointer{Pointer::Tag::kColor, hashdag::RGB8Color{color.Get()}.GetData()};
+	}
+	Chunk GetLeaf(Pointer ptr) const {
+		if (ptr.GetTag() != Pointer::Tag::kLeaf)
+			return {};
+		size_t idx = ptr.GetData() + 1;
+		const size_t nm = leaves[idx], nb = leaves[idx + 1], nw = leaves[idx + 2];
+		idx += 3;
+		std::vector<hashdag::VBRMacroBlock> m(nm);
+		std::vector<hashdag::VBRBlockHeader> b(nb);
+		std::vector<uint32_t> w(nw);
+		std::memcpy(m.data(), leaves.data() + idx, nm * 8);
+		idx += nm * 2;
+		std::memcpy(b.data(), leaves.data() + idx, nb * 8);
+		idx += nb * 2;
+		std::memcpy(w.data(), leaves.data() + idx, nw * 4);
+		return Chunk{std::move(m), std::move(b), hashdag::VBRBitset<uint32_t, hashdag::VBRWriterContainer>{std::move(w)}};
+	}
+	void write_chunk(size_t idx, const Chunk &c) {
+		leaves[idx++] = (uint32_t)c.GetMacroBlocks().size();
+		leaves[idx++] = (uint32_t)c.GetBlockHeaders().size();
+		leaves[idx++] = (uint32_t)c.GetWeightBits().GetWords().size();
+		std::memcpy(leaves.data() + idx, c.GetMacroBlocks().data(), c.GetMacroBlocks().size() * 8);
+		idx += c.GetMacroBlocks().size() * 2;
+		std::memcpy(leaves.data() + idx, c.GetBlockHeaders().data(), c.GetBlockHeaders().size() * 8);
+		idx += c.GetBlockHeaders().size() * 2;
+		std::memcpy(leaves.data() + idx, c.GetWeightBits().GetWords().data(), c.GetWeightBits().GetWords().size() * 4);
+	}
+	Pointer SetLeaf(Pointer ptr, Chunk &&chunk) {
+		const size_t data_size = chunk.GetMacroBlocks().size() * 2 + chunk.GetBlockHeaders().size() * 2 +
+		                         chunk.GetWeightBits().GetWords().size() + 4;
+		size_t append_size = (data_size & 1) ? data_size + 1 : data_size;
+		if (!keep_history && ptr.GetTag() == Pointer::Tag::kLeaf) {
+			const size_t idx = ptr.GetData(), block_size = leaves[idx];
+			if (data_size <= block_size) {
+				write_chunk(idx + 1, chunk);
+				return ptr;
+			}
+			append_size = std::max(block_size << 1, append_size);
+		}
+		const size_t idx = leaves.size();
+		leaves.resize(idx + append_size, 0u);
+		leaves[idx] = (uint32_t)append_size;
+		write_chunk(idx + 1, chunk);
+		return Pointer{Pointer::Tag::kLeaf, (uint32_t)idx};
+	}
+	uint32_t GetLeafLevel() const { return leaf_level; }
+
+	// colour of one voxel (coordinates at voxel resolution), walking the octree
+	// like trace.frag:341-355 and reading leaf chunks with the reference's
+	// VBRChunkIterator
+	hashdag::VBRColor Fetch(Pointer root, uint32_t voxel_level, glm::u32vec3 v) const {
+		Pointer p = root;
+		for (uint32_t l = 0; l < leaf_level; ++l) {
+			if (p.GetTag() != Pointer::Tag::kNode)
+				break;
+			const uint32_t s = voxel_level - 1u - l;
+			p = nodes[p.GetData()][((v.x >> s) & 1u) | (((v.y >> s) & 1u) << 1u) | (((v.z >> s) & 1u) << 2u)];
+		}
+		if (p.GetTag() == Pointer::Tag::kColor)
+			return GetFill(p);
+		if (p.GetTag() != Pointer::Tag::kLeaf)
+			return {};
+		const uint32_t bits = voxel_level - leaf_level, m = (1u << bits) - 1u;
+		uint32_t morton = 0;
+		for (uint32_t b = 0; b < bits; ++b)
+			morton |= (((v.x & m) >> b & 1u) << (3 * b)) | (((v.y & m) >> b & 1u) << (3 * b + 1)) |
+			          (((v.z & m) >> b & 1u) << (3 * b + 2));
+		hashdag::VBRChunkIterator<uint32_t, hashdag::VBRWriterContainer> it{GetLeaf(p)};
+		it.Jump(morton);
+		return it.GetColor();
+	}
+};
+static_assert(hashdag::VBROctree<RefColorPool, uint32_t>);
+
+// Colour editors of src/main.cpp:32-150 (AABBEditor, SphereEditor<kFill>,
+// SphereEditor<kPaint>): the geometry of DescEditor plus the colour rules.
+struct VbrDescEditor {
+	DescEditor geo; // op FILL
+	hashdag::VBRColor color;
+	bool paint;
+	hashdag::EditType EditNode(const hashdag::Config<uint32_t> &config, const hashdag::NodeCoord<uint32_t> &coord,
+	                           hashdag::NodePointer<uint32_t> ptr, hashdag::VBRColor &final_color) const {
+		auto edit_type = geo.EditNode(config, coord, {});
+		if (geo.e.shape == HD_SHAPE_AABB) { // main.cpp:48-58
+			if (edit_type == hashdag::EditType::kFill || !ptr || final_color == color)
+				final_color = color;
+			else
+				final_color = {};
+			return edit_type;
+		}
+		if (edit_type == hashdag::EditType::kFill) { // main.cpp:107-127
+			final_color = color;
+			if (paint)
+				edit_type = hashdag::EditType::kNotAffected;
+		} else if (!ptr || final_color == color) {
+			final_color = color;
+		} else
+			final_color = {};
+		if (paint && !ptr)
+			edit_type = hashdag::EditType::kNotAffected;
+		return edit_type;
+	}
+	bool EditVoxel(const hashdag::Config<uint32_t> &config, const hashdag::NodeCoord<uint32_t> &coord, bool voxel,
+	               hashdag::VBRColor &c) const {
+		const bool in_range = geo.EditVoxel(config, coord, false); // op FILL: false || in
+		c = in_range || !voxel ? color : c;
+		return paint ? voxel : (voxel || in_range);
+	}
+};
+
 static uint32_t rd(FILE *f) {
 	uint32_t v = 0;
 	if (fread(&v, 4, 1, f) != 1) {
@@ -167,8 +334,49 @@ template <typename HasherT> static int run(FILE *in, FILE *out, uint32_t mode, c
 			k = rd(in);
 		kept.resize(n_keep);
 	}
+	RefColorPool cpool;
+	RefColorPool::Pointer color_root{};
+	struct VbrOp {
+		uint32_t kind, colors, weight, bpw;
+	};
+	std::vector<VbrOp> vops;
+	std::vector<uint32_t> queries;
+	if (mode == 5) {
+		cpool.leaf_level = rd(in);
+		cpool.keep_history = rd(in) != 0;
+		vops.resize(n_edits);
+		for (auto &o : vops)
+			o = {rd(in), rd(in), rd(in), rd(in)};
+		queries.resize(3 * size_t(rd(in)));
+		for (auto &q : queries)
+			q = rd(in);
+	}
 	auto t0 = std::chrono::steady_clock::now();
-	if (mode == 4) {
+	if (mode == 5) {
+		for (uint32_t i = 0; i < n_edits; ++i) {
+			if (vops[i].kind == 0) {
+				root = pool->Edit(root, hashdag::StatelessEditorWrapper<uint32_t, DescEditor>{.editor = DescEditor{edits[i]}});
+				continue;
+			}
+			hashdag::VBRColor c = vops[i].bpw == 0
+			                          ? hashdag::VBRColor{hashdag::RGB8Color{vops[i].colors}}
+			                          : hashdag::VBRColor{hashdag::R5G6B5Color{(uint16_t)(vops[i].colors & 0xFFFFu)},
+			                                              hashdag::R5G6B5Color{(uint16_t)(vops[i].colors >> 16u)},
+			                                              (uint8_t)vops[i].weight, (uint8_t)vops[i].bpw};
+			hd_edit_desc g = edits[i];
+			g.op = HD_OP_FILL;
+			using Wrapper = hashdag::VBREditorWrapper<uint32_t, VbrDescEditor, RefColorPool>;
+			auto res = pool->Edit(root,
+			                      Wrapper{.editor = VbrDescEditor{DescEditor{g}, c, vops[i].kind == 2},
+			                              .p_octree = &cpool,
+			                              .octree_root = color_root},
+			                      [](hashdag::NodePointer<uint32_t> r, auto &&state) {
+				                      return std::make_pair(r, state.octree_node);
+			                      });
+			root = res.first;
+			color_root = res.second;
+		}
+	} else if (mode == 4) {
 		for (uint32_t i = 0; i < n_edits; ++i) {
 			root = pool->Edit(root, hashdag::StatelessEditorWrapper<uint32_t, DescEditor>{.editor = DescEditor{edits[i]}});
 			for (size_t k = 0; k < keep_at.size(); ++k)
@@ -231,6 +439,27 @@ template <typename HasherT> static int run(FILE *in, FILE *out, uint32_t mode, c
 			wr(out, v);
 		for (auto &r : kept)
 			wr(out, *r);
+	}
+	if (mode == 5) {
+		wr(out, color_root.pointer);
+		wr(out, (uint32_t)cpool.nodes.size());
+		for (auto &n : cpool.nodes)
+			for (auto &p : n)
+				wr(out, p.pointer);
+		wr(out, (uint32_t)cpool.leaves.size());
+		fwrite(cpool.leaves.data(), 4, cpool.leaves.size(), out);
+		for (size_t q = 0; q + 2 < queries.size(); q += 3) {
+			const hashdag::VBRColor c =
+			    cpool.Fetch(color_root, config.GetVoxelLevel(), glm::u32vec3{queries[q], queries[q + 1], queries[q + 2]});
+			wr(out, c.HasValue() ? 1u : 0u);
+			wr(out, c.GetColors());
+			wr(out, c.GetWeight());
+			wr(out, c.GetBitsPerWeight());
+			const glm::vec3 rgb = c.Get();
+			fwrite(&rgb.x, 4, 1, out);
+			fwrite(&rgb.y, 4, 1, out);
+			fwrite(&rgb.z, 4, 1, out);
+		}
 	}
 	if (mode == 2) {
 		wr(out, (uint32_t)upsert_ptrs.size());

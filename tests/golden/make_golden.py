@@ -193,6 +193,44 @@ def gc_golden(s):
     return rec
 
 
+# Colour edits through VBREditorWrapper into the colour octree
+# (include/hashdag/VBREditor.hpp, VBRColor.hpp; src/DAGColorPool.hpp restated
+# in oracle/ref_driver.cpp), single-threaded NodePoolBase::Edit.
+VBR_CASES = [
+    dict(name="vbr_256_leaf3", res=256, leaf_level=3, keep_history=False, args=dict(n=48, seed=31, r_max=64, side_max=128)),
+    dict(name="vbr_128_leaf5_history", res=128, leaf_level=5, keep_history=True,
+         args=dict(n=64, seed=35, r_max=32, side_max=64)),
+    dict(name="vbr_512_leaf2", res=512, leaf_level=2, keep_history=False, args=dict(n=12, seed=33, r_max=160, side_max=256)),
+    dict(name="vbr_128_leaf0", res=128, leaf_level=0, keep_history=False, args=dict(n=10, seed=34, r_max=40, side_max=64)),
+]
+
+
+def vbr_kinds(v):
+    """ref_driver colour op per edit: 0 stateless (dig), 1 fill, 2 paint."""
+    return [(int({W.OP_DIG: 0, W.OP_FILL: 1, W.OP_PAINT: 2}[int(e["edit"]["op"])]), int(e["colors"]), int(e["weight"]),
+             int(e["bits_per_weight"])) for e in v]
+
+
+def vbr_golden(s):
+    cfg = W.serving_config(s["res"])
+    v = W.vbr_edits(s["res"], **s["args"])
+    edits = np.ascontiguousarray(v["edit"])
+    q = W.point_queries(s["res"], 4096, seed=s["args"]["seed"] + 100)
+    r = oracle.run_reference(oracle.MODE_VBR, cfg.word_bits_per_page, cfg.page_bits_per_bucket,
+                             cfg.bucket_bits_each_level, edits, hasher=cfg.hasher,
+                             vbr=dict(leaf_level=s["leaf_level"], keep_history=s["keep_history"], ops=vbr_kinds(v),
+                                      queries=q))
+    c = r["colors"]
+    rec = dict(s)
+    rec.update(config=cfg_dict(cfg), edits_sha=sha(v), root=r["root"], color_root=r["color_root"],
+               n_nodes=int(len(r["color_nodes"])), nodes_sha=sha(r["color_nodes"]),
+               n_leaf_words=int(len(r["color_leaves"])), leaves_sha=sha(r["color_leaves"]), n_queries=int(len(q)),
+               colors_sha=sha(c["has_value"], c["colors"], c["weight"], c["bpw"], c["rgb"]),
+               colors_head=[[int(c["has_value"][i]), int(c["colors"][i]), int(c["weight"][i]), int(c["bpw"][i]),
+                             [int(x) for x in np.asarray(c["rgb"][i], np.float32).view(np.uint32)]] for i in range(8)])
+    return rec
+
+
 def rays_for(res, n, seed):
     o = W.uniform(seed, 41, 3 * n).reshape(n, 3).astype(np.float32)
     # half the rays start outside the cube
@@ -226,6 +264,7 @@ def main():
     g["traversal"] = [traversal_golden(by["scene256"]), traversal_golden(by["mixed256"], n=384, seed=12),
                       traversal_golden(by["full_then_dig"], n=256, seed=13)]
     g["gc"] = [gc_golden(s) for s in GC_CASES]
+    g["vbr"] = [vbr_golden(s) for s in VBR_CASES]
     with open(OUT, "w") as f:
         json.dump(g, f, indent=1)
     print("wrote", OUT, os.path.getsize(OUT), "bytes")

@@ -89,3 +89,43 @@ def check_pool_structure(orc, pool):
             assert po + n <= wpp, f"bucket {b}: node straddles a page"
             off += n
         assert off == bw[b], f"bucket {b}: word count {bw[b]} does not end on a node ({off})"
+
+
+def vbr_case(golden, name):
+    return next(g for g in golden["vbr"] if g["name"] == name)
+
+
+def vbr_case_inputs(g):
+    """Config, colour edits (VBR_EDIT_DTYPE) and query voxels of a golden colour case."""
+    from vkhashdag_gb300 import workloads as W
+    cfg = W.serving_config(g["res"])
+    v = W.vbr_edits(g["res"], **g["args"])
+    assert sha(v) == g["edits_sha"]
+    q = W.point_queries(g["res"], g["n_queries"], seed=g["args"]["seed"] + 100)
+    return cfg, v, q
+
+
+def colors_sha(c):
+    """Digest of colour records (oracle or engine field names)."""
+    bpw = c["bpw"] if "bpw" in c.dtype.names else c["bits_per_weight"]
+    return sha(np.ascontiguousarray(c["has_value"]), np.ascontiguousarray(c["colors"]),
+               np.ascontiguousarray(c["weight"]), np.ascontiguousarray(bpw),
+               np.ascontiguousarray(c["rgb"], dtype=np.float32))
+
+
+def oracle_vbr_run(orc, g):
+    """Apply a golden colour case with the oracle, edit after edit; returns
+    (pool, colour pool, root, colour root, queries)."""
+    from vkhashdag_gb300 import OP_DIG, OP_PAINT
+    cfg, v, q = vbr_case_inputs(g)
+    pool = orc.OraclePool.from_config(cfg)
+    cp = orc.OracleColorPool(g["leaf_level"], g["keep_history"])
+    root, croot = orc.NULL, orc.OracleColorPool.NULL
+    for e in v:
+        op = int(e["edit"]["op"])
+        if op == OP_DIG:
+            root = pool.edit(root, np.asarray([e["edit"]]))
+        else:
+            root, croot = pool.vbr_edit(root, cp, croot, e["edit"], 2 if op == OP_PAINT else 1, int(e["colors"]),
+                                        int(e["weight"]), int(e["bits_per_weight"]))
+    return pool, cp, root, croot, q

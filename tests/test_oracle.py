@@ -199,3 +199,54 @@ def test_lod_oracle_without_cut_equals_plain_traversal(orc):
     coarse = pool.trace_pinhole_lod(root, cams, w, h, hd.projection_factor(np.pi / 3, h, 8))
     hit = coarse["hit"] == 1
     assert (coarse["size"][hit] >= 1).all() and (coarse["size"][hit] > 1).any()
+
+
+VBR_NAMES = ["vbr_256_leaf3", "vbr_128_leaf5_history", "vbr_512_leaf2", "vbr_128_leaf0"]
+
+
+@pytest.mark.parametrize("name", VBR_NAMES)
+def test_vbr_colour_edit_matches_reference(golden, orc, name):
+    """Colour edits through VBREditorWrapper restated: the same DAG root, colour
+    root, colour octree nodes and leaf words (VBR chunks) as the reference's
+    single-threaded Edit, and the same colour (VBRColor fields and RGB bits)
+    for every query voxel."""
+    from helpers import colors_sha, oracle_vbr_run, vbr_case
+    g = vbr_case(golden, name)
+    pool, cp, root, croot, q = oracle_vbr_run(orc, g)
+    assert root == g["root"] and croot == g["color_root"]
+    nodes, leaves = cp.nodes(), cp.leaves()
+    assert len(nodes) == g["n_nodes"] and sha(nodes) == g["nodes_sha"]
+    assert len(leaves) == g["n_leaf_words"] and sha(leaves) == g["leaves_sha"]
+    c = pool.color_fetch(cp, croot, q)
+    assert colors_sha(c) == g["colors_sha"]
+
+
+def test_vbr_live_reference_when_present(orc):
+    """Where the reference tree is built here, a fresh seeded colour case
+    (weighted colours, paints, digs, two colour leaf levels) against the
+    reference's own VBR writer."""
+    if not orc.reference_available():
+        pytest.skip("reference driver not built here")
+    from vkhashdag_gb300 import workloads as W, OP_DIG, OP_FILL, OP_PAINT
+    for res, leaf_level, seed in [(256, 4, 71), (128, 3, 72)]:
+        cfg = W.serving_config(res)
+        v = W.vbr_edits(res, 24, seed=seed, r_max=res // 4, side_max=res // 2, weighted_frac=0.5)
+        q = W.point_queries(res, 2000, seed=seed)
+        kinds = [({OP_DIG: 0, OP_FILL: 1, OP_PAINT: 2}[int(e["edit"]["op"])], int(e["colors"]), int(e["weight"]),
+                  int(e["bits_per_weight"])) for e in v]
+        r = orc.run_reference(orc.MODE_VBR, cfg.word_bits_per_page, cfg.page_bits_per_bucket,
+                              cfg.bucket_bits_each_level, np.ascontiguousarray(v["edit"]),
+                              vbr=dict(leaf_level=leaf_level, keep_history=False, ops=kinds, queries=q))
+        pool = orc.OraclePool.from_config(cfg)
+        cp = orc.OracleColorPool(leaf_level)
+        root, croot = orc.NULL, orc.OracleColorPool.NULL
+        for e, (k, col, w, b) in zip(v, kinds):
+            if k == 0:
+                root = pool.edit(root, np.asarray([e["edit"]]))
+            else:
+                root, croot = pool.vbr_edit(root, cp, croot, e["edit"], k, col, w, b)
+        assert root == r["root"] and croot == r["color_root"]
+        assert np.array_equal(cp.nodes(), r["color_nodes"]) and np.array_equal(cp.leaves(), r["color_leaves"])
+        c = pool.color_fetch(cp, croot, q)
+        assert np.array_equal(c["colors"], r["colors"]["colors"])
+        assert np.array_equal(c["rgb"].view(np.uint32), r["colors"]["rgb"].view(np.uint32))

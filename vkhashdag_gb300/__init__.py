@@ -43,7 +43,17 @@ CAMERA_DTYPE = np.dtype([("position", "<f4", (3,)), ("look", "<f4", (3,)), ("sid
                          ("up", "<f4", (3,))])
 
 SHAPE_SPHERE, SHAPE_AABB = 0, 1
-OP_FILL, OP_DIG = 0, 1
+OP_FILL, OP_DIG, OP_PAINT = 0, 1, 2
+# hd_vbr_edit: a colour edit (op FILL = coloured fill, PAINT = paint without
+# geometry change, DIG = stateless dig that leaves the colours) and its colour
+# (VBRColor: RGB8 in colors when bits_per_weight is 0, else two R5G6B5 end
+# points, low half first, and a weight below 2^bits_per_weight)
+VBR_EDIT_DTYPE = np.dtype([("edit", EDIT_DTYPE), ("colors", "<u4"), ("weight", "<u4"), ("bits_per_weight", "<u4"),
+                           ("pad", "<u4")], align=True)
+# hd_vbr_color: one voxel's colour (has_value, the VBRColor fields) and its RGB
+# as trace.frag computes it
+COLOR_DTYPE = np.dtype([("has_value", "<u4"), ("colors", "<u4"), ("weight", "<u4"), ("bits_per_weight", "<u4"),
+                        ("rgb", "<f4", (3,))])
 
 STATUS = {0: "ok", 1: "invalid argument", 2: "bucket full", 3: "device page heap exhausted", 4: "dedup index full",
           5: "edit workspace capacity exceeded", 6: "CUDA error", 7: "device wait timed out", 8: "no CUDA device",

@@ -16,7 +16,7 @@ from __future__ import annotations
 
 import numpy as np
 
-from . import EDIT_DTYPE, OP_DIG, OP_FILL, SHAPE_AABB, SHAPE_SPHERE
+from . import EDIT_DTYPE, OP_DIG, OP_FILL, OP_PAINT, SHAPE_AABB, SHAPE_SPHERE, VBR_EDIT_DTYPE
 
 _M = np.uint64(0xFFFFFFFFFFFFFFFF)
 _GOLD = np.uint64(0x9E3779B97F4A7C15)
@@ -165,6 +165,27 @@ def mixed_batch(resolution: int = 32768, n: int = 65536, seed: int = 1, r_max: i
     e["p1"] = np.where(is_sphere[:, None], 0, p1)
     e["r2"] = np.where(is_sphere, r * r, 0)
     return e
+
+
+def vbr_edits(resolution: int, n: int, seed: int = 1, r_max: int = 64, side_max: int = 128, paint_frac: float = 0.3,
+              weighted_frac: float = 0.3) -> np.ndarray:
+    """n colour edits in seed order (the application's colour editing: coloured
+    sphere and box fills, sphere paints, stateless digs): the geometry of
+    mixed_batch; a filling sphere becomes a paint with probability paint_frac;
+    colours are RGB8, or with probability weighted_frac two R5G6B5 end points
+    with 1-3 bits per weight and a weight below 2^bits."""
+    g = mixed_batch(resolution, n, seed, r_max, side_max)
+    v = np.zeros(n, VBR_EDIT_DTYPE)
+    paint = (uniform(seed, 61, n) < paint_frac) & (g["shape"] == SHAPE_SPHERE) & (g["op"] == OP_FILL)
+    g["op"] = np.where(paint, OP_PAINT, g["op"])
+    v["edit"] = g
+    weighted = uniform(seed, 62, n) < weighted_frac
+    bpw = randint(seed, 63, n, 1, 3).astype(np.uint64)
+    cols = u64(seed, 64, n)
+    v["bits_per_weight"] = np.where(weighted, bpw, 0)
+    v["colors"] = np.where(weighted, cols & np.uint64(0xFFFFFFFF), cols & np.uint64(0xFFFFFF))
+    v["weight"] = np.where(weighted, (cols >> np.uint64(32)) % (np.uint64(1) << bpw), 0)
+    return v
 
 
 def point_queries(resolution: int, n: int, seed: int = 7) -> np.ndarray:
