@@ -74,7 +74,8 @@ typedef struct hd_config {
  * the AABB dig follows the same pattern).  A list of edits is applied in
  * order: per voxel the last edit whose shape covers it decides. */
 typedef enum hd_shape { HD_SHAPE_SPHERE = 0, HD_SHAPE_AABB = 1 } hd_shape;
-typedef enum hd_op { HD_OP_FILL = 0, HD_OP_DIG = 1 } hd_op;
+/* HD_OP_PAINT: colour edits only (hd_vbr_edit): recolour without changing the geometry */
+typedef enum hd_op { HD_OP_FILL = 0, HD_OP_DIG = 1, HD_OP_PAINT = 2 } hd_op;
 
 typedef struct hd_edit_desc {
 	uint32_t shape;  /* hd_shape */
@@ -413,6 +414,58 @@ float hd_projection_factor(float fov_y, uint32_t height, uint32_t divisor);
  * Number of grid voxels inside each edit's shape clipped to [0,resolution)^3,
  * summed over the edits (the voxel-edits unit of the benchmark). */
 uint64_t hd_count_voxel_edits(const hd_edit_desc *edits, uint32_t n, uint32_t resolution);
+
+/* ---- colour (VBR) ----------------------------------------------------------
+ * replaces the application's colour octree DAGColorPool
+ * (src/DAGColorPool.hpp:20-218) and colour editing through
+ * hashdag::VBREditorWrapper (include/hashdag/VBREditor.hpp:26-107, the chunk
+ * writer of include/hashdag/VBRColor.hpp:367-488) driven as the application
+ * does (src/main.cpp:224-242), plus the colour lookup of trace.frag:272-356.
+ * Octree pointers: 2-bit tag (0 node, 1 colour, 2 leaf, 3 null) over 30 bits
+ * of data; the words read back by hd_color_pool_read are the ones the
+ * reference's single-threaded NodePoolBase::Edit writes for the same edits. */
+#define HD_COLOR_NULL 0xC0000000u
+typedef struct hd_color_config {
+	uint32_t leaf_level;      /* octree leaf level (src/main.cpp:204-211 uses 10); <= node_levels-1,
+	                             and node_levels+1-leaf_level <= 8 (at most 2^24 voxels per leaf) */
+	uint32_t keep_history;    /* 0: a rewritten leaf reuses its block when it fits (DAGColorPool) */
+	uint64_t max_nodes;       /* octree node capacity (8 words each), <= 2^30 */
+	uint64_t max_leaf_words;  /* leaf word capacity, <= 2^30 */
+} hd_color_config;
+typedef struct hd_vbr_edit_desc {
+	hd_edit_desc edit;        /* op: HD_OP_FILL coloured fill, HD_OP_PAINT recolour (geometry kept),
+	                             HD_OP_DIG stateless dig (colours kept, like the application's digs) */
+	uint32_t colors;          /* VBRColor: RGB8 (r | g << 8 | b << 16) when bits_per_weight is 0, else
+	                             two R5G6B5 end points (low 16 bits first) */
+	uint32_t weight;          /* < 2^bits_per_weight (0 when bits_per_weight is 0) */
+	uint32_t bits_per_weight; /* 0..3 */
+	uint32_t pad;
+} hd_vbr_edit_desc;           /* 56 bytes */
+typedef struct hd_vbr_color {
+	uint32_t has_value, colors, weight, bits_per_weight; /* VBRColor fields */
+	float rgb[3];                                        /* trace.frag's colour (VBRColor::Get) */
+} hd_vbr_color;               /* 28 bytes */
+typedef struct hd_color_pool hd_color_pool;
+/* A colour octree for the voxels of `pool` (device memory of pool's GPU). */
+hd_status hd_color_pool_create(hd_pool *pool, const hd_color_config *cfg, hd_color_pool **out);
+void hd_color_pool_destroy(hd_color_pool *cpool);
+/* Host mirror: node count and leaf word count; with non-null buffers also the
+ * nodes (8 words each) and the leaf words. */
+hd_status hd_color_pool_read(hd_color_pool *cpool, uint32_t *nodes, uint64_t *n_nodes, uint32_t *leaves,
+                             uint64_t *n_leaf_words);
+/* Colour edits applied one after another (each the reference's Edit with a
+ * VBREditorWrapper, or a stateless dig): the colour octree from the DAG as it
+ * was before the edit, then the geometry through hd_edit.  Returns the new
+ * DAG root and colour root.  HD_ERR_POOL_OOM when the octree is full (that
+ * edit's colours are not applied). */
+hd_status hd_vbr_edit(hd_pool *pool, hd_color_pool *cpool, uint32_t root, uint32_t color_root, const hd_vbr_edit_desc *edits,
+                      uint32_t n, uint32_t *out_root, uint32_t *out_color_root);
+/* Colours of n voxels (device buffers: xyz triples at voxel resolution) under
+ * color_root (Color_Fetch, trace.frag:339-356).  Not ordered against a
+ * concurrent hd_vbr_edit of the same colour pool. */
+hd_status hd_color_fetch(hd_color_pool *cpool, uint32_t color_root, const uint32_t *d_xyz, uint32_t n,
+                         hd_vbr_color *d_out, void *stream);
+
 
 const char *hd_status_string(hd_status s);
 /* 1 if a CUDA device is usable, else 0. */

@@ -100,8 +100,10 @@ def test_struct_layouts_match_the_header(hd, tmp_path):
     structs = {
         "hd_config": hd._Config, "hd_pool_stats": hd._Stats, "hd_server_config": hd._ServerConfig,
         "hd_request_result": hd._RequestResult, "hd_server_stats": hd._ServerStats,
+        "hd_color_config": hd._ColorConfig,
     }
-    dtypes = {"hd_edit_desc": hd.EDIT_DTYPE, "hd_hit": hd.HIT_DTYPE, "hd_camera": hd.CAMERA_DTYPE}
+    dtypes = {"hd_edit_desc": hd.EDIT_DTYPE, "hd_hit": hd.HIT_DTYPE, "hd_camera": hd.CAMERA_DTYPE,
+              "hd_vbr_edit_desc": hd.VBR_EDIT_DTYPE, "hd_vbr_color": hd.COLOR_DTYPE}
     lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "hashdag_gpu.h"', "int main(void) {"]
     for name, cls in structs.items():
         lines.append(f'printf("{name} %zu\\n", sizeof({name}));')
@@ -147,3 +149,27 @@ def test_tuning_entry_points_reject_bad_arguments(hd):
     assert lib.hd_edit_set_tuning(None, ctypes.byref(t)) == 1
     assert lib.hd_edit_get_tuning(None, ctypes.byref(t)) == 1
     assert lib.hd_edit_autotune(None, 0, None, 0, None, None, None) == 1
+
+
+def test_colour_entry_points_reject_bad_arguments(hd):
+    lib = hd.lib()
+    out = ctypes.c_void_p()
+    cfg = hd._ColorConfig(3, 0, 1 << 10, 1 << 10)
+    assert lib.hd_color_pool_create(None, ctypes.byref(cfg), ctypes.byref(out)) == 1 and not out.value
+    r, c = ctypes.c_uint32(), ctypes.c_uint32()
+    assert lib.hd_vbr_edit(None, None, 0, 0, None, 0, ctypes.byref(r), ctypes.byref(c)) == 1
+    n1, n2 = ctypes.c_uint64(), ctypes.c_uint64()
+    assert lib.hd_color_pool_read(None, None, ctypes.byref(n1), None, ctypes.byref(n2)) == 1
+    assert lib.hd_color_fetch(None, 0, None, 1, None, None) == 1
+    lib.hd_color_pool_destroy(None)
+
+
+def test_colour_editors_to_descriptors(hd):
+    e = hd.vbr_edits_to_array([
+        hd.SphereEditor((5, 6, 7), 16, hd.EditMode.kPaint, hd.VBRColor.rgb8(1, 2, 3)),
+        hd.AABBEditor((0, 0, 0), (4, 4, 4), hd.EditMode.kFill, hd.VBRColor.weighted(0x1234, 0xABCD, 2, 2)),
+        hd.SphereEditor((1, 1, 1), 4, hd.EditMode.kDig)])
+    assert e["edit"]["op"].tolist() == [hd.OP_PAINT, hd.OP_FILL, hd.OP_DIG]
+    assert e["colors"].tolist() == [0x030201, 0xABCD1234, 0] and e["bits_per_weight"].tolist() == [0, 2, 0]
+    with pytest.raises(ValueError):
+        hd.vbr_edits_to_array([hd.SphereEditor((1, 1, 1), 4, hd.EditMode.kFill)])

@@ -44,7 +44,7 @@ CAMERA_DTYPE = np.dtype([("position", "<f4", (3,)), ("look", "<f4", (3,)), ("sid
 
 SHAPE_SPHERE, SHAPE_AABB = 0, 1
 OP_FILL, OP_DIG, OP_PAINT = 0, 1, 2
-# hd_vbr_edit: a colour edit (op FILL = coloured fill, PAINT = paint without
+# hd_vbr_edit_desc: a colour edit (op FILL = coloured fill, PAINT = paint without
 # geometry change, DIG = stateless dig that leaves the colours) and its colour
 # (VBRColor: RGB8 in colors when bits_per_weight is 0, else two R5G6B5 end
 # points, low half first, and a weight below 2^bits_per_weight)
@@ -114,6 +114,11 @@ class _ServerStats(ctypes.Structure):
                 ("gc_runs", ctypes.c_uint64), ("gc_ms", ctypes.c_double)]
 
 
+class _ColorConfig(ctypes.Structure):
+    _fields_ = [("leaf_level", ctypes.c_uint32), ("keep_history", ctypes.c_uint32), ("max_nodes", ctypes.c_uint64),
+                ("max_leaf_words", ctypes.c_uint64)]
+
+
 _lib = None
 
 
@@ -171,6 +176,11 @@ def lib():
         "hd_server_scene_root": (I, [P, U32, ctypes.POINTER(U32)]),
         "hd_server_get_stats": (I, [P, ctypes.POINTER(_ServerStats)]),
         "hd_count_voxel_edits": (U64, [P, U32, U32]),
+        "hd_color_pool_create": (I, [P, ctypes.POINTER(_ColorConfig), ctypes.POINTER(P)]),
+        "hd_color_pool_destroy": (None, [P]),
+        "hd_color_pool_read": (I, [P, P, ctypes.POINTER(U64), P, ctypes.POINTER(U64)]),
+        "hd_vbr_edit": (I, [P, P, U32, U32, P, U32, ctypes.POINTER(U32), ctypes.POINTER(U32)]),
+        "hd_color_fetch": (I, [P, U32, P, U32, P, P]),
         "hd_status_string": (ctypes.c_char_p, [I]),
         "hd_device_available": (I, []),
     }
@@ -278,17 +288,38 @@ class DefaultConfig:
 
 
 class EditMode(enum.IntEnum):
-    """EditMode of src/main.cpp:72 (kPaint only recolours and is out of scope here)."""
+    """EditMode of src/main.cpp:72 (kPaint recolours only: colour edits)."""
     kFill = OP_FILL
     kDig = OP_DIG
+    kPaint = OP_PAINT
+
+
+@dataclass
+class VBRColor:
+    """hashdag::VBRColor (include/hashdag/VBRColor.hpp:18-43): an RGB8 colour
+    (bits_per_weight 0, colors = r | g << 8 | b << 16) or two R5G6B5 end
+    points (low 16 bits first) mixed by weight / (2^bits_per_weight - 1)."""
+    colors: int = 0
+    weight: int = 0
+    bits_per_weight: int = 0
+
+    @staticmethod
+    def rgb8(r: int, g: int, b: int) -> "VBRColor":
+        return VBRColor(int(r) | int(g) << 8 | int(b) << 16)
+
+    @staticmethod
+    def weighted(left_r5g6b5: int, right_r5g6b5: int, weight: int, bits_per_weight: int) -> "VBRColor":
+        return VBRColor(int(left_r5g6b5) | int(right_r5g6b5) << 16, int(weight), int(bits_per_weight))
 
 
 @dataclass
 class SphereEditor:
-    """SphereEditor<Mode> (src/main.cpp:73-150): voxel p inside iff |p-center|^2 <= r2."""
+    """SphereEditor<Mode> (src/main.cpp:73-150): voxel p inside iff |p-center|^2 <= r2.
+    With a colour it is the colour editor (kFill, kPaint) for hd_vbr_edit."""
     center: Sequence[int]
     r2: int
     mode: EditMode = EditMode.kFill
+    color: Optional[VBRColor] = None
 
     def desc(self):
         return (SHAPE_SPHERE, int(self.mode), tuple(int(c) for c in self.center), (0, 0, 0), int(self.r2))
@@ -296,10 +327,12 @@ class SphereEditor:
 
 @dataclass
 class AABBEditor:
-    """AABBEditor (src/main.cpp:32-63): voxel p inside iff aabb_min <= p < aabb_max; kDig by symmetry."""
+    """AABBEditor (src/main.cpp:32-63): voxel p inside iff aabb_min <= p < aabb_max; kDig by symmetry.
+    With a colour it is the colour editor (kFill; kPaint by symmetry) for hd_vbr_edit."""
     aabb_min: Sequence[int]
     aabb_max: Sequence[int]
     mode: EditMode = EditMode.kFill
+    color: Optional[VBRColor] = None
 
     def desc(self):
         return (SHAPE_AABB, int(self.mode), tuple(int(c) for c in self.aabb_min), tuple(int(c) for c in self.aabb_max), 0)
@@ -308,6 +341,22 @@ class AABBEditor:
 def edits_to_array(editors: Iterable) -> np.ndarray:
     items = [e.desc() for e in editors]
     return np.array(items, dtype=EDIT_DTYPE)
+
+
+def vbr_edits_to_array(editors: Iterable) -> np.ndarray:
+    """Colour edits (VBR_EDIT_DTYPE) from editors; an editor without a colour
+    must dig (the application's stateless digs)."""
+    editors = list(editors)
+    out = np.zeros(len(editors), VBR_EDIT_DTYPE)
+    for i, e in enumerate(editors):
+        out[i]["edit"] = np.array(e.desc(), dtype=EDIT_DTYPE)
+        c = e.color
+        if c is None:
+            if e.mode != EditMode.kDig:
+                raise ValueError("a colour edit that fills or paints needs a colour")
+            continue
+        out[i]["colors"], out[i]["weight"], out[i]["bits_per_weight"] = c.colors, c.weight, c.bits_per_weight
+    return out
 
 
 def projection_factor(fov_y: float, height: int, divisor: int = 1) -> float:
@@ -336,6 +385,7 @@ class NodePool:
         _check(L.hd_pool_create(ctypes.byref(self._cfg), heap_pages, index_log2, device, ctypes.byref(h)),
                "hd_pool_create")
         self._h = h
+        self.device = device
         self.root = NULL
 
     # -- lifecycle -------------------------------------------------------
@@ -423,6 +473,20 @@ class NodePool:
         _check(lib().hd_edit_last_probe_stats(self._h, _ptr(v[0:1]), _ptr(v[1:2]), _ptr(v[2:3])),
                "hd_edit_last_probe_stats")
         return {"probe_steps": int(v[0]), "max_probe": int(v[1]), "cas_retries": int(v[2])}
+
+    def vbr_edit(self, root: int, color_pool: "DAGColorPool", color_root: int, edits) -> tuple:
+        """Colour edits one after another (NodePoolBase::Edit with a
+        VBREditorWrapper into the colour octree, src/main.cpp:224-242; digs are
+        stateless): VBR_EDIT_DTYPE array or colour editors.  Returns (root,
+        colour root)."""
+        if not isinstance(edits, np.ndarray):
+            edits = vbr_edits_to_array(edits)
+        edits = np.ascontiguousarray(edits, dtype=VBR_EDIT_DTYPE)
+        r, c = ctypes.c_uint32(0), ctypes.c_uint32(0)
+        _check(lib().hd_vbr_edit(self._h, color_pool._h, root & 0xFFFFFFFF, color_root & 0xFFFFFFFF,
+                                 _ptr(edits) if len(edits) else None, len(edits), ctypes.byref(r), ctypes.byref(c)),
+               "hd_vbr_edit")
+        return int(r.value), int(c.value)
 
     def gc(self, roots) -> tuple:
         """NodePoolThreadedGC::ThreadedGC: keeps what `roots` (and the filled nodes)
@@ -561,6 +625,55 @@ class NodePool:
 
 
 REQ_EDIT, REQ_CAMERA = 0, 1
+
+
+class DAGColorPool:
+    """The colour octree of a node pool (the application's DAGColorPool,
+    src/DAGColorPool.hpp:20-218, on the device): tagged 32-bit pointers,
+    8-pointer nodes and VBR leaf chunks at ``leaf_level``.  Edited through
+    ``NodePool.vbr_edit``; ``read`` gives back the reference's words."""
+
+    NULL = 0xC0000000
+
+    def __init__(self, pool: "NodePool", leaf_level: int, keep_history: bool = False, max_nodes: int = 1 << 20,
+                 max_leaf_words: int = 1 << 24):
+        self.pool = pool
+        self.leaf_level = leaf_level
+        cfg = _ColorConfig(leaf_level, int(keep_history), max_nodes, max_leaf_words)
+        h = ctypes.c_void_p()
+        _check(lib().hd_color_pool_create(pool._h, ctypes.byref(cfg), ctypes.byref(h)), "hd_color_pool_create")
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().hd_color_pool_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        self.close()
+
+    def read(self):
+        """(nodes (n, 8) uint32, leaf words uint32): the host mirror."""
+        nn, nl = ctypes.c_uint64(0), ctypes.c_uint64(0)
+        _check(lib().hd_color_pool_read(self._h, None, ctypes.byref(nn), None, ctypes.byref(nl)), "hd_color_pool_read")
+        nodes = np.zeros((nn.value, 8), np.uint32)
+        leaves = np.zeros(nl.value, np.uint32)
+        _check(lib().hd_color_pool_read(self._h, _ptr(nodes), ctypes.byref(nn), _ptr(leaves), ctypes.byref(nl)),
+               "hd_color_pool_read")
+        return nodes[:nn.value], leaves[:nl.value]
+
+    def fetch(self, color_root: int, xyz) -> np.ndarray:
+        """Colours of voxels (n, 3) under color_root (trace.frag Color_Fetch): COLOR_DTYPE."""
+        import torch
+        pts = np.ascontiguousarray(xyz, dtype=np.uint32).reshape(-1, 3)
+        dev = torch.device("cuda", self.pool.device)
+        d_in = torch.from_numpy(pts.view(np.int32).copy()).to(dev)
+        d_out = torch.zeros(len(pts) * COLOR_DTYPE.itemsize // 4, dtype=torch.int32, device=dev)
+        stream = torch.cuda.current_stream(dev).cuda_stream
+        _check(lib().hd_color_fetch(self._h, color_root & 0xFFFFFFFF, ctypes.c_void_p(d_in.data_ptr()), len(pts),
+                                    ctypes.c_void_p(d_out.data_ptr()), ctypes.c_void_p(stream)), "hd_color_fetch")
+        torch.cuda.synchronize(dev)
+        return d_out.cpu().numpy().view(COLOR_DTYPE).copy()
 
 
 class Server:

@@ -14,7 +14,8 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libhashdag_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # The read path restates fp32 traversal arithmetic bit for bit: no FMA contraction there.
-PER_FILE = {"hd_trace.cu": ["-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"]}
+PER_FILE = {"hd_trace.cu": ["-fmad=false", "-prec-div=true", "-prec-sqrt=true", "-ftz=false"],
+            "hd_color.cu": ["-fmad=false", "-prec-div=true", "-ftz=false"]}
 
 
 def nvcc():
