@@ -965,6 +965,96 @@ def run_gc(args):
     print(json.dumps(line), flush=True)
 
 
+def run_vbr(args):
+    """Colour (VBR) editing as the application does it: its node pool and
+    colour octree configuration, its start-up colour edits, then interactive
+    coloured sphere fills and paints on the scene's surface, one hd_vbr_edit
+    call per edit (the application edits one at a time)."""
+    import torch
+    world, rank, local = dist_setup()
+    torch.cuda.set_device(local)
+    build_if_needed()
+    import vkhashdag_gb300 as hd
+    from vkhashdag_gb300 import workloads as W
+    cfg = W.vbr_app_config()
+    res = 1 << (cfg.get_node_levels() + 1)
+    leaf_level = W.VBR_APP_LEAF_LEVEL
+    pool = hd.NodePool(cfg, heap_pages=cfg.get_total_pages(), device=local)
+    cp = hd.DAGColorPool(pool, leaf_level, max_nodes=1 << 22, max_leaf_words=1 << 28)
+    scene = W.vbr_app_scene()
+    root, croot = hd.NULL, hd.DAGColorPool.NULL
+    scene_ms = []
+    for i in range(len(scene)):
+        t0 = time.perf_counter()
+        root, croot = pool.vbr_edit(root, cp, croot, scene[i:i + 1])
+        scene_ms.append(1e3 * (time.perf_counter() - t0))
+    n = args.vbr_edits
+    edits = W.vbr_surface_edits(args.warmup + n, seed=5)
+    for i in range(args.warmup):
+        root, croot = pool.vbr_edit(root, cp, croot, edits[i:i + 1])
+    timed = edits[args.warmup:]
+    # CPU: the oracle's colour edit (the reference's algorithm restated, one
+    # thread) from the same state, on the first edits until the time budget
+    cpu, k_cpu, ocp, opool, oroot, ocroot = None, 0, None, None, None, None
+    if rank == 0 and not args.no_cpu:
+        import oracle
+        oracle.build()
+        bw, ids, pages = pool.download()
+        nodes, leaves = cp.read()
+        opool = oracle.OraclePool.from_config(cfg)
+        opool.load(bw, ids, pages, pool.filled_node_pointers())
+        ocp = oracle.OracleColorPool(leaf_level)
+        ocp.load(nodes, leaves)
+        oroot, ocroot, t_cpu = root, croot, 0.0
+        while k_cpu < n and t_cpu < args.cpu_seconds:
+            e = timed[k_cpu]
+            op = int(e["edit"]["op"])
+            tc = time.perf_counter()
+            oroot, ocroot = opool.vbr_edit(oroot, ocp, ocroot, e["edit"], 2 if op == hd.OP_PAINT else 1,
+                                           int(e["colors"]), int(e["weight"]), int(e["bits_per_weight"]))
+            t_cpu += time.perf_counter() - tc
+            k_cpu += 1
+        cpu = {"value": k_cpu / t_cpu, "unit": "colour edits/s", "cores": 1, "kind": "port",
+               "sample": f"the first {k_cpu} timed edits from the same scene state ({t_cpu:.1f} s, oracle "
+                         f"restatement: every voxel of an edited colour leaf, one thread)"}
+    lat, same_after_k = [], None
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        for i in range(n):
+            t0 = time.perf_counter()
+            root, croot = pool.vbr_edit(root, cp, croot, timed[i:i + 1])
+            lat.append(1e3 * (time.perf_counter() - t0))
+            if ocp is not None and i + 1 == k_cpu: # compare with the oracle (outside the timed calls)
+                dn, dl = cp.read()
+                same_after_k = bool(croot == ocroot and np.array_equal(dn, ocp.nodes()) and
+                                    np.array_equal(dl, ocp.leaves()))
+    lat = np.array(lat)
+    total_s = lat.sum() / 1e3
+    ve = hd.count_voxel_edits(np.ascontiguousarray(timed["edit"]), res)
+    nodes, leaves = cp.read()
+    if rank != 0:
+        return
+    line = {
+        "metric": "colour (VBR) edits/s through hd_vbr_edit, one edit per call; p50/p99 edit latency",
+        "value": n / total_s, "unit": "colour edits/s", "n_gpus": 1, "steps": n, "warmup": args.warmup,
+        "ms_per_step": float(lat.mean()), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u32", "data": "synthetic",
+        "config": {"workload": f"application colour editing: {res}^3 world (its node pool config), colour leaves of "
+                               f"{1 << (cfg.get_node_levels() + 1 - leaf_level)}^3 voxels (level {leaf_level}), "
+                               f"its start-up scene (2 box fills, sphere paint, sphere dig), then {n} coloured sphere "
+                               f"fills/paints r in [16,128] on the surface, RGB8",
+                   "node_levels": cfg.get_node_levels(), "colour_leaf_level": leaf_level},
+        "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                       "max": float(lat.max()), "mean": float(lat.mean())},
+        "voxel_edits_per_s": ve / total_s,
+        "scene_ms": scene_ms,
+        "colour_pool": {"nodes": int(len(nodes)), "leaf_words": int(len(leaves))},
+        "cpu_baseline": cpu, "clocks": clocks.summary(),
+        "checks": {"colour_words_equal_oracle_after_cpu_sample": same_after_k},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -979,7 +1069,8 @@ def main():
     ap.add_argument("--ref-step-seconds", type=float, default=6.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
-    ap.add_argument("--mode", default="batched", choices=["batched", "terrain", "rays", "serving", "gc"])
+    ap.add_argument("--mode", default="batched", choices=["batched", "terrain", "rays", "serving", "gc", "vbr"])
+    ap.add_argument("--vbr-edits", type=int, default=256)
     ap.add_argument("--gc-batches", type=int, default=2)
     ap.add_argument("--gc-cpu-resolution", type=int, default=4096)
     ap.add_argument("--rate", type=float, default=1000.0)
@@ -1008,6 +1099,8 @@ def main():
         run_serving(args)
     elif args.mode == "gc":
         run_gc(args)
+    elif args.mode == "vbr":
+        run_vbr(args)
     elif args.mode == "rays":
         if args.resolution == RES:
             args.resolution = TERRAIN_RES

@@ -98,6 +98,7 @@ def lib():
             "orc_color_pool_destroy": (None, [P]),
             "orc_color_nodes": (U64, [P, P]),
             "orc_color_leaves": (U64, [P, P]),
+            "orc_color_pool_load": (None, [P, P, U64, P, U64]),
             "orc_vbr_edit": (None, [P, P, U32, U32, P, U32, U32, U32, U32, P, P]),
             "orc_color_fetch": (None, [P, P, U32, P, U32, P]),
             "orc_hash_inner": (U32, [P, U32]),
@@ -133,6 +134,12 @@ class OracleColorPool:
         out = np.zeros((n, 8), np.uint32)
         lib().orc_color_nodes(self._h, _p(out))
         return out
+
+    def load(self, nodes, leaves):
+        """Replace the octree with (n, 8) nodes and leaf words (a device pool's mirror)."""
+        n = np.ascontiguousarray(nodes, np.uint32).reshape(-1, 8)
+        w = np.ascontiguousarray(leaves, np.uint32)
+        lib().orc_color_pool_load(self._h, _p(n), len(n), _p(w), len(w))
 
     def leaves(self):
         n = lib().orc_color_leaves(self._h, None)

@@ -1413,6 +1413,11 @@ uint64_t orc_color_leaves(const orc_color_pool *c, uint32_t *out) {
 		std::copy(c->cp.leaves.begin(), c->cp.leaves.end(), out);
 	return c->cp.leaves.size();
 }
+void orc_color_pool_load(orc_color_pool *c, const uint32_t *nodes, uint64_t n_nodes, const uint32_t *leaves,
+                         uint64_t n_words) {
+	c->cp.nodes.assign(nodes, nodes + 8 * n_nodes);
+	c->cp.leaves.assign(leaves, leaves + n_words);
+}
 // One VBR edit (kind 1 fill, 2 paint; colour = colors/weight/bpw): the colour
 // octree from the old DAG root, then the geometry (fill only).
 void orc_vbr_edit(orc_pool *p, orc_color_pool *c, uint32_t root, uint32_t color_root, const hd_edit_desc *e,

@@ -124,3 +124,31 @@ def test_vbr_rejects_bad_colours(hd):
         pool.vbr_edit(hd.NULL, cp, hd.DAGColorPool.NULL, v)
     with pytest.raises(hd.HashDagError):
         hd.DAGColorPool(pool, cfg.get_node_levels())  # leaf level below the DAG leaves
+
+
+def test_vbr_sphere_touching_a_node_boundary(orc, hd):
+    """A sphere of radius 1 centred one voxel past a node boundary: the
+    reference's conservative classification (distance to the node's exclusive
+    upper bound) makes it proceed into the node before the boundary too."""
+    from vkhashdag_gb300 import workloads as W, VBR_EDIT_DTYPE, SHAPE_SPHERE, OP_FILL
+    res = 128
+    cfg = W.config_for_resolution(res)
+    scene = W.sphere_scene(res, 16, seed=0)
+    pool = hd.NodePool(cfg, heap_pages=1 << 12)
+    root = pool.edit(hd.NULL, scene)
+    opool = orc.OraclePool.from_config(cfg)
+    oroot = opool.edit(orc.NULL, scene)
+    v = np.zeros(3, VBR_EDIT_DTYPE)
+    v["edit"]["shape"] = SHAPE_SPHERE
+    v["edit"]["op"] = OP_FILL
+    v["edit"]["p0"] = [(48, 65, 123), (64, 64, 64), (31, 96, 33)]
+    v["edit"]["r2"] = [1, 1, 4]
+    v["colors"] = [0x102030, 0x405060, 0x708090]
+    cp = hd.DAGColorPool(pool, 3)
+    r, c = pool.vbr_edit(root, cp, hd.DAGColorPool.NULL, v)
+    ocp = orc.OracleColorPool(3)
+    oc = orc.OracleColorPool.NULL
+    for e in v:
+        oroot, oc = opool.vbr_edit(oroot, ocp, oc, e["edit"], 1, int(e["colors"]))
+    nodes, leaves = cp.read()
+    assert c == oc and np.array_equal(nodes, ocp.nodes()) and np.array_equal(leaves, ocp.leaves())

@@ -450,6 +450,38 @@ struct UnitSum {
 	u32 bits;
 };
 
+// A unit that keeps its old colours is the run of old blocks over its 64
+// voxels (consecutive blocks of a macro block always differ in colours or bits
+// per weight, VBRChunkWriter::append): summarised per block, not per voxel.
+__device__ __forceinline__ UnitSum copy_summary(const Region &g, u32 m0) {
+	UnitSum s{0, 0, 0, 0};
+	if (!g.has_src) {
+		s.first = s.last = key_of(g.fill);
+		s.bits = 64u * g.fill.bpw;
+		return s;
+	}
+	SrcCursor c;
+	c.start(g, m0);
+	const u32 v0 = m0 & (kMacroVoxels - 1u), v1 = v0 + 64u;
+	u32 v = v0;
+	for (;;) {
+		const u32 h1 = g.hdr[2u * c.blk + 1u], bpw = (h1 >> 16) & 3u;
+		const u64 k = (u64)g.hdr[2u * c.blk] | ((u64)bpw << 32);
+		if (v == v0)
+			s.first = k;
+		s.last = k;
+		const u32 stop = c.next_off < v1 ? c.next_off : v1;
+		s.bits += (stop - v) * bpw;
+		if (c.next_off >= v1)
+			break;
+		v = c.next_off;
+		++s.heads;
+		++c.blk;
+		c.next_off = c.blk + 1u < c.end ? (g.hdr[2u * (c.blk + 1u) + 1u] >> 18) : kMacroVoxels;
+	}
+	return s;
+}
+
 __device__ __forceinline__ UnitSum unit_summary(const DevPool &P, const EditArgs &a, const Region &g, u32 u) {
 	UnitSum s{0, 0, 0, 0};
 	u64 leaf = 0;
@@ -460,6 +492,8 @@ __device__ __forceinline__ UnitSum unit_summary(const DevPool &P, const EditArgs
 		s.bits = 64u * a.C.bpw;
 		return s;
 	}
+	if (kind == kUnitCopy)
+		return copy_summary(g, u * 64u);
 	SrcCursor src;
 	src.start(g, u * 64u);
 	for (u32 i = 0; i < 64u; ++i) {
@@ -473,6 +507,78 @@ __device__ __forceinline__ UnitSum unit_summary(const DevPool &P, const EditArgs
 		s.bits += c.bpw;
 	}
 	return s;
+}
+
+// Writes one voxel's weight bits at bit position `bit` of the weight words.
+__device__ __forceinline__ void put_weight(u32 *wb, u64 bit, u32 weight, u32 bpw) {
+	const u32 o = (u32)(bit & 31u);
+	atomicOr(&wb[bit >> 5], weight << o);
+	if (o + bpw > 32u)
+		atomicOr(&wb[(bit >> 5) + 1], weight >> (32u - o));
+}
+
+// Headers and weight bits of unit u: block header index hb and bit position
+// bb of its first voxel, mws = weight start of its macro block.
+__device__ __forceinline__ void emit_unit(const DevPool &P, const EditArgs &a, const Region &g, u32 u, bool head0, u64 hb,
+                                          u64 bb, u64 mws, u32 *hdr, u32 *wb) {
+	u64 leaf = 0;
+	u32 lx = 0, ly = 0, lz = 0;
+	const u32 kind = unit_kind(P, a.e, g, u, &leaf, &lx, &ly, &lz);
+	const u32 m0 = u * 64u;
+	u64 hi = hb, bit = bb;
+	auto header = [&](u32 colors, u32 bpw, u32 m) {
+		hdr[2ull * hi] = colors;
+		hdr[2ull * hi + 1] = ((m & (kMacroVoxels - 1u)) << 18) | (bpw << 16) | (u32)(bit - mws);
+		++hi;
+	};
+	if (kind == kUnitColor || (kind == kUnitCopy && !g.has_src)) {
+		const VCol c = kind == kUnitColor ? a.C : g.fill;
+		if (head0)
+			header(c.colors, c.bpw, m0);
+		if (c.bpw)
+			for (u32 i = 0; i < 64u; ++i, bit += c.bpw)
+				put_weight(wb, bit, c.weight, c.bpw);
+		return;
+	}
+	SrcCursor src;
+	src.start(g, m0);
+	if (kind == kUnitCopy) { // the old blocks over the unit, their weight bits copied
+		const u32 v0 = m0 & (kMacroVoxels - 1u), v1 = v0 + 64u;
+		u32 v = v0;
+		for (;;) {
+			const u32 h0 = g.hdr[2u * src.blk], h1 = g.hdr[2u * src.blk + 1u], bpw = (h1 >> 16) & 3u;
+			if (v != v0 || head0)
+				header(h0, bpw, (m0 - v0) + v);
+			const u32 stop = src.next_off < v1 ? src.next_off : v1;
+			if (bpw)
+				for (u32 x = v; x < stop; ++x, bit += bpw) {
+					const u32 sb = src.wstart + (h1 & 0xFFFFu) + (x - (h1 >> 18)) * bpw, o = sb & 31u;
+					u32 w = g.bits[sb >> 5] >> o;
+					if (o + bpw > 32u)
+						w |= g.bits[(sb >> 5) + 1u] << (32u - o);
+					put_weight(wb, bit, w & ((1u << bpw) - 1u), bpw);
+				}
+			if (src.next_off >= v1)
+				break;
+			v = src.next_off;
+			++src.blk;
+			src.next_off = src.blk + 1u < src.end ? (g.hdr[2u * (src.blk + 1u) + 1u] >> 18) : kMacroVoxels;
+		}
+		return;
+	}
+	u64 prev = 0;
+	for (u32 i = 0; i < 64u; ++i) {
+		const u32 m = m0 + i;
+		const VCol c = unit_voxel(a.e, a, g, kind, leaf, lx, ly, lz, m, i, src);
+		const u64 k = key_of(c);
+		if (i == 0 ? head0 : k != prev)
+			header(c.colors, c.bpw, m);
+		prev = k;
+		if (c.bpw) {
+			put_weight(wb, bit, c.weight, c.bpw);
+			bit += c.bpw;
+		}
+	}
 }
 
 // chunk words (without the block size word) for B blocks and O weight bits
@@ -596,33 +702,8 @@ __global__ void __launch_bounds__(kRegionBlock) k_color_emit(DevPool P, ColorDev
 				macro[2u * (u0 / kRegionBlock)] = (u32)hb;
 				macro[2u * (u0 / kRegionBlock) + 1u] = (u32)bb;
 			}
-			if (valid) {
-				u64 leaf = 0;
-				u32 lx = 0, ly = 0, lz = 0;
-				const u32 kind = unit_kind(P, a.e, g, u, &leaf, &lx, &ly, &lz);
-				SrcCursor src;
-				if (kind != kUnitColor)
-					src.start(g, u * 64u);
-				u64 hi = hb, bit = bb, prev = 0;
-				for (u32 i = 0; i < 64u; ++i) {
-					const u32 m = u * 64u + i;
-					const VCol c = unit_voxel(a.e, a, g, kind, leaf, lx, ly, lz, m, i, src);
-					const u64 k = key_of(c);
-					if (i == 0 ? head0 : k != prev) {
-						hdr[2ull * hi] = c.colors;
-						hdr[2ull * hi + 1] = ((m & (kMacroVoxels - 1u)) << 18) | (c.bpw << 16) | (u32)(bit - O);
-						++hi;
-					}
-					prev = k;
-					if (c.bpw) {
-						const u32 o = (u32)(bit & 31u);
-						atomicOr(&wb[bit >> 5], c.weight << o);
-						if (o + c.bpw > 32u)
-							atomicOr(&wb[(bit >> 5) + 1], c.weight >> (32u - o));
-						bit += c.bpw;
-					}
-				}
-			}
+			if (valid)
+				emit_unit(P, a, g, u, head0, hb, bb, O, hdr, wb);
 			B += th;
 			O += tb;
 			__syncthreads();
@@ -909,6 +990,9 @@ uint64_t isqrt_u64(uint64_t v) {
 
 // Walk items and regions an edit can produce: a node proceeds only where the
 // edit's bounding box overlaps it, and each proceeding node has 8 children.
+// The sphere classification (src/main.cpp:77-106) measures distances to a
+// node's exclusive upper bound, so a sphere also "touches" the nodes that end
+// one voxel before it: its box is widened by one voxel on each side.
 void walk_bounds(const hd_edit_desc &e, uint32_t voxel_level, uint32_t leaf_level, uint64_t *items, uint64_t *regions) {
 	const uint64_t res = 1ull << voxel_level;
 	int64_t lo[3], hi[3];
@@ -918,8 +1002,8 @@ void walk_bounds(const hd_edit_desc &e, uint32_t voxel_level, uint32_t leaf_leve
 			hi[a] = e.p1[a];
 		} else {
 			const int64_t r = (int64_t)isqrt_u64(e.r2);
-			lo[a] = (int64_t)e.p0[a] - r;
-			hi[a] = (int64_t)e.p0[a] + r + 1;
+			lo[a] = (int64_t)e.p0[a] - r - 1;
+			hi[a] = (int64_t)e.p0[a] + r + 2;
 		}
 		lo[a] = std::max<int64_t>(lo[a], 0);
 		hi[a] = std::min<int64_t>(hi[a], (int64_t)res);
@@ -1081,12 +1165,15 @@ hd_status hd_vbr_edit(hd_pool *pool, hd_color_pool *cp, uint32_t root, uint32_t 
 					HD_TRY(cudaMemsetAsync(w.c + 3, 0, sizeof(unsigned long long), st));
 					continue;
 				}
-				if (err == kCErrItems)
-					return HD_ERR_INTERNAL; // bounds above are exact upper bounds
 				if (err == kCErrNodes || err == kCErrLeaves)
 					return HD_ERR_POOL_OOM;
-				if (err)
+				if (err) { // the walk bounds above are upper bounds: a capacity error is a bug
+					fprintf(stderr,
+					        "hashdag_gb300: hd_vbr_edit: colour edit %u failed (code %llu: regions %llu, scratch words "
+					        "%llu, item bound %llu, region bound %llu)\n",
+					        i, err, cp->h_c[0], cp->h_c[1], (unsigned long long)items, (unsigned long long)regions);
 					return HD_ERR_INTERNAL;
+				}
 				break;
 			}
 			const uint64_t R = cp->h_c[0];
@@ -1098,8 +1185,11 @@ hd_status hd_vbr_edit(hd_pool *pool, hd_color_pool *cp, uint32_t root, uint32_t 
 			HD_TRY(cudaGetLastError());
 			HD_TRY(cudaMemcpyAsync(cp->h_c, w.c, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
 			HD_TRY(cudaStreamSynchronize(st));
-			if (cp->h_c[3])
+			if (cp->h_c[3]) {
+				fprintf(stderr, "hashdag_gb300: hd_vbr_edit: colour edit %u failed in the octree update (code %llu)\n",
+				        i, cp->h_c[3]);
 				return HD_ERR_INTERNAL;
+			}
 			color_root = (uint32_t)cp->h_c[4];
 		}
 		if (v.edit.op != HD_OP_PAINT) { // geometry: a fill, or a stateless dig

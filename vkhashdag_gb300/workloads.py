@@ -188,6 +188,60 @@ def vbr_edits(resolution: int, n: int, seed: int = 1, r_max: int = 64, side_max:
     return v
 
 
+def vbr_app_config():
+    """The application's node pool (src/main.cpp:196-203): 2^17 voxels per
+    side, 64 KB pages, 4 pages per bucket, 2^7 buckets on the 9 top levels and
+    2^11 below; its colour octree has leaves at level 10 (src/main.cpp:204-211)."""
+    from . import DefaultConfig
+    return DefaultConfig(level_count=17, top_level_count=9, word_bits_per_page=14, page_bits_per_bucket=2,
+                         bucket_bits_per_top_level=7, bucket_bits_per_bottom_level=11)()
+
+
+VBR_APP_LEAF_LEVEL = 10
+
+
+def vbr_app_scene() -> np.ndarray:
+    """The application's start-up colour edits (src/main.cpp:254-274) in its
+    2^17 world: a white box fill, a cyan box fill, a sphere paint and a
+    stateless sphere dig."""
+    v = np.zeros(4, VBR_EDIT_DTYPE)
+    v[0]["edit"] = (SHAPE_AABB, OP_FILL, (1001, 1000, 1000), (10000, 10000, 10000), 0)
+    v[0]["colors"] = 0xFFFFFF
+    v[1]["edit"] = (SHAPE_AABB, OP_FILL, (0, 0, 0), (5000, 5000, 5000), 0)
+    v[1]["colors"] = 0x00FFFF
+    v[2]["edit"] = (SHAPE_SPHERE, OP_PAINT, (5005, 5000, 5000), (0, 0, 0), 2000 * 2000)
+    v[2]["colors"] = 0x007FFF
+    v[3]["edit"] = (SHAPE_SPHERE, OP_DIG, (10000, 10000, 10000), (0, 0, 0), 4000 * 4000)
+    return v
+
+
+def vbr_surface_edits(n: int, seed: int = 5, r_lo: int = 16, r_hi: int = 128) -> np.ndarray:
+    """Interactive colour edits on the start-up scene (the application's mouse
+    edits, src/main.cpp:321-343): coloured sphere fills and paints (50/50) with
+    radius log-uniform in [r_lo, r_hi], centred on a face of the white box,
+    RGB8 colours."""
+    v = np.zeros(n, VBR_EDIT_DTYPE)
+    face = randint(seed, 71, n, 0, 5)
+    uv = randint(seed, 72, 2 * n, 1001, 9999).reshape(n, 2)
+    jitter = randint(seed, 73, n, -8, 8)
+    c = np.zeros((n, 3), np.int64)
+    axis, hi = face % 3, face >= 3
+    for a in range(3):
+        others = [b for b in range(3) if b != a]
+        sel = axis == a
+        c[sel, a] = np.where(hi[sel], 9999, 1001) + jitter[sel]
+        c[sel, others[0]] = uv[sel, 0]
+        c[sel, others[1]] = uv[sel, 1]
+    r = log_uniform_int(seed, 74, n, r_lo, r_hi)
+    paint = u64(seed, 75, n) & np.uint64(1)
+    v["edit"]["shape"] = SHAPE_SPHERE
+    v["edit"]["op"] = np.where(paint == 1, OP_PAINT, OP_FILL)
+    v["edit"]["p0"] = c
+    v["edit"]["r2"] = r * r
+    v["colors"] = u64(seed, 76, n) & np.uint64(0xFFFFFF)
+    return v
+
+
 def point_queries(resolution: int, n: int, seed: int = 7) -> np.ndarray:
     return randint(seed, 31, 3 * n, 0, resolution - 1).reshape(n, 3).astype(np.uint32)
 
