@@ -446,7 +446,9 @@ typedef struct hd_vbr_color {
 	float rgb[3];                                        /* trace.frag's colour (VBRColor::Get) */
 } hd_vbr_color;               /* 28 bytes */
 typedef struct hd_color_pool hd_color_pool;
-/* A colour octree for the voxels of `pool` (device memory of pool's GPU). */
+/* A colour octree for the voxels of `pool` (device memory of pool's GPU).
+ * Destroy it before `pool` if it is still to be edited; hd_color_pool_destroy,
+ * hd_color_pool_read and hd_color_fetch do not touch the node pool. */
 hd_status hd_color_pool_create(hd_pool *pool, const hd_color_config *cfg, hd_color_pool **out);
 void hd_color_pool_destroy(hd_color_pool *cpool);
 /* Host mirror: node count and leaf word count; with non-null buffers also the

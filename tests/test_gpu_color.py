@@ -152,3 +152,18 @@ def test_vbr_sphere_touching_a_node_boundary(orc, hd):
         oroot, oc = opool.vbr_edit(oroot, ocp, oc, e["edit"], 1, int(e["colors"]))
     nodes, leaves = cp.read()
     assert c == oc and np.array_equal(nodes, ocp.nodes()) and np.array_equal(leaves, ocp.leaves())
+
+
+def test_vbr_node_pool_closes_its_colour_pools_first(hd):
+    """Closing (or collecting) a node pool first closes its colour pools, so
+    no colour pool outlives the node pool it reads; later calls see no stale
+    CUDA error."""
+    from vkhashdag_gb300 import workloads as W
+    cfg = W.serving_config(128)
+    pool = hd.NodePool(cfg, heap_pages=1 << 10)
+    cp = hd.DAGColorPool(pool, 3)
+    pool.close()
+    assert cp._h is None
+    cp.close()
+    p2 = hd.NodePool(cfg, heap_pages=cfg.get_total_pages())
+    assert p2.edit(hd.NULL, W.sphere_scene(128, 2, seed=1)) != hd.NULL

@@ -16,6 +16,7 @@ from __future__ import annotations
 import ctypes
 import enum
 import os
+import weakref
 from dataclasses import dataclass, field
 from typing import Iterable, List, Optional, Sequence
 
@@ -387,10 +388,13 @@ class NodePool:
         self._h = h
         self.device = device
         self.root = NULL
+        self._color_pools = weakref.WeakSet()  # closed before this pool
 
     # -- lifecycle -------------------------------------------------------
     def close(self):
         if getattr(self, "_h", None):
+            for cp in list(getattr(self, "_color_pools", ())):
+                cp.close()
             lib().hd_pool_destroy(self._h)
             self._h = None
 
@@ -643,6 +647,7 @@ class DAGColorPool:
         h = ctypes.c_void_p()
         _check(lib().hd_color_pool_create(pool._h, ctypes.byref(cfg), ctypes.byref(h)), "hd_color_pool_create")
         self._h = h
+        pool._color_pools.add(self)
 
     def close(self):
         if getattr(self, "_h", None):

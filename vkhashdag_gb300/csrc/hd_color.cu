@@ -918,6 +918,8 @@ __global__ void k_color_fetch(ColorDev C, u32 voxel_level, u32 root, const u32 *
 // ------------------------------------------------------------------ host side
 struct hd_color_pool {
 	hd_pool *pool = nullptr;
+	int device = 0;           // kept here: the colour pool may be destroyed after its node pool
+	uint32_t voxel_level = 0;
 	hd_color_config cfg{};
 	ColorDev d{};
 	ColorWs w{};
@@ -1043,6 +1045,8 @@ hd_status hd_color_pool_create(hd_pool *pool, const hd_color_config *cfg, hd_col
 		return HD_ERR_INVALID_ARG;
 	auto *cp = new hd_color_pool;
 	cp->pool = pool;
+	cp->device = pool->device;
+	cp->voxel_level = V;
 	cp->cfg = *cfg;
 	if (cudaSetDevice(pool->device) != cudaSuccess) {
 		delete cp;
@@ -1075,7 +1079,7 @@ hd_status hd_color_pool_create(hd_pool *pool, const hd_color_config *cfg, hd_col
 void hd_color_pool_destroy(hd_color_pool *cp) {
 	if (!cp)
 		return;
-	cudaSetDevice(cp->pool->device);
+	cudaSetDevice(cp->device);
 	if (cp->st)
 		cudaStreamSynchronize(cp->st);
 	cp_free_ws(cp);
@@ -1094,7 +1098,7 @@ hd_status hd_color_pool_read(hd_color_pool *cp, uint32_t *nodes, uint64_t *n_nod
 	if (!cp || !n_nodes || !n_leaf_words)
 		return HD_ERR_INVALID_ARG;
 	std::lock_guard<std::mutex> lk(cp->mtx);
-	HD_TRY(cudaSetDevice(cp->pool->device));
+	HD_TRY(cudaSetDevice(cp->device));
 	unsigned long long c[2];
 	HD_TRY(cudaMemcpyAsync(c, cp->d.ctr, sizeof(c), cudaMemcpyDeviceToHost, cp->st));
 	HD_TRY(cudaStreamSynchronize(cp->st));
@@ -1212,11 +1216,9 @@ hd_status hd_color_fetch(hd_color_pool *cp, uint32_t color_root, const uint32_t 
 		return HD_ERR_INVALID_ARG;
 	if (n == 0)
 		return HD_OK;
-	HD_TRY(cudaSetDevice(cp->pool->device));
+	HD_TRY(cudaSetDevice(cp->device));
 	cudaStream_t st = (cudaStream_t)stream;
-	const uint32_t V = cp->pool->cfg.node_levels + 1;
-	k_color_fetch<<<(n + 255) / 256, 256, 0, st>>>(cp->d, V, color_root, d_xyz, n, d_out);
-	cp->pool->kernel_launches += 1;
+	k_color_fetch<<<(n + 255) / 256, 256, 0, st>>>(cp->d, cp->voxel_level, color_root, d_xyz, n, d_out);
 	return cp_check(cudaGetLastError());
 }
 

@@ -495,16 +495,20 @@ __device__ __forceinline__ u32 leaf_result(const DevPool &P, u64 bits, u64 bits0
 // Read-only lookup of a leaf among the resident nodes.  No slot is pending
 // while the leaves are rebuilt, so a committed entry with equal bits is the
 // node; a short walk that misses leaves the leaf to the claiming probe.
-__device__ __forceinline__ u32 lookup_leaf(const DevPool &P, u64 bits) {
+// The walk starts at index slot s whose entry v0 the caller has loaded (the
+// first slots of a node's changed leaves are loaded together).
+__device__ __forceinline__ u64 leaf_slot(const DevPool &P, u64 bits) {
+	return index_start(hash_leaf(bits), P.cfg.L - 1, P.index_mask);
+}
+__device__ __forceinline__ u32 lookup_leaf_from(const DevPool &P, u64 bits, u64 s, unsigned long long v0) {
 	const u32 L = P.cfg.L, l = L - 1;
 	const u32 h = hash_leaf(bits);
 	const u32 bucket = P.cfg.bucket_base[l] + ((P.cfg.hasher == HD_HASHER_ZERO ? 0u : h) & ((1u << P.cfg.bucket_bits[l]) - 1u));
 	const u32 bucket_shift = P.cfg.wbpp + P.cfg.pbpb;
 	const u64 mask = P.index_mask;
 	const unsigned long long tag = h & 0x7FFFFFFFu;
-	u64 s = index_start(h, l, mask);
 	for (u32 probe = 0; probe < 32u; ++probe, s = (s + 1) & mask) {
-		const unsigned long long v = __ldg(&P.index[s]);
+		const unsigned long long v = probe == 0 ? v0 : __ldg(&P.index[s]);
 		if (v == kSlotEmpty)
 			return kNull;
 		if ((v >> 63) || ((v >> 32) & 0x7FFFFFFFull) != tag)
@@ -620,7 +624,8 @@ __device__ __forceinline__ void leafparent_short_phase(const DevPool &P, Workspa
 				bool cand;
 				u32 r = leaf_result(P, bits, b0, old[c], &cand);
 				if (cand) {
-					r = lookup_leaf(P, bits);
+					const u64 sl = leaf_slot(P, bits);
+					r = lookup_leaf_from(P, bits, sl, __ldg(&P.index[sl]));
 					if (r == kNull) {
 						cb[c] = bits;
 						cand_mask |= 1u << c;
@@ -730,7 +735,8 @@ static __global__ void __launch_bounds__(kBlock) k_leafparent_long(DevPool P, Wo
 		bool cand = false;
 		u32 r = leaf_result(P, bits, b0, old[c], &cand);
 		if (lead && cand) {
-			r = lookup_leaf(P, bits);
+			const u64 sl = leaf_slot(P, bits);
+			r = lookup_leaf_from(P, bits, sl, __ldg(&P.index[sl]));
 			cand = r == kNull;
 		}
 		cand = lead && cand;
