@@ -458,8 +458,8 @@ hd_status hd_color_pool_read(hd_color_pool *cpool, uint32_t *nodes, uint64_t *n_
 /* Colour edits applied one after another (each the reference's Edit with a
  * VBREditorWrapper, or a stateless dig): the colour octree from the DAG as it
  * was before the edit, then the geometry through hd_edit.  Returns the new
- * DAG root and colour root.  HD_ERR_POOL_OOM when the octree is full (that
- * edit's colours are not applied). */
+ * DAG root and colour root.  HD_ERR_POOL_OOM when the octree is full: that
+ * edit is not applied (both roots stay as after the previous edit). */
 hd_status hd_vbr_edit(hd_pool *pool, hd_color_pool *cpool, uint32_t root, uint32_t color_root, const hd_vbr_edit_desc *edits,
                       uint32_t n, uint32_t *out_root, uint32_t *out_color_root);
 /* Colours of n voxels (device buffers: xyz triples at voxel resolution) under

@@ -380,6 +380,8 @@ def run_reference(mode, word_bits_per_page, page_bits_per_bucket, bucket_bits, e
         nq = len(np.asarray(vbr["queries"]).reshape(-1, 3))
         out["colors"] = np.frombuffer(data, COLOR_DTYPE, nq, off).copy()
         off += COLOR_DTYPE.itemsize * nq
+        out["edit_ns"] = np.frombuffer(data, np.uint64, len(edits), off).copy()
+        off += 8 * len(edits)
     if mode == MODE_UPSERT:
         (n,) = struct.unpack_from("<I", data, off)
         off += 4

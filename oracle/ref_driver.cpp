@@ -34,7 +34,8 @@
 //           roots after[n_keep]
 //   mode 5: colour root, n_nodes, nodes[8 n_nodes], n_leaf_words,
 //           leaf_words[n], then per query: has_value, colors, weight,
-//           bits_per_weight, rgb[3] (float, VBRColor::Get())
+//           bits_per_weight, rgb[3] (float, VBRColor::Get()); then the time
+//           of each edit (uint64 ns)
 
 #include <hashdag/NodePool.hpp>
 #include <hashdag/NodePoolThreadedEdit.hpp>
@@ -352,8 +353,18 @@ template <typename HasherT> static int run(FILE *in, FILE *out, uint32_t mode, c
 			q = rd(in);
 	}
 	auto t0 = std::chrono::steady_clock::now();
+	std::vector<uint64_t> edit_ns;
 	if (mode == 5) {
 		for (uint32_t i = 0; i < n_edits; ++i) {
+			const auto te = std::chrono::steady_clock::now();
+			struct Lap {
+				std::vector<uint64_t> &v;
+				std::chrono::steady_clock::time_point t;
+				~Lap() {
+					v.push_back(std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now() - t)
+					                .count());
+				}
+			} lap{edit_ns, te};
 			if (vops[i].kind == 0) {
 				root = pool->Edit(root, hashdag::StatelessEditorWrapper<uint32_t, DescEditor>{.editor = DescEditor{edits[i]}});
 				continue;
@@ -460,6 +471,7 @@ template <typename HasherT> static int run(FILE *in, FILE *out, uint32_t mode, c
 			fwrite(&rgb.y, 4, 1, out);
 			fwrite(&rgb.z, 4, 1, out);
 		}
+		fwrite(edit_ns.data(), 8, edit_ns.size(), out);
 	}
 	if (mode == 2) {
 		wr(out, (uint32_t)upsert_ptrs.size());

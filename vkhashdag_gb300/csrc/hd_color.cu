@@ -167,6 +167,10 @@ struct ColorWs {
 	u64 *r_dest;   // leaf word index of the block
 	u64 *r_append; // appended words (0: rewritten in place)
 	u64 region_cap;
+	// per (region, macro block) q = region * macros + macro: block headers and
+	// weight bits of the macro block, then their offsets inside the chunk
+	u64 *m_blocks, *m_bits, *m_hoff, *m_boff;
+	u32 macros; // macro blocks per colour leaf
 	u32 *scratch;
 	u64 scratch_cap;
 	u32 *app_list; // appended items, level by level in Morton order
@@ -584,36 +588,61 @@ __device__ __forceinline__ void emit_unit(const DevPool &P, const EditArgs &a, c
 // chunk words (without the block size word) for B blocks and O weight bits
 __device__ __forceinline__ u64 chunk_words(u32 M, u64 B, u64 O) { return 3ull + 2ull * M + 2ull * B + (O + 31ull) / 32ull; }
 
+// One CTA per (region, macro block): every macro block starts a VBR block
+// (VBRChunkWriter::append), so macro blocks are independent apart from their
+// offsets in the chunk.
 __global__ void __launch_bounds__(kRegionBlock) k_color_count(DevPool P, ColorDev C, ColorWs W, EditArgs a) {
 	__shared__ u64 s_warp[33];
 	__shared__ u64 s_last[kRegionBlock];
+	const u64 Q = W.c[0] * W.macros;
+	for (u64 q = blockIdx.x; q < Q; q += gridDim.x) {
+		const u32 r = (u32)(q / W.macros), m = (u32)(q % W.macros);
+		const Region g = region_of(P, C, W, r);
+		const u32 u = m * kRegionBlock + threadIdx.x;
+		UnitSum s{0, 0, 0, 0};
+		const bool valid = u < g.units;
+		if (valid)
+			s = unit_summary(P, a, g, u);
+		s_last[threadIdx.x] = s.last;
+		__syncthreads();
+		u32 h = 0;
+		if (valid)
+			h = s.heads + ((threadIdx.x == 0 || s.first != s_last[threadIdx.x - 1]) ? 1u : 0u);
+		u64 th, tb;
+		block_scan(h, s_warp, &th);
+		block_scan(s.bits, s_warp, &tb);
+		if (threadIdx.x == 0) {
+			W.m_blocks[q] = th;
+			W.m_bits[q] = tb;
+		}
+	}
+}
+
+// Per region: offsets of its macro blocks' headers and weight bits, the
+// chunk's size.
+__global__ void __launch_bounds__(kRegionBlock) k_color_region_scan(ColorWs W) {
+	__shared__ u64 s_warp[33];
 	const u64 R = W.c[0];
+	const u32 M = W.macros;
 	for (u64 r = blockIdx.x; r < R; r += gridDim.x) {
-		const Region g = region_of(P, C, W, (u32)r);
 		u64 B = 0, O = 0;
-		for (u32 u0 = 0; u0 < g.units; u0 += kRegionBlock) { // one macro block
-			const u32 u = u0 + threadIdx.x;
-			UnitSum s{0, 0, 0, 0};
-			const bool valid = u < g.units;
-			if (valid)
-				s = unit_summary(P, a, g, u);
-			s_last[threadIdx.x] = s.last;
-			__syncthreads();
-			u32 h = 0;
-			if (valid)
-				h = s.heads + ((threadIdx.x == 0 || s.first != s_last[threadIdx.x - 1]) ? 1u : 0u);
+		for (u32 m0 = 0; m0 < M; m0 += blockDim.x) {
+			const u32 m = m0 + threadIdx.x;
+			const u64 q = r * M + m;
+			const u64 hb = m < M ? W.m_blocks[q] : 0ull, bb = m < M ? W.m_bits[q] : 0ull;
 			u64 th, tb;
-			block_scan(h, s_warp, &th);
-			block_scan(s.bits, s_warp, &tb);
+			const u64 he = block_scan(hb, s_warp, &th), be = block_scan(bb, s_warp, &tb);
+			if (m < M) {
+				W.m_hoff[q] = B + he;
+				W.m_boff[q] = O + be;
+			}
 			B += th;
 			O += tb;
 		}
 		if (threadIdx.x == 0) {
-			const u32 M = (g.units * 64u + kMacroVoxels - 1u) >> kMacroBits;
 			W.r_words[r] = (u32)chunk_words(M, B, O);
 			W.r_blocks[r] = B;
 		}
-		__syncthreads();
 	}
 }
 
@@ -667,57 +696,61 @@ __global__ void __launch_bounds__(kWalkBlock) k_color_place(ColorDev C, ColorWs 
 	}
 }
 
-// The chunk of every region into scratch (VBRChunkWriter, VBRColor.hpp:367-488):
-// per macro block, unit summaries -> block and bit offsets -> headers and
-// weight bits; the region's block count (from k_color_count) places the
-// weight words after the headers.
+// Scratch of the chunks cleared (weight words are OR-ed in).
+__global__ void k_color_zero(ColorWs W) {
+	if (W.c[3])
+		return;
+	const u64 n = W.c[1];
+	for (u64 k = (u64)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (u64)gridDim.x * blockDim.x)
+		W.scratch[k] = 0u;
+}
+
+// The chunks into scratch (VBRChunkWriter, VBRColor.hpp:367-488), one CTA per
+// (region, macro block): unit summaries -> block and bit offsets inside the
+// macro block -> headers and weight bits at the macro block's offsets; the
+// region's block count places the weight words after the headers.
 __global__ void __launch_bounds__(kRegionBlock) k_color_emit(DevPool P, ColorDev C, ColorWs W, EditArgs a) {
 	__shared__ u64 s_warp[33];
 	__shared__ u64 s_last[kRegionBlock];
-	const u64 R = W.c[0];
-	for (u64 r = blockIdx.x; r < R; r += gridDim.x) {
-		const Region g = region_of(P, C, W, (u32)r);
-		const u32 M = (g.units * 64u + kMacroVoxels - 1u) >> kMacroBits;
+	if (W.c[3])
+		return;
+	const u64 Q = W.c[0] * W.macros;
+	for (u64 q = blockIdx.x; q < Q; q += gridDim.x) {
+		const u32 r = (u32)(q / W.macros), m = (u32)(q % W.macros), M = W.macros;
+		const Region g = region_of(P, C, W, r);
 		u32 *out = W.scratch + W.r_scratch[r];
-		const u64 words = W.r_words[r], btotal = W.r_blocks[r];
-		for (u64 k = threadIdx.x; k < words; k += blockDim.x)
-			out[k] = 0u;
-		__syncthreads();
+		const u64 btotal = W.r_blocks[r];
 		u32 *macro = out + 3, *hdr = macro + 2u * M, *wb = hdr + 2ull * btotal;
-		u64 B = 0, O = 0;
-		for (u32 u0 = 0; u0 < g.units; u0 += kRegionBlock) { // macro block u0 / 256
-			const u32 u = u0 + threadIdx.x;
-			const bool valid = u < g.units;
-			UnitSum s{0, 0, 0, 0};
-			if (valid)
-				s = unit_summary(P, a, g, u);
-			s_last[threadIdx.x] = s.last;
-			__syncthreads();
-			const bool head0 = valid && (threadIdx.x == 0 || s.first != s_last[threadIdx.x - 1]);
-			const u32 h = valid ? s.heads + (head0 ? 1u : 0u) : 0u;
-			u64 th, tb;
-			const u64 hb = B + block_scan(h, s_warp, &th);
-			const u64 bb = O + block_scan(s.bits, s_warp, &tb);
-			if (threadIdx.x == 0) {
-				macro[2u * (u0 / kRegionBlock)] = (u32)hb;
-				macro[2u * (u0 / kRegionBlock) + 1u] = (u32)bb;
-			}
-			if (valid)
-				emit_unit(P, a, g, u, head0, hb, bb, O, hdr, wb);
-			B += th;
-			O += tb;
-			__syncthreads();
-		}
-		if (threadIdx.x == 0) {
-			out[0] = M;
-			out[1] = (u32)B;
-			out[2] = (u32)((O + 31u) / 32u);
-		}
+		const u64 B = W.m_hoff[q], O = W.m_boff[q];
+		const u32 u = m * kRegionBlock + threadIdx.x;
+		const bool valid = u < g.units;
+		UnitSum s{0, 0, 0, 0};
+		if (valid)
+			s = unit_summary(P, a, g, u);
+		s_last[threadIdx.x] = s.last;
 		__syncthreads();
+		const bool head0 = valid && (threadIdx.x == 0 || s.first != s_last[threadIdx.x - 1]);
+		const u32 h = valid ? s.heads + (head0 ? 1u : 0u) : 0u;
+		u64 th, tb;
+		const u64 hb = B + block_scan(h, s_warp, &th);
+		const u64 bb = O + block_scan(s.bits, s_warp, &tb);
+		if (threadIdx.x == 0) {
+			macro[2u * m] = (u32)B;
+			macro[2u * m + 1u] = (u32)O;
+			if (m == 0) {
+				out[0] = M;
+				out[1] = (u32)btotal;
+				out[2] = (u32)((W.m_boff[q + M - 1] + W.m_bits[q + M - 1] + 31u) / 32u);
+			}
+		}
+		if (valid)
+			emit_unit(P, a, g, u, head0, hb, bb, O, hdr, wb);
 	}
 }
 
 __global__ void k_color_copy(ColorDev C, ColorWs W) {
+	if (W.c[3])
+		return;
 	const u64 R = W.c[0];
 	for (u64 r = blockIdx.x; r < R; r += gridDim.x) {
 		const u64 dest = W.r_dest[r], words = W.r_words[r];
@@ -747,6 +780,8 @@ __device__ __forceinline__ u64 morton_of(u64 p, u32 l) {
 // (VBREditor.hpp:92-107): appended nodes are numbered in post order.
 __global__ void __launch_bounds__(kWalkBlock) k_color_up(ColorDev C, ColorWs W) {
 	__shared__ u64 s_warp[33];
+	if (W.c[3])
+		return;
 	const u32 LL = C.leaf_level;
 	// decisions, level LL-1 up to 0
 	for (u32 l = LL; l-- > 0;) {
@@ -920,6 +955,7 @@ struct hd_color_pool {
 	hd_pool *pool = nullptr;
 	int device = 0;           // kept here: the colour pool may be destroyed after its node pool
 	uint32_t voxel_level = 0;
+	uint32_t macros = 1;      // macro blocks per colour leaf
 	hd_color_config cfg{};
 	ColorDev d{};
 	ColorWs w{};
@@ -970,10 +1006,13 @@ hd_status cp_reserve(hd_color_pool *cp, uint64_t items, uint64_t regions, uint64
 	    (s = cp_alloc(cp, &n.r_scratch, regions)) || (s = cp_alloc(cp, &n.r_dest, regions)) ||
 	    (s = cp_alloc(cp, &n.r_append, regions)) || (s = cp_alloc(cp, &n.scratch, scratch)) ||
 	    (s = cp_alloc(cp, &n.app_list, items)) || (s = cp_alloc(cp, &n.app_lvl, (uint64_t)HD_MAX_LEVELS + 2)) ||
-	    (s = cp_alloc(cp, &n.app_end, items)) || (s = cp_alloc(cp, &n.c, 8))) {
+	    (s = cp_alloc(cp, &n.app_end, items)) || (s = cp_alloc(cp, &n.c, 8)) ||
+	    (s = cp_alloc(cp, &n.m_blocks, regions * cp->macros)) || (s = cp_alloc(cp, &n.m_bits, regions * cp->macros)) ||
+	    (s = cp_alloc(cp, &n.m_hoff, regions * cp->macros)) || (s = cp_alloc(cp, &n.m_boff, regions * cp->macros))) {
 		cp_free_ws(cp);
 		return s;
 	}
+	n.macros = cp->macros;
 	n.item_cap = items;
 	n.region_cap = regions;
 	n.scratch_cap = scratch;
@@ -1047,6 +1086,7 @@ hd_status hd_color_pool_create(hd_pool *pool, const hd_color_config *cfg, hd_col
 	cp->pool = pool;
 	cp->device = pool->device;
 	cp->voxel_level = V;
+	cp->macros = std::max<uint32_t>(1u, (uint32_t)((1ull << (3u * (V - cfg->leaf_level))) >> kMacroBits));
 	cp->cfg = *cfg;
 	if (cudaSetDevice(pool->device) != cudaSuccess) {
 		delete cp;
@@ -1125,53 +1165,86 @@ hd_status hd_vbr_edit(hd_pool *pool, hd_color_pool *cp, uint32_t root, uint32_t 
 	*out_root = root;
 	*out_color_root = color_root;
 	const uint32_t L = pool->cfg.node_levels, V = L + 1;
-	const int sms = pool->num_sms;
+	const uint64_t sms = (uint64_t)pool->num_sms;
 	for (uint32_t i = 0; i < n; ++i) {
 		const hd_vbr_edit_desc &v = edits[i];
+		const bool colour = v.edit.op != HD_OP_DIG;
 		hd_edit_desc g = v.edit;
-		if (g.op != HD_OP_DIG) { // the colour part, against the DAG before this edit
-			g.op = HD_OP_FILL;
-			EditArgs a{};
+		g.op = HD_OP_FILL;
+		EditArgs a{};
+		uint64_t items = 0, regions = 0;
+		if (colour) {
 			a.e = g;
 			// VBRColor(RGB8Color) keeps 24 bits (Color.hpp:21)
 			a.C = VCol{v.bits_per_weight ? v.colors : (v.colors & 0xFFFFFFu), v.weight, v.bits_per_weight, 1u};
 			a.rgb8 = vcol_rgb8(a.C);
 			a.root = root;
 			a.color_root = color_root;
-			uint64_t items, regions;
 			walk_bounds(g, V, cp->cfg.leaf_level, &items, &regions);
+		}
+		// the colour part of the edit, against the DAG before the edit; it
+		// overlaps the geometry pass (which only adds nodes) and reports
+		// errors on the device, read after both
+		auto launch_colour = [&]() -> hd_status {
 			std::lock_guard<std::mutex> lk2(cp->mtx);
 			std::lock_guard<std::mutex> lk(pool->mtx);
 			HD_TRY(cudaSetDevice(pool->device));
-			hd_status s = cp_reserve(cp, items, regions, cp->w.scratch_cap ? cp->w.scratch_cap : (1ull << 20));
+			hd_status s = cp_reserve(cp, items, regions, cp->w.scratch_cap ? cp->w.scratch_cap : (1ull << 22));
 			if (s)
 				return s;
-			ColorWs &w = cp->w;
+			const ColorWs &w = cp->w;
 			cudaStream_t st = cp->st;
-			HD_TRY(cudaStreamWaitEvent(st, pool->ws_free, 0)); // passes of the DAG pool that write nodes
+			const uint64_t q = regions * cp->macros;
+			const uint32_t gq = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(q, sms * 8));
+			const uint32_t gr = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(regions, sms * 2));
+			HD_TRY(cudaStreamWaitEvent(st, pool->ws_free, 0)); // passes of the DAG pool that wrote nodes
 			HD_TRY(cudaMemsetAsync(w.c, 0, 8 * sizeof(unsigned long long), st));
 			k_color_walk<<<1, kWalkBlock, 0, st>>>(pool->P, cp->d, w, a);
-			const uint32_t grid = (uint32_t)std::min<uint64_t>(regions, (uint64_t)sms * 2);
-			k_color_count<<<grid, kRegionBlock, 0, st>>>(pool->P, cp->d, w, a);
+			k_color_count<<<gq, kRegionBlock, 0, st>>>(pool->P, cp->d, w, a);
+			k_color_region_scan<<<gr, kRegionBlock, 0, st>>>(w);
+			k_color_place<<<1, kWalkBlock, 0, st>>>(cp->d, w);
+			k_color_zero<<<(uint32_t)(sms * 4), 256, 0, st>>>(w);
+			k_color_emit<<<gq, kRegionBlock, 0, st>>>(pool->P, cp->d, w, a);
+			k_color_copy<<<gr, 256, 0, st>>>(cp->d, w);
+			k_color_up<<<1, kWalkBlock, 0, st>>>(cp->d, w);
+			pool->kernel_launches += 8;
+			HD_TRY(cudaGetLastError());
+			HD_TRY(cudaMemcpyAsync(cp->h_c, w.c, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
+			return HD_OK;
+		};
+		if (colour) {
+			hd_status s = launch_colour();
+			if (s)
+				return s;
+		}
+		uint32_t new_root = root;
+		if (v.edit.op != HD_OP_PAINT) { // geometry: a fill, or a stateless dig
+			hd_edit_desc ge = v.edit;
+			hd_status s = hd_edit(pool, root, &ge, 1, &new_root, nullptr);
+			if (s)
+				return s;
+		}
+		if (colour) {
 			for (int attempt = 0;; ++attempt) {
-				k_color_place<<<1, kWalkBlock, 0, st>>>(cp->d, w);
-				HD_TRY(cudaGetLastError());
-				HD_TRY(cudaMemcpyAsync(cp->h_c, w.c, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
-				HD_TRY(cudaStreamSynchronize(st));
+				HD_TRY(cudaStreamSynchronize(cp->st));
 				const unsigned long long err = cp->h_c[3];
-				if (err == kCErrScratch && attempt == 0) { // grow the scratch; counts stay valid
+				if (err == kCErrScratch && attempt == 0) { // more scratch, then the colour part again
 					const uint64_t need = cp->h_c[1];
-					void *q = nullptr;
-					HD_TRY(cudaMalloc(&q, need * 4ull));
-					cp->ws_allocs.push_back(q);
-					w.scratch = static_cast<u32 *>(q);
-					w.scratch_cap = need;
-					HD_TRY(cudaMemsetAsync(w.c + 3, 0, sizeof(unsigned long long), st));
+					{
+						std::lock_guard<std::mutex> lk2(cp->mtx);
+						HD_TRY(cudaSetDevice(pool->device));
+						hd_status s = cp_reserve(cp, items, regions, need);
+						if (s)
+							return s;
+					}
+					hd_status s = launch_colour();
+					if (s)
+						return s;
 					continue;
 				}
 				if (err == kCErrNodes || err == kCErrLeaves)
-					return HD_ERR_POOL_OOM;
-				if (err) { // the walk bounds above are upper bounds: a capacity error is a bug
+					return HD_ERR_POOL_OOM; // this edit not applied: both roots stay
+				if (err) { // the walk bounds are upper bounds: a capacity error is a bug
 					fprintf(stderr,
 					        "hashdag_gb300: hd_vbr_edit: colour edit %u failed (code %llu: regions %llu, scratch words "
 					        "%llu, item bound %llu, region bound %llu)\n",
@@ -1180,30 +1253,9 @@ hd_status hd_vbr_edit(hd_pool *pool, hd_color_pool *cp, uint32_t root, uint32_t 
 				}
 				break;
 			}
-			const uint64_t R = cp->h_c[0];
-			const uint32_t rg = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(R, (uint64_t)sms * 2));
-			k_color_emit<<<rg, kRegionBlock, 0, st>>>(pool->P, cp->d, w, a);
-			k_color_copy<<<rg, 256, 0, st>>>(cp->d, w);
-			k_color_up<<<1, kWalkBlock, 0, st>>>(cp->d, w);
-			pool->kernel_launches += 6;
-			HD_TRY(cudaGetLastError());
-			HD_TRY(cudaMemcpyAsync(cp->h_c, w.c, 8 * sizeof(unsigned long long), cudaMemcpyDeviceToHost, st));
-			HD_TRY(cudaStreamSynchronize(st));
-			if (cp->h_c[3]) {
-				fprintf(stderr, "hashdag_gb300: hd_vbr_edit: colour edit %u failed in the octree update (code %llu)\n",
-				        i, cp->h_c[3]);
-				return HD_ERR_INTERNAL;
-			}
 			color_root = (uint32_t)cp->h_c[4];
 		}
-		if (v.edit.op != HD_OP_PAINT) { // geometry: a fill, or a stateless dig
-			hd_edit_desc ge = v.edit;
-			uint32_t r2;
-			hd_status s = hd_edit(pool, root, &ge, 1, &r2, nullptr);
-			if (s)
-				return s;
-			root = r2;
-		}
+		root = new_root;
 		*out_root = root;
 		*out_color_root = color_root;
 	}
