@@ -722,6 +722,9 @@ def run_serving(args):
         if args.serve_shape:
             e, lf, dd = (int(x) for x in args.serve_shape.split(","))
             pool.set_tuning(expand_blocks_per_sm=e, leaf_blocks_per_sm=lf, dedup_blocks_per_sm=dd)
+        if args.serve_reserve:  # edit workspace sized up front (no growth while serving)
+            items, entries = (int(float(x)) for x in args.serve_reserve.split(","))
+            pool.reserve(items, entries, args.max_pass_edits)
         t0 = time.perf_counter()
         roots0.append(pool.edit(hd.NULL, W.terrain_columns(res, res // 256, seed=0)))
         build_s.append(time.perf_counter() - t0)
@@ -1080,6 +1083,7 @@ def main():
     ap.add_argument("--ray-slots", type=int, default=4)
     ap.add_argument("--verify-seconds", type=float, default=60.0)
     ap.add_argument("--serve-shape", default="", help="expand,leaf,dedup blocks per SM of the serving pools")
+    ap.add_argument("--serve-reserve", default="", help="items,list entries of each serving pool's edit workspace")
     ap.add_argument("--cameras", type=int, default=16)
     ap.add_argument("--width", type=int, default=3840)
     ap.add_argument("--height", type=int, default=2160)

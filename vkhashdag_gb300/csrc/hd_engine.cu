@@ -358,6 +358,18 @@ hd_status pass_graph(hd_pool *pool, cudaGraphExec_t *out) {
 	}
 	if (!pool->capture_stream)
 		HD_TRY(cudaStreamCreateWithFlags(&pool->capture_stream, cudaStreamNonBlocking));
+	// With lazy module loading a kernel is loaded at its first launch, which a
+	// capturing stream does not allow (a serving scene can capture before the
+	// process ever launched the long-list kernels): load every kernel first.
+	cudaFuncAttributes fa;
+	HD_TRY(cudaFuncGetAttributes(&fa, k_root));
+	HD_TRY(cudaFuncGetAttributes(&fa, k_expand_short));
+	HD_TRY(cudaFuncGetAttributes(&fa, k_expand_long));
+	HD_TRY(cudaFuncGetAttributes(&fa, k_leafparent_short));
+	HD_TRY(cudaFuncGetAttributes(&fa, k_leafparent_long));
+	HD_TRY(cudaFuncGetAttributes(&fa, k_dedup<true>));
+	HD_TRY(cudaFuncGetAttributes(&fa, k_dedup<false>));
+	HD_TRY(cudaFuncGetAttributes(&fa, k_finish));
 	cudaStream_t cs = pool->capture_stream;
 	HD_TRY(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
 	hd_status s = HD_OK;
