@@ -197,6 +197,65 @@ __device__ __forceinline__ void write_child_list_thread(const Workspace &W, u32 
 	}
 }
 
+// Classification of the 8 children (cells of 2^shift voxels) of the node at
+// coordinate (px, py, pz) against one edit, 2 bits per child c (x half c&1,
+// y half c>>1&1, z half c>>2&1): kClsNone / kClsPartial / kClsFull.  The
+// formulas of classify() (AABBEditor / SphereEditor::EditNode,
+// src/main.cpp:36-47,77-106) with each axis's terms of the node's two halves
+// computed once for the 4 children sharing them.
+template <typename I, typename U>
+__device__ __forceinline__ u32 classify_children_sphere(const hd_edit_desc &e, const u32 o[3], u32 sz, U r2) {
+	U mx[3][2], mn[3][2];
+#pragma unroll
+	for (int a = 0; a < 3; ++a) {
+		const I d0 = (I)o[a] - (I)e.p0[a], d1 = d0 + (I)sz, d2 = d1 + (I)sz;
+		const U s0 = (U)d0 * (U)d0, s1 = (U)d1 * (U)d1, s2 = (U)d2 * (U)d2;
+		mx[a][0] = s0 > s1 ? s0 : s1;
+		mx[a][1] = s1 > s2 ? s1 : s2;
+		mn[a][0] = (d0 > 0 ? s0 : (U)0) + (d1 < 0 ? s1 : (U)0);
+		mn[a][1] = (d1 > 0 ? s1 : (U)0) + (d2 < 0 ? s2 : (U)0);
+	}
+	u32 r = 0;
+#pragma unroll
+	for (u32 c = 0; c < 8; ++c) {
+		const u32 hx = c & 1u, hy = (c >> 1) & 1u, hz = (c >> 2) & 1u;
+		const U M = mx[0][hx] + mx[1][hy] + mx[2][hz], N = mn[0][hx] + mn[1][hy] + mn[2][hz];
+		r |= (M <= r2 ? kClsFull : (N > r2 ? kClsNone : kClsPartial)) << (2u * c);
+	}
+	return r;
+}
+__device__ __forceinline__ u32 classify_children(const hd_edit_desc &e, u32 shift, u32 px, u32 py, u32 pz) {
+	const u32 sz = 1u << shift;
+	const u32 o[3] = {px << (shift + 1u), py << (shift + 1u), pz << (shift + 1u)};
+	if (e.shape == HD_SHAPE_AABB) {
+		u32 out[3], in[3]; // bit h: half h of the axis
+#pragma unroll
+		for (int a = 0; a < 3; ++a) {
+			out[a] = in[a] = 0;
+#pragma unroll
+			for (u32 h = 0; h < 2; ++h) {
+				const u32 lb = o[a] + sz * h, ub = lb + sz;
+				out[a] |= ((ub <= e.p0[a]) | (lb >= e.p1[a])) ? 1u << h : 0u;
+				in[a] |= ((lb >= e.p0[a]) & (ub <= e.p1[a])) ? 1u << h : 0u;
+			}
+		}
+		u32 r = 0;
+#pragma unroll
+		for (u32 c = 0; c < 8; ++c) {
+			const u32 hx = c & 1u, hy = (c >> 1) & 1u, hz = (c >> 2) & 1u;
+			const bool o_ = ((out[0] >> hx) | (out[1] >> hy) | (out[2] >> hz)) & 1u;
+			const bool i_ = ((in[0] >> hx) & (in[1] >> hy) & (in[2] >> hz)) & 1u;
+			r |= (o_ ? kClsNone : (i_ ? kClsFull : kClsPartial)) << (2u * c);
+		}
+		return r;
+	}
+	// exact in 32 bits when every bound and the centre are <= 2^15 (as in classify)
+	if (o[0] + 2u * sz <= 0x8000u && o[1] + 2u * sz <= 0x8000u && o[2] + 2u * sz <= 0x8000u &&
+	    (e.p0[0] | e.p0[1] | e.p0[2]) < 0x8000u)
+		return classify_children_sphere<int, u32>(e, o, sz, e.r2 > 0xFFFFFFFFull ? 0xFFFFFFFFu : (u32)e.r2);
+	return classify_children_sphere<long long, u64>(e, o, sz, (u64)e.r2);
+}
+
 // ------------------------------------------------------------------ k_expand_short
 // Thread per level-l inner node (l <= L-3) with an edit list of at most
 // long_threshold edits.  Children are inner items of level l+1.
@@ -225,19 +284,61 @@ __device__ __forceinline__ void expand_short_phase(const DevPool &P, Workspace &
 			pos = W.inner.pos[i];
 		}
 		const bool mine = valid && len <= T && list_ok(W, off, len);
-		u32 cbase[8], cfirst[8], ccnt[8], old[8];
+		u32 cbase[8], cfirst[8], ccnt[8], old[8], part[8];
 		u32 n_emit = 0, n_list = 0, n_long = 0;
 		if (mine) {
 			base_children(P, l, b, old);
+			if (len <= 32u) {
+				// one pass over the list: every edit read once and classified
+				// against the 8 children together (bit p of full/part[c]: edit p
+				// covers / partly covers child c; bit p of fills: edit p fills)
+				u32 full[8], fills = 0;
+#pragma unroll
+				for (u32 c = 0; c < 8; ++c)
+					full[c] = part[c] = 0;
+				for (u32 p = 0; p < len; ++p) {
+					const hd_edit_desc e = W.edits[W.lists[off + p]];
+					const u32 k = classify_children(e, shift, pos_x(pos), pos_y(pos), pos_z(pos));
+					fills |= (e.op == HD_OP_FILL ? 1u : 0u) << p;
+#pragma unroll
+					for (u32 c = 0; c < 8; ++c) {
+						const u32 kc = (k >> (2u * c)) & 3u;
+						full[c] |= (kc == kClsFull ? 1u : 0u) << p;
+						part[c] |= (kc == kClsPartial ? 1u : 0u) << p;
+					}
+				}
+				// plan_child_thread from the bits: the last full cover sets the base;
+				// the kept list starts at the first later partial edit that can change it
+#pragma unroll
+				for (u32 c = 0; c < 8; ++c) {
+					const int lastfull = full[c] ? 31 - __clz(full[c]) : -1;
+					const u32 base = lastfull >= 0 ? (((fills >> lastfull) & 1u) ? filled_c : kNull) : old[c];
+					const u32 after = lastfull >= 0 ? (lastfull == 31 ? 0u : ~0u << (lastfull + 1)) : ~0u;
+					const u32 eff = base == kNull ? fills : (base == filled_c ? ~fills : ~0u); // effective()
+					const u32 cand = part[c] & after;
+					const u32 f = cand & eff;
+					cbase[c] = base;
+					cfirst[c] = f ? (u32)(__ffs(f) - 1) : kNull;
+					ccnt[c] = f ? (u32)__popc(cand & (~0u << cfirst[c])) : 0u;
+					part[c] = cand & (f ? (~0u << cfirst[c]) : 0u); // the kept edits
+					if (ccnt[c]) {
+						++n_emit;
+						n_list += ccnt[c];
+						n_long += ccnt[c] > T ? 1u : 0u;
+					}
+				}
+			} else {
 #pragma unroll 1
-			for (u32 c = 0; c < 8; ++c) {
-				u32 cx, cy, cz;
-				child_pos(pos, c, cx, cy, cz);
-				ccnt[c] = plan_child_thread(W, off, len, shift, cx, cy, cz, old[c], filled_c, &cbase[c], &cfirst[c]);
-				if (ccnt[c]) {
-					++n_emit;
-					n_list += ccnt[c];
-					n_long += ccnt[c] > T ? 1u : 0u;
+				for (u32 c = 0; c < 8; ++c) {
+					u32 cx, cy, cz;
+					child_pos(pos, c, cx, cy, cz);
+					ccnt[c] = plan_child_thread(W, off, len, shift, cx, cy, cz, old[c], filled_c, &cbase[c], &cfirst[c]);
+					part[c] = 0;
+					if (ccnt[c]) {
+						++n_emit;
+						n_list += ccnt[c];
+						n_long += ccnt[c] > T ? 1u : 0u;
+					}
 				}
 			}
 		}
@@ -263,7 +364,13 @@ __device__ __forceinline__ void expand_short_phase(const DevPool &P, Workspace &
 				W.inner.parent[it] = (u32)(i * 8u + c);
 				W.inner.lst_off[it] = (u32)lo;
 				W.inner.lst_len[it] = ccnt[c];
-				write_child_list_thread(W, off, len, cfirst[c], shift, cx, cy, cz, W.lists + lo);
+				if (len <= 32u) {
+					u32 k = 0;
+					for (u32 m = part[c]; m; m &= m - 1u)
+						W.lists[lo + k++] = W.lists[off + (u32)(__ffs(m) - 1)];
+				} else {
+					write_child_list_thread(W, off, len, cfirst[c], shift, cx, cy, cz, W.lists + lo);
+				}
 				if (ccnt[c] > T) {
 					if (child_begin + lg < W.inner.cap)
 						W.long_q[child_begin + lg] = (u32)it;
