@@ -135,7 +135,8 @@ def bench_config():
 def workload(rank, n_batches, n_edits, res):
     from vkhashdag_gb300 import workloads as W
     base = W.sphere_scene(res, 64, seed=0)
-    batches = [W.mixed_batch(res, n_edits, seed=1000 + 100 * rank + k) for k in range(n_batches)]
+    from vkhashdag_gb300.replicas import replica_seed
+    batches = [W.mixed_batch(res, n_edits, seed=replica_seed(rank, k)) for k in range(n_batches)]
     return base, batches
 
 
@@ -278,13 +279,9 @@ def run_ours(args):
     # inserted, so the synchronous path must return the very same root
     last_root = int(d_out[n_batches - 1].item()) & 0xFFFFFFFF
     same_roots = pool.edit(root0, batches[n_batches - 1]) == last_root
-    t = torch.tensor([elapsed_ms], dtype=torch.float64, device=f"cuda:{local}")
-    total_ve = torch.tensor([float(sum(ve[args.warmup:]))], dtype=torch.float64, device=f"cuda:{local}")
-    if world > 1:
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        torch.distributed.all_reduce(total_ve, op=torch.distributed.ReduceOp.SUM)
-    elapsed_ms = float(t.item())
-    value = float(total_ve.item()) / (elapsed_ms / 1e3)
+    from vkhashdag_gb300.replicas import replica_totals
+    elapsed_ms, total_ve = replica_totals(elapsed_ms, float(sum(ve[args.warmup:])), device=f"cuda:{local}")
+    value = total_ve / (elapsed_ms / 1e3)
 
     # ---------------- e2e through the public call with host buffers
     e2e_times = []
