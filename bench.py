@@ -15,7 +15,9 @@ voxel-edits = sum over its edits of the grid voxels inside the shape.
              edit array and D2H of root/status inside the timed region)
   per_edit   the plain form on the same edit list: one pass per edit
   roofline   the dedup pass (k_dedup over all levels) against the
-             measured HBM copy bandwidth
+             measured HBM copy bandwidth; beside it the pass's DRAM rate
+             against the measured rate of independent random 8-byte reads
+             (random_access), the ceiling of a random-access kernel
   cpu_baseline  the CPU restatement of the reference's threaded edit
              (oracle, OpenMP on all host cores) on a bounded sample
 
@@ -111,6 +113,31 @@ class ClockSampler:
                     reasons.add(n)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
                 "samples": len(sm)}
+
+
+def random_access_ceiling(device, table_log2=31, reads_log2=27, reps=5):
+    """Sustained rate of independent random 8-byte reads over a 16 GB table
+    (a library gather, used only as a measuring stick): the ceiling of a kernel
+    whose every access is a random DRAM sector.  Returns reads/s and the
+    sector bytes/s (32 B per read) moved."""
+    import torch
+    table = torch.empty(1 << table_log2, dtype=torch.int64, device=device)
+    idx = torch.randint(0, 1 << table_log2, (1 << reads_log2,), device=device)
+    torch.take(table, idx)
+    torch.cuda.synchronize(device)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = None
+    for _ in range(reps):
+        a.record()
+        torch.take(table, idx)
+        b.record()
+        b.synchronize()
+        ms = a.elapsed_time(b)
+        best = ms if best is None or ms < best else best
+    del table, idx
+    torch.cuda.empty_cache()
+    reads = (1 << reads_log2) / (best / 1e3)
+    return {"reads_per_s": reads, "sector_gbs": 32.0 * reads / 1e9, "table_gb": 8.0 * (1 << table_log2) / 1e9}
 
 
 def dist_setup():
@@ -331,6 +358,12 @@ def run_ours(args):
 
     # ---------------- roofline of the dedup pass
     hbm, peak_kind = peaks()
+    ceiling = None
+    if rank == 0 and not args.no_ceiling:
+        try:
+            ceiling = random_access_ceiling(torch.device("cuda", local))
+        except RuntimeError:  # no room for the 16 GB table beside the pool
+            ceiling = None
     per_step_dedup_ms = float(sum(phases[2:2 + L])) / max(1, npass)
     cw, c, iw = counters["candidate_words"], counters["candidates"], counters["inserted_words"]
     dedup_bytes = float(8 * cw.sum() + 8 * c.sum() + 4 * iw.sum())
@@ -386,7 +419,11 @@ def run_ours(args):
         "roofline": {"bound": "hbm", "kernel": "dedup pass (k_dedup, all levels)", "achieved": achieved,
                      "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "algorithmic_bytes_per_step": dedup_bytes,
-                     "dedup_ms_per_step": per_step_dedup_ms},
+                     "dedup_ms_per_step": per_step_dedup_ms,
+                     "dram_gbs": (traffic / (per_step_dedup_ms / 1e3) / 1e9) if traffic else None,
+                     "random_access": ceiling,
+                     "dram_frac_of_random_access": ((traffic / (per_step_dedup_ms / 1e3) / 1e9) / ceiling["sector_gbs"])
+                     if (traffic and ceiling) else None},
         "tuning": tuning,
         "phases_ms_per_step": phase_ms,
         "counters_last_step": {k: [int(x) for x in v] for k, v in counters.items()},
@@ -1069,6 +1106,7 @@ def main():
     ap.add_argument("--ref-step-seconds", type=float, default=6.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--no-ceiling", action="store_true", help="skip the random-access ceiling measurement")
     ap.add_argument("--mode", default="batched", choices=["batched", "terrain", "rays", "serving", "gc", "vbr"])
     ap.add_argument("--vbr-edits", type=int, default=256)
     ap.add_argument("--gc-batches", type=int, default=2)
