@@ -301,6 +301,7 @@ struct Workspace {
 	u64 list_cap;
 	u32 *long_q;       // per inner level: items with long edit lists (same index space as inner)
 	u32 *todo;         // [inner.cap] level-(L-2) items that still need the claiming probe
+	u32 *todo_parent;  // [inner.cap] their parents' child slots (todo record t: bchild/cnew slot begin(L-2)+t)
 	const hd_edit_desc *edits;
 	u32 n_edits;
 	u32 long_threshold; // lists longer than this are expanded by a block (inner) or a warp (level L-2)

@@ -751,6 +751,9 @@ __device__ __forceinline__ void leafparent_short_phase(const DevPool &P, Workspa
 		const u64 tq = warp_reserve(&W.ctr[kWsTodo], (mine && !resolved) ? 1u : 0u);
 		if (!mine)
 			continue;
+		// an unresolved node's children go to its todo record: slot tq of the
+		// level's own range of bchild / cnew (dense for the level-(L-2) dedup)
+		const u64 ri = begin + tq;
 		u64 ci = c0;
 #pragma unroll 1
 		for (u32 c = 0; c < 8; ++c) {
@@ -758,7 +761,7 @@ __device__ __forceinline__ void leafparent_short_phase(const DevPool &P, Workspa
 				continue;
 			if (ci < W.leaf.cap) {
 				W.leaf_new[ci] = cb[c];
-				W.leaf.parent[ci] = (u32)(i * 8u + c);
+				W.leaf.parent[ci] = (u32)(ri * 8u + c);
 			} else {
 				ws_error(W, kErrCapacity);
 			}
@@ -769,8 +772,9 @@ __device__ __forceinline__ void leafparent_short_phase(const DevPool &P, Workspa
 			continue;
 		}
 		W.todo[tq] = (u32)i;
-		uint4 *bc = reinterpret_cast<uint4 *>(W.bchild + i * 8u);
-		uint4 *cn = reinterpret_cast<uint4 *>(W.cnew + i * 8u);
+		W.todo_parent[tq] = W.inner.parent[i];
+		uint4 *bc = reinterpret_cast<uint4 *>(W.bchild + ri * 8u);
+		uint4 *cn = reinterpret_cast<uint4 *>(W.cnew + ri * 8u);
 		bc[0] = make_uint4(old[0], old[1], old[2], old[3]);
 		bc[1] = make_uint4(old[4], old[5], old[6], old[7]);
 		cn[0] = make_uint4(res[0], res[1], res[2], res[3]);
@@ -853,25 +857,32 @@ static __global__ void __launch_bounds__(kBlock) k_leafparent_long(DevPool P, Wo
 #pragma unroll
 		for (u32 k = 0; k < 8; ++k)
 			cmask |= ((cmask_lanes >> (4u * k)) & 1u) << k;
-		unsigned long long c0 = 0;
-		if (lane == 0 && cmask)
-			c0 = atomicAdd(&W.ctr[kWsItems + L - 1], (unsigned long long)__popc(cmask));
+		unsigned long long c0 = 0, tq = 0;
+		if (lane == 0) {
+			if (cmask)
+				c0 = atomicAdd(&W.ctr[kWsItems + L - 1], (unsigned long long)__popc(cmask));
+			tq = atomicAdd(&W.ctr[kWsTodo], 1ull);
+		}
 		c0 = __shfl_sync(kFullMask, c0, 0);
+		tq = __shfl_sync(kFullMask, tq, 0);
+		const u64 ri = begin + tq; // the node's todo record in the level's range
 		if (lead) {
 			if (cand) {
 				const u64 ci = c0 + __popc(cmask & ((1u << c) - 1u));
 				if (ci < W.leaf.cap) {
 					W.leaf_new[ci] = bits;
-					W.leaf.parent[ci] = (u32)(i * 8u + c);
+					W.leaf.parent[ci] = (u32)(ri * 8u + c);
 				} else {
 					ws_error(W, kErrCapacity);
 				}
 			}
-			W.bchild[i * 8u + c] = old[c];
-			W.cnew[i * 8u + c] = cand ? kNull : r;
+			W.bchild[ri * 8u + c] = old[c];
+			W.cnew[ri * 8u + c] = cand ? kNull : r;
 		}
-		if (lane == 0)
-			W.todo[atomicAdd(&W.ctr[kWsTodo], 1ull)] = (u32)i;
+		if (lane == 0) {
+			W.todo[tq] = (u32)i;
+			W.todo_parent[tq] = W.inner.parent[i];
+		}
 	}
 }
 
@@ -1222,19 +1233,18 @@ __device__ __forceinline__ void flush_block_stats(const unsigned long long (&v)[
 // shared-memory cache of leaf bits -> pointer for leaves found resident, so
 // repeated patterns are answered without touching the index.
 static constexpr u32 kLeafCache = 2048;
-// Item t of a level: the t-th entry of the todo list (level L-2) or of the level range.
+// Item t of a level: position t of the level range, or for level L-2 the
+// t-th todo record (slot t of the level's range of bchild / cnew, written by
+// the leaf kernel; the node itself is W.todo[t]).
 __device__ __forceinline__ u64 item_at(const Workspace &W, u32 use_todo, u64 begin, u64 t) {
-	return use_todo ? (u64)W.todo[t] : begin + t;
+	return begin + t;
 }
 __device__ __forceinline__ void dedup_range(const Workspace &W, u32 L, u32 l, u32 use_todo, u64 &begin, u64 &n) {
-	if (use_todo) {
-		begin = 0;
-		n = W.ctr[kWsTodo];
-		if (n > W.inner.cap)
-			n = W.inner.cap;
-		return;
-	}
 	level_range(W, L, l, begin, n);
+	if (use_todo) {
+		const u64 nt = W.ctr[kWsTodo];
+		n = nt < n ? nt : n;
+	}
 }
 __device__ __forceinline__ u32 sat_add(u32 a, u32 b) { return a + b < a ? 0xFFFFFFFFu : a + b; }
 
@@ -1300,7 +1310,7 @@ __device__ __forceinline__ void dedup_phase(const DevPool &P, Workspace &W, u32 
 				const u32 c[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
 				if (a0.x == b0.x && a0.y == b0.y && a0.z == b0.z && a0.w == b0.w && a1.x == b1.x && a1.y == b1.y &&
 				    a1.z == b1.z && a1.w == b1.w) {
-					r = it.base[i]; // no child changed
+					r = it.base[use_todo ? (u64)W.todo[t] : i]; // no child changed
 				} else {
 					u32 mask = 0, k = 1;
 #pragma unroll
@@ -1384,7 +1394,7 @@ __device__ __forceinline__ void dedup_phase(const DevPool &P, Workspace &W, u32 
 				*(volatile u32 *)&s_val[slot_e] = r;
 		}
 		if (valid) {
-			const u32 ps = it.parent[i];
+			const u32 ps = use_todo ? W.todo_parent[t] : it.parent[i];
 			if (ps == kNull) { // the pass's root item, or a node of an upsert call
 				W.ctr[kWsRoot] = r;
 				it.res[i] = r;
