@@ -27,10 +27,11 @@ def _rank(rank, world, port, out):
 
 def test_two_replicas_report_the_slowest_time_and_all_work():
     import torch.multiprocessing as mp
-    mgr = mp.Manager()
+    ctx = mp.get_context("spawn")
+    mgr = ctx.Manager()
     out = mgr.dict()
     port = _free_port()
-    procs = [mp.get_context("spawn").Process(target=_rank, args=(r, 2, port, out)) for r in range(2)]
+    procs = [ctx.Process(target=_rank, args=(r, 2, port, out)) for r in range(2)]
     for p in procs:
         p.start()
     for p in procs:
