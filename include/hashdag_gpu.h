@@ -186,7 +186,7 @@ hd_status hd_edit_last_probe_stats(hd_pool *pool, uint64_t *probe_steps, uint64_
 typedef struct hd_tuning {
 	uint32_t expand_blocks_per_sm;     /* k_expand_short (default 8) */
 	uint32_t leaf_blocks_per_sm;       /* k_leafparent_short (default 12) */
-	uint32_t dedup_blocks_per_sm;      /* k_probe / k_commit (default 32) */
+	uint32_t dedup_blocks_per_sm;      /* k_dedup (default 32) */
 	uint32_t long_blocks_per_sm;       /* k_expand_long / k_leafparent_long (default 4) */
 	uint32_t long_threshold;           /* default 16, at least 1 */
 } hd_tuning;

@@ -45,8 +45,8 @@ struct hd_pool {
 	bool has_checkpoint = false;
 };
 
-// events per profiled pass: start, after expand, after leaf, after probe/commit of
-// every level (2 per level), after finish
+// events per profiled pass: start, after expand, after leaf, after the dedup launch
+// of every level (1 per level), after finish
 inline uint32_t hd_prof_events_per_pass(uint32_t L) { return 3u + L + 1u; }
 
 // hd_engine.cu

@@ -602,7 +602,7 @@ __device__ __forceinline__ u32 leaf_result(const DevPool &P, u64 bits, u64 bits0
 
 // Read-only lookup of a leaf among the resident nodes.  No slot is pending
 // while the leaves are rebuilt, so a committed entry with equal bits is the
-// node; a short walk that misses leaves the leaf to the claiming probe.
+// node; a short walk that misses leaves the leaf to the dedup launch (k_dedup).
 // The walk starts at index slot s whose entry v0 the caller has loaded (the
 // first slots of a node's changed leaves are loaded together).
 __device__ __forceinline__ u64 leaf_slot(const DevPool &P, u64 bits) {
@@ -658,7 +658,7 @@ __device__ __forceinline__ u32 lookup_inner(const DevPool &P, u32 l, const u32 *
 }
 
 // A level-(L-2) node whose 8 children are all known: unchanged, empty, or an
-// existing node found read-only.  Returns false if it needs the claiming probe.
+// existing node found read-only.  Returns false if it needs the dedup launch.
 __device__ __forceinline__ bool resolve_node(const DevPool &P, u32 l, u32 base, const u32 old[8], const u32 res[8],
                                              u32 *out) {
 	bool unchanged = true;
