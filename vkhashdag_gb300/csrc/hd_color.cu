@@ -317,6 +317,8 @@ __global__ void __launch_bounds__(kWalkBlock) k_color_walk(DevPool P, ColorDev C
 		if (threadIdx.x == 0)
 			W.lvl[l + 2] = (u32)(next < W.item_cap ? next : W.item_cap);
 		__syncthreads();
+		if (*(volatile unsigned long long *)&W.c[3]) // out of room: the next level's items were not all written
+			break;
 	}
 	if (threadIdx.x == 0)
 		W.c[0] = n_regions < W.region_cap ? n_regions : W.region_cap;
@@ -1182,11 +1184,13 @@ hd_status hd_vbr_edit(hd_pool *pool, hd_color_pool *cp, uint32_t root, uint32_t 
 			a.color_root = color_root;
 			walk_bounds(g, V, cp->cfg.leaf_level, &items, &regions);
 		}
+		// one edit at a time per colour pool (its workspace and pinned counters);
+		// lock order: colour pool, then node pool (hd_edit takes the latter)
+		std::lock_guard<std::mutex> lk_cp(cp->mtx);
 		// the colour part of the edit, against the DAG before the edit; it
 		// overlaps the geometry pass (which only adds nodes) and reports
 		// errors on the device, read after both
 		auto launch_colour = [&]() -> hd_status {
-			std::lock_guard<std::mutex> lk2(cp->mtx);
 			std::lock_guard<std::mutex> lk(pool->mtx);
 			HD_TRY(cudaSetDevice(pool->device));
 			hd_status s = cp_reserve(cp, items, regions, cp->w.scratch_cap ? cp->w.scratch_cap : (1ull << 22));
@@ -1231,7 +1235,6 @@ hd_status hd_vbr_edit(hd_pool *pool, hd_color_pool *cp, uint32_t root, uint32_t 
 				if (err == kCErrScratch && attempt == 0) { // more scratch, then the colour part again
 					const uint64_t need = cp->h_c[1];
 					{
-						std::lock_guard<std::mutex> lk2(cp->mtx);
 						HD_TRY(cudaSetDevice(pool->device));
 						hd_status s = cp_reserve(cp, items, regions, need);
 						if (s)
