@@ -244,20 +244,32 @@ __device__ __forceinline__ u64 shape_mask(const hd_edit_desc &e, u32 ox, u32 oy,
 			dz2[k] = (u32)(dz * dz);
 		}
 		const u32 r2 = (u32)e.r2;
-		u64 m = 0;
+		// voxel in iff dx2 + dy2 <= r2 - dz2 (for a z slab with dz2 <= r2); every
+		// dx2 + dy2 < 2^32 since each square is < 2^30 + 2^18 + 16
+		u32 xy[4][4];
 #pragma unroll
 		for (u32 yo = 0; yo < 4; ++yo)
 #pragma unroll
-			for (u32 zo = 0; zo < 4; ++zo) {
-				const u32 t = dy2[yo] + dz2[zo];
-				const u32 rem = t <= r2 ? r2 - t : 0u;
-				const u32 ok = t <= r2 ? 1u : 0u;
-				const u32 nib = (ok & (dx2[0] <= rem)) | (ok & (dx2[1] <= rem)) << 1 | (ok & (dx2[2] <= rem)) << 8 |
-				                (ok & (dx2[3] <= rem)) << 9;
+			for (u32 k = 0; k < 4; ++k)
+				xy[yo][k] = dx2[k] + dy2[yo];
+		u32 lo = 0, hi = 0;
+#pragma unroll
+		for (u32 zo = 0; zo < 4; ++zo) {
+			const bool okz = dz2[zo] <= r2;
+			const u32 rz = r2 - dz2[zo];
+#pragma unroll
+			for (u32 yo = 0; yo < 4; ++yo) {
+				u32 nib = u32(xy[yo][0] <= rz) | u32(xy[yo][1] <= rz) << 1 | u32(xy[yo][2] <= rz) << 8 |
+				          u32(xy[yo][3] <= rz) << 9;
+				nib = okz ? nib : 0u;
 				const u32 base = ((yo & 1u) << 1) | ((zo & 1u) << 2) | ((yo >> 1) << 4) | ((zo >> 1) << 5);
-				m |= (u64)nib << base;
+				if (base < 32u)
+					lo |= nib << base;
+				else
+					hi |= nib << (base - 32u);
 			}
-		return m;
+		}
+		return (u64)lo | ((u64)hi << 32);
 	}
 	return sphere_mask_wide(e, ox, oy, oz);
 }
