@@ -206,29 +206,30 @@ static __device__ __noinline__ u64 sphere_mask_wide(const hd_edit_desc &e, u32 o
 	return m;
 }
 
+// 4-bit mask of the offsets k in 0..3 with lo <= o + k < hi.
+__device__ __forceinline__ u32 axis_run(u32 o, u32 lo, u32 hi) {
+	const u32 a = lo > o ? min(lo - o, 4u) : 0u, b = hi > o ? min(hi - o, 4u) : 0u;
+	return b > a ? ((1u << b) - 1u) & ~((1u << a) - 1u) : 0u;
+}
+// The leaf's voxels whose offset along one axis is in m (bit k: offset k), in
+// the voxel order above: the pattern of that axis's 4 offsets (index bits 0,3
+// for x, 1,4 for y, 2,5 for z) copied over the other index bits by one
+// multiply; the copies land on disjoint bits, so nothing carries.
+__device__ __forceinline__ u64 spread_x(u32 m) { return (u64)((m & 3u) | ((m & 0xCu) << 6)) * 0x0055005500550055ull; }
+__device__ __forceinline__ u64 spread_y(u32 m) {
+	return (u64)((m & 1u) | ((m & 2u) << 1) | ((m & 4u) << 14) | ((m & 8u) << 15)) * 0x0000333300003333ull;
+}
+__device__ __forceinline__ u64 spread_z(u32 m) {
+	return ((u64)((m & 1u) | ((m & 2u) << 3)) | ((u64)(m & 4u) << 30) | ((u64)(m & 8u) << 33)) * 0x0F0F0F0Full;
+}
+
 __device__ __forceinline__ u64 shape_mask(const hd_edit_desc &e, u32 ox, u32 oy, u32 oz) {
 	// The leaf's voxels are 16 x-rows of 4 (one per (y,z) offset pair).  Row
 	// (yo,zo) holds voxel indices base+{0,1,8,9} for x offsets 0..3, with
 	// base = (yo&1)<<1 | (zo&1)<<2 | (yo>>1)<<4 | (zo>>1)<<5.
-	if (e.shape == HD_SHAPE_AABB) {
-		u32 mx = 0, my = 0, mz = 0;
-#pragma unroll
-		for (u32 k = 0; k < 4; ++k) {
-			mx |= u32((ox + k) >= e.p0[0] && (ox + k) < e.p1[0]) << k;
-			my |= u32((oy + k) >= e.p0[1] && (oy + k) < e.p1[1]) << k;
-			mz |= u32((oz + k) >= e.p0[2] && (oz + k) < e.p1[2]) << k;
-		}
-		const u64 nib = (u64)((mx & 1u) | ((mx >> 1) & 1u) << 1 | ((mx >> 2) & 1u) << 8 | ((mx >> 3) & 1u) << 9);
-		u64 m = 0;
-#pragma unroll
-		for (u32 yo = 0; yo < 4; ++yo)
-#pragma unroll
-			for (u32 zo = 0; zo < 4; ++zo) {
-				const u32 base = ((yo & 1u) << 1) | ((zo & 1u) << 2) | ((yo >> 1) << 4) | ((zo >> 1) << 5);
-				if ((my >> yo) & (mz >> zo) & 1u)
-					m |= nib << base;
-			}
-		return m;
+	if (e.shape == HD_SHAPE_AABB) { // separable: the voxels whose x, y and z offsets are all inside
+		return spread_x(axis_run(ox, e.p0[0], e.p1[0])) & spread_y(axis_run(oy, e.p0[1], e.p1[1])) &
+		       spread_z(axis_run(oz, e.p0[2], e.p1[2]));
 	}
 	// A leaf that the sphere only partially covers lies within r+4 of the centre
 	// on every axis, so for r2 <= 2^30 every square and every sum of three fits
