@@ -347,3 +347,29 @@ def test_graph_replayed_pass_equals_direct_pass(orc, hd):
         rr = ref.edit(rr, batch)
     ok, counts, dig, _ = canonical_of_device(orc, pool, root)
     assert ok and dig == [str(x) for x in ref.canonical(rr)[2]]
+
+
+def test_graph_survives_a_rollback(orc, hd):
+    """A rollback that leaves the filled pointers as they are keeps the
+    captured pass graph: the next large pass is a replay (no recapture) and
+    builds the same DAG as before the rollback.  The nodes are inserted again
+    by concurrent warps, so the pointers (the root among them) may differ:
+    the DAGs are compared canonically."""
+    from vkhashdag_gb300 import workloads as W
+    res = 512
+    cfg = W.config_for_resolution(res)
+    pool = hd.NodePool(cfg, heap_pages=1 << 15)
+    root = pool.edit(hd.NULL, W.sphere_scene(res, 16, seed=9))
+    pool.checkpoint()
+    batch = W.mixed_batch(res, 5000, seed=77, r_max=24, side_max=48)
+    r1 = pool.edit(root, batch)  # captures (and may grow the workspace)
+    ok, _, want, _ = canonical_of_device(orc, pool, r1)
+    assert ok
+    pool.rollback(0)
+    pool.edit(root, batch)
+    pool.rollback(0)
+    n0 = pool.kernel_launches()
+    r = pool.edit(root, batch)
+    assert pool.kernel_launches() - n0 == 3 * cfg.get_node_levels()  # replayed, not recaptured
+    ok, _, dig, _ = canonical_of_device(orc, pool, r)
+    assert ok and dig == want

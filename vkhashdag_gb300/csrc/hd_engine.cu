@@ -1243,9 +1243,13 @@ hd_status hd_pool_rollback(hd_pool *pool, void *stream) {
 	HD_TRY(cudaMemcpyAsync(pool->P.page_table, pool->ck_page_table, pool->total_pages * 4, cudaMemcpyDeviceToDevice, st));
 	HD_TRY(cudaMemcpyAsync(pool->P.counters, pool->ck_counters, kCtrCount * 4, cudaMemcpyDeviceToDevice, st));
 	HD_TRY(cudaMemcpyAsync(pool->P.index, pool->ck_index, (pool->P.index_mask + 1) * 8, cudaMemcpyDeviceToDevice, st));
-	for (uint32_t l = 0; l < pool->cfg.node_levels; ++l)
+	bool filled_changed = false;
+	for (uint32_t l = 0; l < pool->cfg.node_levels; ++l) {
+		filled_changed = filled_changed || pool->P.cfg.filled[l] != pool->ck_filled[l];
 		pool->P.cfg.filled[l] = pool->ck_filled[l];
-	++pool->shape_gen;
+	}
+	if (filled_changed) // the filled pointers are kernel parameters of a captured pass graph
+		++pool->shape_gen;
 	HD_TRY(cudaEventRecord(pool->ws_free, st));
 	return HD_OK;
 }
