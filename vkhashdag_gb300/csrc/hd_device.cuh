@@ -132,7 +132,7 @@ __device__ __forceinline__ u64 index_start(u32 h, u32 level, u64 mask) {
 // 2 full cover (kFill for FILL, kClear for DIG).
 enum Cls : u32 { kClsNone = 0, kClsPartial = 1, kClsFull = 2 };
 
-__device__ __forceinline__ u32 classify(const hd_edit_desc &e, u32 shift, u32 px, u32 py, u32 pz) {
+__host__ __device__ __forceinline__ u32 classify(const hd_edit_desc &e, u32 shift, u32 px, u32 py, u32 pz) {
 	u32 lb[3] = {px << shift, py << shift, pz << shift};
 	u32 ub[3] = {(px + 1u) << shift, (py + 1u) << shift, (pz + 1u) << shift};
 	if (e.shape == HD_SHAPE_AABB) { // AABBEditor::EditNode (src/main.cpp:36-47)
@@ -181,7 +181,7 @@ __device__ __forceinline__ u32 classify(const hd_edit_desc &e, u32 shift, u32 px
 // 64-bit mask of the leaf voxels at origin (ox,oy,oz) inside the edit's shape
 // (SphereEditor/AABBEditor::VoxelInRange, src/main.cpp:55-57,121-126).
 // Sphere mask in 64-bit arithmetic (r2 > 2^30); rare, kept out of line.
-static __device__ __noinline__ u64 sphere_mask_wide(const hd_edit_desc &e, u32 ox, u32 oy, u32 oz) {
+static __host__ __device__ __noinline__ u64 sphere_mask_wide(const hd_edit_desc &e, u32 ox, u32 oy, u32 oz) {
 	u64 dx2[4], dy2[4], dz2[4];
 #pragma unroll
 	for (u32 k = 0; k < 4; ++k) {
@@ -207,23 +207,23 @@ static __device__ __noinline__ u64 sphere_mask_wide(const hd_edit_desc &e, u32 o
 }
 
 // 4-bit mask of the offsets k in 0..3 with lo <= o + k < hi.
-__device__ __forceinline__ u32 axis_run(u32 o, u32 lo, u32 hi) {
-	const u32 a = lo > o ? min(lo - o, 4u) : 0u, b = hi > o ? min(hi - o, 4u) : 0u;
+__host__ __device__ __forceinline__ u32 axis_run(u32 o, u32 lo, u32 hi) {
+	const u32 a = lo > o ? (lo - o < 4u ? lo - o : 4u) : 0u, b = hi > o ? (hi - o < 4u ? hi - o : 4u) : 0u;
 	return b > a ? ((1u << b) - 1u) & ~((1u << a) - 1u) : 0u;
 }
 // The leaf's voxels whose offset along one axis is in m (bit k: offset k), in
 // the voxel order above: the pattern of that axis's 4 offsets (index bits 0,3
 // for x, 1,4 for y, 2,5 for z) copied over the other index bits by one
 // multiply; the copies land on disjoint bits, so nothing carries.
-__device__ __forceinline__ u64 spread_x(u32 m) { return (u64)((m & 3u) | ((m & 0xCu) << 6)) * 0x0055005500550055ull; }
-__device__ __forceinline__ u64 spread_y(u32 m) {
+__host__ __device__ __forceinline__ u64 spread_x(u32 m) { return (u64)((m & 3u) | ((m & 0xCu) << 6)) * 0x0055005500550055ull; }
+__host__ __device__ __forceinline__ u64 spread_y(u32 m) {
 	return (u64)((m & 1u) | ((m & 2u) << 1) | ((m & 4u) << 14) | ((m & 8u) << 15)) * 0x0000333300003333ull;
 }
-__device__ __forceinline__ u64 spread_z(u32 m) {
+__host__ __device__ __forceinline__ u64 spread_z(u32 m) {
 	return ((u64)((m & 1u) | ((m & 2u) << 3)) | ((u64)(m & 4u) << 30) | ((u64)(m & 8u) << 33)) * 0x0F0F0F0Full;
 }
 
-__device__ __forceinline__ u64 shape_mask(const hd_edit_desc &e, u32 ox, u32 oy, u32 oz) {
+__host__ __device__ __forceinline__ u64 shape_mask(const hd_edit_desc &e, u32 ox, u32 oy, u32 oz) {
 	// The leaf's voxels are 16 x-rows of 4 (one per (y,z) offset pair).  Row
 	// (yo,zo) holds voxel indices base+{0,1,8,9} for x offsets 0..3, with
 	// base = (yo&1)<<1 | (zo&1)<<2 | (yo>>1)<<4 | (zo>>1)<<5.
@@ -276,7 +276,7 @@ __device__ __forceinline__ u64 shape_mask(const hd_edit_desc &e, u32 ox, u32 oy,
 }
 
 // One voxel inside the edit's shape (VoxelInRange, src/main.cpp:55-57,121-126).
-__device__ __forceinline__ bool voxel_in(const hd_edit_desc &e, u32 x, u32 y, u32 z) {
+__host__ __device__ __forceinline__ bool voxel_in(const hd_edit_desc &e, u32 x, u32 y, u32 z) {
 	if (e.shape == HD_SHAPE_AABB)
 		return x >= e.p0[0] && y >= e.p0[1] && z >= e.p0[2] && x < e.p1[0] && y < e.p1[1] && z < e.p1[2];
 	const long long dx = (long long)x - (long long)e.p0[0], dy = (long long)y - (long long)e.p0[1],
