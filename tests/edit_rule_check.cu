@@ -1,18 +1,20 @@
-// leaf_mask_check.cu -- host-side check of the leaf rule of the edit kernels.
+// edit_rule_check.cu -- host-side check of the per-node rules of the edit kernels.
 //
-// The level-(L-2) kernel decides each leaf of a node from one edit in two
-// steps: classify (none / full / partial, the SphereEditor and AABBEditor
-// EditNode of src/main.cpp:36-47,77-106 at leaf granularity) and, for a
-// partial leaf, shape_mask (the 64 voxels inside the shape, VoxelInRange of
-// src/main.cpp:55-57,121-126, in the voxel order of NodeCoord.hpp:32-43).
-// Both are __host__ __device__, so this program runs the kernels' own code on
-// the CPU and compares the resulting 64-bit leaf masks with a per-voxel brute
-// force written here from the reference's predicates:
-//   * the box mask's per-axis runs and spread multiplies for all 16^3
-//     combinations of axis masks and for every run of a small coordinate range;
-//   * boxes (empty, thin, large) and spheres sampled around their surfaces, in
-//     both the 32-bit paths (centre and bounds below 2^15, r2 <= 2^30) and the
-//     64-bit ones (coordinates up to 2^21, r2 above 2^30).
+// The edit kernels decide every node from the classification of the SphereEditor
+// and AABBEditor EditNode (src/main.cpp:36-47,77-106) and every partly covered
+// leaf from VoxelInRange (src/main.cpp:55-57,121-126) in the voxel order of
+// NodeCoord.hpp:32-43.  The functions that do it are __host__ __device__, so this
+// program runs the kernels' own code on the CPU and compares it with rules
+// written here from the reference's predicates:
+//   * the leaf rule (classify at leaf granularity, then shape_mask for a partial
+//     leaf) against a per-voxel brute force: the box mask's per-axis runs and
+//     spread multiplies for all 16^3 combinations of axis masks and for every run
+//     of a small coordinate range; boxes (empty, thin, large) and spheres sampled
+//     around their surfaces, in the 32-bit paths (centre and bounds below 2^15,
+//     r2 <= 2^30) and the 64-bit ones (coordinates up to 2^21, r2 above 2^30);
+//   * the expand kernel's classify_children (the 8 children of a node against
+//     one edit, each axis's terms shared by the children on the same half)
+//     against classify of each child, at every cell size from 4 to 2^20 voxels.
 // Exit status 0 and "ok <counts>" on success; the first mismatches are printed.
 #include "../vkhashdag_gb300/csrc/hd_device.cuh"
 
@@ -162,6 +164,68 @@ static void check_spheres(u32 world, double max_r, int n_edits, int leaves_per_e
 	}
 }
 
+// Nodes of cell size 2^(shift+1) near the edit (and some anywhere in the world):
+// classify_children packs, per child c, classify(e, shift, 2p + half(c)).
+static unsigned long long g_children[3] = {0, 0, 0}; // children classified none / partial / full
+static void check_children(const hd_edit_desc &e, u32 world_bits, int n_nodes) {
+	for (int s = 0; s < n_nodes; ++s) {
+		const u32 shift = 1u + below(world_bits - 1u); // child cell 2^shift, node 2^(shift+1) <= world
+		const u32 nbits = world_bits - shift - 1u;      // node coordinates below 2^nbits
+		u32 p[3];
+		for (int a = 0; a < 3; ++a) {
+			u32 v;
+			if (s & 1) {
+				v = below(1u << world_bits);
+			} else { // near the edit's bounds
+				const u32 c = e.shape == HD_SHAPE_AABB ? ((s & 2) ? e.p0[a] : e.p1[a]) : e.p0[a];
+				const u32 r = e.shape == HD_SHAPE_AABB ? 0u : (u32)std::sqrt((double)e.r2);
+				const long long off = (long long)below(2u * r + 16u) - (long long)r - 8;
+				long long q = (long long)c + off;
+				q = q < 0 ? 0 : (q >= (1ll << world_bits) ? (1ll << world_bits) - 1 : q);
+				v = (u32)q;
+			}
+			p[a] = (v >> (shift + 1u)) & ((1u << nbits) - 1u);
+		}
+		const u32 got = classify_children(e, shift, p[0], p[1], p[2]);
+		u32 want = 0;
+		for (u32 c = 0; c < 8; ++c)
+			want |= classify(e, shift, 2u * p[0] + (c & 1u), 2u * p[1] + ((c >> 1) & 1u), 2u * p[2] + ((c >> 2) & 1u))
+			        << (2u * c);
+		for (u32 c = 0; c < 8; ++c)
+			++g_children[(want >> (2u * c)) & 3u];
+		if (got != want && g_fail++ < 10)
+			std::printf("children mismatch shape %u p0 (%u,%u,%u) p1 (%u,%u,%u) r2 %llu shift %u node (%u,%u,%u): %04x vs %04x\n",
+			            e.shape, e.p0[0], e.p0[1], e.p0[2], e.p1[0], e.p1[1], e.p1[2], (unsigned long long)e.r2, shift,
+			            p[0], p[1], p[2], got, want);
+	}
+}
+
+static void check_children_all(u32 world_bits, double max_r, int n_edits) {
+	const u32 world = 1u << world_bits;
+	for (int t = 0; t < n_edits; ++t) {
+		hd_edit_desc e{};
+		if (t & 1) {
+			e.shape = HD_SHAPE_AABB;
+			for (int a = 0; a < 3; ++a) {
+				const u32 side = (u32)std::exp(unit() * std::log(max_r * 2.0 + 1.0));
+				e.p0[a] = below(world - (side < world ? side : world - 1u));
+				e.p1[a] = (t % 13 == 1) ? e.p0[a] : e.p0[a] + side;
+			}
+		} else {
+			e.shape = HD_SHAPE_SPHERE;
+			for (int a = 0; a < 3; ++a)
+				e.p0[a] = below(world);
+			const double r = std::exp(unit() * std::log(max_r));
+			e.r2 = (u64)(r * r) + below(3);
+			if (t % 8 == 0)
+				e.r2 = (1ull << 30) + (u64)(t / 8 % 3) - 1;
+			if (t % 16 == 2)
+				e.r2 = 0xFFFFFFFFull + (u64)(t / 16 % 3) - 1; // the 32-bit clamp's edge
+		}
+		check_children(e, world_bits, 64);
+	}
+}
+
 int main() {
 	check_spread();
 	check_boxes(1u << 15, 2048, 4000, 64);
@@ -170,10 +234,13 @@ int main() {
 	check_spheres(1u << 15, 32768.0, 1000, 64, true);  // r2 around 2^30
 	check_spheres(1u << 21, 32768.0, 2000, 64, true);  // 64-bit classify, 32-bit mask
 	check_spheres(1u << 21, 1u << 20, 2000, 64, false); // 64-bit classify and mask
+	check_children_all(15, 16384.0, 4000);   // 32-bit child classification
+	check_children_all(21, 1u << 20, 4000);  // 64-bit
 	if (g_fail) {
 		std::printf("FAILED %d\n", g_fail);
 		return 1;
 	}
-	std::printf("ok none %llu partial %llu full %llu\n", g_checked[0], g_checked[1], g_checked[2]);
+	std::printf("ok none %llu partial %llu full %llu child_none %llu child_partial %llu child_full %llu\n",
+	            g_checked[0], g_checked[1], g_checked[2], g_children[0], g_children[1], g_children[2]);
 	return 0;
 }

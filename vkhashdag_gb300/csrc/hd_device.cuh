@@ -176,6 +176,65 @@ __host__ __device__ __forceinline__ u32 classify(const hd_edit_desc &e, u32 shif
 	return mn > e.r2 ? kClsNone : kClsPartial;
 }
 
+// Classification of the 8 children (cells of 2^shift voxels) of the node at
+// coordinate (px, py, pz) against one edit, 2 bits per child c (x half c&1,
+// y half c>>1&1, z half c>>2&1): kClsNone / kClsPartial / kClsFull.  The
+// formulas of classify() (AABBEditor / SphereEditor::EditNode,
+// src/main.cpp:36-47,77-106) with each axis's terms of the node's two halves
+// computed once for the 4 children sharing them.
+template <typename I, typename U>
+__host__ __device__ __forceinline__ u32 classify_children_sphere(const hd_edit_desc &e, const u32 o[3], u32 sz, U r2) {
+	U mx[3][2], mn[3][2];
+#pragma unroll
+	for (int a = 0; a < 3; ++a) {
+		const I d0 = (I)o[a] - (I)e.p0[a], d1 = d0 + (I)sz, d2 = d1 + (I)sz;
+		const U s0 = (U)d0 * (U)d0, s1 = (U)d1 * (U)d1, s2 = (U)d2 * (U)d2;
+		mx[a][0] = s0 > s1 ? s0 : s1;
+		mx[a][1] = s1 > s2 ? s1 : s2;
+		mn[a][0] = (d0 > 0 ? s0 : (U)0) + (d1 < 0 ? s1 : (U)0);
+		mn[a][1] = (d1 > 0 ? s1 : (U)0) + (d2 < 0 ? s2 : (U)0);
+	}
+	u32 r = 0;
+#pragma unroll
+	for (u32 c = 0; c < 8; ++c) {
+		const u32 hx = c & 1u, hy = (c >> 1) & 1u, hz = (c >> 2) & 1u;
+		const U M = mx[0][hx] + mx[1][hy] + mx[2][hz], N = mn[0][hx] + mn[1][hy] + mn[2][hz];
+		r |= (M <= r2 ? kClsFull : (N > r2 ? kClsNone : kClsPartial)) << (2u * c);
+	}
+	return r;
+}
+__host__ __device__ __forceinline__ u32 classify_children(const hd_edit_desc &e, u32 shift, u32 px, u32 py, u32 pz) {
+	const u32 sz = 1u << shift;
+	const u32 o[3] = {px << (shift + 1u), py << (shift + 1u), pz << (shift + 1u)};
+	if (e.shape == HD_SHAPE_AABB) {
+		u32 out[3], in[3]; // bit h: half h of the axis
+#pragma unroll
+		for (int a = 0; a < 3; ++a) {
+			out[a] = in[a] = 0;
+#pragma unroll
+			for (u32 h = 0; h < 2; ++h) {
+				const u32 lb = o[a] + sz * h, ub = lb + sz;
+				out[a] |= ((ub <= e.p0[a]) | (lb >= e.p1[a])) ? 1u << h : 0u;
+				in[a] |= ((lb >= e.p0[a]) & (ub <= e.p1[a])) ? 1u << h : 0u;
+			}
+		}
+		u32 r = 0;
+#pragma unroll
+		for (u32 c = 0; c < 8; ++c) {
+			const u32 hx = c & 1u, hy = (c >> 1) & 1u, hz = (c >> 2) & 1u;
+			const bool o_ = ((out[0] >> hx) | (out[1] >> hy) | (out[2] >> hz)) & 1u;
+			const bool i_ = ((in[0] >> hx) & (in[1] >> hy) & (in[2] >> hz)) & 1u;
+			r |= (o_ ? kClsNone : (i_ ? kClsFull : kClsPartial)) << (2u * c);
+		}
+		return r;
+	}
+	// exact in 32 bits when every bound and the centre are <= 2^15 (as in classify)
+	if (o[0] + 2u * sz <= 0x8000u && o[1] + 2u * sz <= 0x8000u && o[2] + 2u * sz <= 0x8000u &&
+	    (e.p0[0] | e.p0[1] | e.p0[2]) < 0x8000u)
+		return classify_children_sphere<int, u32>(e, o, sz, e.r2 > 0xFFFFFFFFull ? 0xFFFFFFFFu : (u32)e.r2);
+	return classify_children_sphere<long long, u64>(e, o, sz, (u64)e.r2);
+}
+
 // Leaf voxel index i in [0,64) -> offset inside the 4^3 leaf (NodeCoord.hpp:32-43):
 //   x = (i>>2 & 2) | (i & 1), y = (i>>3 & 2) | (i>>1 & 1), z = (i>>4 & 2) | (i>>2 & 1)
 // 64-bit mask of the leaf voxels at origin (ox,oy,oz) inside the edit's shape
