@@ -1,0 +1,155 @@
+/* hashdag_gpu_pool.hpp -- C++ host side of a device HashDAG pool.
+ *
+ * GpuNodePool stands where the application's DAGNodePool stands
+ * (src/DAGNodePool.hpp:31-105): it owns the pool (on the GB300, through the C
+ * ABI of hashdag_gpu.h), takes edits root in / root out, keeps the root the
+ * renderer reads, and holds a host mirror of the pool's words in the
+ * reference's storage layout (HostPoolMirror).  GpuNodePool forwards the
+ * mirror's storage hooks, so it satisfies the reference's NodePool,
+ * ThreadedNodePool and GCNodePool concepts (include/hashdag/NodePool.hpp:22-38)
+ * for code that reads or edits the host copy with the reference's own
+ * algorithms.
+ *
+ *   auto pool = hashdag_gb300::GpuNodePool::Create(config);   // nullptr on failure
+ *   uint32_t root = HD_NULL_PTR;
+ *   pool->Edit(root, edits, &root);                          // one batched pass
+ *   pool->Download();                                        // device -> mirror
+ *   ... read or edit the mirror (ReadPage, GetBucketRefWords, ...) ...
+ *   pool->Upload();                                          // mirror -> device
+ *
+ * Header-only C++20 over libhashdag_gb300.so.  Every call returns the
+ * library's hd_status; nothing falls back to the CPU.
+ */
+#pragma once
+
+#include "hashdag_gpu.h"
+#include "hashdag_host_mirror.hpp"
+
+#include <cstdint>
+#include <memory>
+#include <mutex>
+#include <span>
+#include <vector>
+
+namespace hashdag_gb300 {
+
+class GpuNodePool {
+public:
+	/* DAGNodePool::Create (src/DAGNodePool.cpp:9-47): the pool, or nullptr
+	 * (reason in *status).  heap_pages 0 = one device page per virtual page
+	 * (identity heap); index_log2 0 = index sized from the heap. */
+	static std::unique_ptr<GpuNodePool> Create(const hd_config &config, uint64_t heap_pages = 0, int device = 0,
+	                                           hd_status *status = nullptr, uint32_t index_log2 = 0) {
+		hd_pool *p = nullptr;
+		const uint64_t heap = heap_pages ? heap_pages : (uint64_t)config_total_pages(config);
+		const hd_status s = hd_pool_create(&config, heap, index_log2, device, &p);
+		if (status)
+			*status = s;
+		if (s != HD_OK)
+			return nullptr;
+		return std::unique_ptr<GpuNodePool>(new GpuNodePool(p, config));
+	}
+	~GpuNodePool() { hd_pool_destroy(m_pool); }
+	GpuNodePool(const GpuNodePool &) = delete;
+	GpuNodePool &operator=(const GpuNodePool &) = delete;
+
+	hd_pool *Handle() const { return m_pool; }
+	const hd_config &GetHdConfig() const { return m_mirror.MirrorConfig(); }
+
+	/* NodePoolBase::Edit / NodePoolThreadedEdit::ThreadedEdit
+	 * (include/hashdag/NodePool.hpp:405-417, NodePoolThreadedEdit.hpp:104-126)
+	 * for stateless sphere / box editors: edits applied in order, one pass on
+	 * the device.  On failure *new_root keeps root. */
+	hd_status Edit(uint32_t root, std::span<const hd_edit_desc> edits, uint32_t *new_root, void *stream = nullptr) {
+		return hd_edit(m_pool, root, edits.data(), (uint32_t)edits.size(), new_root, stream);
+	}
+	/* NodePoolThreadedGC::ThreadedGC (NodePoolThreadedGC.hpp:394-403): roots
+	 * remapped in place; the mirror is stale afterwards (Download again). */
+	hd_status GC(std::span<uint32_t> roots, hd_gc_stats *stats = nullptr) {
+		return hd_gc(m_pool, roots.data(), (uint32_t)roots.size(), stats);
+	}
+	/* m_filled_node_pointers (NodePool.hpp:54), one per level. */
+	hd_status FilledPointers(std::vector<uint32_t> *out) const {
+		out->assign(GetHdConfig().node_levels, HD_NULL_PTR);
+		return hd_pool_filled_pointers(m_pool, out->data());
+	}
+	/* SetRoot / GetRoot (src/DAGNodePool.hpp:96-97): the root the renderer traces. */
+	void SetRoot(uint32_t root) { m_root = root; }
+	uint32_t GetRoot() const { return m_root; }
+
+	/* ---- host mirror */
+	HostPoolMirror &Mirror() { return m_mirror; }
+	const HostPoolMirror &Mirror() const { return m_mirror; }
+	/* Device -> mirror: every bucket's word count and every page that holds
+	 * data (the words the reference's hooks would hold); the mirror's other
+	 * pages are dropped.  Waits for the pool's queued passes. */
+	hd_status Download() {
+		HostPoolMirror &m = m_mirror;
+		std::vector<uint32_t> counts(m.TotalBuckets());
+		hd_status s = hd_pool_read_bucket_words(m_pool, 0, m.TotalBuckets(), counts.data());
+		if (s != HD_OK)
+			return s;
+		std::vector<uint8_t> map(m.TotalPages());
+		if ((s = hd_pool_read_page_map(m_pool, map.data())) != HD_OK)
+			return s;
+		std::vector<uint32_t> ids;
+		for (uint32_t i = 0; i < m.TotalPages(); ++i)
+			if (map[i])
+				ids.push_back(i);
+		m.Clear();
+		for (uint32_t b = 0; b < m.TotalBuckets(); ++b)
+			m.GetBucketRefWords(b) = counts[b];
+		const uint32_t wpp = m.WordsPerPage();
+		const uint32_t chunk = kChunkWords / wpp ? kChunkWords / wpp : 1u;
+		std::vector<uint32_t> words((size_t)chunk * wpp);
+		for (size_t first = 0; first < ids.size(); first += chunk) {
+			const uint32_t n = (uint32_t)std::min<size_t>(chunk, ids.size() - first);
+			if ((s = hd_pool_read_pages(m_pool, ids.data() + first, n, words.data())) != HD_OK)
+				return s;
+			for (uint32_t k = 0; k < n; ++k)
+				m.SetPage(ids[first + k], words.data() + (size_t)k * wpp);
+		}
+		return HD_OK;
+	}
+	/* Mirror -> device: replaces the device pool with the mirror's words
+	 * (bucket counts and every page that holds data), rebuilds the dedup index
+	 * and finds the filled nodes again; the mirror is clean afterwards.  Roots
+	 * made on the device before the call are valid only if the mirror holds
+	 * their nodes. */
+	hd_status Upload() {
+		HostPoolMirror &m = m_mirror;
+		const std::vector<uint32_t> ids = m.PageIds();
+		const uint32_t wpp = m.WordsPerPage();
+		std::vector<uint32_t> words(ids.size() * (size_t)wpp);
+		for (size_t k = 0; k < ids.size(); ++k)
+			std::copy(m.ReadPage(ids[k]), m.ReadPage(ids[k]) + wpp, words.data() + k * wpp);
+		const hd_status s = hd_pool_upload(m_pool, m.BucketWords().data(), ids.data(), (uint32_t)ids.size(),
+		                                   words.data(), nullptr);
+		if (s == HD_OK)
+			m.ClearDirty();
+		return s;
+	}
+
+	/* The reference's storage hooks, on the mirror (NodePool.hpp:22-38). */
+	uint32_t &GetBucketRefWords(uint32_t bucket_id) { return m_mirror.GetBucketRefWords(bucket_id); }
+	const uint32_t *ReadPage(uint32_t page_id) const { return m_mirror.ReadPage(page_id); }
+	void ZeroPage(uint32_t page_id, uint32_t page_offset, uint32_t zero_words) {
+		m_mirror.ZeroPage(page_id, page_offset, zero_words);
+	}
+	void WritePage(uint32_t page_id, uint32_t page_offset, std::span<const uint32_t> word_span) {
+		m_mirror.WritePage(page_id, page_offset, word_span);
+	}
+	std::mutex &GetBucketRefMutex(uint32_t bucket_id) { return m_mirror.GetBucketRefMutex(bucket_id); }
+	void FreePage(uint32_t page_id) { m_mirror.FreePage(page_id); }
+
+private:
+	static constexpr uint32_t kChunkWords = 1u << 24; // 64 MB of page words per read
+
+	GpuNodePool(hd_pool *pool, const hd_config &config) : m_pool(pool), m_mirror(config) {}
+
+	hd_pool *m_pool;
+	HostPoolMirror m_mirror;
+	uint32_t m_root = HD_NULL_PTR;
+};
+
+} // namespace hashdag_gb300

@@ -5,8 +5,8 @@
 // reference tree is present, into oracle/_ref/.  It executes the reference's
 // NodePoolBase::Edit, NodePoolThreadedEdit::ThreadedEdit,
 // NodePoolBase::upsert_inner_node / upsert_leaf, NodePoolThreadedGC::ThreadedGC
-// and NodePoolTraversal::Traversal on a vector-backed pool whose storage hooks
-// follow src/DAGNodePool.hpp:56-69, and dumps the resulting pool, so the
+// and NodePoolTraversal::Traversal on the product's host pool mirror (whose
+// storage hooks follow src/DAGNodePool.hpp:56-69), and dumps the resulting pool, so the
 // oracle restatement can be pinned against the reference and golden fixtures
 // can be generated.  The editors restate the stateless SphereEditor<kFill/kDig>
 // and AABBEditor of src/main.cpp:32-150 (they live in the application, not the
@@ -52,6 +52,7 @@
 #include <vector>
 
 #include "../include/hashdag_gpu.h"
+#include "../include/hashdag_host_mirror.hpp"
 
 struct ZeroHasher {
 	inline uint32_t operator()(auto &&) const { return 0; }
@@ -61,38 +62,26 @@ struct ZeroHasher {
 template <typename K, typename V> using GcMap = phmap::flat_hash_map<K, V>;
 template <typename K> using GcSet = phmap::flat_hash_set<K>;
 
+// The pool's storage is the product's host mirror (include/hashdag_host_mirror.hpp,
+// whose hooks follow src/DAGNodePool.hpp:56-74): every run of the reference's
+// algorithms below goes through those hooks, and the static_asserts check that
+// the mirror satisfies the reference's storage concepts.
 template <typename HasherT>
-struct RefPool final : public hashdag::NodePoolBase<RefPool<HasherT>, uint32_t>,
+struct RefPool final : public hashdag_gb300::HostPoolMirror,
+                       public hashdag::NodePoolBase<RefPool<HasherT>, uint32_t>,
                        public hashdag::NodePoolThreadedEdit<RefPool<HasherT>, uint32_t>,
                        public hashdag::NodePoolThreadedGC<RefPool<HasherT>, uint32_t, GcMap, GcSet>,
                        public hashdag::NodePoolTraversal<RefPool<HasherT>, uint32_t> {
 	using WordSpanHasher = HasherT;
 	using Base = hashdag::NodePoolBase<RefPool<HasherT>, uint32_t>;
 
-	std::unique_ptr<uint32_t[]> bucket_words;
-	std::vector<std::unique_ptr<uint32_t[]>> pages;
-	std::array<std::mutex, 1024> mutexes{};
-
-	explicit RefPool(const hashdag::Config<uint32_t> &config) : Base(config) {
-		bucket_words = std::make_unique<uint32_t[]>(this->GetConfig().GetTotalBuckets());
-		pages.resize(this->GetConfig().GetTotalPages());
-	}
+	RefPool(const hashdag::Config<uint32_t> &config, const hd_config &hc)
+	    : hashdag_gb300::HostPoolMirror(hc), Base(config) {}
 	~RefPool() final = default;
-
-	std::mutex &GetBucketRefMutex(uint32_t b) { return mutexes[b % mutexes.size()]; }
-	uint32_t &GetBucketRefWords(uint32_t b) { return bucket_words[b]; }
-	const uint32_t *ReadPage(uint32_t p) const { return pages[p].get(); }
-	uint32_t *page(uint32_t p) {
-		if (!pages[p])
-			pages[p] = std::make_unique<uint32_t[]>(this->GetConfig().GetWordsPerPage()); // zeroed
-		return pages[p].get();
-	}
-	void ZeroPage(uint32_t p, uint32_t off, uint32_t n) { std::fill(page(p) + off, page(p) + off + n, 0u); }
-	void WritePage(uint32_t p, uint32_t off, std::span<const uint32_t> s) {
-		std::copy(s.begin(), s.end(), page(p) + off);
-	}
-	void FreePage(uint32_t p) { pages[p].reset(); }
 };
+static_assert(hashdag::NodePool<RefPool<hashdag::MurmurHasher32>, uint32_t>);
+static_assert(hashdag::ThreadedNodePool<RefPool<hashdag::MurmurHasher32>, uint32_t>);
+static_assert(hashdag::GCNodePool<RefPool<hashdag::MurmurHasher32>, uint32_t>);
 
 // Stateless editors (src/main.cpp:32-150) for one hd_edit_desc.
 struct DescEditor {
@@ -316,12 +305,13 @@ static uint32_t rd(FILE *f) {
 }
 static void wr(FILE *f, uint32_t v) { fwrite(&v, 4, 1, f); }
 
-template <typename HasherT> static int run(FILE *in, FILE *out, uint32_t mode, const hashdag::Config<uint32_t> &config) {
+template <typename HasherT>
+static int run(FILE *in, FILE *out, uint32_t mode, const hashdag::Config<uint32_t> &config, const hd_config &hc) {
 	uint32_t threads = rd(in), max_task_level = rd(in), n_edits = rd(in);
 	std::vector<hd_edit_desc> edits(n_edits);
 	if (n_edits && fread(edits.data(), sizeof(hd_edit_desc), n_edits, in) != n_edits)
 		return 2;
-	auto pool = std::make_unique<RefPool<HasherT>>(config);
+	auto pool = std::make_unique<RefPool<HasherT>>(config, hc);
 	hashdag::NodePointer<uint32_t> root{};
 	std::vector<uint32_t> upsert_ptrs;
 	std::vector<float> rays;
@@ -434,16 +424,13 @@ template <typename HasherT> static int run(FILE *in, FILE *out, uint32_t mode, c
 		wr(out, pool->m_filled_node_pointers.empty() ? 0xFFFFFFFFu : *pool->m_filled_node_pointers[l]);
 	uint32_t tb = config.GetTotalBuckets();
 	wr(out, tb);
-	fwrite(pool->bucket_words.get(), 4, tb, out);
-	uint32_t np = 0;
-	for (auto &p : pool->pages)
-		np += p ? 1 : 0;
-	wr(out, np);
-	for (uint32_t i = 0; i < pool->pages.size(); ++i)
-		if (pool->pages[i]) {
-			wr(out, i);
-			fwrite(pool->pages[i].get(), 4, config.GetWordsPerPage(), out);
-		}
+	fwrite(pool->BucketWords().data(), 4, tb, out);
+	const std::vector<uint32_t> page_ids = pool->PageIds();
+	wr(out, (uint32_t)page_ids.size());
+	for (uint32_t i : page_ids) {
+		wr(out, i);
+		fwrite(pool->ReadPage(i), 4, config.GetWordsPerPage(), out);
+	}
 	if (mode == 4) {
 		wr(out, (uint32_t)kept.size());
 		for (uint32_t v : kept_before)
@@ -512,10 +499,17 @@ int main(int argc, char **argv) {
 	uint32_t L = rd(in), hasher = rd(in);
 	for (uint32_t l = 0; l < L; ++l)
 		config.bucket_bits_each_level.push_back(rd(in));
-	if (!hashdag::Config<uint32_t>::Validate(config))
+	if (L > HD_MAX_LEVELS || !hashdag::Config<uint32_t>::Validate(config))
 		return 3;
-	int rc = hasher == HD_HASHER_ZERO ? run<ZeroHasher>(in, out, mode, config)
-	                                  : run<hashdag::MurmurHasher32>(in, out, mode, config);
+	hd_config hc{};
+	hc.word_bits_per_page = config.word_bits_per_page;
+	hc.page_bits_per_bucket = config.page_bits_per_bucket;
+	hc.node_levels = L;
+	hc.hasher = hasher;
+	for (uint32_t l = 0; l < L; ++l)
+		hc.bucket_bits_each_level[l] = config.bucket_bits_each_level[l];
+	int rc = hasher == HD_HASHER_ZERO ? run<ZeroHasher>(in, out, mode, config, hc)
+	                                  : run<hashdag::MurmurHasher32>(in, out, mode, config, hc);
 	fclose(in);
 	fclose(out);
 	return rc;
