@@ -258,6 +258,13 @@ hd_status hd_pool_read_pages(const hd_pool *pool, const uint32_t *page_ids, uint
  * filled-node pointer per level (NULL = recompute).  Rebuilds the dedup index. */
 hd_status hd_pool_upload(hd_pool *pool, const uint32_t *bucket_words, const uint32_t *page_ids, uint32_t n_pages,
                          const uint32_t *page_words, const uint32_t *filled_levels);
+/* Generation of the pool's committed words, for incremental host mirrors (the
+ * dirty page ranges of src/DAGNodePool.hpp:62-69): every call that rewrites or
+ * drops words already in the pool (hd_gc, hd_pool_rollback, hd_pool_upload)
+ * increments it.  Between two calls that read the same epoch the pool only
+ * appended words: bucket b's new words are [old count, new count) of
+ * hd_pool_read_bucket_words, on the pages that range covers. */
+hd_status hd_pool_epoch(const hd_pool *pool, uint64_t *out);
 
 /* ---- garbage collection -----------------------------------------------------
  * NodePoolThreadedGC::ThreadedGC (include/hashdag/NodePoolThreadedGC.hpp:29-403):

@@ -13,9 +13,11 @@
  *   auto pool = hashdag_gb300::GpuNodePool::Create(config);   // nullptr on failure
  *   uint32_t root = HD_NULL_PTR;
  *   pool->Edit(root, edits, &root);                          // one batched pass
- *   pool->Download();                                        // device -> mirror
- *   ... read or edit the mirror (ReadPage, GetBucketRefWords, ...) ...
+ *   pool->Publish();                                         // device -> mirror, what changed
+ *   ... flush pool->Mirror()'s written ranges and freed pages, ClearDirty ...
+ *   ... or read / edit the mirror (ReadPage, GetBucketRefWords, ...) ...
  *   pool->Upload();                                          // mirror -> device
+ *   pool->Mirror().Save("pool.hdmp");                        // a checkpoint file
  *
  * Header-only C++20 over libhashdag_gb300.so.  Every call returns the
  * library's hd_status; nothing falls back to the CPU.
@@ -25,6 +27,7 @@
 #include "hashdag_gpu.h"
 #include "hashdag_host_mirror.hpp"
 
+#include <algorithm>
 #include <cstdint>
 #include <memory>
 #include <mutex>
@@ -64,7 +67,8 @@ public:
 		return hd_edit(m_pool, root, edits.data(), (uint32_t)edits.size(), new_root, stream);
 	}
 	/* NodePoolThreadedGC::ThreadedGC (NodePoolThreadedGC.hpp:394-403): roots
-	 * remapped in place; the mirror is stale afterwards (Download again). */
+	 * remapped in place; the mirror is stale afterwards (the next Publish
+	 * reads everything). */
 	hd_status GC(std::span<uint32_t> roots, hd_gc_stats *stats = nullptr) {
 		return hd_gc(m_pool, roots.data(), (uint32_t)roots.size(), stats);
 	}
@@ -82,12 +86,17 @@ public:
 	const HostPoolMirror &Mirror() const { return m_mirror; }
 	/* Device -> mirror: every bucket's word count and every page that holds
 	 * data (the words the reference's hooks would hold); the mirror's other
-	 * pages are dropped.  Waits for the pool's queued passes. */
+	 * pages are dropped and nothing is marked dirty.  Waits for the pool's
+	 * queued passes. */
 	hd_status Download() {
 		HostPoolMirror &m = m_mirror;
-		std::vector<uint32_t> counts(m.TotalBuckets());
-		hd_status s = hd_pool_read_bucket_words(m_pool, 0, m.TotalBuckets(), counts.data());
+		uint64_t epoch = 0;
+		hd_status s = hd_pool_epoch(m_pool, &epoch);
 		if (s != HD_OK)
+			return s;
+		m_synced = false;
+		std::vector<uint32_t> counts(m.TotalBuckets());
+		if ((s = hd_pool_read_bucket_words(m_pool, 0, m.TotalBuckets(), counts.data())) != HD_OK)
 			return s;
 		std::vector<uint8_t> map(m.TotalPages());
 		if ((s = hd_pool_read_page_map(m_pool, map.data())) != HD_OK)
@@ -109,13 +118,72 @@ public:
 			for (uint32_t k = 0; k < n; ++k)
 				m.SetPage(ids[first + k], words.data() + (size_t)k * wpp);
 		}
+		m_epoch = epoch;
+		m_synced = true;
+		return HD_OK;
+	}
+	/* Device -> mirror, only what changed: the dirty-range publish of the
+	 * application's pool (src/DAGNodePool.hpp:62-69, Flush in
+	 * src/DAGNodePool.cpp:56-85).  While the pool's epoch (hd_pool_epoch) is
+	 * the one of the mirror's last sync the pool only appended, so only the
+	 * pages covering each bucket's new words are read, and those words become
+	 * the pages' written ranges.  After a GC, rollback or upload (a new epoch),
+	 * or before the first sync, everything is read: each page the pool holds
+	 * then counts as written in full and each page it no longer holds as
+	 * freed.  Dirty state accumulates until ClearDirty.  *full (may be NULL)
+	 * tells which form ran.  No other thread may rewrite the pool meanwhile. */
+	hd_status Publish(bool *full = nullptr) {
+		HostPoolMirror &m = m_mirror;
+		uint64_t epoch = 0;
+		hd_status s = hd_pool_epoch(m_pool, &epoch);
+		if (s != HD_OK)
+			return s;
+		std::vector<uint32_t> counts(m.TotalBuckets());
+		std::vector<AppendedPage> pages;
+		bool incremental = m_synced && epoch == m_epoch;
+		if (incremental) {
+			if ((s = hd_pool_read_bucket_words(m_pool, 0, m.TotalBuckets(), counts.data())) != HD_OK)
+				return s;
+			incremental = m.AppendedPages(counts, &pages);
+		}
+		if (full)
+			*full = !incremental;
+		if (!incremental)
+			return publish_all();
+		const uint32_t wpp = m.WordsPerPage();
+		const uint32_t chunk = kChunkWords / wpp ? kChunkWords / wpp : 1u;
+		std::vector<uint32_t> ids, words((size_t)chunk * wpp);
+		for (size_t first = 0; first < pages.size(); first += chunk) {
+			const uint32_t n = (uint32_t)std::min<size_t>(chunk, pages.size() - first);
+			ids.clear();
+			for (uint32_t k = 0; k < n; ++k)
+				ids.push_back(pages[first + k].page_id);
+			if ((s = hd_pool_read_pages(m_pool, ids.data(), n, words.data())) != HD_OK)
+				return s;
+			for (uint32_t k = 0; k < n; ++k) {
+				const PageRange r = pages[first + k].words;
+				m.WritePage(ids[k], r.begin,
+				            std::span<const uint32_t>(words.data() + (size_t)k * wpp + r.begin, r.end - r.begin));
+			}
+		}
+		for (uint32_t b = 0; b < m.TotalBuckets(); ++b)
+			m.GetBucketRefWords(b) = counts[b];
+		uint64_t after = 0;
+		if ((s = hd_pool_epoch(m_pool, &after)) != HD_OK)
+			return s;
+		if (after != epoch) { // rewritten while it was read
+			if (full)
+				*full = true;
+			return publish_all();
+		}
 		return HD_OK;
 	}
 	/* Mirror -> device: replaces the device pool with the mirror's words
 	 * (bucket counts and every page that holds data), rebuilds the dedup index
-	 * and finds the filled nodes again; the mirror is clean afterwards.  Roots
-	 * made on the device before the call are valid only if the mirror holds
-	 * their nodes. */
+	 * and finds the filled nodes again (appending them if the mirror lacks
+	 * them; the mirror then receives those words as written ranges, else it is
+	 * clean afterwards).  Roots made on the device before the call are valid
+	 * only if the mirror holds their nodes. */
 	hd_status Upload() {
 		HostPoolMirror &m = m_mirror;
 		const std::vector<uint32_t> ids = m.PageIds();
@@ -123,11 +191,19 @@ public:
 		std::vector<uint32_t> words(ids.size() * (size_t)wpp);
 		for (size_t k = 0; k < ids.size(); ++k)
 			std::copy(m.ReadPage(ids[k]), m.ReadPage(ids[k]) + wpp, words.data() + k * wpp);
-		const hd_status s = hd_pool_upload(m_pool, m.BucketWords().data(), ids.data(), (uint32_t)ids.size(),
-		                                   words.data(), nullptr);
-		if (s == HD_OK)
-			m.ClearDirty();
-		return s;
+		hd_status s = hd_pool_upload(m_pool, m.BucketWords().data(), ids.data(), (uint32_t)ids.size(), words.data(),
+		                             nullptr);
+		m_synced = false;
+		if (s != HD_OK)
+			return s;
+		m.ClearDirty();
+		// the upload found or inserted the filled nodes: bring their words over
+		uint64_t epoch = 0;
+		if ((s = hd_pool_epoch(m_pool, &epoch)) != HD_OK)
+			return s;
+		m_epoch = epoch;
+		m_synced = true;
+		return Publish();
 	}
 
 	/* The reference's storage hooks, on the mirror (NodePool.hpp:22-38). */
@@ -145,11 +221,30 @@ public:
 private:
 	static constexpr uint32_t kChunkWords = 1u << 24; // 64 MB of page words per read
 
+	hd_status publish_all() {
+		HostPoolMirror &m = m_mirror;
+		std::vector<uint8_t> had(m.TotalPages());
+		for (uint32_t i = 0; i < m.TotalPages(); ++i)
+			had[i] = m.HasPage(i) || m.IsFreed(i);
+		const hd_status s = Download();
+		if (s != HD_OK)
+			return s;
+		for (uint32_t i = 0; i < m.TotalPages(); ++i) {
+			if (m.HasPage(i))
+				m.MarkWritten(i, PageRange{0u, m.WordsPerPage()});
+			else if (had[i])
+				m.FreePage(i);
+		}
+		return HD_OK;
+	}
+
 	GpuNodePool(hd_pool *pool, const hd_config &config) : m_pool(pool), m_mirror(config) {}
 
 	hd_pool *m_pool;
 	HostPoolMirror m_mirror;
 	uint32_t m_root = HD_NULL_PTR;
+	uint64_t m_epoch = 0; // hd_pool_epoch at the mirror's last full or incremental sync
+	bool m_synced = false;
 };
 
 } // namespace hashdag_gb300

@@ -1,8 +1,9 @@
 // gpu_pool_check.cpp -- checks of the C++ host side of the pool
-// (include/hashdag_gpu_pool.hpp, include/hashdag_host_mirror.hpp), linked
-// against libhashdag_gb300.so by tests/test_cpp_pool.py.
+// (include/hashdag_gpu_pool.hpp, include/hashdag_host_mirror.hpp), built by
+// tests/test_cpp_pool.py.
 //
-//   gpu_pool_check mirror    HostPoolMirror's storage hooks on their own
+// Linked against libhashdag_gb300.so:
+//   gpu_pool_check mirror    HostPoolMirror's storage hooks and bookkeeping
 //   gpu_pool_check nodevice  GpuNodePool::Create with no usable device:
 //                            nullptr and HD_ERR_NO_DEVICE, like DAGNodePool::Create
 //   gpu_pool_check device    on a GPU: edits on the device, Download into the
@@ -10,12 +11,22 @@
 //                            (word for word the same pool, same filled
 //                            pointers), the same further edits on both, and
 //                            occupancy against the edits' own predicates;
-//                            then GC through the class and the same check.
+//                            then GC through the class and the same check
+//   gpu_pool_check publish   on a GPU: incremental Publish after edits equals a
+//                            full Download; after a GC it re-reads everything
+// Built with -DHD_FAKE_DEVICE instead (no library, no GPU): the pool entry
+// points GpuNodePool calls are served by an in-memory pool below, and
+//   gpu_pool_check fake_publish   Publish: full on the first sync and after an
+//                                 epoch change (freed pages reported), else
+//                                 only the appended words, as written ranges
+//   gpu_pool_check dump           Save / Load of a pool dump
+//   gpu_pool_check dump_copy IN OUT   Load IN, Save OUT (format round trips)
 // Prints "ok <mode>" and exits 0, or prints the first failure and exits 1.
 #include "hashdag_gpu_pool.hpp"
 
 #include <cstdio>
 #include <cstring>
+#include <string>
 #include <vector>
 
 using hashdag_gb300::GpuNodePool;
@@ -37,12 +48,87 @@ using hashdag_gb300::HostPoolMirror;
 		}                                                                                                             \
 	} while (0)
 
+#ifdef HD_FAKE_DEVICE
+// DefaultConfig for a 256^3 grid written out (hd_config_default lives in the library)
+static hd_config small_config() {
+	hd_config c{};
+	c.word_bits_per_page = 9;
+	c.page_bits_per_bucket = 2;
+	c.node_levels = 7;
+	c.hasher = HD_HASHER_MURMUR32;
+	for (uint32_t l = 0; l < 7; ++l)
+		c.bucket_bits_each_level[l] = 10;
+	return c;
+}
+
+// The pool entry points GpuNodePool calls, on an in-memory pool: its words in
+// a HostPoolMirror and the epoch the library keeps (hd_pool_epoch).
+struct hd_pool {
+	explicit hd_pool(const hd_config &c) : words(c) {}
+	HostPoolMirror words;
+	uint64_t epoch = 0;
+};
+extern "C" {
+hd_status hd_pool_create(const hd_config *config, uint64_t, uint32_t, int, hd_pool **out) {
+	*out = new hd_pool(*config);
+	return HD_OK;
+}
+void hd_pool_destroy(hd_pool *p) { delete p; }
+hd_status hd_pool_epoch(const hd_pool *p, uint64_t *out) {
+	*out = p->epoch;
+	return HD_OK;
+}
+hd_status hd_pool_read_bucket_words(const hd_pool *p, uint32_t first, uint32_t count, uint32_t *out) {
+	if ((uint64_t)first + count > p->words.TotalBuckets())
+		return HD_ERR_INVALID_ARG;
+	std::copy(p->words.BucketWords().begin() + first, p->words.BucketWords().begin() + first + count, out);
+	return HD_OK;
+}
+hd_status hd_pool_read_page_map(const hd_pool *p, uint8_t *out) {
+	for (uint32_t i = 0; i < p->words.TotalPages(); ++i)
+		out[i] = p->words.HasPage(i) ? 1 : 0;
+	return HD_OK;
+}
+hd_status hd_pool_read_pages(const hd_pool *p, const uint32_t *ids, uint32_t n, uint32_t *out) {
+	const uint32_t wpp = p->words.WordsPerPage();
+	for (uint32_t k = 0; k < n; ++k) {
+		if (ids[k] >= p->words.TotalPages())
+			return HD_ERR_INVALID_ARG;
+		const uint32_t *w = p->words.ReadPage(ids[k]);
+		for (uint32_t i = 0; i < wpp; ++i)
+			out[(size_t)k * wpp + i] = w ? w[i] : 0u; // an unmapped page reads as zeros
+	}
+	return HD_OK;
+}
+hd_status hd_pool_upload(hd_pool *p, const uint32_t *bucket_words, const uint32_t *ids, uint32_t n,
+                         const uint32_t *page_words, const uint32_t *) {
+	++p->epoch;
+	p->words.Clear();
+	for (uint32_t b = 0; b < p->words.TotalBuckets(); ++b)
+		p->words.GetBucketRefWords(b) = bucket_words[b];
+	for (uint32_t k = 0; k < n; ++k)
+		p->words.SetPage(ids[k], page_words + (size_t)k * p->words.WordsPerPage());
+	return HD_OK;
+}
+const char *hd_status_string(hd_status) { return "status"; }
+}
+#else
 static hd_config small_config() {
 	hd_config c;
 	// DefaultConfig for a 256^3 grid: level_count 8, 9 top levels of 2^10
 	// buckets (so every one of the 7 node levels), 512-word pages, 4 per bucket
 	hd_config_default(8, 9, 9, 2, 10, 16, &c);
 	return c;
+}
+#endif
+
+static bool same_mirror(const HostPoolMirror &a, const HostPoolMirror &b) {
+	if (a.BucketWords() != b.BucketWords() || a.PageIds() != b.PageIds())
+		return false;
+	for (uint32_t id : a.PageIds())
+		if (std::memcmp(a.ReadPage(id), b.ReadPage(id), a.WordsPerPage() * 4u) != 0)
+			return false;
+	return true;
 }
 
 static int check_mirror() {
@@ -79,6 +165,7 @@ static int check_mirror() {
 	return 0;
 }
 
+#ifndef HD_FAKE_DEVICE
 static int check_nodevice() {
 	hd_status s = HD_OK;
 	auto pool = GpuNodePool::Create(small_config(), 0, 0, &s);
@@ -145,15 +232,6 @@ static int check_occupancy(GpuNodePool &pool, uint32_t root, const std::vector<h
 	}
 	*set_out = set;
 	return 0;
-}
-
-static bool same_mirror(const HostPoolMirror &a, const HostPoolMirror &b) {
-	if (a.BucketWords() != b.BucketWords() || a.PageIds() != b.PageIds())
-		return false;
-	for (uint32_t id : a.PageIds())
-		if (std::memcmp(a.ReadPage(id), b.ReadPage(id), a.WordsPerPage() * 4u) != 0)
-			return false;
-	return true;
 }
 
 static int check_device() {
@@ -228,18 +306,238 @@ static int check_device() {
 	return 0;
 }
 
+
+// Incremental publish on a device that only appended: after one Publish, the
+// real-device form must give the mirror a full Download gives, and a GC makes
+// the next Publish read everything.
+static int check_publish() {
+	const hd_config c = small_config();
+	hd_status s = HD_OK;
+	auto a = GpuNodePool::Create(c, 0, 0, &s);
+	CHECK_OK(s);
+	bool full = false;
+	CHECK_OK(a->Publish(&full));
+	CHECK(full);
+	uint32_t root = HD_NULL_PTR;
+	const std::vector<hd_edit_desc> e1 = {sphere(HD_OP_FILL, 128, 128, 128, 60), box(HD_OP_DIG, 100, 0, 0, 256, 140, 256)};
+	CHECK_OK(a->Edit(HD_NULL_PTR, e1, &root));
+	a->Mirror().ClearDirty();
+	CHECK_OK(a->Publish(&full));
+	CHECK(!full);
+	uint32_t dirty = 0;
+	for (uint32_t id = 0; id < a->Mirror().TotalPages(); ++id)
+		dirty += a->Mirror().IsDirty(id) ? 1u : 0u;
+	CHECK(dirty > 0);
+	const std::vector<hd_edit_desc> e2 = {sphere(HD_OP_DIG, 90, 160, 100, 40), box(HD_OP_FILL, 0, 0, 0, 60, 250, 30)};
+	uint32_t root2 = HD_NULL_PTR;
+	CHECK_OK(a->Edit(root, e2, &root2));
+	CHECK_OK(a->Publish(&full));
+	CHECK(!full);
+	// the same words as a full read of the device
+	HostPoolMirror &m = a->Mirror();
+	std::vector<uint32_t> counts(m.TotalBuckets());
+	CHECK_OK(hd_pool_read_bucket_words(a->Handle(), 0, m.TotalBuckets(), counts.data()));
+	CHECK(counts == m.BucketWords());
+	std::vector<uint8_t> map(m.TotalPages());
+	CHECK_OK(hd_pool_read_page_map(a->Handle(), map.data()));
+	std::vector<uint32_t> words(m.WordsPerPage());
+	for (uint32_t id = 0; id < m.TotalPages(); ++id) {
+		CHECK((map[id] != 0) == m.HasPage(id));
+		if (!map[id])
+			continue;
+		CHECK_OK(hd_pool_read_pages(a->Handle(), &id, 1, words.data()));
+		CHECK(std::memcmp(words.data(), m.ReadPage(id), m.WordsPerPage() * 4u) == 0);
+	}
+	// a collection rewrites: the next Publish reads everything
+	uint32_t keep[1] = {root2};
+	CHECK_OK(a->GC(std::span<uint32_t>(keep, 1)));
+	m.ClearDirty();
+	CHECK_OK(a->Publish(&full));
+	CHECK(full);
+	CHECK_OK(hd_pool_read_bucket_words(a->Handle(), 0, m.TotalBuckets(), counts.data()));
+	CHECK(counts == m.BucketWords());
+	return 0;
+}
+#else
+static uint64_t g_rng = 0x9E3779B97F4A7C15ull;
+static uint32_t rnd(uint32_t n) {
+	g_rng ^= g_rng << 13, g_rng ^= g_rng >> 7, g_rng ^= g_rng << 17;
+	return (uint32_t)(g_rng >> 32) % n;
+}
+
+// Appends a node of n words to bucket b the way upsert_node does
+// (include/hashdag/NodePool.hpp:159-212): a node that would straddle a page
+// starts on the next one (the skipped tail stays zero).
+static bool append_node(HostPoolMirror &m, uint32_t b, uint32_t n) {
+	const hd_config &c = m.MirrorConfig();
+	const uint32_t wpp = m.WordsPerPage(), wpb = wpp << c.page_bits_per_bucket;
+	uint32_t at = m.GetBucketRefWords(b);
+	if ((at & (wpp - 1u)) + n > wpp)
+		at = (at + wpp - 1u) & ~(wpp - 1u);
+	if (at + n > wpb)
+		return false;
+	std::vector<uint32_t> w(n);
+	for (auto &x : w)
+		x = 1u + rnd(0xFFFFFFF0u);
+	m.WritePage((b << c.page_bits_per_bucket) | (at >> c.word_bits_per_page), at & (wpp - 1u), w);
+	m.GetBucketRefWords(b) = at + n;
+	return true;
+}
+static void append_nodes(HostPoolMirror &m, int count, uint32_t buckets) {
+	for (int i = 0; i < count; ++i)
+		append_node(m, rnd(buckets), 2u + rnd(8));
+}
+
+// Publish against the in-memory pool: the first sync and every epoch change
+// read everything (present pages written in full, vanished pages freed);
+// otherwise exactly the words appended since, as each page's written range.
+static int check_fake_publish() {
+	const hd_config c = small_config();
+	auto pool = GpuNodePool::Create(c);
+	CHECK(pool != nullptr);
+	hd_pool *dev = pool->Handle();
+	HostPoolMirror &m = pool->Mirror();
+	const uint32_t wpp = m.WordsPerPage();
+	append_nodes(dev->words, 3000, 64);
+	bool full = false;
+	CHECK_OK(pool->Publish(&full));
+	CHECK(full && same_mirror(dev->words, m));
+	for (uint32_t id = 0; id < m.TotalPages(); ++id)
+		CHECK(m.HasPage(id) ? m.WrittenRange(id) == (hashdag_gb300::PageRange{0, wpp}) : !m.IsDirty(id));
+	m.ClearDirty();
+	for (int round = 0; round < 4; ++round) {
+		const std::vector<uint32_t> before = dev->words.BucketWords();
+		append_nodes(dev->words, 500 + 700 * round, 64 + 200 * round);
+		CHECK_OK(pool->Publish(&full));
+		CHECK(!full && same_mirror(dev->words, m));
+		// the written range of every page: the words [old, new) of its bucket on it
+		std::vector<hashdag_gb300::PageRange> want(m.TotalPages());
+		for (uint32_t b = 0; b < m.TotalBuckets(); ++b)
+			for (uint32_t w = before[b]; w < dev->words.BucketWords()[b]; ++w) {
+				const uint32_t page = (b << c.page_bits_per_bucket) | (w >> c.word_bits_per_page);
+				want[page].unite(w & (wpp - 1u), (w & (wpp - 1u)) + 1u);
+			}
+		for (uint32_t id = 0; id < m.TotalPages(); ++id)
+			CHECK(m.WrittenRange(id) == want[id] && !m.IsFreed(id));
+		m.ClearDirty();
+	}
+	CHECK_OK(pool->Publish(&full)); // nothing new
+	CHECK(!full);
+	for (uint32_t id = 0; id < m.TotalPages(); ++id)
+		CHECK(!m.IsDirty(id));
+	// a rewrite (as a collection does): buckets 0..9 emptied, their pages freed,
+	// another bucket's words changed in place
+	++dev->epoch;
+	std::vector<uint32_t> gone;
+	for (uint32_t b = 0; b < 10; ++b) {
+		for (uint32_t p = 0; p < (1u << c.page_bits_per_bucket); ++p) {
+			const uint32_t id = (b << c.page_bits_per_bucket) | p;
+			if (dev->words.HasPage(id)) {
+				dev->words.FreePage(id);
+				gone.push_back(id);
+			}
+		}
+		dev->words.GetBucketRefWords(b) = 0;
+	}
+	CHECK(!gone.empty());
+	const uint32_t w7 = 7u;
+	dev->words.WritePage(20u << c.page_bits_per_bucket, 0, std::span<const uint32_t>(&w7, 1));
+	CHECK_OK(pool->Publish(&full));
+	CHECK(full && same_mirror(dev->words, m));
+	for (uint32_t id : gone)
+		CHECK(m.IsFreed(id) && !m.HasPage(id));
+	for (uint32_t id = 0; id < m.TotalPages(); ++id)
+		if (m.HasPage(id))
+			CHECK(m.WrittenRange(id) == (hashdag_gb300::PageRange{0, wpp}));
+	m.ClearDirty();
+	// a count that went down within an epoch is not an append: full read
+	dev->words.GetBucketRefWords(30) = dev->words.GetBucketRefWords(30) / 2;
+	CHECK_OK(pool->Publish(&full));
+	CHECK(full && same_mirror(dev->words, m));
+	m.ClearDirty();
+	// Upload: the device takes the mirror's words (a new epoch), and the next
+	// Publish has nothing to read
+	append_nodes(m, 200, 300);
+	const uint64_t e0 = dev->epoch;
+	CHECK_OK(pool->Upload());
+	CHECK(dev->epoch == e0 + 1 && same_mirror(dev->words, m));
+	for (uint32_t id = 0; id < m.TotalPages(); ++id)
+		CHECK(!m.IsDirty(id));
+	CHECK_OK(pool->Publish(&full));
+	CHECK(!full);
+	for (uint32_t id = 0; id < m.TotalPages(); ++id)
+		CHECK(!m.IsDirty(id));
+	return 0;
+}
+
+static int check_dump(const char *dir) {
+	const hd_config c = small_config();
+	HostPoolMirror m(c);
+	append_nodes(m, 4000, 500);
+	const std::string path = std::string(dir) + "/pool.hdmp";
+	CHECK(m.Save(path.c_str()));
+	HostPoolMirror n(c);
+	CHECK(n.Load(path.c_str()) && same_mirror(m, n));
+	for (uint32_t id = 0; id < n.TotalPages(); ++id)
+		CHECK(n.HasPage(id) ? n.WrittenRange(id) == (hashdag_gb300::PageRange{0, n.WordsPerPage()}) : !n.IsDirty(id));
+	hd_config other = c;
+	other.bucket_bits_each_level[3] = 9;
+	HostPoolMirror o(other);
+	CHECK(!o.Load(path.c_str()) && o.PageIds().empty());
+	// a truncated file is refused and leaves the mirror empty
+	FILE *f = std::fopen(path.c_str(), "rb");
+	CHECK(f != nullptr);
+	std::vector<char> bytes(1 << 20);
+	const size_t len = std::fread(bytes.data(), 1, bytes.size(), f);
+	std::fclose(f);
+	const std::string cut = std::string(dir) + "/cut.hdmp";
+	f = std::fopen(cut.c_str(), "wb");
+	CHECK(f != nullptr && std::fwrite(bytes.data(), 1, len / 2, f) == len / 2);
+	std::fclose(f);
+	HostPoolMirror t(c);
+	CHECK(!t.Load(cut.c_str()) && t.PageIds().empty() && t.BucketWords()[0] == 0);
+	return 0;
+}
+
+// Loads a dump (any configuration) and saves it again.
+static int dump_copy(const char *in, const char *out) {
+	FILE *f = std::fopen(in, "rb");
+	CHECK(f != nullptr);
+	hd_config c{};
+	char head[8];
+	CHECK(std::fread(head, 1, 8, f) == 8 && std::fread(&c, sizeof c, 1, f) == 1);
+	std::fclose(f);
+	HostPoolMirror m(c);
+	CHECK(m.Load(in));
+	CHECK(m.Save(out));
+	return 0;
+}
+#endif
+
 int main(int argc, char **argv) {
-	if (argc != 2) {
-		std::printf("usage: gpu_pool_check mirror|nodevice|device\n");
+	if (argc < 2) {
+		std::printf("usage: gpu_pool_check MODE [ARGS]\n");
 		return 2;
 	}
+	const std::string mode = argv[1];
 	int rc = 2;
-	if (!std::strcmp(argv[1], "mirror"))
+	if (mode == "mirror")
 		rc = check_mirror();
-	else if (!std::strcmp(argv[1], "nodevice"))
+#ifndef HD_FAKE_DEVICE
+	else if (mode == "nodevice")
 		rc = check_nodevice();
-	else if (!std::strcmp(argv[1], "device"))
+	else if (mode == "device")
 		rc = check_device();
+	else if (mode == "publish")
+		rc = check_publish();
+#else
+	else if (mode == "fake_publish")
+		rc = check_fake_publish();
+	else if (mode == "dump" && argc == 3)
+		rc = check_dump(argv[2]);
+	else if (mode == "dump_copy" && argc == 4)
+		rc = dump_copy(argv[2], argv[3]);
+#endif
 	if (rc == 0)
 		std::printf("ok %s\n", argv[1]);
 	return rc;

@@ -26,6 +26,7 @@ __all__ = [
     "NULL", "Config", "DefaultConfig", "EditMode", "SphereEditor", "AABBEditor", "NodePool",
     "HashDagError", "EDIT_DTYPE", "HIT_DTYPE", "CAMERA_DTYPE", "edits_to_array", "lib", "library_path",
     "count_voxel_edits", "device_available", "Server", "REQ_EDIT", "REQ_CAMERA", "projection_factor",
+    "write_pool_dump", "read_pool_dump",
 ]
 
 NULL = 0xFFFFFFFF
@@ -162,6 +163,7 @@ def lib():
         "hd_pool_read_page_map": (I, [P, P]),
         "hd_pool_read_pages": (I, [P, P, U32, P]),
         "hd_pool_upload": (I, [P, P, P, U32, P, P]),
+        "hd_pool_epoch": (I, [P, P]),
         "hd_query": (I, [P, U32, P, U32, P, P]),
         "hd_trace": (I, [P, U32, P, P, U32, P, P]),
         "hd_trace_pinhole_async": (I, [P, U32, P, U32, U32, U32, P, P, P]),
@@ -371,6 +373,61 @@ def count_voxel_edits(edits: np.ndarray, resolution: int) -> int:
     return int(lib().hd_count_voxel_edits(_ptr(edits), len(edits), resolution))
 
 
+_DUMP_MAGIC = b"HDMP"
+_DUMP_VERSION = 1
+
+
+def write_pool_dump(path: str, config: Config, bucket_words, page_ids, pages):
+    """Writes a pool dump, byte for byte the file HostPoolMirror::Save writes
+    (include/hashdag_host_mirror.hpp): "HDMP", version 1, the hd_config, total
+    buckets, the bucket word counts, the number of pages, then per page its id
+    and words; little-endian uint32.  Pages in ascending id order."""
+    bw = np.ascontiguousarray(bucket_words, dtype="<u4")
+    ids = np.ascontiguousarray(page_ids, dtype="<u4")
+    pg = np.ascontiguousarray(pages, dtype="<u4").reshape(len(ids), config.get_words_per_page())
+    if len(bw) != config.get_total_buckets() or (len(ids) > 1 and np.any(np.diff(ids.astype(np.int64)) <= 0)):
+        raise ValueError("bucket words of another configuration, or page ids not ascending")
+    rec = np.empty((len(ids), 1 + pg.shape[1]), dtype="<u4")
+    rec[:, 0] = ids
+    rec[:, 1:] = pg
+    with open(path, "wb") as f:
+        f.write(_DUMP_MAGIC)
+        f.write(np.array([_DUMP_VERSION], "<u4").tobytes())
+        f.write(bytes(config.to_c()))
+        f.write(np.array([len(bw)], "<u4").tobytes())
+        f.write(bw.tobytes())
+        f.write(np.array([len(ids)], "<u4").tobytes())
+        f.write(rec.tobytes())
+
+
+def read_pool_dump(path: str):
+    """(config, bucket_words, page_ids, pages) of a pool dump (write_pool_dump,
+    HostPoolMirror::Save); ValueError on a malformed file."""
+    raw = open(path, "rb").read()
+    csize = ctypes.sizeof(_Config)
+    if raw[:4] != _DUMP_MAGIC or len(raw) < 8 + csize + 4:
+        raise ValueError("not a pool dump")
+    if int(np.frombuffer(raw, "<u4", 1, 4)[0]) != _DUMP_VERSION:
+        raise ValueError("unknown pool dump version")
+    c = _Config.from_buffer_copy(raw[8:8 + csize])
+    if not 1 <= c.node_levels <= MAX_LEVELS:
+        raise ValueError("malformed pool dump")
+    config = Config(c.word_bits_per_page, c.page_bits_per_bucket, list(c.bucket_bits_each_level[:c.node_levels]),
+                    c.hasher)
+    off = 8 + csize
+    nb = int(np.frombuffer(raw, "<u4", 1, off)[0])
+    if nb != config.get_total_buckets() or len(raw) < off + 4 * (nb + 2):
+        raise ValueError("malformed pool dump")
+    bw = np.frombuffer(raw, "<u4", nb, off + 4).copy()
+    off += 4 * (nb + 1)
+    n_pages = int(np.frombuffer(raw, "<u4", 1, off)[0])
+    wpp = config.get_words_per_page()
+    if len(raw) != off + 4 + 4 * n_pages * (1 + wpp):
+        raise ValueError("malformed pool dump")
+    rec = np.frombuffer(raw, "<u4", n_pages * (1 + wpp), off + 4).reshape(n_pages, 1 + wpp)
+    return config, bw, rec[:, 0].copy(), rec[:, 1:].copy()
+
+
 class NodePool:
     """A device-resident node pool (NodePoolBase + DAGNodePool storage, on the GPU).
 
@@ -546,6 +603,13 @@ class NodePool:
     def kernel_launches(self) -> int:
         return int(lib().hd_pool_kernel_launches(self._h))
 
+    def epoch(self) -> int:
+        """Generation of the committed words (hd_pool_epoch): changes with every
+        GC, rollback or upload; between equal values the pool only appended."""
+        e = ctypes.c_uint64(0)
+        _check(lib().hd_pool_epoch(self._h, ctypes.byref(e)), "hd_pool_epoch")
+        return int(e.value)
+
     def reserve(self, max_items: int, max_list_entries: int, max_edits: int):
         _check(lib().hd_edit_reserve(self._h, max_items, max_list_entries, max_edits), "hd_edit_reserve")
 
@@ -586,6 +650,18 @@ class NodePool:
         pm = self.page_map()
         ids = np.nonzero(pm)[0].astype(np.uint32)
         return self.bucket_words(), ids, self.read_pages(ids)
+
+    def save(self, path: str):
+        """The pool as a dump file (write_pool_dump; HostPoolMirror::Load reads it)."""
+        bw, ids, pages = self.download()
+        write_pool_dump(path, self.config, bw, ids, pages)
+
+    def load(self, path: str):
+        """Replaces the pool with a dump of a pool of the same configuration."""
+        config, bw, ids, pages = read_pool_dump(path)
+        if bytes(config.to_c()) != bytes(self.config.to_c()):
+            raise ValueError("the dump holds a pool of another configuration")
+        self.upload(bw, ids, pages)
 
     def upload(self, bucket_words, page_ids, pages, filled=None):
         bw = np.ascontiguousarray(bucket_words, dtype=np.uint32)

@@ -1196,6 +1196,13 @@ hd_status hd_edit_profile_end(hd_pool *pool, float *out_ms, uint32_t *out_passes
 
 uint64_t hd_pool_kernel_launches(const hd_pool *pool) { return pool ? pool->kernel_launches.load() : 0; }
 
+hd_status hd_pool_epoch(const hd_pool *pool, uint64_t *out) {
+	if (!pool || !out)
+		return HD_ERR_INVALID_ARG;
+	*out = pool->epoch.load();
+	return HD_OK;
+}
+
 hd_status hd_pool_checkpoint(hd_pool *pool) {
 	if (!pool)
 		return HD_ERR_INVALID_ARG;
@@ -1235,6 +1242,7 @@ hd_status hd_pool_rollback(hd_pool *pool, void *stream) {
 	std::lock_guard<std::mutex> lk(pool->mtx);
 	if (!pool->has_checkpoint)
 		return HD_ERR_INVALID_ARG;
+	++pool->epoch; // later passes write over the words dropped here
 	HD_TRY(cudaSetDevice(pool->device));
 	cudaStream_t st = (cudaStream_t)stream;
 	HD_TRY(cudaStreamWaitEvent(st, pool->ws_free, 0));
@@ -1380,6 +1388,7 @@ hd_status hd_pool_upload(hd_pool *pool, const uint32_t *bucket_words, const uint
 			return HD_ERR_INVALID_ARG;
 		pt[page_ids[i]] = pool->P.identity ? page_ids[i] : i + 1;
 	}
+	++pool->epoch; // every word is replaced
 	HD_TRY(cudaMemcpy(pool->P.bucket_words, bucket_words, pool->total_buckets * 4, cudaMemcpyHostToDevice));
 	HD_TRY(cudaMemcpy(pool->P.page_table, pt.data(), pool->total_pages * 4, cudaMemcpyHostToDevice));
 	HD_TRY(cudaMemset(pool->P.heap, 0, (uint64_t)pool->P.heap_pages * wp * 4));

@@ -506,6 +506,7 @@ extern "C" hd_status hd_gc(hd_pool *pool, uint32_t *roots, uint32_t n_roots, hd_
 	cudaStream_t st = nullptr;
 	if (cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking) != cudaSuccess)
 		return HD_ERR_CUDA;
+	++pool->epoch; // even a failed collection is treated as a rewrite (mirrors re-read everything)
 	hd_status s = gc_impl(pool, roots, n_roots, stats, st);
 	cudaStreamSynchronize(st);
 	cudaStreamDestroy(st);

@@ -43,6 +43,10 @@ struct hd_pool {
 	unsigned long long *ck_index = nullptr;
 	uint32_t ck_filled[HD_MAX_LEVELS] = {};
 	bool has_checkpoint = false;
+	// generation of the committed words: bumped by every call that rewrites or
+	// drops words already in the pool (hd_gc, hd_pool_rollback, hd_pool_upload);
+	// between two equal values the pool only appended (hd_pool_epoch)
+	std::atomic<uint64_t> epoch{0};
 };
 
 // events per profiled pass: start, after expand, after leaf, after the dedup launch
