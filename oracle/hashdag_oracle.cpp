@@ -543,12 +543,20 @@ struct Pool {
 			child_pos(pos, i, cps[i]);
 			fork[i] = edit_switch(e, u[1 + i], level + 1, cps[i], &nc[i]);
 		}
-		for (Word i = 0; i < 8; ++i) {
+		// every forked child but the last becomes a task, the last runs on this
+		// thread (NodePoolThreadedEdit.hpp:58-74: .fork() except for the last)
+		Word last = 8;
+		for (Word i = 0; i < 8; ++i)
+			if (fork[i])
+				last = i;
+		for (Word i = 0; i < last; ++i) {
 			if (!fork[i])
 				continue;
 #pragma omp task default(none) firstprivate(i, level, max_task_level) shared(e, u, nc, cps, ok)
 			nc[i] = t_edit_node(e, u[1 + i], level + 1, cps[i], max_task_level, ok);
 		}
+		if (last < 8)
+			nc[last] = t_edit_node(e, u[1 + last], level + 1, cps[last], max_task_level, ok);
 #pragma omp taskwait
 		bool changed = false;
 		for (Word i = 0; i < 8; ++i) {
@@ -565,17 +573,25 @@ struct Pool {
 		return upsert<true>(false, level, u.data(), len, ptr, ok);
 	}
 
-	// NodePoolThreadedEdit.hpp:104-126
-	Word threaded_edit(Word root, const hd_edit_desc &e, Word max_task_level, int threads, bool *ok) {
-		make_filled(ok);
+	// NodePoolThreadedEdit.hpp:104-126, called by one thread of a running team
+	Word threaded_edit_in_team(Word root, const hd_edit_desc &e, Word max_task_level, bool *ok) {
 		Word zero[3] = {0, 0, 0}, out;
 		if (!edit_switch(e, root, 0, zero, &out))
 			return out;
-		Word r = kNull;
-#pragma omp parallel num_threads(threads) default(none) shared(r, e, zero, max_task_level, ok, root)
+		return t_edit_node(e, root, 0, zero, max_task_level, ok);
+	}
+	// ThreadedEdit of each edit in turn on one thread team that lives across
+	// the edits, as the application's lf::busy_pool does (src/main.cpp:159,
+	// busy_pool.hpp:117-145): the other threads wait in the team for the
+	// tasks of the next edit instead of being woken per edit.
+	Word threaded_edits(Word root, const hd_edit_desc *e, Word n, Word max_task_level, int threads, bool *ok) {
+		make_filled(ok);
+		Word r = root;
+#pragma omp parallel num_threads(threads) default(none) shared(r, e, n, max_task_level, ok)
 		{
 #pragma omp single
-			r = t_edit_node(e, root, 0, zero, max_task_level, ok);
+			for (Word i = 0; i < n; ++i)
+				r = threaded_edit_in_team(r, e[i], max_task_level, ok);
 		}
 		return r;
 	}
@@ -1293,9 +1309,7 @@ uint32_t orc_edit(orc_pool *p, uint32_t root, const hd_edit_desc *e, uint32_t n)
 // Threaded edits (NodePoolThreadedEdit::ThreadedEdit per edit).
 uint32_t orc_threaded_edit(orc_pool *p, uint32_t root, const hd_edit_desc *e, uint32_t n, uint32_t max_task_level,
                            int threads) {
-	for (uint32_t i = 0; i < n; ++i)
-		root = p->pool.threaded_edit(root, e[i], max_task_level, threads, &p->ok);
-	return root;
+	return p->pool.threaded_edits(root, e, n, max_task_level, threads, &p->ok);
 }
 
 int orc_max_threads(void) {
