@@ -101,6 +101,7 @@ def lib():
             "orc_color_pool_load": (None, [P, P, U64, P, U64]),
             "orc_vbr_edit": (None, [P, P, U32, U32, P, U32, U32, U32, U32, P, P]),
             "orc_color_fetch": (None, [P, P, U32, P, U32, P]),
+            "orc_vbr_set_per_voxel": (None, [I]),
             "orc_hash_inner": (U32, [P, U32]),
             "orc_hash_leaf": (U32, [U32, U32]),
         }

@@ -1189,6 +1189,176 @@ static void vbr_region(const Pool &dag, const hd_edit_desc &g, const VColor &C, 
 	}
 }
 
+// ---- the same leaf rewrite in runs.  The reference's writer copies and fills
+// whole runs (VBRChunkIterator / VBRChunkWriter::Copy, Edit, VBRColor.hpp:286-488);
+// this form does too: the new voxel sequence is a list of segments, each
+// either "the edit's colour" or "the old colours of these voxels", and only the
+// DAG leaves the edit partly covers are decided voxel by voxel.  Its chunk is
+// word for word encode_leaf's of the per-voxel form (a test compares the two).
+static bool g_vbr_per_voxel = false; // the per-voxel form above (tests compare the two)
+
+struct SrcBlock {      // voxels [m0, m1) of one block of the old chunk
+	uint64_t m0, m1;
+	Word colors, bpw;
+	uint64_t bit0;     // weight of voxel m: bpw bits at bit0 + (m - m0) * bpw
+};
+struct SrcChunk {
+	std::vector<SrcBlock> blocks;
+	const Word *bits = nullptr;
+	Word n_words = 0;
+	Word weight(uint64_t bit, Word bpw) const { // as decode_leaf reads it
+		const uint64_t two = uint64_t(bits[bit >> 5]) | (((bit >> 5) + 1 < n_words) ? uint64_t(bits[(bit >> 5) + 1]) << 32 : 0);
+		return Word(two >> (bit & 31)) & ((1u << bpw) - 1u);
+	}
+};
+static SrcChunk source_blocks(const ColorPool &cp, Word p, size_t n) {
+	SrcChunk s;
+	if (ctag(p) != kTagLeaf) {
+		const VColor f = fill_of(p);
+		s.blocks.push_back({0, n, f.colors, f.bpw, 0});
+		return s;
+	}
+	const Word *w = cp.leaves.data() + cdata(p);
+	const Word M = w[1], B = w[2];
+	const Word *macro = w + 4, *hdr = macro + 2 * M;
+	s.bits = hdr + 2 * B;
+	s.n_words = w[3];
+	for (Word k = 0; k < M; ++k) {
+		const Word first = macro[2 * k], end = k + 1 < M ? macro[2 * k + 2] : B, wstart = macro[2 * k + 1];
+		for (Word b = first; b < end; ++b) {
+			const Word v0 = hdr[2 * b + 1] >> 18, v1 = b + 1 < end ? hdr[2 * (b + 1) + 1] >> 18 : (1u << kMacroBits);
+			const uint64_t m0 = (uint64_t(k) << kMacroBits) + v0, m1 = std::min<uint64_t>(n, (uint64_t(k) << kMacroBits) + v1);
+			if (m0 < m1)
+				s.blocks.push_back({m0, m1, hdr[2 * b], (hdr[2 * b + 1] >> 16) & 3u,
+				                    uint64_t(wstart) + (hdr[2 * b + 1] & 0xFFFFu)});
+		}
+	}
+	return s;
+}
+
+struct Seg {
+	bool copy; // old colours of voxels [m, m + len), else the edit's colour
+	uint64_t m, len;
+};
+static inline void push_seg(std::vector<Seg> &segs, bool copy, uint64_t m, uint64_t len) {
+	if (!segs.empty() && segs.back().copy == copy && segs.back().m + segs.back().len == m)
+		segs.back().len += len;
+	else
+		segs.push_back({copy, m, len});
+}
+// vbr_region as segments
+static void vbr_region_runs(const Pool &dag, const hd_edit_desc &g, Word level, const Word pos[3], Word dptr,
+                            Word leaf_level, uint64_t m0, std::vector<Seg> &segs) {
+	const Word V = dag.cfg.voxel_level(), L = dag.cfg.node_levels();
+	const uint64_t count = uint64_t(1) << (3 * (V - level));
+	if (level > leaf_level) {
+		const EditType t = edit_node_type(g, V, level, pos);
+		if (t == kFill || dptr == kNull) {
+			push_seg(segs, false, m0, count);
+			return;
+		}
+		if (t == kNotAffected) {
+			push_seg(segs, true, m0, count);
+			return;
+		}
+	}
+	if (level == L - 1) {
+		const Word *p = dag.read_node(dptr);
+		for (Word i = 0; i < 64; ++i) {
+			const Word vp[3] = {(pos[0] << 2) | ((i >> 2) & 2u) | (i & 1u), (pos[1] << 2) | ((i >> 3) & 2u) | ((i >> 1) & 1u),
+			                    (pos[2] << 2) | ((i >> 4) & 2u) | ((i >> 2) & 1u)};
+			const bool old = (p[i >> 5] >> (i & 31)) & 1u;
+			push_seg(segs, !(voxel_in_shape(g, vp) || !old), m0 + i, 1);
+		}
+		return;
+	}
+	const std::array<Word, 9> u = dag.unpack(dptr);
+	for (Word c = 0; c < 8; ++c) {
+		Word cp[3];
+		Pool::child_pos(pos, c, cp);
+		vbr_region_runs(dag, g, level + 1, cp, u[1 + c], leaf_level, m0 + c * (count >> 3), segs);
+	}
+}
+
+// encode_leaf fed by pieces of one colour instead of single voxels
+struct RunEncoder {
+	std::vector<Word> macros, hdrs, wbits;
+	uint64_t bit = 0, macro_wstart = 0;
+	Word pc = 0, pb = 0;
+	void put_bits(Word v, Word nb) {
+		for (Word b = 0; b < nb; ++b, ++bit) {
+			if ((bit & 31) == 0)
+				wbits.push_back(0u);
+			wbits.back() |= ((v >> b) & 1u) << (bit & 31);
+		}
+	}
+	// voxels [m, m + len) of colour (colors, bpw); weight(k) of voxel m + k
+	template <typename WeightF> void piece(uint64_t m, uint64_t len, Word colors, Word bpw, WeightF &&weight) {
+		const uint64_t macro_mask = (uint64_t(1) << kMacroBits) - 1;
+		for (uint64_t k = 0; k < len;) {
+			const uint64_t mm = m + k, in_macro = mm & macro_mask;
+			const uint64_t chunk = std::min(len - k, (macro_mask + 1) - in_macro);
+			if (in_macro == 0) {
+				macro_wstart = bit;
+				macros.push_back(Word(hdrs.size() / 2));
+				macros.push_back(Word(bit));
+			}
+			if (in_macro == 0 || colors != pc || bpw != pb) {
+				hdrs.push_back(colors);
+				hdrs.push_back(Word(in_macro << 18) | (bpw << 16) | Word(bit - macro_wstart));
+			}
+			pc = colors;
+			pb = bpw;
+			if (bpw)
+				for (uint64_t j = 0; j < chunk; ++j)
+					put_bits(weight(k + j), bpw);
+			k += chunk;
+		}
+	}
+	std::vector<Word> chunk(size_t n) const {
+		const size_t M = (n + (size_t(1) << kMacroBits) - 1) >> kMacroBits;
+		std::vector<Word> out = {Word(M), Word(hdrs.size() / 2), Word(wbits.size())};
+		out.insert(out.end(), macros.begin(), macros.end());
+		out.insert(out.end(), hdrs.begin(), hdrs.end());
+		out.insert(out.end(), wbits.begin(), wbits.end());
+		return out;
+	}
+};
+
+// The new chunk of a colour leaf being edited, in runs.
+static std::vector<Word> vbr_leaf_runs(const ColorPool &cp, const Pool &dag, const hd_edit_desc &g, const VColor &C,
+                                       Word level, const Word pos[3], Word optr, Word dptr) {
+	const size_t n = size_t(1) << (3 * (dag.cfg.voxel_level() - level));
+	const SrcChunk src = source_blocks(cp, optr, n);
+	std::vector<Seg> segs;
+	vbr_region_runs(dag, g, level, pos, dptr, cp.leaf_level, 0, segs);
+	RunEncoder enc;
+	size_t bi = 0;
+	for (const Seg &sg : segs) {
+		if (!sg.copy) {
+			enc.piece(sg.m, sg.len, C.colors, C.bpw, [&](uint64_t) { return C.weight; });
+			continue;
+		}
+		uint64_t m = sg.m;
+		const uint64_t end = sg.m + sg.len;
+		while (m < end) {
+			while (bi < src.blocks.size() && src.blocks[bi].m1 <= m)
+				++bi;
+			if (bi == src.blocks.size() || src.blocks[bi].m0 > m) { // not covered by the old chunk: zeros
+				const uint64_t e = bi == src.blocks.size() ? end : std::min(end, src.blocks[bi].m0);
+				enc.piece(m, e - m, 0u, 0u, [](uint64_t) { return 0u; });
+				m = e;
+				continue;
+			}
+			const SrcBlock &b = src.blocks[bi];
+			const uint64_t e = std::min(end, b.m1), base = b.bit0 + (m - b.m0) * b.bpw;
+			enc.piece(m, e - m, b.colors, b.bpw, [&](uint64_t k) { return src.weight(base + k * b.bpw, b.bpw); });
+			m = e;
+		}
+	}
+	return enc.chunk(n);
+}
+
 // The colour octree part of one VBR edit at or above the colour leaf level:
 // VBREditorWrapper::EditNode/JoinNode (VBREditor.hpp:40-80,92-107) with
 // FillNode/ClearNode/SetNode/SetLeaf.  Returns the node's new pointer.
@@ -1201,6 +1371,8 @@ static Word vbr_walk(ColorPool &cp, const Pool &dag, const hd_edit_desc &g, cons
 	if (t == kNotAffected)
 		return optr;
 	if (level == cp.leaf_level) {
+		if (!g_vbr_per_voxel)
+			return cp.set_leaf(optr, vbr_leaf_runs(cp, dag, g, C, level, pos, optr, dptr));
 		const size_t n = size_t(1) << (3 * (V - level));
 		const VStream src = decode_leaf(cp, optr, n);
 		VStream dst(n);
@@ -1460,6 +1632,10 @@ void orc_color_fetch(const orc_pool *p, const orc_color_pool *c, uint32_t color_
 		std::memcpy(o + 4, rgb, 12);
 	}
 }
+
+// 1: colour leaves rewritten voxel by voxel; 0 (default): in runs.  The two
+// give the same words; tests compare them.
+void orc_vbr_set_per_voxel(int on) { orc::g_vbr_per_voxel = on != 0; }
 
 uint32_t orc_hash_inner(const uint32_t *w, uint32_t n) { return orc::murmur_words(w, n); }
 uint32_t orc_hash_leaf(uint32_t w0, uint32_t w1) { return orc::murmur_leaf(w0, w1); }

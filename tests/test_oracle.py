@@ -250,3 +250,52 @@ def test_vbr_live_reference_when_present(orc):
         c = pool.color_fetch(cp, croot, q)
         assert np.array_equal(c["colors"], r["colors"]["colors"])
         assert np.array_equal(c["rgb"].view(np.uint32), r["colors"]["rgb"].view(np.uint32))
+
+
+def _oracle_vbr_words(orc, cfg, v, leaf_level, keep_history):
+    from vkhashdag_gb300 import OP_DIG, OP_PAINT
+    pool = orc.OraclePool.from_config(cfg)
+    cp = orc.OracleColorPool(leaf_level, keep_history)
+    root, croot = orc.NULL, orc.OracleColorPool.NULL
+    for e in v:
+        op = int(e["edit"]["op"])
+        if op == OP_DIG:
+            root = pool.edit(root, np.asarray([e["edit"]]))
+        else:
+            root, croot = pool.vbr_edit(root, cp, croot, e["edit"], 2 if op == OP_PAINT else 1, int(e["colors"]),
+                                        int(e["weight"]), int(e["bits_per_weight"]))
+    return croot, cp.nodes(), cp.leaves()
+
+
+@pytest.mark.parametrize("res,leaf_level,keep_history,seed",
+                         [(256, 3, False, 81), (256, 5, True, 82), (512, 2, False, 83), (128, 0, False, 84),
+                          (1024, 4, False, 85)])
+def test_vbr_leaf_rewrite_in_runs_equals_voxel_by_voxel(orc, res, leaf_level, keep_history, seed):
+    """The oracle rewrites an edited colour leaf in runs (whole runs copied or
+    filled, as the reference's chunk iterator and writer do); the per-voxel form
+    (decode every voxel, re-encode) must give the same octree and leaf words,
+    with weighted colours, paints, digs, macro blocks (1024^3 with leaves of
+    64^3 voxels: 16 macro blocks per leaf) and kept history."""
+    from vkhashdag_gb300 import workloads as W
+    cfg = W.serving_config(res)
+    v = W.vbr_edits(res, 30, seed=seed, r_max=res // 4, side_max=res // 2, weighted_frac=0.5)
+    try:
+        orc.lib().orc_vbr_set_per_voxel(1)
+        want = _oracle_vbr_words(orc, cfg, v, leaf_level, keep_history)
+    finally:
+        orc.lib().orc_vbr_set_per_voxel(0)
+    got = _oracle_vbr_words(orc, cfg, v, leaf_level, keep_history)
+    assert got[0] == want[0] and np.array_equal(got[1], want[1]) and np.array_equal(got[2], want[2])
+    assert len(got[2]) > 0
+
+
+def test_vbr_per_voxel_form_matches_reference(golden, orc):
+    """The per-voxel form is pinned too (it is the cross-check of the runs)."""
+    from helpers import oracle_vbr_run, vbr_case
+    g = vbr_case(golden, "vbr_512_leaf2")
+    try:
+        orc.lib().orc_vbr_set_per_voxel(1)
+        pool, cp, root, croot, q = oracle_vbr_run(orc, g)
+    finally:
+        orc.lib().orc_vbr_set_per_voxel(0)
+    assert croot == g["color_root"] and sha(cp.leaves()) == g["leaves_sha"] and sha(cp.nodes()) == g["nodes_sha"]
