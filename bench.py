@@ -961,9 +961,10 @@ def run_gc(args):
         t_gc = time.perf_counter() - t0
     same = bool(np.array_equal(pool.query(new_root, q), occ))
     moved = 4.0 * 2 * st["words_after"]  # live words read once and written once
-    # CPU: the oracle's collector (the reference's algorithm, one thread) on a
-    # smaller pool of the same workload; the device collects the same pool, and
-    # both results must be word-identical
+    # CPU: the oracle's collector (the reference's algorithm, all host threads,
+    # as fast as the reference's ThreadedGC on as many workers) on a smaller
+    # pool of the same workload; the device collects the same pool, and both
+    # results must be word-identical
     cpu = None
     if rank == 0 and not args.no_cpu:
         import oracle
@@ -973,8 +974,9 @@ def run_gc(args):
         bw, ids, pages = cpool.download()
         opool = oracle.OraclePool.from_config(ccfg)
         opool.load(bw, ids, pages, cpool.filled_node_pointers())
+        threads = os.cpu_count() or 1
         tc = time.perf_counter()
-        (oroot,) = opool.gc([croot])
+        (oroot,) = opool.gc([croot], threads)
         t_cpu = time.perf_counter() - tc
         tg = time.perf_counter()
         (groot,), cst = cpool.gc([croot])
@@ -982,9 +984,9 @@ def run_gc(args):
         wb, pb = ccfg.word_bits_per_page, ccfg.page_bits_per_bucket
         identical = (oroot == groot and oracle.pool_words_digest(*opool.dump(), wb, pb) ==
                      oracle.pool_words_digest(*cpool.download(), wb, pb))
-        cpu = {"value": cst["live_nodes"] / t_cpu, "unit": "live nodes/s", "cores": 1, "kind": "port",
+        cpu = {"value": cst["live_nodes"] / t_cpu, "unit": "live nodes/s", "cores": threads, "kind": "port",
                "sample": f"{cres}^3 pool of the same workload ({cst['live_nodes']} live nodes, "
-                         f"{cst['words_before']} words before): oracle collector {t_cpu:.2f} s vs device "
+                         f"{cst['words_before']} words before): oracle collector on {threads} threads {t_cpu:.2f} s vs device "
                          f"{t_dev_small * 1e3:.1f} ms",
                "device_value_same_pool": cst["live_nodes"] / t_dev_small, "word_identical": bool(identical)}
     if rank != 0:

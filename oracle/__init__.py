@@ -92,7 +92,8 @@ def lib():
             "orc_dense": (None, [P, U32, P]),
             "orc_trace": (None, [P, U32, P, P, U32, P]),
             "orc_trace_threads": (None, [P, U32, P, P, U32, P, I]),
-            "orc_gc": (None, [P, P, U32]),
+            "orc_gc": (None, [P, P, U32, I]),
+            "orc_gc_serial": (None, [P, P, U32]),
             "orc_trace_pinhole_lod": (None, [P, U32, P, U32, U32, U32, ctypes.c_float, ctypes.c_float, P, I]),
             "orc_color_pool_create": (P, [U32, I]),
             "orc_color_pool_destroy": (None, [P]),
@@ -246,10 +247,17 @@ class OraclePool:
         lib().orc_color_fetch(self._h, color_pool._h, color_root, _p(q), len(q), _p(out))
         return out
 
-    def gc(self, roots):
-        """NodePoolThreadedGC::ThreadedGC (one-worker order); returns the remapped roots."""
+    def gc(self, roots, threads=0):
+        """NodePoolThreadedGC::ThreadedGC, the pool laid out in the one-worker
+        order whatever `threads` (0 = all); returns the remapped roots."""
         r = np.ascontiguousarray(roots, np.uint32).copy()
-        lib().orc_gc(self._h, _p(r), len(r))
+        lib().orc_gc(self._h, _p(r), len(r), threads)
+        return [int(x) for x in r]
+
+    def gc_serial(self, roots):
+        """The same collection on one thread, node by node (the cross-check of gc)."""
+        r = np.ascontiguousarray(roots, np.uint32).copy()
+        lib().orc_gc_serial(self._h, _p(r), len(r))
         return [int(x) for x in r]
 
     def canonical(self, root):
@@ -369,6 +377,8 @@ def run_reference(mode, word_bits_per_page, page_bits_per_bucket, bucket_bits, e
         off += 4 * n
         out["roots_after"] = list(struct.unpack_from(f"<{n}I", data, off))
         off += 4 * n
+        (out["gc_ns"],) = struct.unpack_from("<Q", data, off)
+        off += 8
     if mode == MODE_VBR:
         (out["color_root"], nn) = struct.unpack_from("<2I", data, off)
         off += 8

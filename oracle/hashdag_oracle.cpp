@@ -335,7 +335,7 @@ struct Pool {
 	// (:189-213); roots remapped at level 0 (:323-328); filled pointers made
 	// again (:378-381).  A bucket cache that outgrows its bucket clears `ok`
 	// (the reference would write past the bucket there).
-	void gc(Word *roots, Word n_roots, bool *ok) {
+	void gc_serial(Word *roots, Word n_roots, bool *ok) {
 		const Word L = cfg.node_levels(), wbpb = cfg.wbpp + cfg.pbpb, wpp = cfg.words_per_page();
 		std::vector<std::vector<Word>> bucket_nodes(cfg.total_buckets());
 		if (!filled.empty() && filled[0] != kNull)
@@ -419,6 +419,176 @@ struct Pool {
 						roots[i] = cur_map.at(roots[i]);
 			std::swap(child_map, cur_map);
 		}
+		filled.clear();
+		make_filled(ok);
+	}
+
+	// The same collection on several threads.  Each level's live nodes are a
+	// bitmap over the level's pointer space (a bit per word); the sorted list of
+	// live nodes (pointer order is bucket-major, so each bucket's run is its
+	// sorted, unique node list) and old -> new pointers (the rank of a node's
+	// bit) come from it.  Reading the live nodes' children, the per-bucket leaf
+	// re-append, the remap and re-hash of inner nodes and the per-bucket layout
+	// of the new caches run on all threads.  The caches take the nodes in the
+	// one-worker order (a stable counting sort by new bucket of the level's
+	// old-pointer order), so the pool is word for word gc_serial's; a test
+	// compares the two.
+	struct LiveLevel {
+		Word base = 0;               // first word of the level's pointer space
+		std::vector<uint64_t> bits;  // a bit per word: a live node starts there
+		std::vector<Word> before;    // live nodes in the bit words before each bit word
+		std::vector<Word> nodes;     // the live nodes, ascending
+		std::vector<Word> fresh;     // their new pointers
+		size_t rank(Word ptr) const {
+			const size_t i = ptr - base;
+			return before[i >> 6] + size_t(std::popcount(bits[i >> 6] & ((uint64_t(1) << (i & 63)) - 1)));
+		}
+		void set(Word ptr) {
+			const size_t i = ptr - base;
+			std::atomic_ref<uint64_t>(bits[i >> 6]).fetch_or(uint64_t(1) << (i & 63), std::memory_order_relaxed);
+		}
+		void build_list(int threads) { // before[] and nodes[] from bits[]
+			const size_t nw = bits.size();
+			before.assign(nw + 1, 0);
+			const size_t parts = size_t(std::max(1, threads)) * 4, per = (nw + parts - 1) / parts;
+			std::vector<size_t> part_count(parts + 1, 0);
+#pragma omp parallel for num_threads(threads) schedule(static, 1)
+			for (size_t k = 0; k < parts; ++k) {
+				size_t c = 0;
+				for (size_t w = k * per; w < std::min(nw, (k + 1) * per); ++w)
+					c += size_t(std::popcount(bits[w]));
+				part_count[k + 1] = c;
+			}
+			for (size_t k = 0; k < parts; ++k)
+				part_count[k + 1] += part_count[k];
+			nodes.resize(part_count[parts]);
+#pragma omp parallel for num_threads(threads) schedule(static, 1)
+			for (size_t k = 0; k < parts; ++k) {
+				size_t c = part_count[k];
+				for (size_t w = k * per; w < std::min(nw, (k + 1) * per); ++w) {
+					before[w] = Word(c);
+					for (uint64_t m = bits[w]; m; m &= m - 1)
+						nodes[c++] = base + Word(w * 64 + size_t(std::countr_zero(m)));
+				}
+			}
+			before[nw] = Word(part_count[parts]);
+		}
+	};
+	void gc(Word *roots, Word n_roots, bool *ok, int threads) {
+		const Word L = cfg.node_levels(), wbpb = cfg.wbpp + cfg.pbpb, wpp = cfg.words_per_page();
+		if (threads < 1)
+			threads = omp_get_max_threads();
+		std::vector<LiveLevel> lv(L);
+		for (Word l = 0; l < L; ++l) {
+			lv[l].base = bases[l] << wbpb;
+			lv[l].bits.assign(((size_t(cfg.buckets_at(l)) << wbpb) + 63) / 64, 0);
+		}
+		if (!filled.empty() && filled[0] != kNull)
+			lv[0].set(filled[0]);
+		for (Word i = 0; i < n_roots; ++i)
+			if (roots[i] != kNull)
+				lv[0].set(roots[i]);
+		for (Word l = 0; l < L; ++l) { // mark: the children of the live nodes of level l
+			lv[l].build_list(threads);
+			if (l + 1 == L)
+				break;
+			const std::vector<Word> &cur = lv[l].nodes;
+			LiveLevel &nxt = lv[l + 1];
+#pragma omp parallel for num_threads(threads) schedule(static)
+			for (size_t i = 0; i < cur.size(); ++i) {
+				const Word *pn = read_node(cur[i]);
+				const Word n = Word(std::popcount(pn[0] & 0xFFu));
+				for (Word j = 1; j <= n; ++j)
+					nxt.set(pn[j]);
+			}
+		}
+		std::atomic<bool> all_ok{true};
+		for (Word l = L - 1; l != Word(-1); --l) {
+			LiveLevel &me = lv[l];
+			const std::vector<Word> &cur = me.nodes;
+			me.fresh.assign(cur.size(), kNull);
+			const Word b0 = bases[l], nb_count = cfg.buckets_at(l);
+			if (l == L - 1) { // leaves re-appended to their own bucket in pointer order
+				std::vector<size_t> run(size_t(nb_count) + 1, 0); // each bucket's run of the sorted list
+				for (Word p : cur)
+					++run[(p >> wbpb) - b0 + 1];
+				for (Word k = 0; k < nb_count; ++k)
+					run[k + 1] += run[k];
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 64)
+				for (Word k = 0; k < nb_count; ++k) {
+					const Word b = b0 + k;
+					Word nbw = 0;
+					for (size_t i = run[k]; i < run[k + 1]; ++i) {
+						const Word *pn = read_node(cur[i]);
+						const Word w[2] = {pn[0], pn[1]};
+						auto [np, nb] = append_node(b, nbw, w, 2);
+						if (np == kNull) {
+							all_ok = false;
+							break;
+						}
+						me.fresh[i] = np;
+						nbw = nb;
+					}
+					bucket_words[b] = nbw;
+				}
+			} else {
+				// remapped words and new bucket of every live node
+				const LiveLevel &below = lv[l + 1];
+				std::vector<std::array<Word, 9>> words(cur.size());
+				std::vector<Word> len(cur.size()), nbk(cur.size());
+#pragma omp parallel for num_threads(threads) schedule(static)
+				for (size_t i = 0; i < cur.size(); ++i) {
+					const Word *pn = read_node(cur[i]);
+					const Word n = inner_node_words(pn);
+					words[i][0] = pn[0];
+					for (Word j = 1; j < n; ++j)
+						words[i][j] = below.fresh[below.rank(pn[j])];
+					len[i] = n;
+					nbk[i] = node_hash(false, words[i].data(), n) & (nb_count - 1u);
+				}
+				// stable counting sort by new bucket: a bucket's cache in old-pointer order
+				std::vector<size_t> start(size_t(nb_count) + 1, 0), order(cur.size());
+				for (size_t i = 0; i < cur.size(); ++i)
+					++start[nbk[i] + 1];
+				for (Word k = 0; k < nb_count; ++k)
+					start[k + 1] += start[k];
+				{
+					std::vector<size_t> fill(start.begin(), start.end() - 1);
+					for (size_t i = 0; i < cur.size(); ++i)
+						order[fill[nbk[i]]++] = i;
+				}
+#pragma omp parallel for num_threads(threads) schedule(dynamic, 64)
+				for (Word k = 0; k < nb_count; ++k) {
+					const Word b = b0 + k;
+					std::vector<Word> cache;
+					for (size_t j = start[k]; j < start[k + 1]; ++j) {
+						const size_t i = order[j];
+						Word off = Word(cache.size());
+						if ((off & (wpp - 1u)) + len[i] > wpp)
+							off = ((off >> cfg.wbpp) + 1u) << cfg.wbpp;
+						cache.resize(off + len[i], 0u);
+						std::copy(words[i].begin(), words[i].begin() + len[i], cache.begin() + off);
+						me.fresh[i] = (b << wbpb) | off;
+					}
+					if (cache.size() > cfg.words_per_bucket()) {
+						all_ok = false;
+						continue;
+					}
+					for (Word off = 0; off < cache.size(); off += wpp)
+						write_page((b << cfg.pbpb) | (off >> cfg.wbpp), 0, cache.data() + off,
+						           std::min<Word>(wpp, Word(cache.size()) - off));
+					bucket_words[b] = Word(cache.size());
+				}
+			}
+			if (l == 0)
+				for (Word i = 0; i < n_roots; ++i)
+					if (roots[i] != kNull)
+						roots[i] = me.fresh[me.rank(roots[i])];
+			if (l + 1 < L)
+				lv[l + 1] = LiveLevel{}; // the level below is no longer needed
+		}
+		if (!all_ok && ok)
+			*ok = false;
 		filled.clear();
 		make_filled(ok);
 	}
@@ -1576,7 +1746,12 @@ void orc_trace_pinhole_lod(const orc_pool *p, uint32_t root, const hd_camera *ca
 	orc::trace_pinhole_lod(p->pool, root, cams, n_cams, w, h, proj, beam_proj, out, threads);
 }
 
-void orc_gc(orc_pool *p, uint32_t *roots, uint32_t n_roots) { p->pool.gc(roots, n_roots, &p->ok); }
+// ThreadedGC restated: threads 0 = all; the result does not depend on it.
+void orc_gc(orc_pool *p, uint32_t *roots, uint32_t n_roots, int threads) {
+	p->pool.gc(roots, n_roots, &p->ok, threads);
+}
+// The one-thread form kept as the cross-check of orc_gc (same words).
+void orc_gc_serial(orc_pool *p, uint32_t *roots, uint32_t n_roots) { p->pool.gc_serial(roots, n_roots, &p->ok); }
 
 // ---- VBR colour (test infrastructure)
 struct orc_color_pool {

@@ -20,7 +20,8 @@
 //   mode 2: n_ops, then per op: level, len, words[len]
 //   mode 3: n_rays, then origins[3n] and dirs[3n] (float)
 //   mode 4: n_keep, keep[n_keep] (keep the root after edit keep[i]; the roots
-//           are the GC roots, collected by ThreadedGC on a one-worker pool)
+//           are the GC roots, collected by ThreadedGC on a pool of `threads`
+//           workers, one for the deterministic layout of the golden cases)
 //   mode 5 (colour edits through VBREditorWrapper): color_leaf_level,
 //           keep_history, per edit: kind (0 stateless, 1 VBR fill, 2 VBR
 //           paint), colors, weight, bits_per_weight; then n_queries and
@@ -31,7 +32,7 @@
 //   mode 2: n_ops, ptrs[n_ops] (after the pool dump)
 //   mode 3: n_rays, per ray: hit, pos[3] (float)
 //   mode 4: the dump is the pool after GC; then n_keep, roots before[n_keep],
-//           roots after[n_keep]
+//           roots after[n_keep], the collection's time (uint64 ns)
 //   mode 5: colour root, n_nodes, nodes[8 n_nodes], n_leaf_words,
 //           leaf_words[n], then per query: has_value, colors, weight,
 //           bits_per_weight, rgb[3] (float, VBRColor::Get()); then the time
@@ -318,6 +319,7 @@ static int run(FILE *in, FILE *out, uint32_t mode, const hashdag::Config<uint32_
 	std::vector<uint32_t> keep_at;
 	std::vector<hashdag::NodePointer<uint32_t>> kept;
 	std::vector<uint32_t> kept_before;
+	uint64_t gc_ns = 0;
 	if (mode == 4) {
 		uint32_t n_keep = rd(in);
 		keep_at.resize(n_keep);
@@ -386,8 +388,10 @@ static int run(FILE *in, FILE *out, uint32_t mode, const hashdag::Config<uint32_
 		}
 		for (auto &r : kept)
 			kept_before.push_back(*r);
-		lf::busy_pool busy(1);
+		lf::busy_pool busy(threads ? threads : 1); // one worker: the deterministic layout of the golden cases
+		const auto g0 = std::chrono::steady_clock::now();
 		kept = pool->ThreadedGC(&busy, kept);
+		gc_ns = std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now() - g0).count();
 		root = kept.empty() ? hashdag::NodePointer<uint32_t>{} : kept.back();
 	} else if (mode == 0 || mode == 3) {
 		for (auto &e : edits)
@@ -437,6 +441,7 @@ static int run(FILE *in, FILE *out, uint32_t mode, const hashdag::Config<uint32_
 			wr(out, v);
 		for (auto &r : kept)
 			wr(out, *r);
+		fwrite(&gc_ns, 8, 1, out);
 	}
 	if (mode == 5) {
 		wr(out, color_root.pointer);

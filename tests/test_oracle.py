@@ -299,3 +299,32 @@ def test_vbr_per_voxel_form_matches_reference(golden, orc):
     finally:
         orc.lib().orc_vbr_set_per_voxel(0)
     assert croot == g["color_root"] and sha(cp.leaves()) == g["leaves_sha"] and sha(cp.nodes()) == g["nodes_sha"]
+
+
+@pytest.mark.parametrize("threads", [1, 3, 0])
+@pytest.mark.parametrize("hasher", [0, 1])
+def test_gc_on_threads_equals_one_thread(orc, threads, hasher):
+    """The oracle's collector sorts each level's live nodes and lays out the
+    buckets on several threads; it must leave the pool word for word as the
+    one-thread, node-by-node form (the reference's one-worker order) does, with
+    several roots, whatever the thread count (the zero hasher: every node of a
+    level in one bucket, so one cache takes a whole level)."""
+    from vkhashdag_gb300 import workloads as W, Config
+    res, n_edits, scene = (512, 256, 16) if hasher == 0 else (64, 24, 4)
+    base = W.config_for_resolution(res, bottom_bits=12, top_levels=6)
+    cfg = Config(base.word_bits_per_page if hasher == 0 else 12, base.page_bits_per_bucket,
+                 base.bucket_bits_each_level, hasher)
+    a, b = orc.OraclePool.from_config(cfg), orc.OraclePool.from_config(cfg)
+    roots = []
+    ra = rb = orc.NULL
+    edits = [W.sphere_scene(res, scene, seed=9)] + [
+        W.mixed_batch(res, n_edits, seed=40 + k, r_max=res // 16, side_max=res // 8) for k in range(3)]
+    for e in edits:
+        ra, rb = a.edit(ra, e), b.edit(rb, e)
+        roots.append(ra)
+    assert ra == rb and a.ok and b.ok
+    wb, pb = cfg.word_bits_per_page, cfg.page_bits_per_bucket
+    new_a, new_b = a.gc(roots[1::2], threads), b.gc_serial(roots[1::2])
+    assert new_a == new_b and a.ok and b.ok
+    assert orc.pool_words_digest(*a.dump(), wb, pb) == orc.pool_words_digest(*b.dump(), wb, pb)
+    assert a.make_filled() == b.make_filled()
