@@ -402,6 +402,8 @@ def run_reference(mode, word_bits_per_page, page_bits_per_bucket, bucket_bits, e
         off += 4
         rec = np.frombuffer(data, np.dtype([("hit", "<u4"), ("pos", "<f4", (3,))]), n, off)
         out["hits"] = rec.copy()
+        off += 16 * n
+        (out["trace_ns"],) = struct.unpack_from("<Q", data, off)
     return out
 
 

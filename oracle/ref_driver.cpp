@@ -30,7 +30,8 @@
 //   magic 'HDRS', root, ok, elapsed_ns (uint64), filled[node_levels],
 //   total_buckets, bucket_words[total_buckets], n_pages, then per page: id, words[wpp]
 //   mode 2: n_ops, ptrs[n_ops] (after the pool dump)
-//   mode 3: n_rays, per ray: hit, pos[3] (float)
+//   mode 3: n_rays, per ray: hit, pos[3] (float); then the traversals' time
+//           (uint64 ns, one thread)
 //   mode 4: the dump is the pool after GC; then n_keep, roots before[n_keep],
 //           roots after[n_keep], the collection's time (uint64 ns)
 //   mode 5: colour root, n_nodes, nodes[8 n_nodes], n_leaf_words,
@@ -475,13 +476,23 @@ static int run(FILE *in, FILE *out, uint32_t mode, const hashdag::Config<uint32_
 		if (n && (fread(o.data(), 4, o.size(), in) != o.size() || fread(d.data(), 4, d.size(), in) != d.size()))
 			return 2;
 		wr(out, n);
+		std::vector<float> hits(4 * size_t(n));
+		const auto r0 = std::chrono::steady_clock::now();
 		for (uint32_t i = 0; i < n; ++i) {
 			auto r = pool->template Traversal<float>(root, glm::vec3{o[3 * i], o[3 * i + 1], o[3 * i + 2]},
 			                                          glm::vec3{d[3 * i], d[3 * i + 1], d[3 * i + 2]});
-			wr(out, r ? 1u : 0u);
-			float p[3] = {r ? r->x : 0.f, r ? r->y : 0.f, r ? r->z : 0.f};
-			fwrite(p, 4, 3, out);
+			hits[4 * size_t(i)] = r ? 1.f : 0.f;
+			hits[4 * size_t(i) + 1] = r ? r->x : 0.f;
+			hits[4 * size_t(i) + 2] = r ? r->y : 0.f;
+			hits[4 * size_t(i) + 3] = r ? r->z : 0.f;
 		}
+		const uint64_t trace_ns =
+		    std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now() - r0).count();
+		for (uint32_t i = 0; i < n; ++i) {
+			wr(out, hits[4 * size_t(i)] != 0.f ? 1u : 0u);
+			fwrite(&hits[4 * size_t(i) + 1], 4, 3, out);
+		}
+		fwrite(&trace_ns, 8, 1, out);
 	}
 	return 0;
 }
