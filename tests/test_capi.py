@@ -173,3 +173,23 @@ def test_colour_editors_to_descriptors(hd):
     assert e["colors"].tolist() == [0x030201, 0xABCD1234, 0] and e["bits_per_weight"].tolist() == [0, 2, 0]
     with pytest.raises(ValueError):
         hd.vbr_edits_to_array([hd.SphereEditor((1, 1, 1), 4, hd.EditMode.kFill)])
+
+
+def test_headers_compile_standalone(tmp_path):
+    """The C ABI header is plain C99; the C++ host headers compile on their own
+    with every warning on (they depend on nothing but hashdag_gpu.h)."""
+    import shutil
+    import subprocess
+    inc = os.path.join(ROOT, "include")
+    gcc, gxx = shutil.which("gcc"), shutil.which("g++")
+    if not gcc or not gxx:
+        pytest.skip("gcc / g++ not found")
+    r = subprocess.run([gcc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-fsyntax-only", "-x", "c",
+                        os.path.join(inc, "hashdag_gpu.h")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    for h in ("hashdag_host_mirror.hpp", "hashdag_gpu_pool.hpp"):
+        src = tmp_path / (h + ".cpp")
+        src.write_text(f'#include "{h}"\nint main() {{ return 0; }}\n')
+        r = subprocess.run([gxx, "-std=c++20", "-Wall", "-Wextra", "-pedantic", "-Werror", "-fsyntax-only", "-I", inc,
+                            str(src)], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
