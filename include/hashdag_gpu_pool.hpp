@@ -247,4 +247,82 @@ private:
 	bool m_synced = false;
 };
 
+/* The application's colour octree DAGColorPool (src/DAGColorPool.hpp:20-218)
+ * on the device, for the voxels of one GpuNodePool, edited with it as the
+ * application's vbr_edit lambda does (src/main.cpp:224-242: Edit with a
+ * VBREditorWrapper, then set_root of both roots).  Destroy it before its
+ * node pool. */
+class GpuColorPool {
+public:
+	static constexpr uint32_t kNull = HD_COLOR_NULL;
+
+	/* DAGColorPool::Create (src/DAGColorPool.cpp:9-47, Config leaf_level and
+	 * keep_history): the pool, or nullptr (reason in *status). */
+	static std::unique_ptr<GpuColorPool> Create(GpuNodePool &nodes, uint32_t leaf_level, bool keep_history = false,
+	                                            uint64_t max_nodes = uint64_t(1) << 20,
+	                                            uint64_t max_leaf_words = uint64_t(1) << 24, hd_status *status = nullptr) {
+		hd_color_config c{};
+		c.leaf_level = leaf_level;
+		c.keep_history = keep_history ? 1u : 0u;
+		c.max_nodes = max_nodes;
+		c.max_leaf_words = max_leaf_words;
+		hd_color_pool *p = nullptr;
+		const hd_status s = hd_color_pool_create(nodes.Handle(), &c, &p);
+		if (status)
+			*status = s;
+		if (s != HD_OK)
+			return nullptr;
+		return std::unique_ptr<GpuColorPool>(new GpuColorPool(nodes, p, leaf_level));
+	}
+	~GpuColorPool() { hd_color_pool_destroy(m_pool); }
+	GpuColorPool(const GpuColorPool &) = delete;
+	GpuColorPool &operator=(const GpuColorPool &) = delete;
+
+	hd_color_pool *Handle() const { return m_pool; }
+	uint32_t GetLeafLevel() const { return m_leaf_level; }
+	/* SetRoot / GetRoot (src/DAGColorPool.hpp) */
+	void SetRoot(uint32_t color_root) { m_root = color_root; }
+	uint32_t GetRoot() const { return m_root; }
+
+	/* Colour edits in order from the node pool's and this pool's roots; on
+	 * success both roots are set (set_root of src/main.cpp:239-243).  A full
+	 * octree fails the edit that overflowed it, with both roots as after the
+	 * edit before. */
+	hd_status VbrEdit(std::span<const hd_vbr_edit_desc> edits) {
+		uint32_t root = m_nodes.GetRoot(), color_root = m_root;
+		const hd_status s = hd_vbr_edit(m_nodes.Handle(), m_pool, root, color_root, edits.data(),
+		                                (uint32_t)edits.size(), &root, &color_root);
+		if (s == HD_OK || s == HD_ERR_POOL_OOM) {
+			m_nodes.SetRoot(root);
+			m_root = color_root;
+		}
+		return s;
+	}
+	/* The host mirror: the node and leaf word vectors of DAGColorPool, the
+	 * words its Flush uploads (src/DAGColorPool.cpp:49-80). */
+	hd_status Read(std::vector<uint32_t> *nodes, std::vector<uint32_t> *leaf_words) const {
+		uint64_t nn = 0, nl = 0;
+		hd_status s = hd_color_pool_read(m_pool, nullptr, &nn, nullptr, &nl);
+		if (s != HD_OK)
+			return s;
+		nodes->resize(nn * 8);
+		leaf_words->resize(nl);
+		return hd_color_pool_read(m_pool, nodes->data(), &nn, leaf_words->data(), &nl);
+	}
+	/* Colours of n voxels under the current colour root (trace.frag Color_Fetch;
+	 * device buffers). */
+	hd_status Fetch(const uint32_t *d_xyz, uint32_t n, hd_vbr_color *d_out, void *stream = nullptr) const {
+		return hd_color_fetch(m_pool, m_root, d_xyz, n, d_out, stream);
+	}
+
+private:
+	GpuColorPool(GpuNodePool &nodes, hd_color_pool *pool, uint32_t leaf_level)
+	    : m_nodes(nodes), m_pool(pool), m_leaf_level(leaf_level) {}
+
+	GpuNodePool &m_nodes;
+	hd_color_pool *m_pool;
+	uint32_t m_leaf_level;
+	uint32_t m_root = kNull;
+};
+
 } // namespace hashdag_gb300

@@ -14,6 +14,8 @@
 //                            then GC through the class and the same check
 //   gpu_pool_check publish   on a GPU: incremental Publish after edits equals a
 //                            full Download; after a GC it re-reads everything
+//   gpu_pool_check color     on a GPU: GpuColorPool, the same colour edits one
+//                            per call and in one call give the same octree words
 // Built with -DHD_FAKE_DEVICE instead (no library, no GPU): the pool entry
 // points GpuNodePool calls are served by an in-memory pool below, and
 //   gpu_pool_check fake_publish   Publish: full on the first sync and after an
@@ -358,6 +360,53 @@ static int check_publish() {
 	CHECK(counts == m.BucketWords());
 	return 0;
 }
+
+// GpuColorPool: the same coloured edits applied one per call and all in one
+// call leave the same octree words and roots; digs keep the colour root.
+static int color_run(bool one_call, std::vector<uint32_t> *nodes, std::vector<uint32_t> *leaves, uint32_t *croot) {
+	const hd_config c = small_config();
+	hd_status s = HD_OK;
+	auto pool = GpuNodePool::Create(c, 0, 0, &s);
+	CHECK_OK(s);
+	auto colors = hashdag_gb300::GpuColorPool::Create(*pool, 3, false, 1u << 16, 1u << 22, &s);
+	CHECK_OK(s);
+	CHECK(colors != nullptr && colors->GetRoot() == HD_COLOR_NULL && colors->GetLeafLevel() == 3);
+	std::vector<hd_vbr_edit_desc> v(6);
+	const hd_edit_desc g[6] = {box(HD_OP_FILL, 10, 10, 10, 200, 120, 200), sphere(HD_OP_FILL, 128, 120, 100, 40),
+	                           sphere(HD_OP_PAINT, 100, 100, 100, 30), box(HD_OP_DIG, 0, 0, 0, 60, 60, 60),
+	                           sphere(HD_OP_FILL, 60, 60, 60, 20), sphere(HD_OP_PAINT, 180, 110, 150, 25)};
+	for (int i = 0; i < 6; ++i) {
+		v[i] = hd_vbr_edit_desc{};
+		v[i].edit = g[i];
+		v[i].colors = 0x102030u * uint32_t(i + 1);
+	}
+	v[2].bits_per_weight = 2; // a weighted paint: two R5G6B5 end points
+	v[2].weight = 3;
+	v[2].colors = 0x001F07E0u;
+	if (one_call) {
+		CHECK_OK(colors->VbrEdit(v));
+	} else {
+		for (size_t i = 0; i < v.size(); ++i) {
+			const uint32_t before = colors->GetRoot();
+			CHECK_OK(colors->VbrEdit(std::span<const hd_vbr_edit_desc>(v.data() + i, 1)));
+			if (v[i].edit.op == HD_OP_DIG)
+				CHECK(colors->GetRoot() == before);
+		}
+	}
+	CHECK(pool->GetRoot() != HD_NULL_PTR && colors->GetRoot() != HD_COLOR_NULL);
+	CHECK_OK(colors->Read(nodes, leaves));
+	CHECK(!nodes->empty() && !leaves->empty() && nodes->size() % 8 == 0);
+	*croot = colors->GetRoot();
+	return 0;
+}
+static int check_color() {
+	std::vector<uint32_t> n1, l1, n2, l2;
+	uint32_t r1 = 0, r2 = 0;
+	if (color_run(false, &n1, &l1, &r1) || color_run(true, &n2, &l2, &r2))
+		return 1;
+	CHECK(r1 == r2 && n1 == n2 && l1 == l2);
+	return 0;
+}
 #else
 static uint64_t g_rng = 0x9E3779B97F4A7C15ull;
 static uint32_t rnd(uint32_t n) {
@@ -530,6 +579,8 @@ int main(int argc, char **argv) {
 		rc = check_device();
 	else if (mode == "publish")
 		rc = check_publish();
+	else if (mode == "color")
+		rc = check_color();
 #else
 	else if (mode == "fake_publish")
 		rc = check_fake_publish();

@@ -132,3 +132,10 @@ def test_device_pool_download_upload_round_trip(hd, tmp_path):
     edits on both, occupancy against the edits' predicates, GC through the
     class."""
     run_check(build_check(hd, tmp_path), "device")
+
+
+@pytest.mark.gpu
+def test_colour_pool_class(hd, tmp_path):
+    """GpuColorPool over the colour entry points: one edit per call and all in
+    one call give the same octree words and roots; digs keep the colour root."""
+    run_check(build_check(hd, tmp_path), "color")
