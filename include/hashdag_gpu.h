@@ -173,7 +173,10 @@ hd_status hd_edit_reserve(hd_pool *pool, uint64_t max_items, uint64_t max_list_e
 /* Per-level counters of the last edit pass (arrays of node_levels entries,
  * any may be NULL): items = nodes visited (frontier size), candidates = nodes
  * that went through the dedup pass and their words, inserted = nodes newly
- * appended to buckets and their words. */
+ * appended to buckets and their words.  For diagnosis, the environment
+ * variable HD_DEBUG_SYNC (any value) makes every pass launch its kernels
+ * directly (no graph), synchronise after each phase and print the pass
+ * counters to stderr; the results are the same. */
 hd_status hd_edit_last_counters(hd_pool *pool, uint64_t *items, uint64_t *candidates, uint64_t *candidate_words,
                                 uint64_t *inserted, uint64_t *inserted_words);
 /* Dedup-index statistics of the last edit pass (any may be NULL): index slots
