@@ -328,3 +328,26 @@ def test_gc_on_threads_equals_one_thread(orc, threads, hasher):
     assert new_a == new_b and a.ok and b.ok
     assert orc.pool_words_digest(*a.dump(), wb, pb) == orc.pool_words_digest(*b.dump(), wb, pb)
     assert a.make_filled() == b.make_filled()
+
+
+@pytest.mark.parametrize("threads", [1, 3, 8])
+@pytest.mark.parametrize("depth", ["root", "mid", "deep"])
+def test_threaded_edit_any_team_and_depth(orc, threads, depth):
+    """The threaded restatement forks every child but the last (run on the
+    forking thread, as lf_edit_node does) on one thread team for the whole edit
+    sequence: whatever the team size and the task depth, the same canonical DAG
+    as the serial edit, and the same point occupancy."""
+    from vkhashdag_gb300 import workloads as W
+    res = 512
+    cfg = W.config_for_resolution(res)
+    L = cfg.get_node_levels()
+    mtl = {"root": 0, "mid": max(0, L - 5), "deep": L - 1}[depth]
+    edits = np.concatenate([W.sphere_scene(res, 16, seed=11), W.mixed_batch(res, 400, seed=12, r_max=32, side_max=64)])
+    serial = orc.OraclePool.from_config(cfg)
+    rs = serial.edit(orc.NULL, edits)
+    threaded = orc.OraclePool.from_config(cfg)
+    rt = threaded.threaded_edit(orc.NULL, edits, mtl, threads)
+    ok, _, dig = threaded.canonical(rt)
+    assert ok and threaded.ok and dig == serial.canonical(rs)[2]
+    q = W.point_queries(res, 1 << 14, seed=13)
+    assert np.array_equal(threaded.query(rt, q), serial.query(rs, q))
