@@ -16,10 +16,17 @@
 //     one edit, each axis's terms shared by the children on the same half)
 //     against classify of each child, at every cell size from 4 to 2^20 voxels.
 // Exit status 0 and "ok <counts>" on success; the first mismatches are printed.
+//
+// `edit_rule_check hashes IN OUT` hashes nodes the way the dedup kernel does
+// (Murmur over an inner node's words finished with its length; hash_leaf of a
+// leaf's 64 bits, low word first) for records of IN (kind 0 inner / 1 leaf,
+// length, words; uint32) and writes one uint32 per record to OUT, for a test
+// to compare with the oracle's hashes (Hasher.hpp:21-48).
 #include "../vkhashdag_gb300/csrc/hd_device.cuh"
 
 #include <cmath>
 #include <cstdio>
+#include <cstring>
 
 using namespace hd;
 
@@ -226,7 +233,34 @@ static void check_children_all(u32 world_bits, double max_r, int n_edits) {
 	}
 }
 
-int main() {
+static int hashes(const char *in, const char *out) {
+	FILE *f = std::fopen(in, "rb"), *g = std::fopen(out, "wb");
+	if (!f || !g)
+		return 2;
+	u32 kind, len, w[9];
+	while (std::fread(&kind, 4, 1, f) == 1 && std::fread(&len, 4, 1, f) == 1) {
+		if (len < 1 || len > 9 || std::fread(w, 4, len, f) != len)
+			return 2;
+		u32 h;
+		if (kind == 1) {
+			h = hash_leaf((u64)w[0] | ((u64)w[1] << 32));
+		} else {
+			Murmur m;
+			for (u32 k = 0; k < len; ++k)
+				m.add(w[k]);
+			h = m.finish(len);
+		}
+		std::fwrite(&h, 4, 1, g);
+	}
+	std::fclose(f);
+	std::fclose(g);
+	std::printf("ok hashes\n");
+	return 0;
+}
+
+int main(int argc, char **argv) {
+	if (argc == 4 && std::strcmp(argv[1], "hashes") == 0)
+		return hashes(argv[2], argv[3]);
 	check_spread();
 	check_boxes(1u << 15, 2048, 4000, 64);
 	check_boxes(1u << 21, 1u << 20, 2000, 64);

@@ -76,7 +76,7 @@ __device__ __forceinline__ void set_error(u32 *slot, u32 code) { atomicCAS(slot,
 // include/hashdag/Hasher.hpp:21-39: MurmurHash3 x86-32 body, seed 0, length = words
 struct Murmur {
 	u32 h = 0;
-	__device__ __forceinline__ void add(u32 k) {
+	__host__ __device__ __forceinline__ void add(u32 k) {
 		k *= 0xcc9e2d51u;
 		k = (k << 15) | (k >> 17);
 		k *= 0x1b873593u;
@@ -84,7 +84,7 @@ struct Murmur {
 		h = (h << 13) | (h >> 19);
 		h = h * 5u + 0xe6546b64u;
 	}
-	__device__ __forceinline__ u32 finish(u32 n) const {
+	__host__ __device__ __forceinline__ u32 finish(u32 n) const {
 		u32 x = h ^ n;
 		x ^= x >> 16;
 		x *= 0x85ebca6bu;
@@ -95,7 +95,7 @@ struct Murmur {
 	}
 };
 // include/hashdag/Hasher.hpp:40-48: 64-bit finaliser truncated to 32 bits (leaves)
-__device__ __forceinline__ u32 hash_leaf(u64 v) {
+__host__ __device__ __forceinline__ u32 hash_leaf(u64 v) {
 	v ^= v >> 33;
 	v *= 0xff51afd7ed558ccdull;
 	v ^= v >> 33;
