@@ -101,7 +101,10 @@ def run_scenario(s):
     op.load(r["bucket_words"], r["page_ids"], r["pages"], r["filled"])
     ok, counts, digests = op.canonical(r["root"])
     assert ok, s["name"]
-    q = W.point_queries(s["res"], 1 << 16, seed=7)
+    # 2^20 seeded point queries on the 1024^3 sphere scene (the CPU-runnable
+    # configuration's verification), 2^16 elsewhere
+    n_queries = 1 << 20 if s["name"] == "scene1024" else 1 << 16
+    q = W.point_queries(s["res"], n_queries, seed=7)
     occ = op.query(r["root"], q)
     # threaded run of the reference: same canonical DAG
     L = cfg.get_node_levels()
@@ -115,7 +118,7 @@ def run_scenario(s):
     rec.update(config=cfg_dict(cfg), edits_sha=sha(edits), n_edits=int(len(edits)), root=r["root"],
                filled=r["filled"], pool_sha=sha(r["bucket_words"], r["page_ids"], r["pages"]),
                canonical_counts=counts, canonical_digests=[str(d) for d in digests],
-               query_seed=7, n_queries=1 << 16, query_sha=sha(occ), query_set=int(occ.sum()),
+               query_seed=7, n_queries=n_queries, query_sha=sha(occ), query_set=int(occ.sum()),
                threaded_canonical_equal=bool(ok2 and d2 == digests))
     if s["name"] == "aabb_kat":  # roots after each step (test/test.cpp:161-199 intent)
         roots = []
