@@ -168,8 +168,9 @@ def workload(rank, n_batches, n_edits, res):
 
 
 # ---------------------------------------------------------------------- CPU (oracle) timing
-def cpu_sample_rate(orc_pool, root, edits, res, budget_s, threads, max_task_level):
-    """Threaded CPU editor over a growing prefix of `edits` until budget_s is spent."""
+def cpu_sample_rate(orc_pool, root, edits, res, budget_s, threads, max_task_level, serial=False):
+    """Threaded CPU editor (or the serial one) over a growing prefix of `edits`
+    until budget_s is spent."""
     import vkhashdag_gb300 as hd
     done, t_used, ve = 0, 0.0, 0
     r = root
@@ -177,12 +178,39 @@ def cpu_sample_rate(orc_pool, root, edits, res, budget_s, threads, max_task_leve
     while done < len(edits) and t_used < budget_s:
         e = edits[done:done + chunk]
         t0 = time.perf_counter()
-        r = orc_pool.threaded_edit(r, e, max_task_level, threads)
+        r = orc_pool.edit(r, e) if serial else orc_pool.threaded_edit(r, e, max_task_level, threads)
         t_used += time.perf_counter() - t0
         ve += hd.count_voxel_edits(e, res)
         done += len(e)
         chunk = min(chunk * 2, 256)
     return ve / t_used, done, t_used
+
+
+def cpu_model():
+    """The host CPU's model name (x86 /proc/cpuinfo, else lscpu: Arm cores)."""
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    return "unknown"
+
+
+def serial_baseline(orc_pool, root, edits, res, budget_s):
+    """The reference's serial NodePoolBase::Edit (restated), one thread, on the
+    same edits as the threaded baseline, for budget_s seconds."""
+    rate, n_done, t_used = cpu_sample_rate(orc_pool, root, edits, res, budget_s, 1, 0, serial=True)
+    return {"value": rate, "unit": "voxel-edits/s", "cores": 1,
+            "sample": f"first {n_done} edits, one Edit each ({t_used:.1f} s)"}
 
 
 def run_reference(args):
@@ -198,7 +226,8 @@ def run_reference(args):
     L = cfg.get_node_levels()
     threads = os.cpu_count() or 1
     mtl = max(0, L - 4)
-    base, batches = workload(0, args.warmup + args.steps, args.n_edits, args.resolution)
+    base, batches = workload(0, args.warmup + args.steps + 1, args.n_edits, args.resolution)
+    serial_batch = batches.pop()  # edits no step applies: the serial editor's sample
     pool = oracle.OraclePool.from_config(cfg)
     t0 = time.perf_counter()
     root0 = pool.threaded_edit(oracle.NULL, base, mtl, threads)
@@ -213,6 +242,7 @@ def run_reference(args):
     value = float(np.mean(rates))
     n_done = sum(s[0] for s in samples)
     t_all = sum(s[1] for s in samples)
+    serial = serial_baseline(pool, root0, serial_batch, args.resolution, args.ref_step_seconds)
     sample = (f"first {n_done // max(1, len(samples))} edits (on average) of each of {args.steps} batches of "
               f"{args.n_edits}, applied one by one by the threaded CPU editor to the seeded {args.resolution}^3 scene "
               f"(scene build {t_base:.1f} s untimed)")
@@ -222,7 +252,8 @@ def run_reference(args):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
         "config": {"workload": f"batched-{args.n_edits}-mixed-edits-{args.resolution}^3", "node_levels": L,
                    "bucket_bits": BUCKET_BITS, "max_task_level": mtl},
-        "cpu_baseline": {"value": value, "unit": "voxel-edits/s", "cores": threads, "kind": "port", "sample": sample},
+        "cpu_baseline": {"value": value, "unit": "voxel-edits/s", "cores": threads, "kind": "port", "sample": sample,
+                         "cpu_model": cpu_model(), "serial": serial},
         "e2e": {"value": value, "unit": "voxel-edits/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -390,9 +421,13 @@ def run_ours(args):
         threads = os.cpu_count() or 1
         rate, n_done, t_used = cpu_sample_rate(opool, root0, batches[args.warmup], res, args.cpu_seconds, threads,
                                                max(0, L - 4))
+        # the serial editor on the next batch (edits the threaded sample did not apply)
+        serial = serial_baseline(opool, root0, batches[(args.warmup + 1) % len(batches)], res,
+                                 args.cpu_seconds / 3)
         cpu = {"value": rate, "unit": "voxel-edits/s", "cores": threads, "kind": "port",
                "sample": f"first {n_done} edits of the first timed batch, one ThreadedEdit each, on the seeded "
-                         f"scene downloaded from the device ({t_used:.1f} s of CPU time)"}
+                         f"scene downloaded from the device ({t_used:.1f} s of CPU time)",
+               "cpu_model": cpu_model(), "serial": serial}
         del opool
 
     if rank != 0:
