@@ -170,8 +170,9 @@ def workload(rank, n_batches, n_edits, res):
 # ---------------------------------------------------------------------- CPU (oracle) timing
 def cpu_sample_rate(orc_pool, root, edits, res, budget_s, threads, max_task_level, serial=False):
     """Threaded CPU editor (or the serial one) over a growing prefix of `edits`
-    until budget_s is spent."""
-    import vkhashdag_gb300 as hd
+    until budget_s is spent.  Returns (voxel-edits/s, edits applied, seconds,
+    root after them)."""
+    import oracle
     done, t_used, ve = 0, 0.0, 0
     r = root
     chunk = 8
@@ -180,10 +181,10 @@ def cpu_sample_rate(orc_pool, root, edits, res, budget_s, threads, max_task_leve
         t0 = time.perf_counter()
         r = orc_pool.edit(r, e) if serial else orc_pool.threaded_edit(r, e, max_task_level, threads)
         t_used += time.perf_counter() - t0
-        ve += hd.count_voxel_edits(e, res)
+        ve += oracle.count_voxel_edits(e, res)
         done += len(e)
         chunk = min(chunk * 2, 256)
-    return ve / t_used, done, t_used
+    return ve / t_used, done, t_used, r
 
 
 def cpu_model():
@@ -206,36 +207,131 @@ def cpu_model():
 
 
 def serial_baseline(orc_pool, root, edits, res, budget_s):
-    """The reference's serial NodePoolBase::Edit (restated), one thread, on the
-    same edits as the threaded baseline, for budget_s seconds."""
-    rate, n_done, t_used = cpu_sample_rate(orc_pool, root, edits, res, budget_s, 1, 0, serial=True)
+    """The reference's serial NodePoolBase::Edit (restated), one thread, for
+    budget_s seconds."""
+    rate, n_done, t_used, _ = cpu_sample_rate(orc_pool, root, edits, res, budget_s, 1, 0, serial=True)
     return {"value": rate, "unit": "voxel-edits/s", "cores": 1,
             "sample": f"first {n_done} edits, one Edit each ({t_used:.1f} s)"}
 
 
+def replica_seed_of(rank, batch):
+    from vkhashdag_gb300.replicas import replica_seed
+    return replica_seed(rank, batch)
+
+
+def leaf_roofline(counters, work, L, n_edits, leaf_ms, hbm, peak_kind):
+    """Roofline of the level-(L-2) leaf kernels (k_leafparent_short/_long) from
+    the pass's own work counters.  Algorithmic bytes: per level-(L-2) node its
+    item record (24 B: position, base, list offset and length, parent slot),
+    per (node, edit) pair its list entry (4 B), the base node's words, every
+    old leaf read (8 B), per changed leaf its index slot (8 B) and, when found,
+    the resident leaf (8 B); written: each new leaf candidate (12 B), each
+    unresolved node's todo record (72 B) or each resolved node's parent slot
+    (4 B); and every edit descriptor once (40 B)."""
+    nodes, pairs = work["nodes"], work["pairs"]
+    cand_leaf = int(counters["items"][L - 1])
+    todo = int(counters["candidates"][L - 2]) if L >= 2 else 0
+    found = max(0, work["lookups"] - cand_leaf)
+    alg = (24 * nodes + 4 * pairs + 4 * work["base_words"] + 8 * work["old_leaves"] + 8 * work["lookups"] +
+           8 * found + 12 * cand_leaf + 72 * todo + 4 * max(0, nodes - todo) + 40 * n_edits)
+    achieved = alg / (leaf_ms / 1e3) / 1e9
+    return {"bound": "hbm", "kernel": "leaf kernels (k_leafparent_short/_long)", "achieved": achieved, "peak": hbm,
+            "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm, "algorithmic_bytes_per_step": float(alg),
+            "leaf_ms_per_step": leaf_ms, "work_last_step": work,
+            "leaf_edit_evaluations_per_s": 8.0 * pairs / (leaf_ms / 1e3),
+            "issue_efficiency": _profile_value("leaf_issue.json", "active_lanes_per_inst", 1.0 / 32.0),
+            "note": "integer voxel-mask work with divergent lanes, not DRAM bound; issue_efficiency = active lanes "
+                    "per issued instruction / 32 from the committed ncu capture"}
+
+
+def batched_config(cfg, res, n_edits, ve_per_step, world):
+    """The `config` of the batched workload; both arms print this same object."""
+    return {"workload": f"batched-{n_edits}-mixed-edits-{res}^3", "resolution": res, "edits_per_step": n_edits,
+            "voxel_edits_per_step": float(ve_per_step),
+            "seeded_scene": "sphere r=9600 fill + 64 sphere digs r in [512,2048] (1024^3 scene x32)",
+            "node_levels": cfg.get_node_levels(), "bucket_bits": list(cfg.bucket_bits_each_level),
+            "word_bits_per_page": cfg.word_bits_per_page, "page_bits_per_bucket": cfg.page_bits_per_bucket,
+            "rollback_to_seeded_scene_each_step": True,
+            "l2": "working set of a step (pool + frontier, tens of GB) far above L2; no flush",
+            "parallelism": f"replicas x{world}"}
+
+
+def sequential_oracle_leg(cfg, base, batch, res, threads, budget_s, serial_batch, queries):
+    """The CPU leg of the batched benchmark, on the oracle alone (all host
+    threads): it builds the seeded scene itself, times the first budget_s of
+    the batch with the threaded editor (NodePoolThreadedEdit::ThreadedEdit
+    restated: the reference's sequential semantics, edits in seed order), then
+    applies the rest of the batch and returns the canonical DAG and point
+    occupancy of the result beside the CPU rates."""
+    import oracle
+    L = cfg.get_node_levels()
+    mtl = max(0, L - 4)
+    opool = oracle.OraclePool.from_config(cfg)
+    t0 = time.perf_counter()
+    r0 = opool.threaded_edit(oracle.NULL, base, mtl, threads)
+    t_scene = time.perf_counter() - t0
+    rate, n_done, t_used, r = cpu_sample_rate(opool, r0, batch, res, budget_s, threads, mtl)
+    t0 = time.perf_counter()
+    if n_done < len(batch):
+        r = opool.threaded_edit(r, batch[n_done:], mtl, threads)
+    t_rest = time.perf_counter() - t0
+    serial = serial_baseline(opool, r0, serial_batch, res, budget_s / 3)
+    t0 = time.perf_counter()
+    ok, counts, digests = opool.canonical(r)
+    occ = opool.query(r, queries)
+    t_canon = time.perf_counter() - t0
+    pool_ok = opool.ok
+    del opool
+    cpu = {"value": rate, "unit": "voxel-edits/s", "cores": threads, "kind": "port",
+           "sample": f"first {n_done} edits of the last timed batch, one ThreadedEdit each ({t_used:.1f} s of CPU "
+                     f"time), on the seeded scene the CPU editor built itself ({t_scene:.1f} s, untimed)",
+           "cpu_model": cpu_model(), "max_task_level": mtl, "serial": serial}
+    ref = {"ok": bool(ok and pool_ok), "counts": counts, "digests": digests, "occupancy": occ,
+           "seconds": {"scene": t_scene, "batch": t_used + t_rest, "canonical_and_queries": t_canon}}
+    return cpu, ref
+
+
+def device_canonical(cfg, snapshot, filled, root):
+    """Canonical DAG of a device pool snapshot (downloaded words) under root,
+    by the oracle's canonicaliser."""
+    import oracle
+    mirror = oracle.OraclePool.from_config(cfg)
+    mirror.load(*snapshot, filled)
+    ok, counts, digests = mirror.canonical(root)
+    del mirror
+    return ok, counts, digests
+
+
 def run_reference(args):
-    """--impl reference: the CPU restatement of the reference's threaded editor,
-    all host threads, same workload (bounded samples per step)."""
+    """--impl reference: the CPU restatement of the reference's threaded editor
+    (the oracle, OpenMP on all host threads) on the same workload, bounded
+    samples per step.  Nothing of the engine runs here: the edits come from the
+    seeded generators (numpy), voxel-edits are counted by the oracle, and the
+    engine's library is never loaded."""
     world, rank, _ = dist_setup()
     if rank != 0:
         return
     import oracle
     oracle.build()
-    import vkhashdag_gb300 as hd  # host helpers only (voxel counting, workload arrays)
-    cfg = bench_config()
+    if args.resolution == RES:
+        cfg = bench_config()
+    else:
+        from vkhashdag_gb300 import workloads as W
+        cfg = W.config_for_resolution(args.resolution, bottom_bits=16, top_levels=6)
     L = cfg.get_node_levels()
     threads = os.cpu_count() or 1
     mtl = max(0, L - 4)
     base, batches = workload(0, args.warmup + args.steps + 1, args.n_edits, args.resolution)
     serial_batch = batches.pop()  # edits no step applies: the serial editor's sample
+    ve_timed = [oracle.count_voxel_edits(b, args.resolution) for b in batches[args.warmup:]]
     pool = oracle.OraclePool.from_config(cfg)
     t0 = time.perf_counter()
     root0 = pool.threaded_edit(oracle.NULL, base, mtl, threads)
     t_base = time.perf_counter() - t0
     rates, samples = [], []
     for k in range(args.warmup + args.steps):
-        rate, n_done, t_used = cpu_sample_rate(pool, root0, batches[k], args.resolution, args.ref_step_seconds,
-                                              threads, mtl)
+        rate, n_done, t_used, _ = cpu_sample_rate(pool, root0, batches[k], args.resolution, args.ref_step_seconds,
+                                                 threads, mtl)
         if k >= args.warmup:
             rates.append(rate)
             samples.append((n_done, t_used))
@@ -250,10 +346,9 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "voxel-edits/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_all / max(1, len(samples)),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": {"workload": f"batched-{args.n_edits}-mixed-edits-{args.resolution}^3", "node_levels": L,
-                   "bucket_bits": BUCKET_BITS, "max_task_level": mtl},
+        "config": batched_config(cfg, args.resolution, args.n_edits, float(np.mean(ve_timed)), world),
         "cpu_baseline": {"value": value, "unit": "voxel-edits/s", "cores": threads, "kind": "port", "sample": sample,
-                         "cpu_model": cpu_model(), "serial": serial},
+                         "cpu_model": cpu_model(), "max_task_level": mtl, "serial": serial},
         "e2e": {"value": value, "unit": "voxel-edits/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -333,9 +428,18 @@ def run_ours(args):
         raise RuntimeError(f"device error {err} in the timed region")
     counters = pool.last_counters_full()
     probe_stats = pool.last_probe_stats()
+    leaf_work = pool.last_leaf_work()
+    last_root = int(d_out[n_batches - 1].item()) & 0xFFFFFFFF
+    # the timed result itself, for the check against the sequential CPU editor
+    # at the end (outside every timed region): the pool's words and 2^20 point
+    # queries under the last timed batch's root
+    queries = W.point_queries(res, 1 << 20, seed=7)
+    snapshot, dev_occ = None, None
+    if rank == 0 and not args.no_cpu:
+        snapshot = pool.download()
+        dev_occ = pool.query(last_root, queries)
     # self-check: re-running the last batch on the same pool finds every node it
     # inserted, so the synchronous path must return the very same root
-    last_root = int(d_out[n_batches - 1].item()) & 0xFFFFFFFF
     same_roots = pool.edit(root0, batches[n_batches - 1]) == last_root
     from vkhashdag_gb300.replicas import replica_totals
     elapsed_ms, total_ve = replica_totals(elapsed_ms, float(sum(ve[args.warmup:])), device=f"cuda:{local}")
@@ -351,41 +455,68 @@ def run_ours(args):
         e2e_times.append(time.perf_counter() - t0)
     e2e_value = sum(ve[args.warmup:]) / sum(e2e_times)
 
-    # ---------------- plain form: one pass per edit, same edit list
+    # ---------------- plain form against one batched pass, on the same edit list
+    plain = np.ascontiguousarray(batches[args.warmup][: args.per_edit])
+    plain_ve = hd.count_voxel_edits(plain, res)
+    d_plain = torch.from_numpy(plain.view(np.uint8).copy()).to(f"cuda:{local}")
+    d_root = torch.zeros(1, dtype=torch.int32, device=f"cuda:{local}")
+    d_root0 = torch.full((1,), root0 if root0 < (1 << 31) else root0 - (1 << 32), dtype=torch.int32,
+                         device=f"cuda:{local}")
+    # (1) wall latency of hd_edit, one call per edit (host edits, host root)
     pool.rollback(0)
     torch.cuda.synchronize()
-    plain = batches[args.warmup][: args.per_edit]
     lat = []
     r = root0
     for k in range(len(plain)):
         t0 = time.perf_counter()
         r = pool.edit(r, plain[k:k + 1])
         lat.append(time.perf_counter() - t0)
+    plain_root = r
     lat_ms = np.array(lat) * 1e3
-    plain_ve = hd.count_voxel_edits(plain, res)
-    plain_rate = plain_ve / (lat_ms.sum() / 1e3)
-    # device time of the same plain passes, back to back on the stream
+    plain_wall_s = float(lat_ms.sum()) / 1e3
+    # (2) device time of the same passes back to back on the stream: the root
+    # stays on the device, the host copies of the edits size every launch as
+    # hd_edit does (grids from bounding boxes, small passes as one CTA)
     pool.rollback(0)
-    d_plain = d_batches[args.warmup]
-    d_root = torch.zeros(1, dtype=torch.int32, device=f"cuda:{local}")
     torch.cuda.synchronize()
     s2, e2 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    d_root.copy_(d_root0)
+    torch.cuda.synchronize()
     s2.record(stream)
-    d_root_ptr = d_root.data_ptr()
     for k in range(len(plain)):
-        if k == 0:
-            pool.edit_async(root0, d_plain.data_ptr(), 1, d_root_ptr, sp)
-        else:
-            pool.edit_async_droot(d_root_ptr, d_plain.data_ptr() + 40 * k, 1, d_root_ptr, sp)
+        pool.edit_async_droot_hinted(d_root.data_ptr(), d_plain.data_ptr() + 40 * k, plain[k:k + 1],
+                                     d_root.data_ptr(), sp)
     e2.record(stream)
     torch.cuda.synchronize()
     plain_dev_ms = s2.elapsed_time(e2)
-    # re-running the chain finds every node: same final root
-    rr = root0
+    plain_dev_root = int(d_root.item()) & 0xFFFFFFFF
+    # (3) the same edits as ONE batched pass: device time and hd_edit wall time
+    pool.rollback(0)
+    d_root.copy_(d_root0)
+    torch.cuda.synchronize()
+    s2.record(stream)
+    pool.edit_async_droot_hinted(d_root.data_ptr(), d_plain.data_ptr(), plain, d_root.data_ptr(), sp)
+    e2.record(stream)
+    torch.cuda.synchronize()
+    batched_dev_ms = s2.elapsed_time(e2)
+    batched_dev_root = int(d_root.item()) & 0xFFFFFFFF
+    bw_times = []
+    for _ in range(3):
+        pool.rollback(0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        batched_root = pool.edit(root0, plain)
+        bw_times.append(time.perf_counter() - t0)
+    batched_wall_s = float(np.median(bw_times))
+    # all forms end on one root: the pool is fully deduplicated, so equal
+    # occupancy means the very same pointer (the plain chain re-run on the
+    # batched pass's pool finds every node of its final DAG)
+    r = root0
     for k in range(len(plain)):
-        rr = pool.edit(rr, plain[k:k + 1])
-    plain_same = (int(d_root.item()) & 0xFFFFFFFF) == rr
-    plain_dev_rate = plain_ve / (plain_dev_ms / 1e3)
+        r = pool.edit(r, plain[k:k + 1])
+    plain_same = r == batched_root == plain_root == plain_dev_root == batched_dev_root
+    if pool.error():
+        raise RuntimeError(f"device error {pool.error()} in the plain/batched comparison")
 
     # ---------------- roofline of the dedup pass
     hbm, peak_kind = peaks()
@@ -407,28 +538,35 @@ def run_ours(args):
     # DRAM bytes of the dedup pass per step, from the committed ncu summary of a
     # smaller case scaled to this workload (only meaningful for the default one)
     traffic = _profile_value("dedup_traffic.json", "bytes_per_step") if (res, n_edits) == (RES, N_EDITS) else None
+    leaf_roof = leaf_roofline(counters, leaf_work, L, n_edits, float(phases[1]) / npass, hbm, peak_kind)
 
-    # ---------------- CPU baseline (rank 0, bounded sample), oracle on host cores
-    cpu = None
+    # ---------------- CPU leg (rank 0): the oracle's threaded editor on the
+    # host cores, timed on a bounded sample of the last timed batch and then
+    # run to the end of that batch; its canonical DAG must equal the device's
+    cpu, checks = None, {"rerun_of_last_batch_finds_same_root": bool(same_roots)}
     if rank == 0 and not args.no_cpu:
         import oracle
         oracle.build()
-        pool.rollback(0)
-        torch.cuda.synchronize()
-        bw, ids, pages = pool.download()
-        opool = oracle.OraclePool.from_config(cfg)
-        opool.load(bw, ids, pages, pool.filled_node_pointers())
         threads = os.cpu_count() or 1
-        rate, n_done, t_used = cpu_sample_rate(opool, root0, batches[args.warmup], res, args.cpu_seconds, threads,
-                                               max(0, L - 4))
-        # the serial editor on the next batch (edits the threaded sample did not apply)
-        serial = serial_baseline(opool, root0, batches[(args.warmup + 1) % len(batches)], res,
-                                 args.cpu_seconds / 3)
-        cpu = {"value": rate, "unit": "voxel-edits/s", "cores": threads, "kind": "port",
-               "sample": f"first {n_done} edits of the first timed batch, one ThreadedEdit each, on the seeded "
-                         f"scene downloaded from the device ({t_used:.1f} s of CPU time)",
-               "cpu_model": cpu_model(), "serial": serial}
-        del opool
+        cpu, ref = sequential_oracle_leg(cfg, base, batches[n_batches - 1], res, threads, args.cpu_seconds,
+                                         batches[args.warmup], queries)
+        t0 = time.perf_counter()
+        dok, dcounts, ddigests = device_canonical(cfg, snapshot, pool.filled_node_pointers(), last_root)
+        t_dev_canon = time.perf_counter() - t0
+        del snapshot
+        equal = bool(ref["ok"] and dok and dcounts == ref["counts"] and ddigests == ref["digests"])
+        checks["canonical_equal_sequential_oracle"] = equal
+        checks["point_queries_equal_sequential_oracle"] = bool(np.array_equal(dev_occ, ref["occupancy"]))
+        checks["sequential_oracle"] = {
+            "what": f"the last timed batch ({n_edits} edits) applied in seed order by the oracle's threaded editor "
+                    f"to the seeded scene it built itself; canonical DAG (per level, the sorted unique node tuples "
+                    f"with child pointers renumbered) and {len(queries)} seeded point queries against the device's "
+                    f"result of the timed step",
+            "batch_seed": int(replica_seed_of(rank, n_batches - 1)),
+            "canonical_counts": dcounts, "canonical_digests": [str(d) for d in ddigests],
+            "oracle_canonical_digests": [str(d) for d in ref["digests"]],
+            "occupied_queries": int(dev_occ.sum()),
+            "seconds": dict(ref["seconds"], device_canonical=t_dev_canon)}
 
     if rank != 0:
         return
@@ -437,20 +575,24 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": "voxel-edits/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": elapsed_ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": {"workload": f"batched-{n_edits}-mixed-edits-{res}^3", "resolution": res, "edits_per_step": n_edits,
-                   "voxel_edits_per_step": float(np.mean(ve[args.warmup:])),
-                   "seeded_scene": "sphere r=9600 fill + 64 sphere digs r in [512,2048] (1024^3 scene x32)",
-                   "node_levels": L, "bucket_bits": list(cfg.bucket_bits_each_level), "word_bits_per_page": 9,
-                   "page_bits_per_bucket": 2, "rollback_to_seeded_scene_each_step": True,
-                   "l2": "working set of a step (pool + frontier, tens of GB) far above L2; no flush",
-                   "parallelism": f"replicas x{world}"},
+        "config": batched_config(cfg, res, n_edits, float(np.mean(ve[args.warmup:])), world),
         "e2e": {"value": e2e_value, "unit": "voxel-edits/s", "h2d_bytes_per_step": int(n_edits * 40),
                 "d2h_bytes_per_step": int(224 * 8 + 4), "ms_per_step": 1e3 * float(np.mean(e2e_times))},
-        "per_edit": {"edits": len(plain), "voxel_edits_per_s_e2e": plain_rate, "voxel_edits_per_s_device": plain_dev_rate,
+        "per_edit": {"edits": len(plain), "voxel_edits": int(plain_ve),
+                     "voxel_edits_per_s_e2e": plain_ve / plain_wall_s,
+                     "voxel_edits_per_s_device": plain_ve / (plain_dev_ms / 1e3),
                      "p50_ms": float(np.percentile(lat_ms, 50)), "p99_ms": float(np.percentile(lat_ms, 99)),
-                     "mean_ms": float(lat_ms.mean()), "device_ms_per_edit": plain_dev_ms / len(plain),
-                     "same_root_as_sync": bool(plain_same)},
-        "batched_vs_per_edit": {"e2e": e2e_value / plain_rate, "device": value / plain_dev_rate},
+                     "mean_ms": float(lat_ms.mean()), "device_ms_per_edit": plain_dev_ms / len(plain)},
+        "batched_vs_per_edit": {
+            "edits": len(plain),
+            "what": f"the first {len(plain)} edits of a timed batch: one hd_edit pass per edit against one batched "
+                    f"pass over all of them, from the same seeded scene",
+            "device": plain_dev_ms / batched_dev_ms, "e2e": plain_wall_s / batched_wall_s,
+            "batched_device_ms": batched_dev_ms, "batched_e2e_ms": 1e3 * batched_wall_s,
+            "plain_device_ms": plain_dev_ms, "plain_e2e_ms": 1e3 * plain_wall_s,
+            "same_root_all_forms": bool(plain_same),
+            "full_batch_rate_vs_plain_rate": {"device": value / (plain_ve / (plain_dev_ms / 1e3)),
+                                              "e2e": e2e_value / (plain_ve / plain_wall_s)}},
         "roofline": {"bound": "hbm", "kernel": "dedup pass (k_dedup, all levels)", "achieved": achieved,
                      "peak": hbm, "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm,
                      "traffic": traffic, "algorithmic_bytes_per_step": dedup_bytes,
@@ -459,6 +601,7 @@ def run_ours(args):
                      "random_access": ceiling,
                      "dram_frac_of_random_access": ((traffic / (per_step_dedup_ms / 1e3) / 1e9) / ceiling["sector_gbs"])
                      if (traffic and ceiling) else None},
+        "roofline_leaf": leaf_roof,
         "tuning": tuning,
         "phases_ms_per_step": phase_ms,
         "counters_last_step": {k: [int(x) for x in v] for k, v in counters.items()},
@@ -466,7 +609,7 @@ def run_ours(args):
         "cpu_baseline": cpu,
         "gpu_launches": int(launches),
         "clocks": clk,
-        "checks": {"rerun_of_last_batch_finds_same_root": bool(same_roots)},
+        "checks": checks,
     }
     print(json.dumps(line), flush=True)
     if world > 1:
@@ -686,6 +829,36 @@ def run_terrain(args):
     for k in range(len(edits)):
         r = pool.edit(r, edits[k:k + 1])
     same = r == (int(d_root.item()) & 0xFFFFFFFF)
+    # the sequential CPU editor (the oracle's threaded edit, the reference's
+    # semantics) builds the terrain and applies the spheres in order on its own
+    # pool; its canonical DAG and 2^20 point queries must equal the device's
+    check = None
+    if not args.no_cpu:
+        import oracle
+        oracle.build()
+        queries = W.point_queries(res, 1 << 20, seed=7)
+        dev_occ = pool.query(final_plain, queries)
+        snapshot = pool.download()
+        threads = os.cpu_count() or 1
+        mtl = max(0, cfg.get_node_levels() - 4)
+        opool = oracle.OraclePool.from_config(cfg)
+        t0 = time.perf_counter()
+        orr = opool.threaded_edit(oracle.NULL, cols, mtl, threads)
+        orr = opool.threaded_edit(orr, edits, mtl, threads)
+        t_cpu = time.perf_counter() - t0
+        ook, ocounts, odigests = opool.canonical(orr)
+        o_occ = opool.query(orr, queries)
+        o_ok = ook and opool.ok
+        del opool
+        dok, dcounts, ddigests = device_canonical(cfg, snapshot, pool.filled_node_pointers(), final_plain)
+        del snapshot
+        check = {"canonical_equal_sequential_oracle": bool(o_ok and dok and dcounts == ocounts and
+                                                           ddigests == odigests),
+                 "point_queries_equal_sequential_oracle": bool(np.array_equal(dev_occ, o_occ)),
+                 "what": f"{len(cols)} column edits then the {len(edits)} spheres in order, by the oracle's threaded "
+                         f"editor on its own pool ({t_cpu:.1f} s, {threads} threads), against the device's plain "
+                         f"one-pass-per-edit result (the batched pass ends on the same root)",
+                 "canonical_counts": dcounts, "canonical_digests": [str(d) for d in ddigests]}
     line = {
         "metric": "voxel-edits/s per-edit (plain form) on the 16384^3 terrain; p99 edit latency",
         "value": ve / wall, "unit": "voxel-edits/s", "n_gpus": world, "steps": len(edits), "warmup": 64,
@@ -698,6 +871,7 @@ def run_terrain(args):
                        "max": float(lat_ms.max())},
         "batched_same_edits": {"ms": batched_ms, "voxel_edits_per_s": ve / (batched_ms / 1e3),
                                "speedup_vs_plain": (wall * 1e3) / batched_ms, "same_dag_as_plain": bool(same)},
+        "checks": check,
         "clocks": clocks.summary(),
     }
     print(json.dumps(line), flush=True)
@@ -721,7 +895,10 @@ def _serving_requests(hd, W, n, seed, rate):
     for k in range(n):
         res = SERVE_RES[scene[k]]
         if kind[k]:
-            e = W.mixed_batch(res, int(n_edits[k]), seed=seed * 100003 + k, r_max=512, side_max=1024)
+            # config-2 edits: spheres on the terrain's surface band (the scene's
+            # column blocks), radii log-uniform in [4,256] voxels, 50/50 fill/dig
+            e = W.surface_spheres(res, int(n_edits[k]), seed=seed * 100003 + k, band=64, block=res // 256,
+                                  r_lo=4, r_hi=256, absolute=True)
             reqs.append((float(t[k]), "edit", int(scene[k]), e))
         else:
             width = 1024
@@ -934,8 +1111,9 @@ def run_serving(args):
         "steps": len(reqs), "warmup": len(warm), "ms_per_step": 1e3 * wall_s / len(reqs), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
         "config": {"workload": f"{len(SERVE_RES)} resident terrain scenes {SERVE_RES}, Poisson {args.rate:g} req/s "
-                               f"for {args.serve_seconds:g} s; edit batches 1..4096 mixed edits (spheres r<=512, "
-                               f"boxes <=1024), ray batches 2^16..2^22 rays (1024 wide)",
+                               f"for {args.serve_seconds:g} s; edit batches of 1..4096 surface spheres (radius "
+                               f"log-uniform [4,256] voxels, 50/50 fill/dig, as the 16384^3 terrain workload), ray "
+                               f"batches 2^16..2^22 rays (1024 wide)",
                    "word_bits_per_page": 14, "page_bits_per_bucket": 2, "heap_pages_per_scene": heap_pages,
                    "max_pass_edits": args.max_pass_edits, "ray_slots": args.ray_slots,
                    "launch_shape": pools[0].tuning(),

@@ -167,6 +167,14 @@ hd_status hd_edit_async(hd_pool *pool, uint32_t root, const hd_edit_desc *d_edit
  * chain of edits can run without any host round trip. */
 hd_status hd_edit_async_droot(hd_pool *pool, const uint32_t *d_root, const hd_edit_desc *d_edits, uint32_t n,
                               uint32_t *d_out_root, void *stream);
+/* hd_edit_async_droot for a caller that also holds the edits on the host:
+ * h_edits (the same n edits, host memory, read before the call returns) sizes
+ * the launch the way hd_edit does -- grids from the edits' bounding boxes, and
+ * a small pass as one CTA -- while the kernels read d_edits.  Same entry point
+ * as the reference's Edit (include/hashdag/NodePool.hpp:405-417) for an edit
+ * loop that keeps its root on the device. */
+hd_status hd_edit_async_droot_hinted(hd_pool *pool, const uint32_t *d_root, const hd_edit_desc *d_edits,
+                                     const hd_edit_desc *h_edits, uint32_t n, uint32_t *d_out_root, void *stream);
 /* Size the edit workspace for batches of up to max_edits touching up to
  * max_items nodes per batch and max_list_entries (node, edit) pairs. */
 hd_status hd_edit_reserve(hd_pool *pool, uint64_t max_items, uint64_t max_list_entries, uint32_t max_edits);
@@ -183,6 +191,12 @@ hd_status hd_edit_last_counters(hd_pool *pool, uint64_t *items, uint64_t *candid
  * visited by all find-or-insert probes, the longest single probe, and failed
  * compare-and-swap attempts on bucket word counts (contention). */
 hd_status hd_edit_last_probe_stats(hd_pool *pool, uint64_t *probe_steps, uint64_t *max_probe, uint64_t *cas_retries);
+/* Work of the last pass's level-(L-2) leaf kernels (no reference counterpart:
+ * the numerator of that phase's roofline): out[0] level-(L-2) nodes rebuilt,
+ * out[1] (node, edit) pairs of their edit lists, out[2] base-node words read,
+ * out[3] old leaves read from the heap, out[4] read-only index lookups of
+ * changed leaves. */
+hd_status hd_edit_last_leaf_work(hd_pool *pool, uint64_t *out);
 /* Launch shape of the batched pass: grid caps in blocks per SM for each kernel
  * family and the edit-list length above which a node is expanded by a block
  * (level L-2: a warp) instead of a thread.  Results never depend on them. */
@@ -234,13 +248,19 @@ hd_status hd_upsert(hd_pool *pool, uint32_t level, const uint32_t *words, const 
  * an edit loop that must not take the device synchronisation a cudaMalloc /
  * cudaFree can cause.  Same result as hd_upsert, but device inputs and
  * outputs, stream-ordered, no host synchronisation, and the per-node scratch
- * in a static device array of the library (about 5.5 MB, held by every GPU
- * that loads the library until the process exits) instead of the pool's
- * workspace.  d_nodes: n nodes on the device, 8 child pointers each (Null =
- * 0xFFFFFFFF, child order) below the leaf level, 2 words each at the leaf
- * level.  d_out_ptrs: n pointers (device).  At most 65536 nodes per call;
- * larger n returns HD_ERR_INVALID_ARG without running anything.  Failures
- * inside the kernels go to the pool's sticky error (hd_pool_get_error).  The
+ * in a static device array of the library (about 4.7 MB: 224 counters of 8
+ * bytes plus 18 words per node for 65536 nodes, held by every GPU that loads
+ * the library until the process exits) instead of the pool's workspace.
+ * d_nodes: n nodes on the device, 8 child pointers each (Null = 0xFFFFFFFF,
+ * child order) below the leaf level, 2 words each at the leaf level.
+ * d_out_ptrs: n pointers (device).  At most 65536 nodes per call; larger n
+ * returns HD_ERR_INVALID_ARG without running anything.  Failures inside the
+ * kernels go to the pool's sticky error (hd_pool_get_error), and then every
+ * d_out_ptrs entry of the call is Null: an inner node whose 8 children are all
+ * Null (which hd_upsert rejects on the host) sets HD_ERR_INVALID_ARG there,
+ * as does any other failure of the call.  A leaf of two zero words is stored
+ * like any other leaf, as the reference's upsert_leaf does (edits never
+ * produce one: an emptied leaf becomes Null).  The
  * first call on a device looks up the array's device address (make it before
  * any stream capture).  All calls on a device share the one array: calls that
  * overlap on the GPU race. */

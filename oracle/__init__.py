@@ -88,6 +88,8 @@ def lib():
             "orc_read_page": (I, [P, U32, P]),
             "orc_pool_load": (None, [P, P, P, U32, P, P]),
             "orc_canonical": (I, [P, U32, P, P]),
+            "orc_canonical_simple": (I, [P, U32, P, P]),
+            "orc_count_voxel_edits": (U64, [P, U32, U32]),
             "orc_query": (None, [P, U32, P, U32, P]),
             "orc_dense": (None, [P, U32, P]),
             "orc_trace": (None, [P, U32, P, P, U32, P]),
@@ -267,6 +269,13 @@ class OraclePool:
         ok = lib().orc_canonical(self._h, root, _p(c), _p(d))
         return bool(ok), [int(x) for x in c], [int(x) for x in d]
 
+    def canonical_simple(self, root):
+        """canonical() computed node by node on one thread (its cross-check)."""
+        c = np.zeros(self.L, np.uint64)
+        d = np.zeros(self.L, np.uint64)
+        ok = lib().orc_canonical_simple(self._h, root, _p(c), _p(d))
+        return bool(ok), [int(x) for x in c], [int(x) for x in d]
+
     def query(self, root, xyz) -> np.ndarray:
         pts = np.ascontiguousarray(xyz, np.uint32).reshape(-1, 3)
         out = np.zeros(len(pts), np.uint8)
@@ -288,6 +297,12 @@ class OraclePool:
         else:
             lib().orc_trace_threads(self._h, root, _p(o), _p(d), len(o), _p(out), threads)
         return out
+
+
+def count_voxel_edits(edits, resolution) -> int:
+    """Sum over the edits of the grid voxels inside each shape (exact)."""
+    e = np.ascontiguousarray(edits, dtype=EDIT_DTYPE)
+    return int(lib().orc_count_voxel_edits(_p(e), len(e), resolution))
 
 
 def hash_inner(words) -> int:

@@ -26,6 +26,7 @@
 #include <cstring>
 #include <memory>
 #include <mutex>
+#include <parallel/algorithm>
 #include <unordered_map>
 #include <unordered_set>
 #include <vector>
@@ -820,7 +821,7 @@ static bool valid_ptr(const Pool &pool, Word ptr, Word level) {
 	return (ptr >> pool.cfg.wbpp) < pool.pages.size() && pool.pages[ptr >> pool.cfg.wbpp] != nullptr;
 }
 
-static Canon canonical(const Pool &pool, Word root) {
+static Canon canonical_simple(const Pool &pool, Word root) {
 	Word L = pool.cfg.node_levels();
 	Canon c;
 	c.counts.assign(L, 0);
@@ -894,6 +895,133 @@ static Canon canonical(const Pool &pool, Word root) {
 			}
 		}
 		c.counts[l] = tuples.empty() ? 0 : rank + 1;
+		c.digests[l] = d;
+		rank_below.swap(rank_here);
+	}
+	return c;
+}
+
+// The same canonical form for large DAGs (10^8 nodes): the reachable
+// pointers of a level are a sorted array (children gathered on all threads,
+// then sorted and made unique), a child's rank is a binary search in the
+// level below, and the tuples of a level are sorted on all threads.  Tuples
+// are compared word by word with zero padding and then by length, which is the
+// order std::vector<Word> gives (a prefix sorts first), so counts and digests
+// equal canonical_simple's.
+struct CanonTuple {
+	Word w[9];
+	Word len;
+	Word idx; // position in the level's sorted pointer array
+};
+static bool tuple_less(const CanonTuple &a, const CanonTuple &b) {
+	for (int k = 0; k < 9; ++k)
+		if (a.w[k] != b.w[k])
+			return a.w[k] < b.w[k];
+	return a.len < b.len;
+}
+static bool tuple_same(const CanonTuple &a, const CanonTuple &b) {
+	if (a.len != b.len)
+		return false;
+	for (Word k = 0; k < a.len; ++k)
+		if (a.w[k] != b.w[k])
+			return false;
+	return true;
+}
+
+static Canon canonical(const Pool &pool, Word root) {
+	const Word L = pool.cfg.node_levels();
+	Canon c;
+	c.counts.assign(L, 0);
+	c.digests.assign(L, 0);
+	if (root == kNull)
+		return c;
+	if (!valid_ptr(pool, root, 0)) {
+		c.ok = false;
+		c.bad_level = 0;
+		return c;
+	}
+	std::vector<std::vector<Word>> lv(L);
+	lv[0].push_back(root);
+	for (Word l = 0; l + 1 < L; ++l) {
+		const std::vector<Word> &cur = lv[l];
+		std::vector<Word> kids;
+		std::atomic<int> bad{0};
+#pragma omp parallel
+		{
+			std::vector<Word> mine;
+#pragma omp for schedule(static) nowait
+			for (int64_t i = 0; i < int64_t(cur.size()); ++i) {
+				const Word *n = pool.read_node(cur[i]);
+				const Word k = std::popcount(n[0] & 0xFFu);
+				for (Word j = 0; j < k; ++j) {
+					if (!valid_ptr(pool, n[1 + j], l + 1))
+						bad = 1;
+					else
+						mine.push_back(n[1 + j]);
+				}
+			}
+#pragma omp critical
+			kids.insert(kids.end(), mine.begin(), mine.end());
+		}
+		if (bad) {
+			c.ok = false;
+			c.bad_level = int(l + 1);
+			return c;
+		}
+		__gnu_parallel::sort(kids.begin(), kids.end());
+		kids.erase(std::unique(kids.begin(), kids.end()), kids.end());
+		lv[l + 1].swap(kids);
+	}
+	std::vector<Word> rank_below, rank_here;
+	for (Word l = L; l-- > 0;) {
+		const std::vector<Word> &ptrs = lv[l];
+		const std::vector<Word> &below = l + 1 < L ? lv[l + 1] : ptrs;
+		std::vector<CanonTuple> t(ptrs.size());
+		std::atomic<int> missing{0};
+#pragma omp parallel for schedule(static)
+		for (int64_t i = 0; i < int64_t(ptrs.size()); ++i) {
+			CanonTuple &x = t[i];
+			std::fill(x.w, x.w + 9, 0u);
+			x.idx = Word(i);
+			const Word *n = pool.read_node(ptrs[i]);
+			if (l == L - 1) {
+				x.w[0] = n[0];
+				x.w[1] = n[1];
+				x.len = 2;
+				continue;
+			}
+			const Word k = std::popcount(n[0] & 0xFFu);
+			x.w[0] = n[0];
+			x.len = k + 1;
+			for (Word j = 0; j < k; ++j) {
+				auto it = std::lower_bound(below.begin(), below.end(), n[1 + j]);
+				if (it == below.end() || *it != n[1 + j]) {
+					missing = 1;
+					x.w[1 + j] = kNull;
+				} else
+					x.w[1 + j] = rank_below[it - below.begin()];
+			}
+		}
+		if (missing)
+			c.ok = false;
+		__gnu_parallel::sort(t.begin(), t.end(), tuple_less);
+		rank_here.assign(ptrs.size(), 0);
+		uint64_t d = 0x6a09e667f3bcc909ull ^ l;
+		Word rank = 0;
+		for (size_t i = 0; i < t.size(); ++i) {
+			const bool same = i > 0 && tuple_same(t[i], t[i - 1]);
+			if (same)
+				c.ok = false; // duplicate content at one level: the DAG is not reduced
+			else if (i > 0)
+				++rank;
+			rank_here[t[i].idx] = rank;
+			if (!same) {
+				d = mix64(d ^ t[i].len);
+				for (Word k = 0; k < t[i].len; ++k)
+					d = mix64(d ^ t[i].w[k]);
+			}
+		}
+		c.counts[l] = t.empty() ? 0 : rank + 1;
 		c.digests[l] = d;
 		rank_below.swap(rank_here);
 	}
@@ -1713,6 +1841,18 @@ int orc_canonical(const orc_pool *p, uint32_t root, uint64_t *counts, uint64_t *
 	return c.ok ? 1 : 0;
 }
 
+// The node-by-node canonicaliser (the cross-check of orc_canonical).
+int orc_canonical_simple(const orc_pool *p, uint32_t root, uint64_t *counts, uint64_t *digests) {
+	orc::Canon c = orc::canonical_simple(p->pool, root);
+	if (c.bad_level >= 0)
+		counts[0] = ~0ull - uint64_t(c.bad_level);
+	for (size_t i = 0; i < c.counts.size(); ++i) {
+		counts[i] = c.counts[i];
+		digests[i] = c.digests[i];
+	}
+	return c.ok ? 1 : 0;
+}
+
 void orc_query(const orc_pool *p, uint32_t root, const uint32_t *xyz, uint32_t n, uint8_t *out) {
 	for (uint32_t i = 0; i < n; ++i)
 		out[i] = p->pool.query(root, xyz + 3 * size_t(i)) ? 1 : 0;
@@ -1814,5 +1954,63 @@ void orc_vbr_set_per_voxel(int on) { orc::g_vbr_per_voxel = on != 0; }
 
 uint32_t orc_hash_inner(const uint32_t *w, uint32_t n) { return orc::murmur_words(w, n); }
 uint32_t orc_hash_leaf(uint32_t w0, uint32_t w1) { return orc::murmur_leaf(w0, w1); }
+
+// Voxel-edits of an edit list: the number of grid voxels of [0,res)^3 inside
+// each edit's shape (VoxelInRange of src/main.cpp:55-57,121-126), summed.  A
+// sphere is counted row by row: for every (y, z) row the x extent is
+// cx +- isqrt(r2 - dy^2 - dz^2), clipped to the grid; spheres that lie inside
+// the grid depend only on r2 and are counted once per r2.
+static uint64_t isqrt_u64(uint64_t v) {
+	uint64_t r = (uint64_t)std::sqrt((long double)v);
+	while (r * r > v)
+		--r;
+	while ((r + 1) * (r + 1) <= v)
+		++r;
+	return r;
+}
+static uint64_t sphere_voxels(int64_t cx, int64_t cy, int64_t cz, uint64_t r2, int64_t res) {
+	const int64_t r = (int64_t)isqrt_u64(r2);
+	uint64_t total = 0;
+	for (int64_t z = std::max<int64_t>(0, cz - r); z <= std::min<int64_t>(res - 1, cz + r); ++z) {
+		const uint64_t dz2 = uint64_t((z - cz) * (z - cz));
+		for (int64_t y = std::max<int64_t>(0, cy - r); y <= std::min<int64_t>(res - 1, cy + r); ++y) {
+			const uint64_t d2 = dz2 + uint64_t((y - cy) * (y - cy));
+			if (d2 > r2)
+				continue;
+			const int64_t w = (int64_t)isqrt_u64(r2 - d2);
+			const int64_t lo = std::max<int64_t>(0, cx - w), hi = std::min<int64_t>(res - 1, cx + w);
+			if (hi >= lo)
+				total += uint64_t(hi - lo + 1);
+		}
+	}
+	return total;
+}
+uint64_t orc_count_voxel_edits(const hd_edit_desc *e, uint32_t n, uint32_t res) {
+	std::unordered_map<uint64_t, uint64_t> inside; // r2 -> voxels of a sphere inside the grid
+	uint64_t total = 0;
+	for (uint32_t i = 0; i < n; ++i) {
+		if (e[i].shape == HD_SHAPE_AABB) {
+			uint64_t v = 1;
+			for (int a = 0; a < 3; ++a) {
+				const uint64_t lo = std::min<uint64_t>(e[i].p0[a], res), hi = std::min<uint64_t>(e[i].p1[a], res);
+				v *= hi > lo ? hi - lo : 0;
+			}
+			total += v;
+			continue;
+		}
+		const int64_t r = (int64_t)isqrt_u64(e[i].r2);
+		bool in = true;
+		for (int a = 0; a < 3; ++a)
+			in = in && int64_t(e[i].p0[a]) - r >= 0 && int64_t(e[i].p0[a]) + r < int64_t(res);
+		if (in) {
+			auto it = inside.find(e[i].r2);
+			if (it == inside.end())
+				it = inside.emplace(e[i].r2, sphere_voxels(r, r, r, e[i].r2, 2 * r + 1)).first;
+			total += it->second;
+		} else
+			total += sphere_voxels(e[i].p0[0], e[i].p0[1], e[i].p0[2], e[i].r2, res);
+	}
+	return total;
+}
 
 } // extern "C"

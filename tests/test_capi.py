@@ -193,3 +193,14 @@ def test_headers_compile_standalone(tmp_path):
         r = subprocess.run([gxx, "-std=c++20", "-Wall", "-Wextra", "-pedantic", "-Werror", "-fsyntax-only", "-I", inc,
                             str(src)], capture_output=True, text=True)
         assert r.returncode == 0, r.stderr
+
+
+def test_oracle_and_engine_count_the_same_voxel_edits(hd, orc):
+    """The reference arm of the benchmark counts voxel-edits with the oracle,
+    the engine's arm with hd_count_voxel_edits: equal on the benchmark's own
+    batch (65,536 mixed edits on 32768^3) and on the terrain spheres."""
+    from vkhashdag_gb300 import workloads as W
+    e = W.mixed_batch(32768, 65536, seed=5)
+    assert orc.count_voxel_edits(e, 32768) == hd.count_voxel_edits(e, 32768)
+    s = W.surface_spheres(16384, 512, seed=0, band=64, block=32)
+    assert orc.count_voxel_edits(s, 16384) == hd.count_voxel_edits(s, 16384)

@@ -351,3 +351,33 @@ def test_threaded_edit_any_team_and_depth(orc, threads, depth):
     assert ok and threaded.ok and dig == serial.canonical(rs)[2]
     q = W.point_queries(res, 1 << 14, seed=13)
     assert np.array_equal(threaded.query(rt, q), serial.query(rs, q))
+
+
+@pytest.mark.parametrize("name", ["scene256", "scene1024", "mixed512", "terrain256", "zero_hasher16", "tiny_pages64"])
+def test_parallel_canonical_equals_node_by_node(golden, orc, name):
+    """The all-threads canonicaliser (sorted pointer arrays, parallel tuple
+    sort) gives the counts and digests of the node-by-node form."""
+    s = scenario(golden, name)
+    cfg = config_from(s["config"])
+    pool = orc.OraclePool.from_config(cfg)
+    root = pool.edit(orc.NULL, scenario_edits(s))
+    assert pool.canonical(root) == pool.canonical_simple(root)
+    assert pool.canonical(orc.NULL) == pool.canonical_simple(orc.NULL)
+
+
+def test_oracle_voxel_count_matches_brute_force(orc):
+    """Row-by-row sphere counting and clipped box volumes against a dense
+    evaluation of the editors' voxel predicates, clipped spheres included."""
+    from vkhashdag_gb300 import workloads as W
+    res = 48
+    e = W.mixed_batch(res, 60, seed=11, r_max=24, side_max=40)
+    g = np.stack(np.meshgrid(np.arange(res), np.arange(res), np.arange(res), indexing="ij"), -1).reshape(-1, 3)
+    want = 0
+    for x in e:
+        if x["shape"] == 1:
+            inside = np.all((g >= x["p0"].astype(np.int64)) & (g < x["p1"].astype(np.int64)), axis=1)
+        else:
+            d = g - x["p0"].astype(np.int64)
+            inside = (d * d).sum(1) <= int(x["r2"])
+        want += int(inside.sum())
+    assert orc.count_voxel_edits(e, res) == want

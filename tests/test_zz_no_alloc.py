@@ -33,16 +33,27 @@ def _nodes(rng, n, level_words):
     return packed, slots
 
 
-def _noalloc(hd, pool, level, dev_nodes, n):
+def _noalloc(hd, pool, level, dev_nodes, n, expect_error=0):
     import torch
-    out = torch.zeros(n, dtype=torch.int64, device="cuda")[:0]  # placeholder to keep torch on the device
     out = torch.empty(n, dtype=torch.int32, device="cuda")
     st = hd.lib().hd_upsert_noalloc(pool.handle, level, ctypes.c_void_p(dev_nodes.data_ptr()), n,
                                     ctypes.c_void_p(out.data_ptr()), None)
     assert st == 0
     torch.cuda.synchronize()
-    assert pool.error() == 0
+    assert pool.error() == expect_error
     return [int(x) & 0xFFFFFFFF for x in out.cpu().numpy()]
+
+
+def _slots(nodes):
+    """Packed inner nodes (mask, children...) as the call's 8-slot rows."""
+    rows = np.full((len(nodes), 8), 0xFFFFFFFF, np.uint32)
+    for i, w in enumerate(nodes):
+        k = 1
+        for c in range(8):
+            if (w[0] >> c) & 1:
+                rows[i, c] = w[k]
+                k += 1
+    return rows
 
 
 def test_noalloc_upsert_matches_upsert(hd):
@@ -84,3 +95,64 @@ def test_noalloc_rejects_oversized_calls(hd):
     st = hd.lib().hd_upsert_noalloc(pool.handle, 1, ctypes.c_void_p(big.data_ptr()), 65537,
                                     ctypes.c_void_p(out.data_ptr()), None)
     assert st == 1  # HD_ERR_INVALID_ARG, nothing ran
+
+
+def test_noalloc_known_answers(golden, hd):
+    """The reference's upsert known answers (test/test.cpp:118-147, run through
+    the reference's own headers into golden.json), one node per no-alloc call:
+    the same pointers and the same pool words as the reference."""
+    import hashlib
+    import torch
+    from helpers import config_from
+    k = golden["upsert_kat"]
+    cfg = config_from(k["config"])
+    L = cfg.get_node_levels()
+    pool = hd.NodePool(cfg, heap_pages=1 << 10)
+    assert pool.filled_node_pointers() == k["filled"]
+    ptrs = []
+    for level, words in k["ops"]:
+        row = np.array(words, np.uint32) if level == L - 1 else _slots([words]).reshape(-1)
+        d = torch.from_numpy(row.view(np.int32).copy()).cuda()
+        ptrs.append(_noalloc(hd, pool, level, d, 1)[0])
+    assert ptrs == k["ptrs"]
+    bw, ids, pages = pool.download()
+    h = hashlib.sha256()
+    for a in (bw, ids, pages):
+        h.update(np.ascontiguousarray(a).tobytes())
+    assert h.hexdigest() == k["pool_sha"]
+
+
+def test_noalloc_failed_call_returns_null_not_stale_pointers(hd):
+    """A call that fails inside the kernels (here: an inner node whose 8
+    children are all Null, an invalid argument found on the device) reports
+    the error through the pool and writes Null for every node, although the
+    shared scratch still holds the previous call's results; after the error
+    is cleared the same pool serves the next call normally."""
+    import torch
+    cfg = hd.DefaultConfig(level_count=6)()
+    pool = hd.NodePool(cfg, heap_pages=1 << 10)
+    good = [[0b11, 5, 7], [0b101, 9, 9], [0b1, 3]]
+    d_good = torch.from_numpy(_slots(good).reshape(-1).view(np.int32).copy()).cuda()
+    want = pool.upsert_nodes(1, good)
+    assert _noalloc(hd, pool, 1, d_good, 3) == want
+    bad = _slots(good)
+    bad[1, :] = 0xFFFFFFFF
+    d_bad = torch.from_numpy(bad.reshape(-1).view(np.int32).copy()).cuda()
+    assert _noalloc(hd, pool, 1, d_bad, 3, expect_error=1) == [hd.NULL] * 3  # HD_ERR_INVALID_ARG
+    pool.clear_error()
+    assert _noalloc(hd, pool, 1, d_good, 3) == want
+
+
+def test_noalloc_zero_leaf_is_stored_like_any_leaf(hd):
+    """A leaf of two zero words (only an upsert can make one) is found again
+    by the next call and by hd_upsert, between other leaves."""
+    import torch
+    cfg = hd.DefaultConfig(level_count=6)()
+    L = cfg.get_node_levels()
+    pool = hd.NodePool(cfg, heap_pages=1 << 10)
+    leaves = np.array([[0, 0], [5, 6], [0, 0], [7, 0], [0, 0]], np.uint32)
+    d = torch.from_numpy(leaves.reshape(-1).view(np.int32).copy()).cuda()
+    first = _noalloc(hd, pool, L - 1, d, len(leaves))
+    assert first[0] == first[2] == first[4] != hd.NULL and len(set(first)) == 3
+    assert _noalloc(hd, pool, L - 1, d, len(leaves)) == first
+    assert pool.upsert_nodes(L - 1, [list(map(int, x)) for x in leaves]) == first

@@ -145,6 +145,8 @@ def lib():
         "hd_edit": (I, [P, U32, P, U32, P, P]),
         "hd_edit_async": (I, [P, U32, P, U32, P, P]),
         "hd_edit_async_droot": (I, [P, P, P, U32, P, P]),
+        "hd_edit_async_droot_hinted": (I, [P, P, P, P, U32, P, P]),
+        "hd_edit_last_leaf_work": (I, [P, P]),
         "hd_edit_reserve": (I, [P, U64, U64, U32]),
         "hd_edit_last_counters": (I, [P, P, P, P, P, P]),
         "hd_edit_last_probe_stats": (I, [P, P, P, P]),
@@ -495,6 +497,15 @@ class NodePool:
         _check(lib().hd_edit_async_droot(self._h, ctypes.c_void_p(d_root), ctypes.c_void_p(d_edits), n,
                                          ctypes.c_void_p(d_out_root), ctypes.c_void_p(stream)), "hd_edit_async_droot")
 
+    def edit_async_droot_hinted(self, d_root: int, d_edits: int, h_edits: np.ndarray, d_out_root: int,
+                                stream: int = 0):
+        """edit_async_droot with a host copy of the same edits sizing the launch
+        (bounding-box grids, one-CTA small passes) as edit() does."""
+        h = np.ascontiguousarray(h_edits, dtype=EDIT_DTYPE)
+        _check(lib().hd_edit_async_droot_hinted(self._h, ctypes.c_void_p(d_root), ctypes.c_void_p(d_edits), _ptr(h),
+                                                len(h), ctypes.c_void_p(d_out_root), ctypes.c_void_p(stream)),
+               "hd_edit_async_droot_hinted")
+
     def error(self) -> int:
         e = ctypes.c_uint32(0)
         _check(lib().hd_pool_get_error(self._h, ctypes.byref(e)), "hd_pool_get_error")
@@ -527,6 +538,12 @@ class NodePool:
         arrs = {k: np.zeros(n, np.uint64) for k in names}
         _check(lib().hd_edit_last_counters(self._h, *[_ptr(arrs[k]) for k in names]), "hd_edit_last_counters")
         return arrs
+
+    def last_leaf_work(self) -> dict:
+        """Work of the last pass's level-(L-2) leaf kernels."""
+        v = np.zeros(5, np.uint64)
+        _check(lib().hd_edit_last_leaf_work(self._h, _ptr(v)), "hd_edit_last_leaf_work")
+        return dict(zip(["nodes", "pairs", "base_words", "old_leaves", "lookups"], (int(x) for x in v)))
 
     def last_probe_stats(self) -> dict:
         """Index slots visited by the last pass's probes, longest probe, bucket CAS retries."""

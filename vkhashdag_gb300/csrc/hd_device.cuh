@@ -403,6 +403,12 @@ enum WsCtr : u32 {
 	kWsProbeSteps = 69, // index slots visited in the pass
 	kWsCasRetry = 70,   // failed bucket-count CAS attempts
 	kWsTodo = 71,       // entries in Workspace::todo
+	// work of the level-(L-2) leaf kernels (the algorithmic bytes of that phase)
+	kWsLeafNodes = 72,   // level-(L-2) nodes rebuilt
+	kWsLeafPairs = 73,   // (node, edit) pairs: edit-list entries of those nodes
+	kWsLeafBaseW = 74,   // words of their base nodes read
+	kWsLeafOld = 75,     // old leaves read from the heap
+	kWsLeafLookup = 76,  // read-only index lookups of changed leaves
 	kWsCand = 96,
 	kWsCandWords = 128,
 	kWsIns = 160,

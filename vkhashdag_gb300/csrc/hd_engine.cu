@@ -1014,6 +1014,22 @@ hd_status hd_edit_async_droot(hd_pool *pool, const uint32_t *d_root, const hd_ed
 	return hd_check(cudaEventRecord(pool->ws_free, st)); // hd_pool_get_error waits for this
 }
 
+hd_status hd_edit_async_droot_hinted(hd_pool *pool, const uint32_t *d_root, const hd_edit_desc *d_edits,
+                                     const hd_edit_desc *h_edits, uint32_t n, uint32_t *d_out_root, void *stream) {
+	if (!pool || !d_out_root || !d_edits || !d_root || !h_edits || n == 0)
+		return HD_ERR_INVALID_ARG;
+	std::lock_guard<std::mutex> lk(pool->mtx);
+	HD_TRY(cudaSetDevice(pool->device));
+	cudaStream_t st = (cudaStream_t)stream;
+	hd_status s = launch_pass(pool, d_edits, n, kNull, d_root, d_out_root, st, h_edits);
+	if (s)
+		return s;
+	k_error_from_ws<<<1, 32, 0, st>>>(pool->P, pool->ws.d);
+	pool->kernel_launches++;
+	HD_TRY(cudaGetLastError());
+	return hd_check(cudaEventRecord(pool->ws_free, st));
+}
+
 hd_status hd_edit_get_tuning(const hd_pool *pool, hd_tuning *out) {
 	if (!pool || !out)
 		return HD_ERR_INVALID_ARG;
@@ -1300,6 +1316,19 @@ hd_status hd_edit_last_probe_stats(hd_pool *pool, uint64_t *probe_steps, uint64_
 		*max_probe = c[kWsMaxProbe];
 	if (cas_retries)
 		*cas_retries = c[kWsCasRetry];
+	return HD_OK;
+}
+
+hd_status hd_edit_last_leaf_work(hd_pool *pool, uint64_t *out) {
+	if (!pool || !out)
+		return HD_ERR_INVALID_ARG;
+	std::lock_guard<std::mutex> lk(pool->mtx);
+	HD_TRY(cudaSetDevice(pool->device));
+	HD_TRY(cudaEventSynchronize(pool->ws_free));
+	unsigned long long c[5];
+	HD_TRY(cudaMemcpy(c, pool->ws.d.ctr + kWsLeafNodes, sizeof(c), cudaMemcpyDeviceToHost));
+	for (int k = 0; k < 5; ++k)
+		out[k] = c[k];
 	return HD_OK;
 }
 

@@ -637,6 +637,18 @@ __device__ __forceinline__ void hand_to_parent(Workspace &W, u64 i, u32 r) {
 		W.cnew[ps] = r;
 }
 
+// Work counters of the leaf kernels, summed over the warp and added with one
+// atomic per counter and warp (all 32 lanes call this after their loop).
+__device__ __forceinline__ void add_leaf_work(Workspace &W, u32 nodes, u32 pairs, u32 basew, u32 old, u32 lookup) {
+	const u32 v[5] = {nodes, pairs, basew, old, lookup};
+#pragma unroll
+	for (int k = 0; k < 5; ++k) {
+		const u32 x = __reduce_add_sync(kFullMask, v[k]);
+		if (lane_id() == 0 && x)
+			atomicAdd(&W.ctr[kWsLeafNodes + k], (unsigned long long)x);
+	}
+}
+
 // Thread per level-(L-2) node with a short edit list: computes its 8 leaves.
 __device__ __forceinline__ void leafparent_short_phase(const DevPool &P, Workspace &W, u64 tbase, u64 tstride) {
 	if (ws_failed(W))
@@ -646,6 +658,7 @@ __device__ __forceinline__ void leafparent_short_phase(const DevPool &P, Workspa
 	level_range(W, L, l, begin, n);
 	const u32 T = W.long_threshold;
 	const u64 stride = tstride;
+	u32 st_nodes = 0, st_pairs = 0, st_basew = 0, st_old = 0, st_lookup = 0; // work counters
 	for (u64 w0 = tbase + (threadIdx.x & ~31u); w0 < n; w0 += stride) {
 		const u64 t = w0 + lane_id();
 		const u64 i = begin + t;
@@ -664,17 +677,22 @@ __device__ __forceinline__ void leafparent_short_phase(const DevPool &P, Workspa
 		u32 cand_mask = 0;
 		if (mine) {
 			base_children(P, l, b, old);
+			st_nodes += 1;
+			st_pairs += len;
+			st_basew += (b == kNull || b == P.cfg.filled[l]) ? 0u : 1u + __popc(__ldg(node_addr(P, b)) & 0xFFu);
 #pragma unroll 1
 			for (u32 c = 0; c < 8; ++c) { // not unrolled: one copy of the leaf code keeps the i-cache warm
 				u32 cx, cy, cz;
 				child_pos(pos, c, cx, cy, cz);
 				const u64 b0 = leaf_bits(P, old[c]);
+				st_old += (old[c] == kNull || old[c] == P.cfg.filled[L - 1]) ? 0u : 1u;
 				const u64 bits = rebuild_leaf(W, off, len, cx, cy, cz, b0);
 				bool cand;
 				u32 r = leaf_result(P, bits, b0, old[c], &cand);
 				if (cand) {
 					const u64 sl = leaf_slot(P, bits);
 					r = lookup_leaf_from(P, bits, sl, __ldg(&P.index[sl]));
+					st_lookup += 1;
 					if (r == kNull) {
 						cb[c] = bits;
 						cand_mask |= 1u << c;
@@ -721,6 +739,7 @@ __device__ __forceinline__ void leafparent_short_phase(const DevPool &P, Workspa
 		cn[0] = make_uint4(res[0], res[1], res[2], res[3]);
 		cn[1] = make_uint4(res[4], res[5], res[6], res[7]);
 	}
+	add_leaf_work(W, st_nodes, st_pairs, st_basew, st_old, st_lookup);
 }
 static __global__ void __launch_bounds__(kBlock, 4) k_leafparent_short(DevPool P, Workspace W) {
 	apply_pass_desc(W);
@@ -739,6 +758,7 @@ static __global__ void __launch_bounds__(kBlock) k_leafparent_long(DevPool P, Wo
 	const u64 n = W.ctr[kWsLong + l];
 	const u32 lane = lane_id(), c = lane >> 2, q = lane & 3u;
 	const u64 warps = (u64)gridDim.x * (blockDim.x / 32);
+	u32 lw_nodes = 0, lw_pairs = 0, lw_basew = 0, lw_old = 0, lw_lookup = 0; // work counters
 	for (u64 k = (u64)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32; k < n; k += warps) {
 		const u64 qi = begin + k;
 		if (qi >= W.inner.cap)
@@ -758,9 +778,16 @@ static __global__ void __launch_bounds__(kBlock) k_leafparent_long(DevPool P, Wo
 		}
 		u32 old[8];
 		base_children(P, l, b, old);
+		if (lane == 0) {
+			lw_nodes += 1;
+			lw_pairs += len;
+			lw_basew += (b == kNull || b == P.cfg.filled[l]) ? 0u : 1u + __popc(__ldg(node_addr(P, b)) & 0xFFu);
+		}
 		u32 cx, cy, cz;
 		child_pos(pos, c, cx, cy, cz);
 		const u64 b0 = leaf_bits(P, old[c]);
+		if (q == 0)
+			lw_old += (old[c] == kNull || old[c] == P.cfg.filled[L - 1]) ? 0u : 1u;
 		u32 mine = (u32)(b0 >> (16u * q)) & 0xFFFFu;
 		for (u32 p = 0; p < len; ++p) {
 			const hd_edit_desc e = W.edits[W.lists[off + p]];
@@ -791,6 +818,7 @@ static __global__ void __launch_bounds__(kBlock) k_leafparent_long(DevPool P, Wo
 			const u64 sl = leaf_slot(P, bits);
 			r = lookup_leaf_from(P, bits, sl, __ldg(&P.index[sl]));
 			cand = r == kNull;
+			lw_lookup += 1;
 		}
 		cand = lead && cand;
 		const u32 cmask_lanes = __ballot_sync(kFullMask, cand); // bit 4c set for candidate child c
@@ -825,6 +853,7 @@ static __global__ void __launch_bounds__(kBlock) k_leafparent_long(DevPool P, Wo
 			W.todo_parent[tq] = W.inner.parent[i];
 		}
 	}
+	add_leaf_work(W, lw_nodes, lw_pairs, lw_basew, lw_old, lw_lookup);
 }
 
 // ------------------------------------------------------------------ k_root
@@ -1199,7 +1228,7 @@ __device__ __forceinline__ void dedup_phase(const DevPool &P, Workspace &W, u32 
 	__shared__ u32 s_val[Leaf ? kLeafCache : 1];
 	if (Leaf)
 		for (u32 e = threadIdx.x; e < kLeafCache; e += blockDim.x) {
-			s_key[e] = 0ull; // no leaf candidate is all-empty
+			s_key[e] = 0ull; // empty slot (all-zero leaves are never cached)
 			s_val[e] = kNull;
 		}
 	__shared__ unsigned long long s_acc[7];
@@ -1275,7 +1304,10 @@ __device__ __forceinline__ void dedup_phase(const DevPool &P, Workspace &W, u32 
 		// cached leaf: found without a probe
 		bool hit = false;
 		u32 slot_e = 0;
-		if (Leaf && cand) {
+		// key 0 marks an empty cache slot, so an all-zero leaf (possible only
+		// through the upsert calls) is never cached and always probes
+		const bool cacheable = Leaf && cand && (nw.w[0] | nw.w[1]) != 0u;
+		if (cacheable) {
 			const u64 bits = (u64)nw.w[0] | ((u64)nw.w[1] << 32);
 			slot_e = (h ^ (h >> 13)) & (kLeafCache - 1u);
 			if (s_key[slot_e] == bits) {
@@ -1329,7 +1361,7 @@ __device__ __forceinline__ void dedup_phase(const DevPool &P, Workspace &W, u32 
 		const u32 lres = __shfl_sync(kFullMask, mine, leader);
 		if (probe_me)
 			r = follower ? lres : mine;
-		if (Leaf && probe_me && !follower && !ins && r != kNull) { // found resident: remember it in the block
+		if (cacheable && probe_me && !follower && !ins && r != kNull) { // found resident: remember it in the block
 			const u64 bits = (u64)nw.w[0] | ((u64)nw.w[1] << 32);
 			if (s_key[slot_e] == 0ull && atomicCAS(&s_key[slot_e], 0ull, (unsigned long long)bits) == 0ull)
 				*(volatile u32 *)&s_val[slot_e] = r;

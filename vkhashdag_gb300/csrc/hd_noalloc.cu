@@ -87,6 +87,9 @@ Workspace scratch_workspace(unsigned char *base, uint32_t n, bool leaf) {
 
 // Loads the caller's nodes into the scratch.  Inner level: 8 child pointers per
 // node (Null = 0xFFFFFFFF), in child order.  Leaf level: 2 words per node.
+// An inner node with no child is an invalid argument (hd_upsert rejects it on
+// the host): it fails the whole call through the workspace error word, so the
+// dedup launch inserts nothing and every result becomes Null.
 __global__ void k_noalloc_load(Workspace W, const uint32_t *nodes, uint32_t n, uint32_t level, uint32_t leaf) {
 	const u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x;
 	if (i == 0)
@@ -97,18 +100,35 @@ __global__ void k_noalloc_load(Workspace W, const uint32_t *nodes, uint32_t n, u
 		W.leaf_new[i] = (u64)nodes[2 * i] | ((u64)nodes[2 * i + 1] << 32);
 		W.leaf.parent[i] = kNull;
 	} else {
+		u32 any = 0;
 		for (int c = 0; c < 8; ++c) {
-			W.cnew[i * 8 + c] = nodes[i * 8 + c];
-			W.bchild[i * 8 + c] = 0xFFFFFFFEu; // never equal to a child: the node is always looked up
+			const u32 v = nodes[i * 8 + c];
+			W.cnew[i * 8 + c] = v;
+			// the base children differ from the new ones in every slot, so the
+			// dedup launch always builds and looks up the node; it never takes
+			// its "no child changed" branch, which reads a base node this
+			// scratch does not have
+			W.bchild[i * 8 + c] = v ^ 1u;
+			any |= v != kNull ? 1u : 0u;
 		}
+		if (!any)
+			atomicCAS(&W.ctr[kWsError], 0ull, (unsigned long long)kErrInvalidRoot);
 		W.inner.parent[i] = kNull;
 	}
 }
 
-__global__ void k_noalloc_store(Workspace W, uint32_t n, uint32_t leaf, uint32_t *out) {
+// Copies the results out.  A failed call (its own workspace error, or the
+// pool's sticky error, which the dedup launch may have just set) writes Null
+// for every node, so no pointer of an earlier call left in the shared scratch
+// can come back; the workspace error also becomes the pool's error.
+__global__ void k_noalloc_store(DevPool P, Workspace W, uint32_t n, uint32_t leaf, uint32_t *out) {
 	const u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x;
+	const unsigned long long ws_err = *(volatile unsigned long long *)&W.ctr[kWsError];
+	if (i == 0 && ws_err)
+		set_error(&P.counters[kCtrError], (u32)ws_err);
+	const bool failed = ws_err != 0 || *(volatile u32 *)&P.counters[kCtrError] != 0;
 	if (i < n)
-		out[i] = leaf ? W.leaf.res[i] : W.inner.res[i];
+		out[i] = failed ? kNull : (leaf ? W.leaf.res[i] : W.inner.res[i]);
 }
 
 } // namespace
@@ -144,7 +164,7 @@ extern "C" hd_status hd_upsert_noalloc(hd_pool *pool, uint32_t level, const uint
 	else
 		k_dedup<false><<<grid, kBlock, 0, st>>>(pool->P, W, level, 0u);
 	k_finish<<<1, 32, 0, st>>>(pool->P, W, nullptr);
-	k_noalloc_store<<<grid, kBlock, 0, st>>>(W, n, leaf ? 1u : 0u, d_out_ptrs);
+	k_noalloc_store<<<grid, kBlock, 0, st>>>(pool->P, W, n, leaf ? 1u : 0u, d_out_ptrs);
 	if (cudaGetLastError() != cudaSuccess || cudaEventRecord(pool->ws_free, st) != cudaSuccess)
 		return HD_ERR_CUDA;
 	pool->kernel_launches += 4;

@@ -130,10 +130,12 @@ def terrain_columns(resolution: int = 16384, block: int = 32, seed: int = 0) -> 
 
 
 def surface_spheres(resolution: int = 16384, n: int = 4096, seed: int = 0, band: int = 64, block: int = 32,
-                    r_lo: int = 4, r_hi: int = 256) -> np.ndarray:
+                    r_lo: int = 4, r_hi: int = 256, absolute: bool = False) -> np.ndarray:
     """Spheres centred within `band` voxels of the terrain surface (block heights),
-    integer radii log-uniform in [r_lo, r_hi], alternating-free 50/50 fill/dig."""
-    s = resolution / 16384.0
+    integer radii log-uniform in [r_lo, r_hi], alternating-free 50/50 fill/dig.
+    Radii and band are given for a 16384^3 terrain and scale with the
+    resolution, unless `absolute` (then they are voxels at any resolution)."""
+    s = 1.0 if absolute else resolution / 16384.0
     x = randint(seed, 11, n, 0, resolution - 1)
     z = randint(seed, 12, n, 0, resolution - 1)
     bx, bz = x // block, z // block
