@@ -462,6 +462,16 @@ def run_ours(args):
     d_root = torch.zeros(1, dtype=torch.int32, device=f"cuda:{local}")
     d_root0 = torch.full((1,), root0 if root0 < (1 << 31) else root0 - (1 << 32), dtype=torch.int32,
                          device=f"cuda:{local}")
+    # Every form runs on the seeded scene restored by a rollback, and each
+    # result is checked in its own pool state: re-running the other form there
+    # finds every node of the same DAG, so it must return the very same root
+    # (pointers from different rollbacks differ: insertion order does).
+    def plain_chain(start):
+        r = start
+        for k in range(len(plain)):
+            r = pool.edit(r, plain[k:k + 1])
+        return r
+
     # (1) wall latency of hd_edit, one call per edit (host edits, host root)
     pool.rollback(0)
     torch.cuda.synchronize()
@@ -471,7 +481,7 @@ def run_ours(args):
         t0 = time.perf_counter()
         r = pool.edit(r, plain[k:k + 1])
         lat.append(time.perf_counter() - t0)
-    plain_root = r
+    same = [pool.edit(root0, plain) == r]
     lat_ms = np.array(lat) * 1e3
     plain_wall_s = float(lat_ms.sum()) / 1e3
     # (2) device time of the same passes back to back on the stream: the root
@@ -489,7 +499,7 @@ def run_ours(args):
     e2.record(stream)
     torch.cuda.synchronize()
     plain_dev_ms = s2.elapsed_time(e2)
-    plain_dev_root = int(d_root.item()) & 0xFFFFFFFF
+    same.append(pool.edit(root0, plain) == (int(d_root.item()) & 0xFFFFFFFF))
     # (3) the same edits as ONE batched pass: device time and hd_edit wall time
     pool.rollback(0)
     d_root.copy_(d_root0)
@@ -499,7 +509,7 @@ def run_ours(args):
     e2.record(stream)
     torch.cuda.synchronize()
     batched_dev_ms = s2.elapsed_time(e2)
-    batched_dev_root = int(d_root.item()) & 0xFFFFFFFF
+    same.append(plain_chain(root0) == (int(d_root.item()) & 0xFFFFFFFF))
     bw_times = []
     for _ in range(3):
         pool.rollback(0)
@@ -508,13 +518,8 @@ def run_ours(args):
         batched_root = pool.edit(root0, plain)
         bw_times.append(time.perf_counter() - t0)
     batched_wall_s = float(np.median(bw_times))
-    # all forms end on one root: the pool is fully deduplicated, so equal
-    # occupancy means the very same pointer (the plain chain re-run on the
-    # batched pass's pool finds every node of its final DAG)
-    r = root0
-    for k in range(len(plain)):
-        r = pool.edit(r, plain[k:k + 1])
-    plain_same = r == batched_root == plain_root == plain_dev_root == batched_dev_root
+    same.append(plain_chain(root0) == batched_root)
+    plain_same = all(same)
     if pool.error():
         raise RuntimeError(f"device error {pool.error()} in the plain/batched comparison")
 

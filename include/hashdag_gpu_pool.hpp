@@ -13,6 +13,7 @@
  *   auto pool = hashdag_gb300::GpuNodePool::Create(config);   // nullptr on failure
  *   uint32_t root = HD_NULL_PTR;
  *   pool->Edit(root, edits, &root);                          // one batched pass
+ *   root = pool->ThreadedEdit(&busy_pool, root, SphereEditor<EditMode::kDig>{c, r2}, 10); // the app's call
  *   pool->Publish();                                         // device -> mirror, what changed
  *   ... flush pool->Mirror()'s written ranges and freed pages, ClearDirty ...
  *   ... or read / edit the mirror (ReadPage, GetBucketRefWords, ...) ...
@@ -28,13 +29,133 @@
 #include "hashdag_host_mirror.hpp"
 
 #include <algorithm>
+#include <concepts>
 #include <cstdint>
 #include <memory>
+#include <type_traits>
 #include <mutex>
 #include <span>
 #include <vector>
 
 namespace hashdag_gb300 {
+
+/* ---- editors ---------------------------------------------------------------
+ * The reference passes editors as compile-time objects (the Editor and
+ * StatelessEditor concepts, include/hashdag/Editor.hpp:36-55) whose EditNode /
+ * EditVoxel run inside its CPU recursion.  The device runs the shapes of the
+ * application's editors (src/main.cpp:32-150) instead, so an editor object is
+ * lowered to an hd_edit_desc at the boundary:
+ *   - a sphere: members `center` (.x .y .z) and `r2` -- SphereEditor<Mode> of
+ *     src/main.cpp:65-150, Mode from the application's EditMode (kFill = 0,
+ *     kDig = 1, kPaint = 2; paint changes colours only, so it is accepted by
+ *     the colour path alone);
+ *   - a box: members `aabb_min` and `aabb_max` (.x .y .z) -- AABBEditor of
+ *     src/main.cpp:32-63 (a fill); a class template with one mode argument and
+ *     these members (e.g. a box editor with kDig) digs or paints by its mode;
+ *   - any other type E: specialise EditorLowering<E> with
+ *     `static hd_edit_desc Lower(const E &)` (and, for colour edits,
+ *     `static hd_vbr_edit_desc LowerColor(const E &)`).
+ * Anything else does not compile: there is no CPU path that could run an
+ * arbitrary EditNode. */
+template <class E> struct EditorLowering {};
+
+namespace detail {
+template <class V> concept Vec3 = requires(const V v) {
+	{ v.x } -> std::convertible_to<uint32_t>;
+	{ v.y } -> std::convertible_to<uint32_t>;
+	{ v.z } -> std::convertible_to<uint32_t>;
+};
+template <class E> concept SphereShape = requires(const E e) {
+	requires Vec3<decltype(e.center)>;
+	{ e.r2 } -> std::convertible_to<uint64_t>;
+};
+template <class E> concept BoxShape = requires(const E e) {
+	requires Vec3<decltype(e.aabb_min)>;
+	requires Vec3<decltype(e.aabb_max)>;
+};
+// The mode argument of an editor class template (SphereEditor<EditMode::kDig>):
+// its value as an integer in the application's EditMode order; -1 without one.
+template <class E> struct ModeOf : std::integral_constant<int, -1> {};
+template <template <auto> class T, auto M> struct ModeOf<T<M>> : std::integral_constant<int, static_cast<int>(M)> {};
+// VBRColor (include/hashdag/VBRColor.hpp:18-43) through its accessors.
+template <class C> concept VbrColorLike = requires(const C c) {
+	{ c.GetColors() } -> std::convertible_to<uint32_t>;
+	{ c.GetWeight() } -> std::convertible_to<uint32_t>;
+	{ c.GetBitsPerWeight() } -> std::convertible_to<uint32_t>;
+};
+template <class E> concept ColorMember = requires(const E e) { requires VbrColorLike<decltype(e.color)>; };
+template <class> inline constexpr bool kAlwaysFalse = false;
+} // namespace detail
+
+template <class E> concept CustomEditor = requires(const E e) {
+	{ EditorLowering<E>::Lower(e) } -> std::same_as<hd_edit_desc>;
+};
+/* Editor types the device can apply to the geometry. */
+template <class E> concept DeviceEditor =
+    CustomEditor<E> || ((detail::SphereShape<E> || detail::BoxShape<E>) && detail::ModeOf<E>::value != 2);
+/* Editor types the device can apply as colour edits (VBREditorWrapper,
+ * include/hashdag/VBREditor.hpp:26-107): the shapes above with a `color`. */
+template <class E> concept DeviceColorEditor =
+    requires(const E e) {
+	    { EditorLowering<E>::LowerColor(e) } -> std::same_as<hd_vbr_edit_desc>;
+    } || ((detail::SphereShape<E> || detail::BoxShape<E>) && detail::ColorMember<E>);
+
+namespace detail {
+template <class E> hd_edit_desc lower_shape(const E &e, uint32_t op) {
+	hd_edit_desc d{};
+	d.op = op;
+	if constexpr (SphereShape<E>) {
+		d.shape = HD_SHAPE_SPHERE;
+		d.p0[0] = (uint32_t)e.center.x;
+		d.p0[1] = (uint32_t)e.center.y;
+		d.p0[2] = (uint32_t)e.center.z;
+		d.r2 = (uint64_t)e.r2;
+	} else {
+		d.shape = HD_SHAPE_AABB;
+		d.p0[0] = (uint32_t)e.aabb_min.x;
+		d.p0[1] = (uint32_t)e.aabb_min.y;
+		d.p0[2] = (uint32_t)e.aabb_min.z;
+		d.p1[0] = (uint32_t)e.aabb_max.x;
+		d.p1[1] = (uint32_t)e.aabb_max.y;
+		d.p1[2] = (uint32_t)e.aabb_max.z;
+	}
+	return d;
+}
+} // namespace detail
+
+/* One editor object as the descriptor the device applies (geometry). */
+template <class E> hd_edit_desc LowerEditor(const E &e) {
+	if constexpr (CustomEditor<E>) {
+		return EditorLowering<E>::Lower(e);
+	} else if constexpr (DeviceEditor<E>) {
+		constexpr int mode = detail::ModeOf<E>::value;
+		static_assert(mode == -1 || mode == 0 || mode == 1, "unknown editor mode (EditMode: kFill, kDig, kPaint)");
+		return detail::lower_shape(e, mode == 1 ? HD_OP_DIG : HD_OP_FILL);
+	} else {
+		static_assert(detail::kAlwaysFalse<E>, "not an editor the device can apply: give it center/r2 or "
+		                                       "aabb_min/aabb_max, or specialise hashdag_gb300::EditorLowering");
+		return {};
+	}
+}
+/* One colour editor object as a colour edit (its shape, its mode -- fill, or
+ * paint for EditMode::kPaint -- and its VBRColor). */
+template <class E> hd_vbr_edit_desc LowerColorEditor(const E &e) {
+	if constexpr (requires { EditorLowering<E>::LowerColor(e); }) {
+		return EditorLowering<E>::LowerColor(e);
+	} else if constexpr (DeviceColorEditor<E>) {
+		constexpr int mode = detail::ModeOf<E>::value;
+		static_assert(mode == -1 || mode == 0 || mode == 2, "colour edits fill or paint (a dig is a geometry edit)");
+		hd_vbr_edit_desc d{};
+		d.edit = detail::lower_shape(e, mode == 2 ? HD_OP_PAINT : HD_OP_FILL);
+		d.colors = (uint32_t)e.color.GetColors();
+		d.weight = (uint32_t)e.color.GetWeight();
+		d.bits_per_weight = (uint32_t)e.color.GetBitsPerWeight();
+		return d;
+	} else {
+		static_assert(detail::kAlwaysFalse<E>, "not a colour editor the device can apply");
+		return {};
+	}
+}
 
 class GpuNodePool {
 public:
@@ -66,6 +187,38 @@ public:
 	hd_status Edit(uint32_t root, std::span<const hd_edit_desc> edits, uint32_t *new_root, void *stream = nullptr) {
 		return hd_edit(m_pool, root, edits.data(), (uint32_t)edits.size(), new_root, stream);
 	}
+	/* The same for the reference's editor objects (lowered by LowerEditor):
+	 * one editor, or a span of editors of one type applied in order in one
+	 * batched pass. */
+	template <DeviceEditor E>
+	hd_status Edit(uint32_t root, const E &editor, uint32_t *new_root, void *stream = nullptr) {
+		const hd_edit_desc d = LowerEditor(editor);
+		return hd_edit(m_pool, root, &d, 1u, new_root, stream);
+	}
+	template <DeviceEditor E>
+	hd_status Edit(uint32_t root, std::span<const E> editors, uint32_t *new_root, void *stream = nullptr) {
+		std::vector<hd_edit_desc> d;
+		d.reserve(editors.size());
+		for (const E &e : editors)
+			d.push_back(LowerEditor(e));
+		return hd_edit(m_pool, root, d.data(), (uint32_t)d.size(), new_root, stream);
+	}
+	/* The reference's own call forms, root in and root out: NodePoolBase::Edit
+	 * (NodePool.hpp:405-417) and NodePoolThreadedEdit::ThreadedEdit
+	 * (NodePoolThreadedEdit.hpp:104-126, as src/main.cpp:214-223 calls it).
+	 * The task pool and max_task_level only schedule the reference's CPU
+	 * recursion; the device pass takes their place and ignores them.  On
+	 * failure the old root comes back and LastStatus() says why. */
+	template <DeviceEditor E> uint32_t Edit(uint32_t root, const E &editor) {
+		uint32_t r = root;
+		m_last_status = Edit(root, editor, &r);
+		return m_last_status == HD_OK ? r : root;
+	}
+	template <class TaskPool, DeviceEditor E>
+	uint32_t ThreadedEdit(TaskPool * /*busy_pool*/, uint32_t root, const E &editor, uint32_t /*max_task_level*/) {
+		return Edit(root, editor);
+	}
+	hd_status LastStatus() const { return m_last_status; }
 	/* NodePoolThreadedGC::ThreadedGC (NodePoolThreadedGC.hpp:394-403): roots
 	 * remapped in place; the mirror is stale afterwards (the next Publish
 	 * reads everything). */
@@ -243,6 +396,7 @@ private:
 	hd_pool *m_pool;
 	HostPoolMirror m_mirror;
 	uint32_t m_root = HD_NULL_PTR;
+	hd_status m_last_status = HD_OK;
 	uint64_t m_epoch = 0; // hd_pool_epoch at the mirror's last full or incremental sync
 	bool m_synced = false;
 };
@@ -297,6 +451,13 @@ public:
 			m_root = color_root;
 		}
 		return s;
+	}
+	/* The application's colour editor objects (VBREditorWrapper over
+	 * SphereEditor<kFill / kPaint> or AABBEditor with their VBRColor,
+	 * src/main.cpp:224-242), lowered by LowerColorEditor. */
+	template <DeviceColorEditor E> hd_status VbrEdit(const E &editor) {
+		const hd_vbr_edit_desc d = LowerColorEditor(editor);
+		return VbrEdit(std::span<const hd_vbr_edit_desc>(&d, 1));
 	}
 	/* The host mirror: the node and leaf word vectors of DAGColorPool, the
 	 * words its Flush uploads (src/DAGColorPool.cpp:49-80). */

@@ -16,6 +16,14 @@
 //                            full Download; after a GC it re-reads everything
 //   gpu_pool_check color     on a GPU: GpuColorPool, the same colour edits one
 //                            per call and in one call give the same octree words
+//   gpu_pool_check editors EDITS DUMP  on a GPU: the hd_edit_desc records in
+//                            file EDITS as the application's editor objects
+//                            (SphereEditor<kFill/kDig>, AABBEditor, a box dig),
+//                            applied one per call through the reference's call
+//                            forms (ThreadedEdit(&busy_pool, root, editor, mtl)
+//                            and Edit(root, editor)), against one batched pass
+//                            of the descriptors; the pool is saved to DUMP and
+//                            "root R" printed for the caller's canonical check
 // Built with -DHD_FAKE_DEVICE instead (no library, no GPU): the pool entry
 // points GpuNodePool calls are served by an in-memory pool below, and
 //   gpu_pool_check fake_publish   Publish: full on the first sync and after an
@@ -23,6 +31,8 @@
 //                                 only the appended words, as written ranges
 //   gpu_pool_check dump           Save / Load of a pool dump
 //   gpu_pool_check dump_copy IN OUT   Load IN, Save OUT (format round trips)
+//   gpu_pool_check lowering       LowerEditor / LowerColorEditor of the
+//                                 application's editor layouts
 // Prints "ok <mode>" and exits 0, or prints the first failure and exits 1.
 #include "hashdag_gpu_pool.hpp"
 
@@ -123,6 +133,82 @@ static hd_config small_config() {
 	return c;
 }
 #endif
+
+// The application's editor objects (src/main.cpp:32-150), restated with their
+// member names and template shape: glm::u32vec3 fields, an EditMode template
+// argument, and a colour with VBRColor's accessors
+// (include/hashdag/VBRColor.hpp:18-43).  Their EditNode / EditVoxel run only in
+// the reference's CPU recursion; the device lowers the objects to descriptors.
+namespace app {
+struct u32vec3 {
+	uint32_t x, y, z;
+};
+enum class EditMode { kFill, kDig, kPaint };
+class VBRColor {
+public:
+	constexpr VBRColor() = default;
+	constexpr VBRColor(uint32_t colors, uint8_t weight, uint8_t bpw)
+	    : m_colors(colors), m_weight(weight), m_bits_per_weight(bpw), m_has_value(true) {}
+	constexpr uint32_t GetColors() const { return m_colors; }
+	constexpr uint8_t GetWeight() const { return m_weight; }
+	constexpr uint8_t GetBitsPerWeight() const { return m_bits_per_weight; }
+	constexpr bool HasValue() const { return m_has_value; }
+
+private:
+	uint32_t m_colors{};
+	uint8_t m_weight{}, m_bits_per_weight{};
+	bool m_has_value{false};
+};
+struct AABBEditor {
+	u32vec3 aabb_min, aabb_max;
+	VBRColor color;
+};
+template <EditMode Mode = EditMode::kFill> struct SphereEditor {
+	u32vec3 center{};
+	uint64_t r2{};
+	VBRColor color;
+};
+// the box dig of the benchmark's workloads (the application's AABBEditor fills only)
+template <EditMode Mode> struct BoxEditor {
+	u32vec3 aabb_min, aabb_max;
+};
+struct BusyPool {}; // stands for lf::busy_pool: the device pass ignores it
+} // namespace app
+
+static_assert(hashdag_gb300::DeviceEditor<app::AABBEditor>);
+static_assert(hashdag_gb300::DeviceEditor<app::SphereEditor<app::EditMode::kFill>>);
+static_assert(hashdag_gb300::DeviceEditor<app::SphereEditor<app::EditMode::kDig>>);
+static_assert(!hashdag_gb300::DeviceEditor<app::SphereEditor<app::EditMode::kPaint>>); // colours only
+static_assert(hashdag_gb300::DeviceEditor<app::BoxEditor<app::EditMode::kDig>>);
+static_assert(!hashdag_gb300::DeviceEditor<hd_edit_desc> && !hashdag_gb300::DeviceEditor<int>);
+static_assert(hashdag_gb300::DeviceColorEditor<app::SphereEditor<app::EditMode::kPaint>>);
+static_assert(hashdag_gb300::DeviceColorEditor<app::AABBEditor>);
+static_assert(!hashdag_gb300::DeviceColorEditor<app::BoxEditor<app::EditMode::kDig>>); // no colour
+
+[[maybe_unused]] static bool same_desc(const hd_edit_desc &a, const hd_edit_desc &b) {
+	return a.shape == b.shape && a.op == b.op && a.r2 == b.r2 && std::memcmp(a.p0, b.p0, 12) == 0 &&
+	       std::memcmp(a.p1, b.p1, 12) == 0;
+}
+
+static int check_lowering() {
+	using namespace app;
+	const hd_edit_desc s = hashdag_gb300::LowerEditor(SphereEditor<EditMode::kDig>{{7, 8, 9}, 400, {}});
+	CHECK(s.shape == HD_SHAPE_SPHERE && s.op == HD_OP_DIG && s.p0[0] == 7 && s.p0[1] == 8 && s.p0[2] == 9 &&
+	      s.r2 == 400 && s.p1[0] == 0);
+	const hd_edit_desc f = hashdag_gb300::LowerEditor(SphereEditor<>{{1, 2, 3}, 25, {}});
+	CHECK(f.shape == HD_SHAPE_SPHERE && f.op == HD_OP_FILL && f.r2 == 25);
+	const hd_edit_desc b = hashdag_gb300::LowerEditor(AABBEditor{{1, 2, 3}, {4, 5, 6}, {}});
+	CHECK(b.shape == HD_SHAPE_AABB && b.op == HD_OP_FILL && b.p0[2] == 3 && b.p1[0] == 4 && b.p1[2] == 6 && b.r2 == 0);
+	const hd_edit_desc d = hashdag_gb300::LowerEditor(BoxEditor<EditMode::kDig>{{0, 0, 0}, {64, 64, 64}});
+	CHECK(d.shape == HD_SHAPE_AABB && d.op == HD_OP_DIG && d.p1[1] == 64);
+	const hd_vbr_edit_desc p =
+	    hashdag_gb300::LowerColorEditor(SphereEditor<EditMode::kPaint>{{5, 5, 5}, 9, VBRColor(0x123456u, 3, 2)});
+	CHECK(p.edit.op == HD_OP_PAINT && p.edit.shape == HD_SHAPE_SPHERE && p.colors == 0x123456u && p.weight == 3 &&
+	      p.bits_per_weight == 2);
+	const hd_vbr_edit_desc c = hashdag_gb300::LowerColorEditor(AABBEditor{{1, 1, 1}, {2, 2, 2}, VBRColor(0xFFu, 0, 0)});
+	CHECK(c.edit.op == HD_OP_FILL && c.edit.shape == HD_SHAPE_AABB && c.colors == 0xFFu && c.bits_per_weight == 0);
+	return 0;
+}
 
 static bool same_mirror(const HostPoolMirror &a, const HostPoolMirror &b) {
 	if (a.BucketWords() != b.BucketWords() || a.PageIds() != b.PageIds())
@@ -563,6 +649,75 @@ static int dump_copy(const char *in, const char *out) {
 }
 #endif
 
+#ifndef HD_FAKE_DEVICE
+// Applies the descriptors of file `edits` as the application's editor objects
+// through the reference's call forms, one per call, and checks the result
+// against one batched pass of the descriptors (a fully deduplicated pool gives
+// equal DAGs equal pointers).  Saves the pool to `dump`, prints the root.
+static int check_editors(const char *edits, const char *dump) {
+	using namespace app;
+	FILE *f = std::fopen(edits, "rb");
+	CHECK(f != nullptr);
+	std::vector<hd_edit_desc> e;
+	hd_edit_desc x;
+	while (std::fread(&x, sizeof x, 1, f) == 1)
+		e.push_back(x);
+	std::fclose(f);
+	CHECK(!e.empty());
+	hd_config c{};
+	// the configuration follows the edits' file name: EDITS.cfg holds an hd_config
+	const std::string cfg_path = std::string(edits) + ".cfg";
+	f = std::fopen(cfg_path.c_str(), "rb");
+	CHECK(f != nullptr && std::fread(&c, sizeof c, 1, f) == 1);
+	std::fclose(f);
+	hd_status st = HD_OK;
+	auto pool = GpuNodePool::Create(c, 0, 0, &st);
+	CHECK_OK(st);
+	BusyPool busy;
+	uint32_t root = HD_NULL_PTR;
+	for (size_t i = 0; i < e.size(); ++i) {
+		const hd_edit_desc &d = e[i];
+		const u32vec3 p0{d.p0[0], d.p0[1], d.p0[2]}, p1{d.p1[0], d.p1[1], d.p1[2]};
+		hd_edit_desc lowered{};
+		// every other edit through Edit(root, editor), the rest through ThreadedEdit
+		auto apply = [&](const auto &editor) {
+			lowered = hashdag_gb300::LowerEditor(editor);
+			root = (i & 1u) ? pool->Edit(root, editor) : pool->ThreadedEdit(&busy, root, editor, 5u);
+		};
+		if (d.shape == HD_SHAPE_SPHERE && d.op == HD_OP_FILL)
+			apply(SphereEditor<EditMode::kFill>{p0, d.r2, {}});
+		else if (d.shape == HD_SHAPE_SPHERE)
+			apply(SphereEditor<EditMode::kDig>{p0, d.r2, {}});
+		else if (d.op == HD_OP_FILL)
+			apply(AABBEditor{p0, p1, {}});
+		else
+			apply(BoxEditor<EditMode::kDig>{p0, p1});
+		CHECK_OK(pool->LastStatus());
+		CHECK(same_desc(lowered, d));
+	}
+	// a span of editor objects of one type in one batched pass
+	std::vector<SphereEditor<EditMode::kDig>> digs;
+	for (const hd_edit_desc &d : e)
+		if (d.shape == HD_SHAPE_SPHERE && d.op == HD_OP_DIG)
+			digs.push_back({{d.p0[0], d.p0[1], d.p0[2]}, d.r2, {}});
+	uint32_t batched = HD_NULL_PTR, dug = HD_NULL_PTR, dug_desc = HD_NULL_PTR;
+	CHECK_OK(pool->Edit(HD_NULL_PTR, std::span<const hd_edit_desc>(e), &batched));
+	CHECK(batched == root);
+	if (!digs.empty()) {
+		std::vector<hd_edit_desc> dd;
+		for (const auto &g : digs)
+			dd.push_back(hashdag_gb300::LowerEditor(g));
+		CHECK_OK(pool->Edit(root, std::span<const SphereEditor<EditMode::kDig>>(digs), &dug));
+		CHECK_OK(pool->Edit(root, std::span<const hd_edit_desc>(dd), &dug_desc));
+		CHECK(dug == dug_desc);
+	}
+	CHECK_OK(pool->Download());
+	CHECK(pool->Mirror().Save(dump));
+	std::printf("root %u\n", root);
+	return 0;
+}
+#endif
+
 int main(int argc, char **argv) {
 	if (argc < 2) {
 		std::printf("usage: gpu_pool_check MODE [ARGS]\n");
@@ -572,6 +727,8 @@ int main(int argc, char **argv) {
 	int rc = 2;
 	if (mode == "mirror")
 		rc = check_mirror();
+	else if (mode == "lowering")
+		rc = check_lowering();
 #ifndef HD_FAKE_DEVICE
 	else if (mode == "nodevice")
 		rc = check_nodevice();
@@ -581,6 +738,8 @@ int main(int argc, char **argv) {
 		rc = check_publish();
 	else if (mode == "color")
 		rc = check_color();
+	else if (mode == "editors" && argc == 4)
+		rc = check_editors(argv[2], argv[3]);
 #else
 	else if (mode == "fake_publish")
 		rc = check_fake_publish();

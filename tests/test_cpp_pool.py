@@ -139,3 +139,66 @@ def test_colour_pool_class(hd, tmp_path):
     """GpuColorPool over the colour entry points: one edit per call and all in
     one call give the same octree words and roots; digs keep the colour root."""
     run_check(build_check(hd, tmp_path), "color")
+
+
+def test_editor_objects_lower_to_descriptors(tmp_path):
+    """LowerEditor / LowerColorEditor turn the application's editor objects
+    (SphereEditor<kFill/kDig/kPaint>, AABBEditor, a box dig) into the
+    descriptors the device applies; the concepts accept exactly those."""
+    run_check(build_fake(tmp_path), "lowering")
+
+
+@pytest.mark.parametrize("body", [
+    "struct Weird { int q; }; auto d = hashdag_gb300::LowerEditor(Weird{1});",
+    "struct Weird { int q; }; uint32_t r; auto p = hashdag_gb300::GpuNodePool::Create(hd_config{}); "
+    "p->Edit(0u, Weird{1}, &r);",
+    "enum class EditMode { kFill, kDig, kPaint }; struct V { unsigned x, y, z; }; "
+    "template <EditMode M> struct SphereEditor { V center; unsigned long long r2; }; uint32_t r; "
+    "auto p = hashdag_gb300::GpuNodePool::Create(hd_config{}); "
+    "p->Edit(0u, SphereEditor<EditMode::kPaint>{{1, 2, 3}, 4}, &r);",
+])
+def test_other_editors_do_not_compile(tmp_path, body):
+    """An editor the device cannot apply (no sphere or box members, or a paint
+    as a geometry edit) is a compile error, not a CPU fallback."""
+    gxx = shutil.which("g++")
+    if not gxx:
+        pytest.skip("g++ not found")
+    src = tmp_path / "bad.cpp"
+    src.write_text('#include "hashdag_gpu_pool.hpp"\nint main() { ' + body + ' return 0; }\n')
+    r = subprocess.run([gxx, "-std=c++20", "-fsyntax-only", "-I", os.path.join(ROOT, "include"), str(src)],
+                       capture_output=True, text=True)
+    assert r.returncode != 0
+    ok = tmp_path / "ok.cpp"
+    ok.write_text('#include "hashdag_gpu_pool.hpp"\nint main() { return 0; }\n')
+    r = subprocess.run([gxx, "-std=c++20", "-fsyntax-only", "-I", os.path.join(ROOT, "include"), str(ok)],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["full_then_dig", "scene64", "aabb_kat"])
+def test_reference_editor_objects_on_device(hd, orc, golden, tmp_path, name):
+    """The application's editor objects through the reference's call forms
+    (ThreadedEdit(&busy_pool, root, editor, max_task_level) and
+    Edit(root, editor), src/main.cpp:214-223) on the device: the DAG equals the
+    reference's (canonical digests of the golden scenario) and one batched pass
+    of the same edits ends on the same root."""
+    import numpy as np
+    from helpers import config_from, scenario, scenario_edits
+    from vkhashdag_gb300 import read_pool_dump
+    s = scenario(golden, name)
+    cfg = config_from(s["config"])
+    edits = np.ascontiguousarray(scenario_edits(s))
+    path = tmp_path / "edits.bin"
+    path.write_bytes(edits.tobytes())
+    (tmp_path / "edits.bin.cfg").write_bytes(bytes(cfg.to_c()))
+    exe = build_check(hd, tmp_path)
+    dump = str(tmp_path / "pool.hdmp")
+    r = subprocess.run([exe, "editors", str(path), dump], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0 and r.stdout.strip().endswith("ok editors"), r.stdout + r.stderr
+    root = int(next(ln for ln in r.stdout.splitlines() if ln.startswith("root "))[5:])
+    c2, bw, ids, pages = read_pool_dump(dump)
+    mirror = orc.OraclePool.from_config(c2)
+    mirror.load(bw, ids, pages)
+    ok, counts, digests = mirror.canonical(root)
+    assert ok and counts == s["canonical_counts"] and [str(d) for d in digests] == s["canonical_digests"]

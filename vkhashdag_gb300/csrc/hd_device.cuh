@@ -374,6 +374,16 @@ struct Workspace {
 	u32 *long_q;       // per inner level: items with long edit lists (same index space as inner)
 	u32 *todo;         // [inner.cap] level-(L-2) items that still need the claiming probe
 	u32 *todo_parent;  // [inner.cap] their parents' child slots (todo record t: bchild/cnew slot begin(L-2)+t)
+	// Leaf-pattern cache of the leaf kernels: leaf bits -> pointer of the
+	// resident leaf with those bits, 2-way sets of slots (2k, 2k+1), cleared
+	// at the start of every multi-kernel pass (key 0 = empty, value Null =
+	// not yet written).  A pass's changed leaves repeat few patterns (a box
+	// face cuts every leaf it crosses the same way), so most of its read-only
+	// leaf lookups are answered from this L2-resident table instead of a
+	// random index slot and a random heap read.  lc_key null: not used.
+	unsigned long long *lc_key; // [lc_mask + 1]
+	u32 *lc_val;                // [lc_mask + 1]
+	u32 lc_mask;
 	const hd_edit_desc *edits;
 	u32 n_edits;
 	u32 long_threshold; // lists longer than this are expanded by a block (inner) or a warp (level L-2)
@@ -408,7 +418,9 @@ enum WsCtr : u32 {
 	kWsLeafPairs = 73,   // (node, edit) pairs: edit-list entries of those nodes
 	kWsLeafBaseW = 74,   // words of their base nodes read
 	kWsLeafOld = 75,     // old leaves read from the heap
-	kWsLeafLookup = 76,  // read-only index lookups of changed leaves
+	kWsLeafLookup = 76,  // read-only lookups of changed leaves
+	kWsLeafCacheHit = 77, // of these, answered by the leaf-pattern cache
+	kWsLeafInner = 78,    // read-only index lookups of level-(L-2) nodes whose children are all known
 	kWsCand = 96,
 	kWsCandWords = 128,
 	kWsIns = 160,

@@ -572,6 +572,53 @@ __device__ __forceinline__ u32 lookup_leaf_from(const DevPool &P, u64 bits, u64 
 	return kNull;
 }
 
+// Work counters of the leaf kernels, packed into two 64-bit registers per
+// thread to keep the kernel within its register budget:
+//   a = pairs | lookups << 24 | cache hits << 44
+//   b = base-node words | old leaves << 22 | inner lookups << 43
+// A thread handles at most inner.cap / (152 * 256) < 2^14 nodes, so no field
+// carries into the next (pairs <= 16 per node, lookups and hits <= 8, words
+// <= 9, old leaves <= 8, inner lookups <= 1).  Summed over the warp and added
+// with one atomic per counter and warp; all 32 lanes call this after their
+// loop.
+struct LeafWork {
+	u64 a = 0, b = 0;
+	__device__ __forceinline__ void pairs(u32 n) { a += n; }
+	__device__ __forceinline__ void lookup() { a += 1ull << 24; }
+	__device__ __forceinline__ void hit() { a += 1ull << 44; }
+	__device__ __forceinline__ void base_words(u32 n) { b += n; }
+	__device__ __forceinline__ void old_leaf() { b += 1ull << 22; }
+	__device__ __forceinline__ void inner() { b += 1ull << 43; }
+};
+// Read-only lookup of a changed leaf: the leaf-pattern cache first (two slots
+// in one 16-byte L2 load), then the index; a leaf found in the index is
+// entered into an empty slot of its set (key by CAS, then the pointer).
+// Entries only ever name committed leaves, so a hit is exact.
+__device__ __forceinline__ u32 lookup_leaf_cached(const DevPool &P, const Workspace &W, u64 bits, LeafWork &work) {
+	if (!W.lc_key) {
+		const u64 sl = leaf_slot(P, bits);
+		return lookup_leaf_from(P, bits, sl, __ldg(&P.index[sl]));
+	}
+	const u32 set = hash_leaf(bits) & W.lc_mask & ~1u;
+	const ulonglong2 k = __ldcg(reinterpret_cast<const ulonglong2 *>(W.lc_key + set));
+	const u32 way = k.x == bits ? 0u : (k.y == bits ? 1u : 2u);
+	if (way < 2u) {
+		const u32 v = __ldcg(W.lc_val + set + way);
+		if (v != kNull) {
+			work.hit();
+			return v;
+		}
+	}
+	const u64 sl = leaf_slot(P, bits);
+	const u32 r = lookup_leaf_from(P, bits, sl, __ldg(&P.index[sl]));
+	if (r != kNull && way == 2u) {
+		const u32 e = k.x == 0ull ? 0u : (k.y == 0ull ? 1u : 2u);
+		if (e < 2u && atomicCAS(W.lc_key + set + e, 0ull, (unsigned long long)bits) == 0ull)
+			__stcg(W.lc_val + set + e, r);
+	}
+	return r;
+}
+
 // Read-only lookup of an inner node (packed words) at level l among the resident nodes.
 __device__ __forceinline__ u32 lookup_inner(const DevPool &P, u32 l, const u32 *w, u32 n, u32 h) {
 	const u32 bucket = P.cfg.bucket_base[l] + ((P.cfg.hasher == HD_HASHER_ZERO ? 0u : h) & ((1u << P.cfg.bucket_bits[l]) - 1u));
@@ -601,7 +648,7 @@ __device__ __forceinline__ u32 lookup_inner(const DevPool &P, u32 l, const u32 *
 // A level-(L-2) node whose 8 children are all known: unchanged, empty, or an
 // existing node found read-only.  Returns false if it needs the dedup launch.
 __device__ __forceinline__ bool resolve_node(const DevPool &P, u32 l, u32 base, const u32 old[8], const u32 res[8],
-                                             u32 *out) {
+                                             u32 *out, LeafWork &work) {
 	bool unchanged = true;
 	u32 mask = 0, w[9], k = 1;
 #pragma unroll
@@ -624,6 +671,7 @@ __device__ __forceinline__ bool resolve_node(const DevPool &P, u32 l, u32 base, 
 	Murmur mm;
 	for (u32 q = 0; q < k; ++q)
 		mm.add(w[q]);
+	work.inner();
 	const u32 r = lookup_inner(P, l, w, k, mm.finish(k));
 	*out = r;
 	return r != kNull;
@@ -637,12 +685,16 @@ __device__ __forceinline__ void hand_to_parent(Workspace &W, u64 i, u32 r) {
 		W.cnew[ps] = r;
 }
 
-// Work counters of the leaf kernels, summed over the warp and added with one
-// atomic per counter and warp (all 32 lanes call this after their loop).
-__device__ __forceinline__ void add_leaf_work(Workspace &W, u32 nodes, u32 pairs, u32 basew, u32 old, u32 lookup) {
-	const u32 v[5] = {nodes, pairs, basew, old, lookup};
+__device__ __forceinline__ void add_leaf_work(Workspace &W, u32 nodes, const LeafWork &w) {
+	const u32 v[7] = {nodes,
+	                  (u32)(w.a & 0xFFFFFFu),
+	                  (u32)(w.b & 0x3FFFFFu),
+	                  (u32)((w.b >> 22) & 0x1FFFFFu),
+	                  (u32)((w.a >> 24) & 0xFFFFFu),
+	                  (u32)(w.a >> 44),
+	                  (u32)(w.b >> 43)};
 #pragma unroll
-	for (int k = 0; k < 5; ++k) {
+	for (int k = 0; k < 7; ++k) {
 		const u32 x = __reduce_add_sync(kFullMask, v[k]);
 		if (lane_id() == 0 && x)
 			atomicAdd(&W.ctr[kWsLeafNodes + k], (unsigned long long)x);
@@ -658,7 +710,8 @@ __device__ __forceinline__ void leafparent_short_phase(const DevPool &P, Workspa
 	level_range(W, L, l, begin, n);
 	const u32 T = W.long_threshold;
 	const u64 stride = tstride;
-	u32 st_nodes = 0, st_pairs = 0, st_basew = 0, st_old = 0, st_lookup = 0; // work counters
+	u32 st_nodes = 0;
+	LeafWork work;
 	for (u64 w0 = tbase + (threadIdx.x & ~31u); w0 < n; w0 += stride) {
 		const u64 t = w0 + lane_id();
 		const u64 i = begin + t;
@@ -678,21 +731,22 @@ __device__ __forceinline__ void leafparent_short_phase(const DevPool &P, Workspa
 		if (mine) {
 			base_children(P, l, b, old);
 			st_nodes += 1;
-			st_pairs += len;
-			st_basew += (b == kNull || b == P.cfg.filled[l]) ? 0u : 1u + __popc(__ldg(node_addr(P, b)) & 0xFFu);
+			work.pairs(len);
+			if (b != kNull && b != P.cfg.filled[l])
+				work.base_words(1u + __popc(__ldg(node_addr(P, b)) & 0xFFu));
 #pragma unroll 1
 			for (u32 c = 0; c < 8; ++c) { // not unrolled: one copy of the leaf code keeps the i-cache warm
 				u32 cx, cy, cz;
 				child_pos(pos, c, cx, cy, cz);
 				const u64 b0 = leaf_bits(P, old[c]);
-				st_old += (old[c] == kNull || old[c] == P.cfg.filled[L - 1]) ? 0u : 1u;
+				if (old[c] != kNull && old[c] != P.cfg.filled[L - 1])
+					work.old_leaf();
 				const u64 bits = rebuild_leaf(W, off, len, cx, cy, cz, b0);
 				bool cand;
 				u32 r = leaf_result(P, bits, b0, old[c], &cand);
 				if (cand) {
-					const u64 sl = leaf_slot(P, bits);
-					r = lookup_leaf_from(P, bits, sl, __ldg(&P.index[sl]));
-					st_lookup += 1;
+					r = lookup_leaf_cached(P, W, bits, work);
+					work.lookup();
 					if (r == kNull) {
 						cb[c] = bits;
 						cand_mask |= 1u << c;
@@ -704,7 +758,7 @@ __device__ __forceinline__ void leafparent_short_phase(const DevPool &P, Workspa
 		// Every lane of the warp reaches both reservations below (lanes without
 		// a node of their own reserve 0).
 		u32 done = kNull;
-		const bool resolved = mine && !cand_mask && resolve_node(P, l, b, old, res, &done); // no dedup round trip
+		const bool resolved = mine && !cand_mask && resolve_node(P, l, b, old, res, &done, work); // no dedup round trip
 		// the node's leaf candidates are contiguous, in child order
 		const u64 c0 = warp_reserve(&W.ctr[kWsItems + L - 1], __popc(cand_mask));
 		const u64 tq = warp_reserve(&W.ctr[kWsTodo], (mine && !resolved) ? 1u : 0u);
@@ -739,7 +793,7 @@ __device__ __forceinline__ void leafparent_short_phase(const DevPool &P, Workspa
 		cn[0] = make_uint4(res[0], res[1], res[2], res[3]);
 		cn[1] = make_uint4(res[4], res[5], res[6], res[7]);
 	}
-	add_leaf_work(W, st_nodes, st_pairs, st_basew, st_old, st_lookup);
+	add_leaf_work(W, st_nodes, work);
 }
 static __global__ void __launch_bounds__(kBlock, 4) k_leafparent_short(DevPool P, Workspace W) {
 	apply_pass_desc(W);
@@ -758,7 +812,8 @@ static __global__ void __launch_bounds__(kBlock) k_leafparent_long(DevPool P, Wo
 	const u64 n = W.ctr[kWsLong + l];
 	const u32 lane = lane_id(), c = lane >> 2, q = lane & 3u;
 	const u64 warps = (u64)gridDim.x * (blockDim.x / 32);
-	u32 lw_nodes = 0, lw_pairs = 0, lw_basew = 0, lw_old = 0, lw_lookup = 0; // work counters
+	u32 lw_nodes = 0;
+	LeafWork work;
 	for (u64 k = (u64)blockIdx.x * (blockDim.x / 32) + threadIdx.x / 32; k < n; k += warps) {
 		const u64 qi = begin + k;
 		if (qi >= W.inner.cap)
@@ -780,14 +835,15 @@ static __global__ void __launch_bounds__(kBlock) k_leafparent_long(DevPool P, Wo
 		base_children(P, l, b, old);
 		if (lane == 0) {
 			lw_nodes += 1;
-			lw_pairs += len;
-			lw_basew += (b == kNull || b == P.cfg.filled[l]) ? 0u : 1u + __popc(__ldg(node_addr(P, b)) & 0xFFu);
+			work.pairs(len);
+			if (b != kNull && b != P.cfg.filled[l])
+				work.base_words(1u + __popc(__ldg(node_addr(P, b)) & 0xFFu));
 		}
 		u32 cx, cy, cz;
 		child_pos(pos, c, cx, cy, cz);
 		const u64 b0 = leaf_bits(P, old[c]);
-		if (q == 0)
-			lw_old += (old[c] == kNull || old[c] == P.cfg.filled[L - 1]) ? 0u : 1u;
+		if (q == 0 && old[c] != kNull && old[c] != P.cfg.filled[L - 1])
+			work.old_leaf();
 		u32 mine = (u32)(b0 >> (16u * q)) & 0xFFFFu;
 		for (u32 p = 0; p < len; ++p) {
 			const hd_edit_desc e = W.edits[W.lists[off + p]];
@@ -815,10 +871,9 @@ static __global__ void __launch_bounds__(kBlock) k_leafparent_long(DevPool P, Wo
 		bool cand = false;
 		u32 r = leaf_result(P, bits, b0, old[c], &cand);
 		if (lead && cand) {
-			const u64 sl = leaf_slot(P, bits);
-			r = lookup_leaf_from(P, bits, sl, __ldg(&P.index[sl]));
+			r = lookup_leaf_cached(P, W, bits, work);
 			cand = r == kNull;
-			lw_lookup += 1;
+			work.lookup();
 		}
 		cand = lead && cand;
 		const u32 cmask_lanes = __ballot_sync(kFullMask, cand); // bit 4c set for candidate child c
@@ -853,7 +908,7 @@ static __global__ void __launch_bounds__(kBlock) k_leafparent_long(DevPool P, Wo
 			W.todo_parent[tq] = W.inner.parent[i];
 		}
 	}
-	add_leaf_work(W, lw_nodes, lw_pairs, lw_basew, lw_old, lw_lookup);
+	add_leaf_work(W, lw_nodes, work);
 }
 
 // ------------------------------------------------------------------ k_root
