@@ -670,6 +670,47 @@ def host_rays(cams, width, height, rows):
     return o, d
 
 
+def sphere_cameras(hd, W, n, seed=4, width=3840, height=2160, fov=np.pi / 3):
+    """Seeded pinhole cameras around the sphere scene (a sphere of radius
+    0.29 at the centre of the unit cube): on a shell of radius 0.42-0.48 about
+    the centre, looking at the centre with a jitter of up to 0.1."""
+    cams = np.zeros(n, hd.CAMERA_DTYPE)
+    th = 2 * np.pi * W.uniform(seed, 61, n)
+    ph = np.arccos(1 - 2 * W.uniform(seed, 62, n))
+    rad = 0.42 + 0.06 * W.uniform(seed, 63, n)
+    dirv = np.stack([np.sin(ph) * np.cos(th), np.cos(ph), np.sin(ph) * np.sin(th)], 1)
+    pos = 0.5 + rad[:, None] * dirv
+    target = 0.5 + 0.1 * (np.stack([W.uniform(seed, 64 + k, n) for k in range(3)], 1) - 0.5)
+    look = target - pos
+    look /= np.linalg.norm(look, axis=1, keepdims=True)
+    tg, aspect = np.tan(fov / 2), width / height
+    side = np.cross(look, np.array([0.0, 1.0, 0.0]))
+    side /= np.linalg.norm(side, axis=1, keepdims=True)
+    up = np.cross(side, look)
+    cams["position"] = pos
+    cams["look"], cams["side"], cams["up"] = look, side * tg * aspect, up * tg
+    return cams
+
+
+def time_pinhole(pool, root, cams, width, height, out, ctr, stackless, steps, warmup, stream):
+    """CUDA-event time per step of one pinhole kernel on the launching stream,
+    after warm-up; counters summed over the timed steps."""
+    import torch
+    sp = stream.cuda_stream
+    fn = pool.trace_pinhole_stackless_async if stackless else pool.trace_pinhole_async
+    for _ in range(warmup):
+        fn(root, cams, width, height, out.data_ptr(), 0, sp)
+    ctr.zero_()
+    torch.cuda.synchronize()
+    s0, s1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s0.record(stream)
+    for _ in range(steps):
+        fn(root, cams, width, height, out.data_ptr(), ctr.data_ptr(), sp)
+    s1.record(stream)
+    torch.cuda.synchronize()
+    return s0.elapsed_time(s1) / steps, [int(x) for x in ctr.cpu()]
+
+
 def run_rays(args):
     import torch
     world, rank, local = dist_setup()
@@ -712,6 +753,38 @@ def run_rays(args):
             host.copy_(out, non_blocking=True)
         stream.synchronize()
     e2e = n_rays * args.steps / (time.perf_counter() - t0)
+    # the stackless warp-coherent kernel on the same cameras: same hit records
+    sout = torch.empty_like(out)
+    sl_ms, sl_ctr = time_pinhole(pool, root, cams, width, height, sout, ctr, True, args.steps, args.warmup, stream)
+    pool.trace_pinhole_async(root, cams, width, height, out.data_ptr(), 0, sp)
+    torch.cuda.synchronize()
+    stackless = {"rays_per_s": n_rays / (sl_ms / 1e3), "ms_per_step": sl_ms,
+                 "steps_per_ray": sl_ctr[0] / (n_rays * args.steps),
+                 "node_words_per_ray": sl_ctr[1] / (n_rays * args.steps),
+                 "same_hits_as_stackful": bool(torch.equal(out, sout)),
+                 "speedup_vs_stackful": (ms / args.steps) / sl_ms}
+    del sout
+    # the sphere scene of the 1024^3 workload (one r=300 fill, 64 digs), the
+    # secondary scene of the ray workload: both kernels, the same camera count
+    sphere = None
+    if not args.no_sphere_rays:
+        scfg = W.config_for_resolution(1024)
+        spool = hd.NodePool(scfg, heap_pages=scfg.get_total_pages(), device=local)
+        sroot = spool.edit(hd.NULL, W.sphere_scene(1024, 64, seed=0))
+        scams = sphere_cameras(hd, W, n_cams, width=width, height=height)
+        sa = torch.empty(n_rays * 40, dtype=torch.uint8, device=f"cuda:{local}")
+        sb = torch.empty_like(sa)
+        a_ms, a_ctr = time_pinhole(spool, sroot, scams, width, height, sa, ctr, False, args.steps, args.warmup, stream)
+        b_ms, b_ctr = time_pinhole(spool, sroot, scams, width, height, sb, ctr, True, args.steps, args.warmup, stream)
+        sphere = {"scene": "1024^3 sphere scene (r=300 fill + 64 digs r in [16,64])", "cameras": n_cams,
+                  "stackful": {"rays_per_s": n_rays / (a_ms / 1e3), "ms_per_step": a_ms,
+                               "steps_per_ray": a_ctr[0] / (n_rays * args.steps)},
+                  "stackless": {"rays_per_s": n_rays / (b_ms / 1e3), "ms_per_step": b_ms,
+                                "node_words_per_ray": b_ctr[1] / (n_rays * args.steps)},
+                  "hit_fraction": a_ctr[2] / (n_rays * args.steps),
+                  "same_hits": bool(torch.equal(sa, sb))}
+        del sa, sb
+        spool.close()
     # the renderer's form: level of detail (trace.frag:148), alone and with the
     # 8x8 beam prepass (beam.frag), same cameras, projection factors of a 60 deg
     # vertical field of view (src/rg/TracePass.cpp:114-118, BeamPass.cpp:90-94)
@@ -779,7 +852,8 @@ def run_rays(args):
                              "the hit output",
                      "algorithmic_bytes_per_step": alg, "steps_per_ray": steps / (n_rays * args.steps),
                      "node_words_per_ray": reads / (n_rays * args.steps)},
-        "hit_fraction": hits / (n_rays * args.steps), "lod": lod, "cpu_baseline": cpu,
+        "hit_fraction": hits / (n_rays * args.steps), "stackless": stackless, "sphere_scene": sphere,
+        "lod": lod, "cpu_baseline": cpu,
         "gpu_launches": pool.kernel_launches() - launches0, "clocks": clocks.summary(),
     }
     print(json.dumps(line), flush=True)
@@ -1343,6 +1417,7 @@ def main():
     ap.add_argument("--width", type=int, default=3840)
     ap.add_argument("--height", type=int, default=2160)
     ap.add_argument("--cpu-rows", type=int, default=64)
+    ap.add_argument("--no-sphere-rays", action="store_true", help="rays mode: skip the sphere scene")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

@@ -324,6 +324,15 @@ hd_status hd_trace(hd_pool *pool, uint32_t root, const float *origins, const flo
  * loop iterations, node words read and hits.  Async on stream. */
 hd_status hd_trace_pinhole_async(hd_pool *pool, uint32_t root, const hd_camera *cameras, uint32_t n_cameras,
                                  uint32_t width, uint32_t height, hd_hit *d_out, uint64_t *d_counters, void *stream);
+/* The same rays and the same hit records (bit for bit, same positions) from
+ * the stackless warp-coherent kernel: no per-ray parent stack (the nodes of
+ * the last four pushed scales in registers; a pop past them re-descends from
+ * the root along the cell's position bits, which arrives at the node the
+ * reference's stack holds, NodePoolTraversal.hpp:151-243), and every warp on
+ * an 8 x 4 pixel tile.  The node-word counter includes the re-descents. */
+hd_status hd_trace_pinhole_stackless_async(hd_pool *pool, uint32_t root, const hd_camera *cameras,
+                                           uint32_t n_cameras, uint32_t width, uint32_t height, hd_hit *d_out,
+                                           uint64_t *d_counters, void *stream);
 
 /* ---- serving loop ------------------------------------------------------------
  * Several resident scenes (one hd_pool each, all on one device) served from

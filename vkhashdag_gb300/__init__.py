@@ -169,6 +169,7 @@ def lib():
         "hd_query": (I, [P, U32, P, U32, P, P]),
         "hd_trace": (I, [P, U32, P, P, U32, P, P]),
         "hd_trace_pinhole_async": (I, [P, U32, P, U32, U32, U32, P, P, P]),
+        "hd_trace_pinhole_stackless_async": (I, [P, U32, P, U32, U32, U32, P, P, P]),
         "hd_trace_pinhole_lod_async": (I, [P, U32, P, U32, U32, U32, ctypes.c_float, ctypes.c_float, P, P, P]),
         "hd_projection_factor": (ctypes.c_float, [ctypes.c_float, U32, U32]),
         "hd_server_create": (I, [P, P, U32, ctypes.POINTER(_ServerConfig), ctypes.POINTER(P)]),
@@ -703,6 +704,14 @@ class NodePool:
         _check(lib().hd_trace_pinhole_async(self._h, root & 0xFFFFFFFF, _ptr(cams), len(cams), width, height,
                                             ctypes.c_void_p(d_out), ctypes.c_void_p(d_counters or None),
                                             ctypes.c_void_p(stream)), "hd_trace_pinhole_async")
+
+    def trace_pinhole_stackless_async(self, root: int, cameras: np.ndarray, width: int, height: int, d_out: int,
+                                      d_counters: int = 0, stream: int = 0):
+        """trace_pinhole_async through the stackless warp-coherent kernel (same hits)."""
+        cams = np.ascontiguousarray(cameras, dtype=CAMERA_DTYPE)
+        _check(lib().hd_trace_pinhole_stackless_async(self._h, root & 0xFFFFFFFF, _ptr(cams), len(cams), width, height,
+                                                      ctypes.c_void_p(d_out), ctypes.c_void_p(d_counters or None),
+                                                      ctypes.c_void_p(stream)), "hd_trace_pinhole_stackless_async")
 
     def trace_pinhole_lod_async(self, root: int, cameras: np.ndarray, width: int, height: int, proj_factor: float,
                                 beam_proj_factor: float, d_out: int, d_counters: int = 0, stream: int = 0):

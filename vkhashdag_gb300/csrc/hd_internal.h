@@ -60,6 +60,9 @@ hd_status hd_remake_filled(hd_pool *pool); // filled-node pointers found or inse
 // hd_trace.cu (no wait for edit passes on other streams; the caller orders)
 hd_status hd_launch_pinhole(hd_pool *pool, uint32_t root, const hd_camera *d_cams, uint32_t n_cameras, uint32_t width,
                             uint32_t height, hd_hit *d_out, uint64_t *d_counters, cudaStream_t st);
+hd_status hd_launch_pinhole_stackless(hd_pool *pool, uint32_t root, const hd_camera *d_cams, uint32_t n_cameras,
+                                      uint32_t width, uint32_t height, hd_hit *d_out, uint64_t *d_counters,
+                                      cudaStream_t st);
 hd_status hd_launch_rays(hd_pool *pool, uint32_t root, const float *d_o, const float *d_d, uint32_t n, hd_hit *d_out,
                          cudaStream_t st);
 void hd_grid_for_levels(const hd_pool *pool, const hd_edit_desc *host_edits, uint32_t n, uint32_t *grid_per_level);

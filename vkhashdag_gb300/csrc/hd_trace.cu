@@ -24,11 +24,59 @@ __device__ __forceinline__ float fmin_ref(float x, float y) { return (y < x) ? y
 __device__ __forceinline__ float fmax_ref(float x, float y) { return (x < y) ? y : x; } // glm::max
 __device__ __forceinline__ float abs_ref(float x) { return x >= 0.0f ? x : -x; }
 
+// Stackless form of the traversal's parent stack.  The reference keeps one
+// node per scale (23 entries per ray) and pops by reading it back.  Here a ray
+// keeps only the nodes of its last four pushed scales in registers (a ring
+// indexed by scale & 3, with each entry's scale in one byte of `sc`); a pop
+// to a scale the ring no longer holds re-descends from the root along the
+// position bits of the ray's current cell, which name the child taken at
+// every scale, so it arrives at the very node the reference's stack holds.
+// Only node pointers come from the stack (no t value is restored on a pop),
+// so every float operation of the traversal, and its result, is unchanged.
+struct ParentRing {
+	u32 n0, n1, n2, n3;
+	u32 sc = 0xFFFFFFFFu; // byte k: scale of entry k, 0xFF = empty
+	__device__ __forceinline__ void push(int scale, u32 node) {
+		const u32 k = (u32)scale & 3u;
+		n0 = k == 0u ? node : n0;
+		n1 = k == 1u ? node : n1;
+		n2 = k == 2u ? node : n2;
+		n3 = k == 3u ? node : n3;
+		sc = (sc & ~(0xFFu << (8u * k))) | ((u32)scale << (8u * k));
+	}
+	// The node of `scale` if the ring holds it; kNull otherwise.  Entries of
+	// lower scales belong to the subtree being left and are dropped.
+	__device__ __forceinline__ u32 pop(int scale) {
+		const u32 k = (u32)scale & 3u;
+		const bool have = ((sc >> (8u * k)) & 0xFFu) == (u32)scale;
+		const u32 node = k == 0u ? n0 : (k == 1u ? n1 : (k == 2u ? n2 : n3));
+		sc |= __vcmpltu4(sc, 0x01010101u * (u32)scale); // bytes below `scale` -> 0xFF
+		return have ? node : kNull;
+	}
+};
+// The node at `scale` on the path of the cell at pos (scale > leaf scale):
+// from the root, each scale's child index is that scale's position bit per
+// axis, mirrored by the octant (as in the descent).
+__device__ __forceinline__ u32 descend_to(const DevPool &P, u32 root, int top, int scale, const float pos[3], u32 octant,
+                                          u32 *reads) {
+	u32 node = root;
+	for (int sc = top; sc > scale; --sc) {
+		const u32 idx = ((__float_as_uint(pos[0]) >> sc) & 1u) | (((__float_as_uint(pos[1]) >> sc) & 1u) << 1) |
+		                (((__float_as_uint(pos[2]) >> sc) & 1u) << 2);
+		const u32 cs = idx ^ octant;
+		const u32 *p = node_addr(P, node);
+		node = node_addr(P, node + 1u + __popc(p[0] & ((1u << cs) - 1u)))[0];
+		*reads += 2;
+	}
+	return node;
+}
+
 // steps: loop iterations; reads: node words fetched (mask words, child pointers, leaf words).
 // Lod: the level-of-detail cut of shader/src/trace.frag:148 and beam.frag:128 --
 // descent stops at a cube whose size times proj_factor is below its entry t plus
 // proj_bias; *scale_out receives the size of the cube the ray stopped in.
-template <bool Lod>
+// Stackless: the parent stack is a ParentRing plus re-descents (same result).
+template <bool Lod, bool Stackless = false>
 __device__ hd_hit trace_core(const DevPool &P, u32 root, float ox, float oy, float oz, float dx, float dy, float dz,
                              float proj_factor, float proj_bias, u32 *steps, u32 *reads, float *scale_out) {
 	u32 n_steps = 0, n_reads = 0;
@@ -43,10 +91,14 @@ __device__ hd_hit trace_core(const DevPool &P, u32 root, float ox, float oy, flo
 		return out;
 	constexpr int kStack = 23;
 	const float eps = __uint_as_float((127u - 23u) << 23);
-	u32 stack[kStack];
+	constexpr int kSlots = Stackless ? 1 : kStack;
+	u32 stack[kSlots];
+	ParentRing ring;
+	if (!Stackless) {
 #pragma unroll
-	for (int k = 0; k < kStack; ++k) // every entry holds a node pointer before the first push
-		stack[k] = root;
+		for (int k = 0; k < kSlots; ++k) // every entry holds a node pointer before the first push
+			stack[k] = root;
+	}
 	float o[3] = {ox + 1.0f, oy + 1.0f, oz + 1.0f};
 	float din[3] = {dx, dy, dz}, d[3];
 #pragma unroll
@@ -115,8 +167,12 @@ __device__ hd_hit trace_core(const DevPool &P, u32 root, float ox, float oy, flo
 				tcen[a] = __fadd_rn(__fmul_rn(half, tc[a]), tcor[a]);
 			if (scale < leaf_scale || (Lod && __fmul_rn(scale_exp2, proj_factor) < __fadd_rn(tc_max, proj_bias)))
 				break;
-			if (tc_max < h)
-				stack[scale] = parent;
+			if (tc_max < h) {
+				if (Stackless)
+					ring.push(scale, parent);
+				else
+					stack[scale] = parent;
+			}
 			h = tc_max;
 			if (scale > leaf_scale)
 				parent = node_addr(P, parent + 1u + __popc(child_bits & (child_mask - 1u)))[0];
@@ -156,12 +212,18 @@ __device__ hd_hit trace_core(const DevPool &P, u32 root, float ox, float oy, flo
 				break;
 			}
 			scale_exp2 = __uint_as_float((u32)(scale - kStack + 127) << 23);
-			parent = stack[scale];
 			u32 sh[3];
 #pragma unroll
 			for (int a = 0; a < 3; ++a) {
 				sh[a] = __float_as_uint(pos[a]) >> scale;
 				pos[a] = __uint_as_float(sh[a] << scale);
+			}
+			if (Stackless) {
+				parent = ring.pop(scale);
+				if (parent == kNull)
+					parent = descend_to(P, root, kStack - 1, scale, pos, octant, &n_reads);
+			} else {
+				parent = stack[scale];
 			}
 			idx = (sh[0] & 1u) | ((sh[1] & 1u) << 1) | ((sh[2] & 1u) << 2);
 			h = 0.0f;
@@ -343,6 +405,38 @@ __global__ void k_trace_pinhole(DevPool P, u32 root, const hd_camera *cams, u32 
 		warp_add_counters(counters, my_steps, my_reads, my_hits);
 }
 
+// The pinhole traversal, stackless (ParentRing), with every warp on an 8 x 4
+// tile of pixels instead of 32 pixels of one row: neighbouring rays walk the
+// same nodes, so a warp's loads coalesce and its lanes stay in step longer.
+// Same hit records as k_trace_pinhole, at the same output positions.
+constexpr u32 kTileW = 8, kTileH = 4;
+__global__ void k_trace_pinhole_stackless(DevPool P, u32 root, const hd_camera *cams, u32 n_cams, u32 w, u32 h,
+                                          hd_hit *out, unsigned long long *counters) {
+	const u32 tx = (w + kTileW - 1) / kTileW, ty = (h + kTileH - 1) / kTileH;
+	const u64 tiles = (u64)tx * ty, total = tiles * 32u * n_cams;
+	u64 my_steps = 0, my_reads = 0, my_hits = 0;
+	for (u64 i = (u64)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (u64)gridDim.x * blockDim.x) {
+		const u32 c = (u32)(i / (tiles * 32u));
+		const u64 t = i % (tiles * 32u) / 32u;
+		const u32 lane = (u32)(i & 31u);
+		const u32 px = (u32)(t % tx) * kTileW + (lane % kTileW), py = (u32)(t / tx) * kTileH + (lane / kTileW);
+		if (px >= w || py >= h)
+			continue;
+		const hd_camera cam = cams[c];
+		float d[3];
+		pinhole_dir(cam, px, py, w, h, d);
+		u32 st_ = 0, rd_ = 0;
+		const hd_hit hh = trace_core<false, true>(P, root, cam.position[0], cam.position[1], cam.position[2], d[0], d[1],
+		                                          d[2], 0.0f, 0.0f, &st_, &rd_, nullptr);
+		out[(u64)c * w * h + (u64)py * w + px] = hh;
+		my_steps += st_;
+		my_reads += rd_;
+		my_hits += hh.hit;
+	}
+	if (counters)
+		warp_add_counters(counters, my_steps, my_reads, my_hits);
+}
+
 } // namespace
 
 extern "C" {
@@ -399,6 +493,29 @@ hd_status hd_trace_pinhole_async(hd_pool *pool, uint32_t root, const hd_camera *
 		s = HD_ERR_CUDA;
 	if (!s)
 		s = hd_launch_pinhole(pool, root, d_cams, n_cameras, width, height, d_out, d_counters, st);
+	cudaFreeAsync(d_cams, st);
+	return s;
+}
+
+hd_status hd_trace_pinhole_stackless_async(hd_pool *pool, uint32_t root, const hd_camera *cameras,
+                                           uint32_t n_cameras, uint32_t width, uint32_t height, hd_hit *d_out,
+                                           uint64_t *d_counters, void *stream) {
+	if (!pool || !cameras || !d_out || !n_cameras || !width || !height)
+		return HD_ERR_INVALID_ARG;
+	std::lock_guard<std::mutex> lk(pool->mtx);
+	if (cudaSetDevice(pool->device) != cudaSuccess)
+		return HD_ERR_CUDA;
+	cudaStream_t st = (cudaStream_t)stream;
+	if (cudaStreamWaitEvent(st, pool->ws_free, 0) != cudaSuccess)
+		return HD_ERR_CUDA;
+	hd_camera *d_cams = nullptr;
+	if (cudaMallocAsync((void **)&d_cams, n_cameras * sizeof(hd_camera), st) != cudaSuccess)
+		return HD_ERR_CUDA;
+	hd_status s = HD_OK;
+	if (cudaMemcpyAsync(d_cams, cameras, n_cameras * sizeof(hd_camera), cudaMemcpyHostToDevice, st) != cudaSuccess)
+		s = HD_ERR_CUDA;
+	if (!s)
+		s = hd_launch_pinhole_stackless(pool, root, d_cams, n_cameras, width, height, d_out, d_counters, st);
 	cudaFreeAsync(d_cams, st);
 	return s;
 }
@@ -464,6 +581,17 @@ hd_status hd_launch_pinhole(hd_pool *pool, uint32_t root, const hd_camera *d_cam
 	const uint32_t grid = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((total + 255) / 256, pool->num_sms * 16ull));
 	k_trace_pinhole<<<grid, 256, 0, st>>>(pool->P, root, d_cams, n_cameras, width, height, d_out,
 	                                      reinterpret_cast<unsigned long long *>(d_counters));
+	pool->kernel_launches++;
+	return cudaGetLastError() == cudaSuccess ? HD_OK : HD_ERR_CUDA;
+}
+
+hd_status hd_launch_pinhole_stackless(hd_pool *pool, uint32_t root, const hd_camera *d_cams, uint32_t n_cameras,
+                                      uint32_t width, uint32_t height, hd_hit *d_out, uint64_t *d_counters,
+                                      cudaStream_t st) {
+	const uint64_t lanes = (uint64_t)((width + kTileW - 1) / kTileW) * ((height + kTileH - 1) / kTileH) * 32u * n_cameras;
+	const uint32_t grid = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>((lanes + 255) / 256, pool->num_sms * 16ull));
+	k_trace_pinhole_stackless<<<grid, 256, 0, st>>>(pool->P, root, d_cams, n_cameras, width, height, d_out,
+	                                                reinterpret_cast<unsigned long long *>(d_counters));
 	pool->kernel_launches++;
 	return cudaGetLastError() == cudaSuccess ? HD_OK : HD_ERR_CUDA;
 }
