@@ -291,6 +291,25 @@ def sequential_oracle_leg(cfg, base, batch, res, threads, budget_s, serial_batch
     return cpu, ref
 
 
+def bucket_scan_figures(cfg, bucket_words, counters, levels):
+    """What the reference's linear bucket scan (NodePool.hpp:79-132) would read
+    per candidate at the given levels of the pool after a step: the mean
+    bucket fill in words, and the words a scan reads per candidate (a new node
+    scans its whole bucket, a found one half of it on average)."""
+    bases = cfg.get_level_base_bucket_indices()
+    out = {}
+    for l in levels:
+        nb = cfg.get_buckets_at_level(l)
+        w = np.asarray(bucket_words[bases[l]:bases[l] + nb], np.float64)
+        cand, ins = float(counters["candidates"][l]), float(counters["inserted"][l])
+        mean = float(w.mean())
+        scan = (ins * mean + (cand - ins) * mean / 2) / max(1.0, cand)
+        out[f"l{l}"] = {"buckets": nb, "mean_bucket_words": mean, "max_bucket_words": int(w.max()),
+                        "scan_words_per_candidate": scan,
+                        "candidate_words": float(counters["candidate_words"][l]) / max(1.0, cand)}
+    return out
+
+
 def device_canonical(cfg, snapshot, filled, root):
     """Canonical DAG of a device pool snapshot (downloaded words) under root,
     by the oracle's canonicaliser."""
@@ -549,12 +568,14 @@ def run_ours(args):
     # host cores, timed on a bounded sample of the last timed batch and then
     # run to the end of that batch; its canonical DAG must equal the device's
     cpu, checks = None, {"rerun_of_last_batch_finds_same_root": bool(same_roots)}
+    bucket_scan = None
     if rank == 0 and not args.no_cpu:
         import oracle
         oracle.build()
         threads = os.cpu_count() or 1
         cpu, ref = sequential_oracle_leg(cfg, base, batches[n_batches - 1], res, threads, args.cpu_seconds,
                                          batches[args.warmup], queries)
+        bucket_scan = bucket_scan_figures(cfg, snapshot[0], counters, [L - 4, L - 3, L - 2, L - 1])
         t0 = time.perf_counter()
         dok, dcounts, ddigests = device_canonical(cfg, snapshot, pool.filled_node_pointers(), last_root)
         t_dev_canon = time.perf_counter() - t0
@@ -607,6 +628,7 @@ def run_ours(args):
                      "dram_frac_of_random_access": ((traffic / (per_step_dedup_ms / 1e3) / 1e9) / ceiling["sector_gbs"])
                      if (traffic and ceiling) else None},
         "roofline_leaf": leaf_roof,
+        "bucket_scan_last_step": bucket_scan,
         "tuning": tuning,
         "phases_ms_per_step": phase_ms,
         "counters_last_step": {k: [int(x) for x in v] for k, v in counters.items()},
@@ -891,7 +913,6 @@ def run_terrain(args):
             lat.append(time.perf_counter() - t1)
         wall = time.perf_counter() - t0
     lat_ms = np.array(lat) * 1e3
-    final_plain = r
     # the same edits as one batched pass, on the same scene
     pool.rollback(0)
     torch.cuda.synchronize()
@@ -904,10 +925,12 @@ def run_terrain(args):
     torch.cuda.synchronize()
     batched_ms = s0.elapsed_time(s1)
     # both forms give the same DAG: re-running the plain chain finds every node
+    # (this pool state is the batched pass's: its root is the one to check)
     r = root0
     for k in range(len(edits)):
         r = pool.edit(r, edits[k:k + 1])
     same = r == (int(d_root.item()) & 0xFFFFFFFF)
+    final_plain = r
     # the sequential CPU editor (the oracle's threaded edit, the reference's
     # semantics) builds the terrain and applies the spheres in order on its own
     # pool; its canonical DAG and 2^20 point queries must equal the device's
@@ -935,8 +958,8 @@ def run_terrain(args):
                                                            ddigests == odigests),
                  "point_queries_equal_sequential_oracle": bool(np.array_equal(dev_occ, o_occ)),
                  "what": f"{len(cols)} column edits then the {len(edits)} spheres in order, by the oracle's threaded "
-                         f"editor on its own pool ({t_cpu:.1f} s, {threads} threads), against the device's plain "
-                         f"one-pass-per-edit result (the batched pass ends on the same root)",
+                         f"editor on its own pool ({t_cpu:.1f} s, {threads} threads), against the device's result "
+                         f"(the batched pass and the plain chain re-run on its pool end on the same root)",
                  "canonical_counts": dcounts, "canonical_digests": [str(d) for d in ddigests]}
     line = {
         "metric": "voxel-edits/s per-edit (plain form) on the 16384^3 terrain; p99 edit latency",

@@ -39,6 +39,17 @@ def test_batched_pass_matches_reference(golden, orc, hd, name):
     check_pool_structure(orc, pool)
 
 
+@pytest.mark.parametrize("name", ["scene1024", "mixed512", "terrain256", "full_then_dig"])
+def test_batched_pass_thread_per_node_leaves_matches_reference(golden, orc, hd, name):
+    """The same batched pass with the level-(L-2) leaves rebuilt thread per node
+    (k_leafparent_short) instead of compacted onto whole warps."""
+    s = scenario(golden, name)
+    pool = pool_for(hd, s)
+    pool.set_tuning(leaf_compact=0)
+    root = pool.edit(hd.NULL, scenario_edits(s))
+    check_against_golden(orc, pool, root, s)
+
+
 @pytest.mark.parametrize("name", ["scene64", "scene256", "mixed256", "aabb_kat", "full_then_dig", "zero_hasher16"])
 def test_plain_one_edit_per_pass_matches_reference(golden, orc, hd, name):
     """The plain form: one pass per edit, like NodePoolBase::Edit per edit."""
@@ -301,11 +312,13 @@ def test_launch_shape_never_changes_results(orc, hd):
     batch = W.mixed_batch(res, 3000, seed=12, r_max=64, side_max=128)
     want = pool.edit(root, batch)
     shapes = [dict(long_threshold=1, expand_blocks_per_sm=1, leaf_blocks_per_sm=1, dedup_blocks_per_sm=1,
-                   long_blocks_per_sm=1),
+                   long_blocks_per_sm=1, leaf_compact=0),
               dict(long_threshold=64, expand_blocks_per_sm=32, leaf_blocks_per_sm=24, dedup_blocks_per_sm=32,
-                   long_blocks_per_sm=8),
+                   long_blocks_per_sm=8, leaf_compact=1),
               dict(long_threshold=4, expand_blocks_per_sm=2, leaf_blocks_per_sm=3, dedup_blocks_per_sm=4,
-                   long_blocks_per_sm=2)]
+                   long_blocks_per_sm=2, leaf_compact=0),
+              dict(long_threshold=16, expand_blocks_per_sm=8, leaf_blocks_per_sm=1, dedup_blocks_per_sm=8,
+                   long_blocks_per_sm=4, leaf_compact=1)]
     for sh in shapes:
         pool.set_tuning(**sh)
         assert pool.edit(root, batch) == want, sh

@@ -83,7 +83,7 @@ class _Stats(ctypes.Structure):
 class _Tuning(ctypes.Structure):
     _fields_ = [("expand_blocks_per_sm", ctypes.c_uint32), ("leaf_blocks_per_sm", ctypes.c_uint32),
                 ("dedup_blocks_per_sm", ctypes.c_uint32), ("long_blocks_per_sm", ctypes.c_uint32),
-                ("long_threshold", ctypes.c_uint32)]
+                ("long_threshold", ctypes.c_uint32), ("leaf_compact", ctypes.c_uint32)]
 
 
 class _GcStats(ctypes.Structure):

@@ -322,7 +322,10 @@ hd_status launch_pass(hd_pool *pool, const hd_edit_desc *d_edits, uint32_t n, ui
 	}
 	mark();
 	if (L >= 2) {
-		k_leafparent_short<<<cap(grid[L - 2], pool->tune.leaf_blocks_per_sm), kBlock, 0, st>>>(P, W);
+		if (pool->tune.leaf_compact)
+			k_leafparent_compact<<<cap(grid[L - 2], pool->tune.leaf_blocks_per_sm), kBlock, 0, st>>>(P, W);
+		else
+			k_leafparent_short<<<cap(grid[L - 2], pool->tune.leaf_blocks_per_sm), kBlock, 0, st>>>(P, W);
 		dbg("leafparent_short", L - 1);
 		++launches;
 		if (longs) {
@@ -379,6 +382,7 @@ hd_status pass_graph(hd_pool *pool, cudaGraphExec_t *out) {
 	HD_TRY(cudaFuncGetAttributes(&fa, k_expand_short));
 	HD_TRY(cudaFuncGetAttributes(&fa, k_expand_long));
 	HD_TRY(cudaFuncGetAttributes(&fa, k_leafparent_short));
+	HD_TRY(cudaFuncGetAttributes(&fa, k_leafparent_compact));
 	HD_TRY(cudaFuncGetAttributes(&fa, k_leafparent_long));
 	HD_TRY(cudaFuncGetAttributes(&fa, k_dedup<true>));
 	HD_TRY(cudaFuncGetAttributes(&fa, k_dedup<false>));
@@ -1052,7 +1056,7 @@ hd_status hd_edit_get_tuning(const hd_pool *pool, hd_tuning *out) {
 hd_status hd_edit_set_tuning(hd_pool *pool, const hd_tuning *t) {
 	if (!pool || !t || !t->expand_blocks_per_sm || !t->leaf_blocks_per_sm || !t->dedup_blocks_per_sm ||
 	    !t->long_blocks_per_sm || !t->long_threshold || t->expand_blocks_per_sm > 64 || t->leaf_blocks_per_sm > 64 ||
-	    t->dedup_blocks_per_sm > 64 || t->long_blocks_per_sm > 64)
+	    t->dedup_blocks_per_sm > 64 || t->long_blocks_per_sm > 64 || t->leaf_compact > 1)
 		return HD_ERR_INVALID_ARG;
 	std::lock_guard<std::mutex> lk(pool->mtx);
 	pool->tune = *t;
@@ -1139,7 +1143,8 @@ hd_status hd_edit_autotune(hd_pool *pool, uint32_t root, const hd_edit_desc *edi
 		uint32_t hd_tuning::*field;
 		std::vector<uint32_t> values;
 	};
-	const std::vector<Knob> knobs = {{&hd_tuning::long_threshold, {8, 16, 32, 64}},
+	const std::vector<Knob> knobs = {{&hd_tuning::leaf_compact, {0, 1}},
+	                                 {&hd_tuning::long_threshold, {8, 16, 32, 64}},
 	                                 {&hd_tuning::leaf_blocks_per_sm, {3, 6, 12, 24}},
 	                                 {&hd_tuning::dedup_blocks_per_sm, {4, 8, 16, 32}},
 	                                 {&hd_tuning::expand_blocks_per_sm, {4, 8, 16, 32}},

@@ -795,6 +795,174 @@ __device__ __forceinline__ void leafparent_short_phase(const DevPool &P, Workspa
 	}
 	add_leaf_work(W, st_nodes, work);
 }
+// The same work with the partly covered leaves of a warp's 32 nodes compacted
+// onto all 32 lanes.  Rebuilding a partly covered leaf (its 64-voxel mask
+// under every edit of the list) is the kernel's costly step, and in the
+// thread-per-node form the lanes of a warp reach it for different leaves at
+// different times, so it ran with about half the lanes active.  Here:
+//   A. every lane classifies its node's 8 leaves against the node's edit list
+//      (EditNode of the leaf cell) and settles the leaves that no edit covers
+//      partly (unchanged, or set / cleared by the last full cover); a leaf
+//      that some edit covers partly is deferred, its old bits staged;
+//   B. the warp's deferred leaves (at most 256) are queued in shared memory
+//      and each lane rebuilds every 32nd of them: the whole edit list applied
+//      to the staged bits in order, exactly as the per-leaf rule does;
+//   C. every lane takes its 8 leaves' bits back and goes on as the
+//      thread-per-node form does (result, read-only lookup, node resolution).
+// The per-leaf rule applied is the same (rebuild_leaf), so the result is too.
+struct LeafWarpStage {
+	u64 bits[32 * 8];   // lane * 8 + leaf: bits after phase A / B
+	u64 pos[32];        // the lane's node
+	u32 off[32], len[32];
+	unsigned char q[256]; // deferred leaves: lane << 3 | leaf
+};
+static constexpr int kLeafWarps = kBlock / 32;
+
+__device__ __forceinline__ void leafparent_compact_phase(const DevPool &P, Workspace &W, u64 tbase, u64 tstride,
+                                                         LeafWarpStage &S) {
+	if (ws_failed(W))
+		return;
+	const u32 L = P.cfg.L, l = L - 2;
+	u64 begin, n;
+	level_range(W, L, l, begin, n);
+	const u32 T = W.long_threshold;
+	const u64 stride = tstride;
+	const u32 lane = lane_id();
+	u32 st_nodes = 0;
+	LeafWork work;
+	for (u64 w0 = tbase + (threadIdx.x & ~31u); w0 < n; w0 += stride) {
+		const u64 t = w0 + lane;
+		const u64 i = begin + t;
+		const bool valid = t < n;
+		u32 len = 0, off = 0, b = kNull;
+		u64 pos = 0;
+		if (valid) {
+			len = W.inner.lst_len[i];
+			off = W.inner.lst_off[i];
+			b = W.inner.base[i];
+			pos = W.inner.pos[i];
+		}
+		const bool mine = valid && len <= T && list_ok(W, off, len);
+		u32 old[8], res[8];
+		u32 defer = 0;
+		// A: leaves without a partly covering edit
+		if (mine) {
+			base_children(P, l, b, old);
+			st_nodes += 1;
+			work.pairs(len);
+			if (b != kNull && b != P.cfg.filled[l])
+				work.base_words(1u + __popc(__ldg(node_addr(P, b)) & 0xFFu));
+#pragma unroll 1
+			for (u32 c = 0; c < 8; ++c) {
+				u32 cx, cy, cz;
+				child_pos(pos, c, cx, cy, cz);
+				u64 bits = leaf_bits(P, old[c]);
+				if (old[c] != kNull && old[c] != P.cfg.filled[L - 1])
+					work.old_leaf();
+				u64 staged = bits;
+				bool partial = false;
+				for (u32 p = 0; p < len; ++p) {
+					const hd_edit_desc &e = W.edits[W.lists[off + p]];
+					const u32 cls = classify(e, 2u, cx, cy, cz);
+					if (cls == kClsPartial) {
+						partial = true;
+						break;
+					}
+					if (cls == kClsFull)
+						bits = e.op == HD_OP_FILL ? ~0ull : 0ull;
+				}
+				S.bits[lane * 8u + c] = partial ? staged : bits;
+				defer |= (partial ? 1u : 0u) << c;
+			}
+			S.pos[lane] = pos;
+			S.off[lane] = off;
+			S.len[lane] = len;
+		}
+		// B: the warp's deferred leaves on all lanes
+		const u32 nd = __popc(defer);
+		u32 incl = nd;
+#pragma unroll
+		for (int d = 1; d < 32; d <<= 1) {
+			const u32 v = __shfl_up_sync(kFullMask, incl, d);
+			if (lane >= (u32)d)
+				incl += v;
+		}
+		const u32 total = __shfl_sync(kFullMask, incl, 31);
+		u32 qpos = incl - nd;
+		for (u32 m = defer; m; m &= m - 1u)
+			S.q[qpos++] = (unsigned char)((lane << 3) | (u32)(__ffs(m) - 1));
+		__syncwarp();
+		for (u32 j = lane; j < total; j += 32u) {
+			const u32 e = S.q[j], src = e >> 3, c = e & 7u;
+			u32 cx, cy, cz;
+			child_pos(S.pos[src], c, cx, cy, cz);
+			S.bits[e] = rebuild_leaf(W, S.off[src], S.len[src], cx, cy, cz, S.bits[e]);
+		}
+		__syncwarp();
+		// C: results, read-only lookups, node resolution
+		u64 cb[8];
+		u32 cand_mask = 0;
+		if (mine) {
+#pragma unroll 1
+			for (u32 c = 0; c < 8; ++c) {
+				const u64 b0 = leaf_bits(P, old[c]);
+				const u64 bits = S.bits[lane * 8u + c];
+				bool cand;
+				u32 r = leaf_result(P, bits, b0, old[c], &cand);
+				if (cand) {
+					r = lookup_leaf_cached(P, W, bits, work);
+					work.lookup();
+					if (r == kNull) {
+						cb[c] = bits;
+						cand_mask |= 1u << c;
+					}
+				}
+				res[c] = r;
+			}
+		}
+		__syncwarp(); // the stage is rewritten by the next iteration
+		u32 done = kNull;
+		const bool resolved = mine && !cand_mask && resolve_node(P, l, b, old, res, &done, work);
+		const u64 c0 = warp_reserve(&W.ctr[kWsItems + L - 1], __popc(cand_mask));
+		const u64 tq = warp_reserve(&W.ctr[kWsTodo], (mine && !resolved) ? 1u : 0u);
+		if (!mine)
+			continue;
+		const u64 ri = begin + tq;
+		u64 ci = c0;
+#pragma unroll 1
+		for (u32 c = 0; c < 8; ++c) {
+			if (!((cand_mask >> c) & 1u))
+				continue;
+			if (ci < W.leaf.cap) {
+				W.leaf_new[ci] = cb[c];
+				W.leaf.parent[ci] = (u32)(ri * 8u + c);
+			} else {
+				ws_error(W, kErrCapacity);
+			}
+			++ci;
+		}
+		if (resolved) {
+			hand_to_parent(W, i, done);
+			continue;
+		}
+		W.todo[tq] = (u32)i;
+		W.todo_parent[tq] = W.inner.parent[i];
+		uint4 *bc = reinterpret_cast<uint4 *>(W.bchild + ri * 8u);
+		uint4 *cn = reinterpret_cast<uint4 *>(W.cnew + ri * 8u);
+		bc[0] = make_uint4(old[0], old[1], old[2], old[3]);
+		bc[1] = make_uint4(old[4], old[5], old[6], old[7]);
+		cn[0] = make_uint4(res[0], res[1], res[2], res[3]);
+		cn[1] = make_uint4(res[4], res[5], res[6], res[7]);
+	}
+	add_leaf_work(W, st_nodes, work);
+}
+static __global__ void __launch_bounds__(kBlock, 4) k_leafparent_compact(DevPool P, Workspace W) {
+	__shared__ LeafWarpStage s_stage[kLeafWarps];
+	apply_pass_desc(W);
+	leafparent_compact_phase(P, W, (u64)blockIdx.x * blockDim.x, (u64)gridDim.x * blockDim.x,
+	                         s_stage[threadIdx.x >> 5]);
+}
+
 static __global__ void __launch_bounds__(kBlock, 4) k_leafparent_short(DevPool P, Workspace W) {
 	apply_pass_desc(W);
 	leafparent_short_phase(P, W, (u64)blockIdx.x * blockDim.x, (u64)gridDim.x * blockDim.x);
