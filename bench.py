@@ -943,7 +943,13 @@ def run_terrain(args):
         snapshot = pool.download()
         threads = os.cpu_count() or 1
         mtl = max(0, cfg.get_node_levels() - 4)
-        opool = oracle.OraclePool.from_config(cfg)
+        # Edit after edit, the 262,144 column edits leave one new root path each:
+        # 2.4 M words of level-0 nodes alone, past the 2 M words of that level's
+        # 1,024 buckets, where the reference's upsert would silently keep a stale
+        # node.  The oracle therefore runs with 2^16 buckets on the six upper
+        # levels; bucket counts change pointers, not the canonical DAG.
+        obits = [max(b, 16) for b in cfg.bucket_bits_each_level[:6]] + list(cfg.bucket_bits_each_level[6:])
+        opool = oracle.OraclePool(cfg.word_bits_per_page, cfg.page_bits_per_bucket, obits, cfg.hasher)
         t0 = time.perf_counter()
         orr = opool.threaded_edit(oracle.NULL, cols, mtl, threads)
         orr = opool.threaded_edit(orr, edits, mtl, threads)
@@ -960,7 +966,9 @@ def run_terrain(args):
                  "what": f"{len(cols)} column edits then the {len(edits)} spheres in order, by the oracle's threaded "
                          f"editor on its own pool ({t_cpu:.1f} s, {threads} threads), against the device's result "
                          f"(the batched pass and the plain chain re-run on its pool end on the same root)",
-                 "canonical_counts": dcounts, "canonical_digests": [str(d) for d in ddigests]}
+                 "oracle_pool_ok": bool(o_ok), "oracle_bucket_bits": obits,
+                 "canonical_counts": dcounts, "canonical_digests": [str(d) for d in ddigests],
+                 "oracle_canonical_digests": [str(d) for d in odigests]}
     line = {
         "metric": "voxel-edits/s per-edit (plain form) on the 16384^3 terrain; p99 edit latency",
         "value": ve / wall, "unit": "voxel-edits/s", "n_gpus": world, "steps": len(edits), "warmup": 64,

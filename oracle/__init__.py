@@ -26,7 +26,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liboracle.so")
 REF_DRIVER = os.path.join(HERE, "_ref", "ref_driver")
-REFERENCE_ROOT = "/root/reference"
+# where the reference tree is read from when the reference driver is built
+REFERENCE_ROOT = os.environ.get("HASHDAG_REFERENCE_ROOT", "/root/reference")
 
 EDIT_DTYPE = np.dtype([("shape", "<u4"), ("op", "<u4"), ("p0", "<u4", (3,)), ("p1", "<u4", (3,)), ("r2", "<u8")],
                       align=True)
