@@ -196,8 +196,7 @@ hd_status hd_edit_last_probe_stats(hd_pool *pool, uint64_t *probe_steps, uint64_
  * out[1] (node, edit) pairs of their edit lists, out[2] base-node words read,
  * out[3] old leaves read from the heap, out[4] read-only lookups of changed
  * leaves, out[5] of these answered by the pass's leaf-pattern cache, out[6]
- * read-only lookups of level-(L-2) nodes whose children were all known,
- * out[7] of these answered by the pass's node-pattern cache. */
+ * read-only index lookups of level-(L-2) nodes whose children were all known. */
 hd_status hd_edit_last_leaf_work(hd_pool *pool, uint64_t *out);
 /* Launch shape of the batched pass: grid caps in blocks per SM for each kernel
  * family and the edit-list length above which a node is expanded by a block

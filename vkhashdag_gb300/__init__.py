@@ -542,10 +542,10 @@ class NodePool:
 
     def last_leaf_work(self) -> dict:
         """Work of the last pass's level-(L-2) leaf kernels."""
-        v = np.zeros(8, np.uint64)
+        v = np.zeros(7, np.uint64)
         _check(lib().hd_edit_last_leaf_work(self._h, _ptr(v)), "hd_edit_last_leaf_work")
-        return dict(zip(["nodes", "pairs", "base_words", "old_leaves", "lookups", "cache_hits", "inner_lookups",
-                         "inner_cache_hits"], (int(x) for x in v)))
+        return dict(zip(["nodes", "pairs", "base_words", "old_leaves", "lookups", "cache_hits", "inner_lookups"],
+                        (int(x) for x in v)))
 
     def last_probe_stats(self) -> dict:
         """Index slots visited by the last pass's probes, longest probe, bucket CAS retries."""

@@ -384,12 +384,6 @@ struct Workspace {
 	unsigned long long *lc_key; // [lc_mask + 1]
 	u32 *lc_val;                // [lc_mask + 1]
 	u32 lc_mask;
-	// Node-pattern cache of the same kernels for their read-only lookups of
-	// level-(L-2) nodes (lookup_inner_cached): 64-byte entries, 16 words each,
-	// cleared to all ones at the start of every multi-kernel pass.  nc null:
-	// not used.
-	u32 *nc;    // [(nc_mask + 1) * 16]
-	u32 nc_mask;
 	const hd_edit_desc *edits;
 	u32 n_edits;
 	u32 long_threshold; // lists longer than this are expanded by a block (inner) or a warp (level L-2)
@@ -426,8 +420,7 @@ enum WsCtr : u32 {
 	kWsLeafOld = 75,     // old leaves read from the heap
 	kWsLeafLookup = 76,  // read-only lookups of changed leaves
 	kWsLeafCacheHit = 77, // of these, answered by the leaf-pattern cache
-	kWsLeafInner = 78,    // read-only lookups of level-(L-2) nodes whose children are all known
-	kWsLeafInnerHit = 79, // of these, answered by the node-pattern cache
+	kWsLeafInner = 78,    // read-only index lookups of level-(L-2) nodes whose children are all known
 	kWsCand = 96,
 	kWsCandWords = 128,
 	kWsIns = 160,

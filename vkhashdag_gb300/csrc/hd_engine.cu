@@ -104,8 +104,6 @@ hd_status alloc_leaf_candidates(hd_ws_host &ws, Items &it, uint64_t cap) {
 // Slots of the leaf-pattern cache of the multi-kernel pass (12 MB: 8-byte
 // keys and 4-byte pointers, small enough to stay in L2).
 constexpr uint32_t kLeafCacheSlots = 1u << 20;
-// Entries of the node-pattern cache of level-(L-2) nodes (16 MB of 64-byte entries).
-constexpr uint32_t kNodeCacheSlots = 1u << 18;
 
 hd_status ws_reserve(hd_pool *pool, uint64_t inner_cap, uint64_t leaf_cap, uint64_t list_cap, uint32_t edit_cap) {
 	hd_ws_host &ws = pool->ws;
@@ -130,7 +128,6 @@ hd_status ws_reserve(hd_pool *pool, uint64_t inner_cap, uint64_t leaf_cap, uint6
 	    (s = ws_alloc(ws, &d.todo_parent, inner_cap)) ||
 	    (s = ws_alloc(ws, &d.lc_key, (uint64_t)kLeafCacheSlots)) ||
 	    (s = ws_alloc(ws, &d.lc_val, (uint64_t)kLeafCacheSlots)) ||
-	    (s = ws_alloc(ws, &d.nc, (uint64_t)kNodeCacheSlots * 16u)) ||
 	    (s = ws_alloc(ws, &d.ctr, (uint64_t)kWsCtrCount)) ||
 	    (s = ws_alloc(ws, &ws.edits, (uint64_t)edit_cap))) {
 		ws_free_all(ws);
@@ -138,7 +135,6 @@ hd_status ws_reserve(hd_pool *pool, uint64_t inner_cap, uint64_t leaf_cap, uint6
 	}
 	d.list_cap = list_cap;
 	d.lc_mask = kLeafCacheSlots - 1u;
-	d.nc_mask = kNodeCacheSlots - 1u;
 	d.long_threshold = 16;
 	ws.edit_cap = edit_cap;
 	ws.d = d;
@@ -270,8 +266,7 @@ hd_status launch_pass(hd_pool *pool, const hd_edit_desc *d_edits, uint32_t n, ui
 		{
 			HD_TRY(cudaStreamWaitEvent(st, pool->ws_free, 0));
 			HD_TRY(cudaMemsetAsync(W.ctr, 0, kWsCtrCount * sizeof(unsigned long long), st));
-			W.lc_key = nullptr; // a one-CTA pass has too few leaves to pay for clearing the caches
-			W.nc = nullptr;
+			W.lc_key = nullptr; // a one-CTA pass has too few leaves to pay for clearing the cache
 			k_small_pass<<<1, kBlock, 0, st>>>(P, W, root_val, root_ptr, d_out);
 			pool->kernel_launches += 1;
 			HD_TRY(cudaGetLastError());
@@ -311,8 +306,6 @@ hd_status launch_pass(hd_pool *pool, const hd_edit_desc *d_edits, uint32_t n, ui
 		HD_TRY(cudaMemsetAsync(W.lc_key, 0, (W.lc_mask + 1ull) * sizeof(unsigned long long), st));
 		HD_TRY(cudaMemsetAsync(W.lc_val, 0xFF, (W.lc_mask + 1ull) * sizeof(uint32_t), st));
 	}
-	if (W.nc) // so does the node-pattern cache
-		HD_TRY(cudaMemsetAsync(W.nc, 0xFF, (W.nc_mask + 1ull) * 16u * sizeof(uint32_t), st));
 	k_root<<<1, kLongBlock, 0, st>>>(P, W, root_val, root_ptr);
 	dbg("root", 0);
 	uint64_t launches = 1;
@@ -1349,9 +1342,9 @@ hd_status hd_edit_last_leaf_work(hd_pool *pool, uint64_t *out) {
 	std::lock_guard<std::mutex> lk(pool->mtx);
 	HD_TRY(cudaSetDevice(pool->device));
 	HD_TRY(cudaEventSynchronize(pool->ws_free));
-	unsigned long long c[8];
+	unsigned long long c[7];
 	HD_TRY(cudaMemcpy(c, pool->ws.d.ctr + kWsLeafNodes, sizeof(c), cudaMemcpyDeviceToHost));
-	for (int k = 0; k < 8; ++k)
+	for (int k = 0; k < 7; ++k)
 		out[k] = c[k];
 	return HD_OK;
 }

@@ -575,23 +575,21 @@ __device__ __forceinline__ u32 lookup_leaf_from(const DevPool &P, u64 bits, u64 
 // Work counters of the leaf kernels, packed into two 64-bit registers per
 // thread to keep the kernel within its register budget:
 //   a = pairs | lookups << 24 | cache hits << 44
-//   b = base-node words | old leaves << 18 | inner lookups << 36 | inner cache hits << 50
+//   b = base-node words | old leaves << 22 | inner lookups << 43
 // A thread handles at most inner.cap / (152 * 256) < 2^14 nodes, so no field
 // carries into the next (pairs <= 16 per node, lookups and hits <= 8, words
-// <= 9, old leaves <= 8, inner lookups and hits <= 1).  Summed over the warp
-// and added with one atomic per counter and warp; all 32 lanes call
-// add_leaf_work after their loop.
+// <= 9, old leaves <= 8, inner lookups <= 1).  Summed over the warp and added
+// with one atomic per counter and warp; all 32 lanes call this after their
+// loop.
 struct LeafWork {
 	u64 a = 0, b = 0;
 	__device__ __forceinline__ void pairs(u32 n) { a += n; }
 	__device__ __forceinline__ void lookup() { a += 1ull << 24; }
 	__device__ __forceinline__ void hit() { a += 1ull << 44; }
 	__device__ __forceinline__ void base_words(u32 n) { b += n; }
-	__device__ __forceinline__ void old_leaf() { b += 1ull << 18; }
-	__device__ __forceinline__ void inner() { b += 1ull << 36; }
-	__device__ __forceinline__ void inner_hit() { b += 1ull << 50; }
+	__device__ __forceinline__ void old_leaf() { b += 1ull << 22; }
+	__device__ __forceinline__ void inner() { b += 1ull << 43; }
 };
-
 // Read-only lookup of a changed leaf: the leaf-pattern cache first (two slots
 // in one 16-byte L2 load), then the index; a leaf found in the index is
 // entered into an empty slot of its set (key by CAS, then the pointer).
@@ -647,50 +645,10 @@ __device__ __forceinline__ u32 lookup_inner(const DevPool &P, u32 l, const u32 *
 	return kNull;
 }
 
-// Read-only lookup of a level-(L-2) node through the node-pattern cache: one
-// 64-byte entry per slot (node words 0..8, unused ones Null; word 9 the
-// pointer; word 10 the claim), cleared to all ones at the start of every
-// multi-kernel pass, so a cleared entry never matches (its mask word is not a
-// mask).  The first thread that finds a node in the index claims the empty
-// slot and writes the words, then the pointer.  No fence is needed: a slot is
-// written by one thread per pass, so a reader that sees all of the node's
-// words and a pointer that is not Null sees that thread's node and pointer;
-// any other mix of old and new words does not match, and the reader falls
-// back to the index.
-__device__ __forceinline__ u32 lookup_inner_cached(const DevPool &P, const Workspace &W, u32 l, const u32 w[9], u32 k,
-                                                   u32 h, LeafWork &work) {
-	if (!W.nc)
-		return lookup_inner(P, l, w, k, h);
-	u32 *e = W.nc + ((u64)(h & W.nc_mask) << 4);
-	const uint4 a = __ldcg(reinterpret_cast<const uint4 *>(e)), b = __ldcg(reinterpret_cast<const uint4 *>(e + 4));
-	const uint2 c = __ldcg(reinterpret_cast<const uint2 *>(e + 8));
-	const u32 ew[9] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w, c.x};
-	bool eq = true;
-#pragma unroll
-	for (u32 q = 0; q < 9; ++q)
-		eq = eq && (q >= k || ew[q] == w[q]);
-	if (eq && c.y != kNull) {
-		work.inner_hit();
-		return c.y;
-	}
-	const u32 r = lookup_inner(P, l, w, k, h);
-	if (r != kNull && a.x == kNull && atomicCAS(e + 10, kNull, 0u) == kNull) {
-		u32 f[9];
-#pragma unroll
-		for (u32 q = 0; q < 9; ++q)
-			f[q] = q < k ? w[q] : kNull;
-		__stcg(reinterpret_cast<uint4 *>(e), make_uint4(f[0], f[1], f[2], f[3]));
-		__stcg(reinterpret_cast<uint4 *>(e + 4), make_uint4(f[4], f[5], f[6], f[7]));
-		__stcg(e + 8, f[8]);
-		__stcg(e + 9, r);
-	}
-	return r;
-}
-
 // A level-(L-2) node whose 8 children are all known: unchanged, empty, or an
 // existing node found read-only.  Returns false if it needs the dedup launch.
-__device__ __forceinline__ bool resolve_node(const DevPool &P, const Workspace &W, u32 l, u32 base, const u32 old[8],
-                                             const u32 res[8], u32 *out, LeafWork &work) {
+__device__ __forceinline__ bool resolve_node(const DevPool &P, u32 l, u32 base, const u32 old[8], const u32 res[8],
+                                             u32 *out, LeafWork &work) {
 	bool unchanged = true;
 	u32 mask = 0, w[9], k = 1;
 #pragma unroll
@@ -714,7 +672,7 @@ __device__ __forceinline__ bool resolve_node(const DevPool &P, const Workspace &
 	for (u32 q = 0; q < k; ++q)
 		mm.add(w[q]);
 	work.inner();
-	const u32 r = lookup_inner_cached(P, W, l, w, k, mm.finish(k), work);
+	const u32 r = lookup_inner(P, l, w, k, mm.finish(k));
 	*out = r;
 	return r != kNull;
 }
@@ -728,16 +686,15 @@ __device__ __forceinline__ void hand_to_parent(Workspace &W, u64 i, u32 r) {
 }
 
 __device__ __forceinline__ void add_leaf_work(Workspace &W, u32 nodes, const LeafWork &w) {
-	const u32 v[8] = {nodes,
+	const u32 v[7] = {nodes,
 	                  (u32)(w.a & 0xFFFFFFu),
-	                  (u32)(w.b & 0x3FFFFu),
-	                  (u32)((w.b >> 18) & 0x3FFFFu),
+	                  (u32)(w.b & 0x3FFFFFu),
+	                  (u32)((w.b >> 22) & 0x1FFFFFu),
 	                  (u32)((w.a >> 24) & 0xFFFFFu),
 	                  (u32)(w.a >> 44),
-	                  (u32)((w.b >> 36) & 0x3FFFu),
-	                  (u32)(w.b >> 50)};
+	                  (u32)(w.b >> 43)};
 #pragma unroll
-	for (int k = 0; k < 8; ++k) {
+	for (int k = 0; k < 7; ++k) {
 		const u32 x = __reduce_add_sync(kFullMask, v[k]);
 		if (lane_id() == 0 && x)
 			atomicAdd(&W.ctr[kWsLeafNodes + k], (unsigned long long)x);
@@ -801,7 +758,7 @@ __device__ __forceinline__ void leafparent_short_phase(const DevPool &P, Workspa
 		// Every lane of the warp reaches both reservations below (lanes without
 		// a node of their own reserve 0).
 		u32 done = kNull;
-		const bool resolved = mine && !cand_mask && resolve_node(P, W, l, b, old, res, &done, work); // no dedup round trip
+		const bool resolved = mine && !cand_mask && resolve_node(P, l, b, old, res, &done, work); // no dedup round trip
 		// the node's leaf candidates are contiguous, in child order
 		const u64 c0 = warp_reserve(&W.ctr[kWsItems + L - 1], __popc(cand_mask));
 		const u64 tq = warp_reserve(&W.ctr[kWsTodo], (mine && !resolved) ? 1u : 0u);
@@ -965,7 +922,7 @@ __device__ __forceinline__ void leafparent_compact_phase(const DevPool &P, Works
 		}
 		__syncwarp(); // the stage is rewritten by the next iteration
 		u32 done = kNull;
-		const bool resolved = mine && !cand_mask && resolve_node(P, W, l, b, old, res, &done, work);
+		const bool resolved = mine && !cand_mask && resolve_node(P, l, b, old, res, &done, work);
 		const u64 c0 = warp_reserve(&W.ctr[kWsItems + L - 1], __popc(cand_mask));
 		const u64 tq = warp_reserve(&W.ctr[kWsTodo], (mine && !resolved) ? 1u : 0u);
 		if (!mine)
@@ -1206,10 +1163,9 @@ static __global__ void __launch_bounds__(kLongBlock) k_root(DevPool P, Workspace
 //     with the claiming item's words in the workspace (written by earlier
 //     launches); when equal it waits for the publication and takes the pointer
 //     without reading the heap;
-//   * a candidate that meets a final entry with its tag and bucket fences
-//     (acquire) after reading it and compares the node through L2 (no L1
-//     copies), so a node published earlier in the same launch is seen
-//     complete; the claim-or-read CAS itself is relaxed.
+//   * a candidate that meets a final entry with its tag has read it with an
+//     acquiring CAS and compares the node through L2 (no L1 copies), so a node
+//     published earlier in the same launch is seen complete.
 struct NodeWords {
 	u32 w[9];
 	u32 n;
@@ -1219,7 +1175,12 @@ struct NodeWords {
 // candidate instead of spinning on.
 static constexpr u32 kSpinLimit = 1u << 20;
 
-__device__ __forceinline__ void fence_acquire() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
+__device__ __forceinline__ unsigned long long cas_acquire(unsigned long long *p, unsigned long long cmp,
+                                                          unsigned long long val) {
+	unsigned long long old;
+	asm volatile("atom.acquire.gpu.global.cas.b64 %0, [%1], %2, %3;" : "=l"(old) : "l"(p), "l"(cmp), "l"(val) : "memory");
+	return old;
+}
 __device__ __forceinline__ unsigned long long load_acquire(const unsigned long long *p) {
 	unsigned long long v;
 	asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
@@ -1378,9 +1339,7 @@ __device__ __forceinline__ u32 find_or_insert(const DevPool &P, u64 i, u32 level
 	for (; probe < limit; ++probe, s = (s + 1) & mask) {
 		// claim-or-read in one atomic: an empty slot is claimed at once, an
 		// occupied one returns its entry
-		// (relaxed: only the path that reads a resident node needs the acquire
-		// ordering, and it takes it with a fence below)
-		const unsigned long long v = atomicCAS(&P.index[s], kSlotEmpty, claim);
+		const unsigned long long v = cas_acquire(&P.index[s], kSlotEmpty, claim);
 		if (v == kSlotEmpty) {
 			u32 ptr, pad;
 			if (!reserve(P, bucket, nw.n, &ptr, &pad, retries)) {
@@ -1405,13 +1364,7 @@ __device__ __forceinline__ u32 find_or_insert(const DevPool &P, u64 i, u32 level
 			break;
 		}
 		const u32 val = (u32)v;
-		if ((val >> bucket_shift) != bucket)
-			continue;
-		// a final entry may have been published earlier in this launch: the
-		// fence after the read of the entry pairs with the publisher's release
-		// store, so its node's words are visible before they are compared
-		fence_acquire();
-		if (equal_resident(P, val, nw)) {
+		if ((val >> bucket_shift) == bucket && equal_resident(P, val, nw)) {
 			r = val;
 			break;
 		}
