@@ -225,15 +225,20 @@ def leaf_roofline(counters, work, L, n_edits, leaf_ms, hbm, peak_kind):
     item record (24 B: position, base, list offset and length, parent slot),
     per (node, edit) pair its list entry (4 B), the base node's words, every
     old leaf read (8 B), per changed leaf its index slot (8 B) and, when found,
-    the resident leaf (8 B); written: each new leaf candidate (12 B), each
-    unresolved node's todo record (72 B) or each resolved node's parent slot
-    (4 B); and every edit descriptor once (40 B)."""
+    the resident leaf (8 B); per read-only lookup of a level-(L-2) node whose
+    children are all known, its index slot (8 B) and one resident copy (the
+    level's mean candidate words, 4 B each); written: each new leaf candidate
+    (12 B), each unresolved node's todo record (72 B) or each resolved node's
+    parent slot (4 B); and every edit descriptor once (40 B)."""
     nodes, pairs = work["nodes"], work["pairs"]
     cand_leaf = int(counters["items"][L - 1])
     todo = int(counters["candidates"][L - 2]) if L >= 2 else 0
     found = max(0, work["lookups"] - cand_leaf)
+    node_words = float(counters["candidate_words"][L - 2]) / max(1.0, float(counters["candidates"][L - 2])) if L >= 2 \
+        else 0.0
     alg = (24 * nodes + 4 * pairs + 4 * work["base_words"] + 8 * work["old_leaves"] + 8 * work["lookups"] +
-           8 * found + 12 * cand_leaf + 72 * todo + 4 * max(0, nodes - todo) + 40 * n_edits)
+           8 * found + (8 + 4 * node_words) * work["inner_lookups"] + 12 * cand_leaf + 72 * todo +
+           4 * max(0, nodes - todo) + 40 * n_edits)
     achieved = alg / (leaf_ms / 1e3) / 1e9
     return {"bound": "hbm", "kernel": "leaf kernels (k_leafparent_short/_long)", "achieved": achieved, "peak": hbm,
             "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm, "algorithmic_bytes_per_step": float(alg),
