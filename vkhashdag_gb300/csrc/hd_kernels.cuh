@@ -734,6 +734,11 @@ __device__ __forceinline__ void leafparent_short_phase(const DevPool &P, Workspa
 			work.pairs(len);
 			if (b != kNull && b != P.cfg.filled[l])
 				work.base_words(1u + __popc(__ldg(node_addr(P, b)) & 0xFFu));
+			// One edit (nearly every node): its 8 leaves classified together with
+			// each axis's terms shared (classify_children, the same formulas as
+			// classify per leaf), so a leaf costs a mask only when partly covered.
+			const u32 e1 = len == 1u ? W.lists[off] : kNull;
+			const u32 cls8 = len == 1u ? classify_children(W.edits[e1], 2u, pos_x(pos), pos_y(pos), pos_z(pos)) : 0u;
 #pragma unroll 1
 			for (u32 c = 0; c < 8; ++c) { // not unrolled: one copy of the leaf code keeps the i-cache warm
 				u32 cx, cy, cz;
@@ -741,7 +746,21 @@ __device__ __forceinline__ void leafparent_short_phase(const DevPool &P, Workspa
 				const u64 b0 = leaf_bits(P, old[c]);
 				if (old[c] != kNull && old[c] != P.cfg.filled[L - 1])
 					work.old_leaf();
-				const u64 bits = rebuild_leaf(W, off, len, cx, cy, cz, b0);
+				u64 bits;
+				if (len == 1u) {
+					const u32 cls = (cls8 >> (2u * c)) & 3u;
+					const hd_edit_desc &e = W.edits[e1];
+					if (cls == kClsNone)
+						bits = b0;
+					else if (cls == kClsFull)
+						bits = e.op == HD_OP_FILL ? ~0ull : 0ull;
+					else {
+						const u64 m = shape_mask(e, cx << 2, cy << 2, cz << 2);
+						bits = e.op == HD_OP_FILL ? (b0 | m) : (b0 & ~m);
+					}
+				} else {
+					bits = rebuild_leaf(W, off, len, cx, cy, cz, b0);
+				}
 				bool cand;
 				u32 r = leaf_result(P, bits, b0, old[c], &cand);
 				if (cand) {
