@@ -71,72 +71,83 @@ __device__ __forceinline__ u32 descend_to(const DevPool &P, u32 root, int top, i
 	return node;
 }
 
+// One ray of the traversal as a state machine: init() is the prologue, each
+// step() one iteration of the reference's loop (true once the ray is done),
+// finish() the hit record.  trace_core runs them back to back; the persistent
+// kernel below interleaves rays on a lane.  The float operations are the
+// reference's, in its order, whichever way the steps are scheduled.
 // steps: loop iterations; reads: node words fetched (mask words, child pointers, leaf words).
 // Lod: the level-of-detail cut of shader/src/trace.frag:148 and beam.frag:128 --
 // descent stops at a cube whose size times proj_factor is below its entry t plus
-// proj_bias; *scale_out receives the size of the cube the ray stopped in.
+// proj_bias; finish() reports the size of the cube the ray stopped in.
 // Stackless: the parent stack is a ParentRing plus re-descents (same result).
-template <bool Lod, bool Stackless = false>
-__device__ hd_hit trace_core(const DevPool &P, u32 root, float ox, float oy, float oz, float dx, float dy, float dz,
-                             float proj_factor, float proj_bias, u32 *steps, u32 *reads, float *scale_out) {
-	u32 n_steps = 0, n_reads = 0;
-	hd_hit out;
-	out.voxel[0] = out.voxel[1] = out.voxel[2] = 0;
-	out.size = 0;
-	out.level = 0;
-	out.hit = 0;
-	out.t = 0.0f;
-	out.pos[0] = out.pos[1] = out.pos[2] = 0.0f;
-	if (root == kNull)
-		return out;
-	constexpr int kStack = 23;
-	const float eps = __uint_as_float((127u - 23u) << 23);
-	constexpr int kSlots = Stackless ? 1 : kStack;
-	u32 stack[kSlots];
+constexpr int kStack = 23;
+// The stackful form keeps its parent stack outside the struct (a local array
+// of the caller, passed to init and step), so the rest of the state stays in
+// registers.
+template <bool Lod, bool Stackless> struct Ray {
 	ParentRing ring;
-	if (!Stackless) {
+	float o[3], d[3], tc[3], tb[3];
+	float t_min, t_max, h, scale_exp2, pos[3];
+	float proj_factor, proj_bias;
+	u32 octant, parent, child_bits, idx, n_steps, n_reads;
+	int scale;
+
+	__device__ __forceinline__ void init(u32 root, float ox, float oy, float oz, float dx, float dy, float dz,
+	                                     float pf, float pb, u32 *stack) {
+		const float eps = __uint_as_float((127u - 23u) << 23);
+		n_steps = n_reads = 0;
+		proj_factor = pf;
+		proj_bias = pb;
+		ring = ParentRing{};
+		if (!Stackless) {
 #pragma unroll
-		for (int k = 0; k < kSlots; ++k) // every entry holds a node pointer before the first push
-			stack[k] = root;
-	}
-	float o[3] = {ox + 1.0f, oy + 1.0f, oz + 1.0f};
-	float din[3] = {dx, dy, dz}, d[3];
-#pragma unroll
-	for (int a = 0; a < 3; ++a)
-		d[a] = abs_ref(din[a]) > eps ? din[a] : (din[a] >= 0.0f ? eps : -eps);
-	float tc[3], tb[3];
-#pragma unroll
-	for (int a = 0; a < 3; ++a) {
-		tc[a] = __fdiv_rn(1.0f, -abs_ref(d[a]));
-		tb[a] = __fmul_rn(tc[a], o[a]);
-	}
-	u32 octant = 0;
-#pragma unroll
-	for (int a = 0; a < 3; ++a)
-		if (d[a] > 0.0f) {
-			octant ^= 1u << a;
-			tb[a] = __fsub_rn(__fmul_rn(3.0f, tc[a]), tb[a]);
+			for (int k = 0; k < kStack; ++k) // every entry holds a node pointer before the first push
+				stack[k] = root;
 		}
-	float t_min = fmax_ref(fmax_ref(__fsub_rn(__fmul_rn(2.0f, tc[0]), tb[0]), __fsub_rn(__fmul_rn(2.0f, tc[1]), tb[1])),
-	                       __fsub_rn(__fmul_rn(2.0f, tc[2]), tb[2]));
-	float t_max = fmin_ref(fmin_ref(__fsub_rn(tc[0], tb[0]), __fsub_rn(tc[1], tb[1])), __fsub_rn(tc[2], tb[2]));
-	float h = t_max;
-	t_min = fmax_ref(t_min, 0.0f);
-	t_max = fmin_ref(t_max, 1.0f);
-	u32 parent = root, child_bits = 0;
-	float pos[3] = {1.0f, 1.0f, 1.0f};
-	u32 idx = 0;
+		o[0] = ox + 1.0f;
+		o[1] = oy + 1.0f;
+		o[2] = oz + 1.0f;
+		const float din[3] = {dx, dy, dz};
 #pragma unroll
-	for (int a = 0; a < 3; ++a)
-		if (__fsub_rn(__fmul_rn(1.5f, tc[a]), tb[a]) > t_min) {
-			idx ^= 1u << a;
-			pos[a] = 1.5f;
+		for (int a = 0; a < 3; ++a)
+			d[a] = abs_ref(din[a]) > eps ? din[a] : (din[a] >= 0.0f ? eps : -eps);
+#pragma unroll
+		for (int a = 0; a < 3; ++a) {
+			tc[a] = __fdiv_rn(1.0f, -abs_ref(d[a]));
+			tb[a] = __fmul_rn(tc[a], o[a]);
 		}
-	int scale = kStack - 1;
-	float scale_exp2 = 0.5f;
-	const u32 leaf_level = P.cfg.L;
-	const int leaf_scale = kStack - (int)leaf_level;
-	for (int guard = 0; guard < (1 << 20); ++guard) { // a ray crosses at most a few thousand cells
+		octant = 0;
+#pragma unroll
+		for (int a = 0; a < 3; ++a)
+			if (d[a] > 0.0f) {
+				octant ^= 1u << a;
+				tb[a] = __fsub_rn(__fmul_rn(3.0f, tc[a]), tb[a]);
+			}
+		t_min = fmax_ref(fmax_ref(__fsub_rn(__fmul_rn(2.0f, tc[0]), tb[0]), __fsub_rn(__fmul_rn(2.0f, tc[1]), tb[1])),
+		                 __fsub_rn(__fmul_rn(2.0f, tc[2]), tb[2]));
+		t_max = fmin_ref(fmin_ref(__fsub_rn(tc[0], tb[0]), __fsub_rn(tc[1], tb[1])), __fsub_rn(tc[2], tb[2]));
+		h = t_max;
+		t_min = fmax_ref(t_min, 0.0f);
+		t_max = fmin_ref(t_max, 1.0f);
+		parent = root;
+		child_bits = 0;
+		pos[0] = pos[1] = pos[2] = 1.0f;
+		idx = 0;
+#pragma unroll
+		for (int a = 0; a < 3; ++a)
+			if (__fsub_rn(__fmul_rn(1.5f, tc[a]), tb[a]) > t_min) {
+				idx ^= 1u << a;
+				pos[a] = 1.5f;
+			}
+		scale = kStack - 1;
+		scale_exp2 = 0.5f;
+	}
+
+	// One loop iteration (NodePoolTraversal.hpp:151-243); true when the ray stops
+	// (a hit below the leaf scale or at the level-of-detail cut, or it leaves the
+	// root), in which case the state is the one the reference's loop breaks with.
+	__device__ __forceinline__ bool step(const DevPool &P, u32 root, int leaf_scale, u32 *stack) {
 		++n_steps;
 		if (child_bits == 0u) {
 			if (scale > leaf_scale) {
@@ -166,7 +177,7 @@ __device__ hd_hit trace_core(const DevPool &P, u32 root, float ox, float oy, flo
 			for (int a = 0; a < 3; ++a)
 				tcen[a] = __fadd_rn(__fmul_rn(half, tc[a]), tcor[a]);
 			if (scale < leaf_scale || (Lod && __fmul_rn(scale_exp2, proj_factor) < __fadd_rn(tc_max, proj_bias)))
-				break;
+				return true;
 			if (tc_max < h) {
 				if (Stackless)
 					ring.push(scale, parent);
@@ -189,27 +200,27 @@ __device__ hd_hit trace_core(const DevPool &P, u32 root, float ox, float oy, flo
 					pos[a] = __fadd_rn(pos[a], scale_exp2);
 				}
 			child_bits = 0;
-			continue;
+			return false;
 		}
-		u32 step = 0;
+		u32 stp = 0;
 #pragma unroll
 		for (int a = 0; a < 3; ++a)
 			if (tcor[a] <= tc_max) {
-				step ^= 1u << a;
+				stp ^= 1u << a;
 				pos[a] = __fsub_rn(pos[a], scale_exp2);
 			}
 		t_min = tc_max;
-		idx ^= step;
-		if ((idx & step) != 0) {
+		idx ^= stp;
+		if ((idx & stp) != 0) {
 			u32 diff = 0;
 #pragma unroll
 			for (int a = 0; a < 3; ++a)
-				if (step & (1u << a))
+				if (stp & (1u << a))
 					diff |= __float_as_uint(pos[a]) ^ __float_as_uint(__fadd_rn(pos[a], scale_exp2));
 			scale = diff ? 31 - __clz(diff) : -1;
 			if (scale >= kStack || scale < 0) {
 				scale = kStack;
-				break;
+				return true;
 			}
 			scale_exp2 = __uint_as_float((u32)(scale - kStack + 127) << 23);
 			u32 sh[3];
@@ -229,40 +240,78 @@ __device__ hd_hit trace_core(const DevPool &P, u32 root, float ox, float oy, flo
 			h = 0.0f;
 			child_bits = 0;
 		}
+		return false;
 	}
-	const bool hit = scale < kStack && t_min <= t_max;
+
+	// The hit record of a stopped ray (trace.frag:223-246 for the voxel output).
+	__device__ __forceinline__ hd_hit finish(u32 leaf_level) const {
+		hd_hit out;
+		out.voxel[0] = out.voxel[1] = out.voxel[2] = 0;
+		out.size = 0;
+		out.level = 0;
+		const bool hit = scale < kStack && t_min <= t_max;
+		out.hit = hit ? 1u : 0u;
+		out.t = t_min;
+		out.pos[0] = out.pos[1] = out.pos[2] = 0.0f;
+		const u32 voxel_level = leaf_level + 1u;
+		const int voxel_scale = kStack - (int)voxel_level;
+		if (hit) {
+			const u32 size = 1u << (scale - voxel_scale);
+#pragma unroll
+			for (int a = 0; a < 3; ++a) {
+				u32 vp = (__float_as_uint(pos[a]) & 0x7FFFFFu) >> voxel_scale;
+				if (octant & (1u << a))
+					vp = (1u << voxel_level) - size - vp;
+				out.voxel[a] = vp;
+			}
+			out.size = size;
+			out.level = voxel_level - (31u - __clz(size));
+#pragma unroll
+			for (int a = 0; a < 3; ++a) {
+				float p = pos[a];
+				if (octant & (1u << a))
+					p = __fsub_rn(__fsub_rn(3.0f, scale_exp2), p);
+				float q = __fadd_rn(o[a], __fmul_rn(t_min, d[a]));
+				q = fmin_ref(fmax_ref(q, p), __fadd_rn(p, scale_exp2));
+				out.pos[a] = __fsub_rn(q, 1.0f);
+			}
+		}
+		return out;
+	}
+};
+
+// A ray that runs past this many loop iterations stops (a ray crosses at most
+// a few thousand cells).
+constexpr u32 kRaySteps = 1u << 20;
+
+template <bool Lod, bool Stackless = false>
+__device__ hd_hit trace_core(const DevPool &P, u32 root, float ox, float oy, float oz, float dx, float dy, float dz,
+                             float proj_factor, float proj_bias, u32 *steps, u32 *reads, float *scale_out) {
+	if (root == kNull) {
+		hd_hit out;
+		out.voxel[0] = out.voxel[1] = out.voxel[2] = 0;
+		out.size = out.level = out.hit = 0;
+		out.t = 0.0f;
+		out.pos[0] = out.pos[1] = out.pos[2] = 0.0f;
+		if (steps)
+			*steps = 0;
+		if (reads)
+			*reads = 0;
+		return out;
+	}
+	Ray<Lod, Stackless> r;
+	u32 stack[Stackless ? 1 : kStack];
+	r.init(root, ox, oy, oz, dx, dy, dz, proj_factor, proj_bias, stack);
+	const int leaf_scale = kStack - (int)P.cfg.L;
+	while (r.n_steps < kRaySteps && !r.step(P, root, leaf_scale, stack)) {
+	}
 	if (steps)
-		*steps = n_steps;
+		*steps = r.n_steps;
 	if (reads)
-		*reads = n_reads;
+		*reads = r.n_reads;
 	if (scale_out)
-		*scale_out = scale_exp2;
-	out.hit = hit ? 1u : 0u;
-	out.t = t_min;
-	const u32 voxel_level = leaf_level + 1u;
-	const int voxel_scale = kStack - (int)voxel_level;
-	if (hit) {
-		const u32 size = 1u << (scale - voxel_scale);
-#pragma unroll
-		for (int a = 0; a < 3; ++a) {
-			u32 vp = (__float_as_uint(pos[a]) & 0x7FFFFFu) >> voxel_scale;
-			if (octant & (1u << a))
-				vp = (1u << voxel_level) - size - vp;
-			out.voxel[a] = vp;
-		}
-		out.size = size;
-		out.level = voxel_level - (31u - __clz(size));
-#pragma unroll
-		for (int a = 0; a < 3; ++a) {
-			float p = pos[a];
-			if (octant & (1u << a))
-				p = __fsub_rn(__fsub_rn(3.0f, scale_exp2), p);
-			float q = __fadd_rn(o[a], __fmul_rn(t_min, d[a]));
-			q = fmin_ref(fmax_ref(q, p), __fadd_rn(p, scale_exp2));
-			out.pos[a] = __fsub_rn(q, 1.0f);
-		}
-	}
-	return out;
+		*scale_out = r.scale_exp2;
+	return r.finish(P.cfg.L);
 }
 
 __device__ __forceinline__ hd_hit trace_one(const DevPool &P, u32 root, float ox, float oy, float oz, float dx,
