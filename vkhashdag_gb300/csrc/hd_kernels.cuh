@@ -520,8 +520,11 @@ __device__ __forceinline__ u64 apply_edit_leaf(const hd_edit_desc &e, u32 lx, u3
 }
 
 // New bits of one leaf after the edits of a list.  Inlined into the leaf
-// kernel, which runs 4 blocks per SM (64 registers): 13 % faster than an
-// out-of-line call at 3 blocks per SM.
+// kernels: 13 % faster than an out-of-line call.  k_leafparent_short runs 6
+// blocks of 256 per SM (40 registers, the rest spilled to L1): the kernel
+// waits on L2 and gains from resident warps more than it loses to the
+// spills (measured on the 32768^3 batch: 3 blocks 30.1 ms, 4: 26.9, 5: 28.5,
+// 6: 26.5, 7: 27.0, 8: 27.1).
 __device__ __forceinline__ u64 rebuild_leaf(const Workspace &W, u32 off, u32 len, u32 lx, u32 ly, u32 lz, u64 bits) {
 	for (u32 p = 0; p < len; ++p)
 		bits = apply_edit_leaf(W.edits[W.lists[off + p]], lx, ly, lz, bits);
@@ -982,7 +985,7 @@ static __global__ void __launch_bounds__(kBlock, 4) k_leafparent_compact(DevPool
 	                         s_stage[threadIdx.x >> 5]);
 }
 
-static __global__ void __launch_bounds__(kBlock, 4) k_leafparent_short(DevPool P, Workspace W) {
+static __global__ void __launch_bounds__(kBlock, 6) k_leafparent_short(DevPool P, Workspace W) {
 	apply_pass_desc(W);
 	leafparent_short_phase(P, W, (u64)blockIdx.x * blockDim.x, (u64)gridDim.x * blockDim.x);
 }
