@@ -150,6 +150,28 @@ template <bool Identity> __device__ __forceinline__ u32 list_at(const Workspace 
 	return Identity ? p : W.lists[off + p];
 }
 
+// A level-(L-2) item with a single edit stores that edit's index in lst_off
+// instead of the offset of a one-entry list: the leaf kernels (the only
+// readers of level-(L-2) lists) skip a dependent load per node, and the
+// expand kernel writes one list entry less.  Every other item stores the
+// offset of its list.
+__device__ __forceinline__ bool direct_edit(u32 L, u32 level, u32 len) { return level + 2u == L && len == 1u; }
+// Edit p of a level-(L-2) item's list.
+__device__ __forceinline__ u32 leaf_list_at(const Workspace &W, u32 off, u32 len, u32 p) {
+	return len == 1u ? off : W.lists[off + p];
+}
+// Consistency check of a level-(L-2) item's edit list (or direct edit index).
+__device__ __forceinline__ bool leaf_list_ok(Workspace &W, u32 off, u32 len) {
+	if (len == 1u) {
+		if (off >= W.n_edits) {
+			ws_error(W, kErrInternal);
+			return false;
+		}
+		return true;
+	}
+	return list_ok(W, off, len);
+}
+
 __device__ __forceinline__ void child_pos(u64 pos, u32 c, u32 &cx, u32 &cy, u32 &cz) {
 	cx = (pos_x(pos) << 1) | (c & 1u);
 	cy = (pos_y(pos) << 1) | ((c >> 1) & 1u);
@@ -264,7 +286,7 @@ __device__ __forceinline__ void expand_short_phase(const DevPool &P, Workspace &
 					part[c] = cand & (f ? (~0u << cfirst[c]) : 0u); // the kept edits
 					if (ccnt[c]) {
 						++n_emit;
-						n_list += ccnt[c];
+						n_list += direct_edit(L, cl, ccnt[c]) ? 0u : ccnt[c];
 						n_long += ccnt[c] > T ? 1u : 0u;
 					}
 				}
@@ -277,7 +299,7 @@ __device__ __forceinline__ void expand_short_phase(const DevPool &P, Workspace &
 					part[c] = 0;
 					if (ccnt[c]) {
 						++n_emit;
-						n_list += ccnt[c];
+						n_list += direct_edit(L, cl, ccnt[c]) ? 0u : ccnt[c];
 						n_long += ccnt[c] > T ? 1u : 0u;
 					}
 				}
@@ -299,13 +321,19 @@ __device__ __forceinline__ void expand_short_phase(const DevPool &P, Workspace &
 			res[c] = kNull; // overwritten by the child's commit
 			u32 cx, cy, cz;
 			child_pos(pos, c, cx, cy, cz);
-			if (it < W.inner.cap && lo + ccnt[c] <= W.list_cap) {
+			const bool direct = direct_edit(L, cl, ccnt[c]);
+			const u32 n_entries = direct ? 0u : ccnt[c];
+			if (it < W.inner.cap && lo + n_entries <= W.list_cap) {
 				W.inner.pos[it] = pack_pos(cx, cy, cz);
 				W.inner.base[it] = cbase[c];
 				W.inner.parent[it] = (u32)(i * 8u + c);
-				W.inner.lst_off[it] = (u32)lo;
 				W.inner.lst_len[it] = ccnt[c];
-				if (len <= 32u) {
+				if (direct) // the one kept edit: the first set bit of part / position cfirst
+					W.inner.lst_off[it] = len <= 32u ? W.lists[off + (u32)(__ffs(part[c]) - 1)] : W.lists[off + cfirst[c]];
+				else
+					W.inner.lst_off[it] = (u32)lo;
+				if (direct) {
+				} else if (len <= 32u) {
 					u32 k = 0;
 					for (u32 m = part[c]; m; m &= m - 1u)
 						W.lists[lo + k++] = W.lists[off + (u32)(__ffs(m) - 1)];
@@ -323,7 +351,7 @@ __device__ __forceinline__ void expand_short_phase(const DevPool &P, Workspace &
 				ws_error(W, kErrCapacity);
 			}
 			++it;
-			lo += ccnt[c];
+			lo += n_entries;
 		}
 		uint4 *bc = reinterpret_cast<uint4 *>(W.bchild + i * 8u);
 		uint4 *cn = reinterpret_cast<uint4 *>(W.cnew + i * 8u);
@@ -423,8 +451,8 @@ __device__ u32 write_child_list_block(const Workspace &W, u32 off, u32 len, u32 
 
 // Emits one inner child item planned by a block; errors go to the workspace.
 template <bool Identity>
-__device__ void emit_child_block(Workspace &W, u32 cl, u64 child_begin, u32 parent_slot, u32 off, u32 len, u32 shift,
-                                 u32 cx, u32 cy, u32 cz, u32 base, u32 first, u32 cnt, u32 *sm) {
+__device__ void emit_child_block(Workspace &W, u32 L, u32 cl, u64 child_begin, u32 parent_slot, u32 off, u32 len,
+                                 u32 shift, u32 cx, u32 cy, u32 cz, u32 base, u32 first, u32 cnt, u32 *sm) {
 	if (threadIdx.x == 0) {
 		sm[34] = (u32)atomicAdd(&W.ctr[kWsItems + cl], 1ull);
 		const unsigned long long lo = atomicAdd(&W.ctr[kWsList], (unsigned long long)cnt);
@@ -442,7 +470,9 @@ __device__ void emit_child_block(Workspace &W, u32 cl, u64 child_begin, u32 pare
 			W.inner.pos[it] = pack_pos(cx, cy, cz);
 			W.inner.base[it] = base;
 			W.inner.parent[it] = parent_slot;
-			W.inner.lst_off[it] = lo;
+			// a one-edit level-(L-2) item holds the edit's index (written to
+			// the list by this block before the barrier of the last iteration)
+			W.inner.lst_off[it] = direct_edit(L, cl, k) ? W.lists[lo] : lo;
 			W.inner.lst_len[it] = k;
 			if (k > W.long_threshold) {
 				const unsigned long long lg = atomicAdd(&W.ctr[kWsLong + cl], 1ull);
@@ -501,7 +531,8 @@ static __global__ void __launch_bounds__(kLongBlock) k_expand_long(DevPool P, Wo
 			W.cnew[i * 8u + c] = cnt ? kNull : cb;
 		}
 		if (cnt)
-			emit_child_block<false>(W, cl, child_begin, (u32)(i * 8u + c), off, len, shift, cx, cy, cz, cb, cf, cnt, sm);
+			emit_child_block<false>(W, L, cl, child_begin, (u32)(i * 8u + c), off, len, shift, cx, cy, cz, cb, cf, cnt,
+			                        sm);
 	}
 }
 
@@ -527,7 +558,7 @@ __device__ __forceinline__ u64 apply_edit_leaf(const hd_edit_desc &e, u32 lx, u3
 // 6: 26.5, 7: 27.0, 8: 27.1).
 __device__ __forceinline__ u64 rebuild_leaf(const Workspace &W, u32 off, u32 len, u32 lx, u32 ly, u32 lz, u64 bits) {
 	for (u32 p = 0; p < len; ++p)
-		bits = apply_edit_leaf(W.edits[W.lists[off + p]], lx, ly, lz, bits);
+		bits = apply_edit_leaf(W.edits[leaf_list_at(W, off, len, p)], lx, ly, lz, bits);
 	return bits;
 }
 
@@ -727,7 +758,7 @@ __device__ __forceinline__ void leafparent_short_phase(const DevPool &P, Workspa
 			b = W.inner.base[i];
 			pos = W.inner.pos[i];
 		}
-		const bool mine = valid && len <= T && list_ok(W, off, len);
+		const bool mine = valid && len <= T && leaf_list_ok(W, off, len);
 		u32 old[8], res[8];
 		u64 cb[8];
 		u32 cand_mask = 0;
@@ -740,7 +771,7 @@ __device__ __forceinline__ void leafparent_short_phase(const DevPool &P, Workspa
 			// One edit (nearly every node): its 8 leaves classified together with
 			// each axis's terms shared (classify_children, the same formulas as
 			// classify per leaf), so a leaf costs a mask only when partly covered.
-			const u32 e1 = len == 1u ? W.lists[off] : kNull;
+			const u32 e1 = len == 1u ? off : kNull; // a one-edit item holds the edit's index
 			const u32 cls8 = len == 1u ? classify_children(W.edits[e1], 2u, pos_x(pos), pos_y(pos), pos_z(pos)) : 0u;
 #pragma unroll 1
 			for (u32 c = 0; c < 8; ++c) { // not unrolled: one copy of the leaf code keeps the i-cache warm
@@ -864,7 +895,7 @@ __device__ __forceinline__ void leafparent_compact_phase(const DevPool &P, Works
 			b = W.inner.base[i];
 			pos = W.inner.pos[i];
 		}
-		const bool mine = valid && len <= T && list_ok(W, off, len);
+		const bool mine = valid && len <= T && leaf_list_ok(W, off, len);
 		u32 old[8], res[8];
 		u32 defer = 0;
 		// A: leaves without a partly covering edit
@@ -884,7 +915,7 @@ __device__ __forceinline__ void leafparent_compact_phase(const DevPool &P, Works
 				u64 staged = bits;
 				bool partial = false;
 				for (u32 p = 0; p < len; ++p) {
-					const hd_edit_desc &e = W.edits[W.lists[off + p]];
+					const hd_edit_desc &e = W.edits[leaf_list_at(W, off, len, p)];
 					const u32 cls = classify(e, 2u, cx, cy, cz);
 					if (cls == kClsPartial) {
 						partial = true;
@@ -1161,7 +1192,7 @@ __device__ __forceinline__ void root_phase(const DevPool &P, Workspace &W, u32 r
 			W.ctr[kWsRoot] = b;
 		return;
 	}
-	emit_child_block<true>(W, 0, 0, kNull, 0, W.n_edits, L + 1u, 0, 0, 0, b, f, cnt, sm);
+	emit_child_block<true>(W, L, 0, 0, kNull, 0, W.n_edits, L + 1u, 0, 0, 0, b, f, cnt, sm);
 }
 static __global__ void __launch_bounds__(kLongBlock) k_root(DevPool P, Workspace W, u32 root_val, const u32 *root_ptr) {
 	apply_pass_desc(W);
