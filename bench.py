@@ -400,7 +400,7 @@ def run_ours(args):
 
     stream = torch.cuda.Stream(device=local)
     sp = stream.cuda_stream
-    pool = hd.NodePool(cfg, heap_pages=heap_pages, device=local)
+    pool = hd.NodePool(cfg, heap_pages=heap_pages, index_log2=args.index_log2, device=local)
     root0 = pool.edit(hd.NULL, base)
     # launch shape from the autotuner, on the first warm-up batch (the pool ends
     # unchanged); the timed batches are different ones
@@ -1431,6 +1431,8 @@ def main():
     ap.add_argument("--resolution", type=int, default=RES)
     ap.add_argument("--n-edits", type=int, default=N_EDITS)
     ap.add_argument("--heap-pages", type=int, default=1 << 22)
+    ap.add_argument("--index-log2", type=int, default=0,
+                    help="dedup index slots of the batched pool (log2; 0 = one slot per two heap words)")
     ap.add_argument("--per-edit", type=int, default=1024)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--ref-step-seconds", type=float, default=6.0)
