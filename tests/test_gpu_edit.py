@@ -387,3 +387,60 @@ def test_graph_survives_a_rollback(orc, hd):
     assert pool.kernel_launches() - n0 == 3 * cfg.get_node_levels()  # replayed, not recaptured
     ok, _, dig, _ = canonical_of_device(orc, pool, r)
     assert ok and dig == want
+
+
+def test_hinted_device_chain_equals_host_chain(orc, hd):
+    """hd_edit_async_droot_hinted: the root stays on the device, a host copy of
+    each edit sizes the launch as hd_edit does.  A chain of single edits (small
+    passes as one CTA, larger ones as the multi-kernel pass) and one batched
+    call end on the roots hd_edit gives on the same pool, and on the oracle's
+    DAG."""
+    import torch
+    from vkhashdag_gb300 import workloads as W
+    from helpers import canonical_of_device
+    res = 512
+    cfg = W.config_for_resolution(res)
+    pool = hd.NodePool(cfg, heap_pages=1 << 15)
+    base = W.sphere_scene(res, 8, seed=6)
+    root0 = pool.edit(hd.NULL, base)
+    edits = np.ascontiguousarray(W.mixed_batch(res, 48, seed=21, r_max=40, side_max=90))
+    d_edits = torch.from_numpy(edits.view(np.uint8).copy()).cuda()
+    d_root = torch.tensor([root0 - (1 << 32) if root0 >= (1 << 31) else root0], dtype=torch.int32, device="cuda")
+    for k in range(len(edits)):
+        pool.edit_async_droot_hinted(d_root.data_ptr(), d_edits.data_ptr() + 40 * k, edits[k:k + 1],
+                                     d_root.data_ptr(), 0)
+    torch.cuda.synchronize()
+    assert pool.error() == 0
+    dev_chain = int(d_root.item()) & 0xFFFFFFFF
+    host_chain = root0
+    for k in range(len(edits)):
+        host_chain = pool.edit(host_chain, edits[k:k + 1])
+    assert dev_chain == host_chain  # the same pool finds every node again
+    d_root.fill_(root0 - (1 << 32) if root0 >= (1 << 31) else root0)
+    pool.edit_async_droot_hinted(d_root.data_ptr(), d_edits.data_ptr(), edits, d_root.data_ptr(), 0)
+    torch.cuda.synchronize()
+    assert (int(d_root.item()) & 0xFFFFFFFF) == host_chain
+    ref = orc.OraclePool.from_config(cfg)
+    rr = ref.edit(ref.edit(orc.NULL, base), edits)
+    ok, counts, digests, _ = canonical_of_device(orc, pool, host_chain)
+    assert ok and digests == [str(d) for d in ref.canonical(rr)[2]]
+
+
+def test_leaf_work_counters(orc, hd):
+    """hd_edit_last_leaf_work after a batched pass: level-(L-2) nodes equal the
+    pass's item count at that level, (node, edit) pairs at least the nodes,
+    cache hits at most the lookups, and leaf candidates at most the lookups."""
+    from vkhashdag_gb300 import workloads as W
+    res = 1024
+    cfg = W.config_for_resolution(res)
+    L = cfg.get_node_levels()
+    pool = hd.NodePool(cfg, heap_pages=1 << 15)
+    root = pool.edit(hd.NULL, W.sphere_scene(res, 16, seed=4))
+    pool.edit(root, W.mixed_batch(res, 5000, seed=13, r_max=64, side_max=128))
+    w = pool.last_leaf_work()
+    c = pool.last_counters_full()
+    assert w["nodes"] == int(c["items"][L - 2]) > 0
+    assert w["pairs"] >= w["nodes"]
+    assert 0 < w["cache_hits"] <= w["lookups"]
+    assert int(c["items"][L - 1]) <= w["lookups"]  # leaf candidates are the lookups that missed
+    assert w["inner_lookups"] <= w["nodes"]

@@ -381,3 +381,28 @@ def test_oracle_voxel_count_matches_brute_force(orc):
             inside = (d * d).sum(1) <= int(x["r2"])
         want += int(inside.sum())
     assert orc.count_voxel_edits(e, res) == want
+
+
+def test_bench_sequential_check_on_the_cpu(orc):
+    """bench.py's check leg on a small workload: the oracle's own sequential
+    result and a snapshot of another pool holding the same DAG (here: the
+    serial editor's) have equal canonical digests and point occupancy."""
+    import bench
+    from vkhashdag_gb300 import workloads as W
+    res = 256
+    cfg = W.config_for_resolution(res, bottom_bits=16, top_levels=6)
+    base, batches = bench.workload(0, 3, 256, res)
+    q = W.point_queries(res, 1 << 12, seed=7)
+    cpu, ref = bench.sequential_oracle_leg(cfg, base, batches[2], res, 2, 0.05, batches[0], q)
+    assert ref["ok"] and cpu["value"] > 0 and cpu["serial"]["value"] > 0
+    p = orc.OraclePool.from_config(cfg)
+    r = p.edit(p.edit(orc.NULL, base), batches[2])
+    ok, counts, digests = bench.device_canonical(cfg, p.dump(), p.make_filled(), r)
+    assert ok and counts == ref["counts"] and digests == ref["digests"]
+    assert np.array_equal(p.query(r, q), ref["occupancy"])
+    scan = bench.bucket_scan_figures(cfg, p.dump()[0], {"candidates": np.full(cfg.get_node_levels(), 10),
+                                                        "inserted": np.full(cfg.get_node_levels(), 4),
+                                                        "candidate_words": np.full(cfg.get_node_levels(), 60)},
+                                     [cfg.get_node_levels() - 2])
+    (fig,) = scan.values()
+    assert fig["mean_bucket_words"] > 0 and 0 < fig["scan_words_per_candidate"] <= fig["max_bucket_words"]
