@@ -375,14 +375,14 @@ struct Workspace {
 	u32 *todo;         // [inner.cap] level-(L-2) items that still need the claiming probe
 	u32 *todo_parent;  // [inner.cap] their parents' child slots (todo record t: bchild/cnew slot begin(L-2)+t)
 	// Leaf-pattern cache of the leaf kernels: leaf bits -> pointer of the
-	// resident leaf with those bits, 2-way sets of slots (2k, 2k+1), cleared
-	// at the start of every multi-kernel pass (key 0 = empty, value Null =
-	// not yet written).  A pass's changed leaves repeat few patterns (a box
+	// resident leaf with those bits, 2-way sets of slots (2k, 2k+1), a slot
+	// 16 bytes (key, then the pointer's complement), cleared to zero at the
+	// start of every multi-kernel pass (key 0 = empty, stored 0 = pointer not
+	// yet written).  A pass's changed leaves repeat few patterns (a box
 	// face cuts every leaf it crosses the same way), so most of its read-only
 	// leaf lookups are answered from this L2-resident table instead of a
 	// random index slot and a random heap read.  lc_key null: not used.
-	unsigned long long *lc_key; // [lc_mask + 1]
-	u32 *lc_val;                // [lc_mask + 1]
+	unsigned long long *lc_key; // [2 * (lc_mask + 1)]: per slot the key, then ~pointer
 	u32 lc_mask;
 	const hd_edit_desc *edits;
 	u32 n_edits;

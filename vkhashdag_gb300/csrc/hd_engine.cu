@@ -101,8 +101,8 @@ hd_status alloc_leaf_candidates(hd_ws_host &ws, Items &it, uint64_t cap) {
 
 // (Re)allocates the workspace with at least the given capacities; keeps the
 // counters.  Frees the old one first.
-// Slots of the leaf-pattern cache of the multi-kernel pass (12 MB: 8-byte
-// keys and 4-byte pointers, small enough to stay in L2).
+// Slots of the leaf-pattern cache of the multi-kernel pass (16 MB: an 8-byte
+// key and the pointer in 16 bytes per slot, small enough to stay in L2).
 constexpr uint32_t kLeafCacheSlots = 1u << 20;
 
 hd_status ws_reserve(hd_pool *pool, uint64_t inner_cap, uint64_t leaf_cap, uint64_t list_cap, uint32_t edit_cap) {
@@ -126,8 +126,7 @@ hd_status ws_reserve(hd_pool *pool, uint64_t inner_cap, uint64_t leaf_cap, uint6
 	    (s = ws_alloc(ws, &d.leaf_new, leaf_cap)) || (s = ws_alloc(ws, &d.lists, list_cap)) ||
 	    (s = ws_alloc(ws, &d.long_q, inner_cap)) || (s = ws_alloc(ws, &d.todo, inner_cap)) ||
 	    (s = ws_alloc(ws, &d.todo_parent, inner_cap)) ||
-	    (s = ws_alloc(ws, &d.lc_key, (uint64_t)kLeafCacheSlots)) ||
-	    (s = ws_alloc(ws, &d.lc_val, (uint64_t)kLeafCacheSlots)) ||
+	    (s = ws_alloc(ws, &d.lc_key, 2ull * kLeafCacheSlots)) ||
 	    (s = ws_alloc(ws, &d.ctr, (uint64_t)kWsCtrCount)) ||
 	    (s = ws_alloc(ws, &ws.edits, (uint64_t)edit_cap))) {
 		ws_free_all(ws);
@@ -303,8 +302,7 @@ hd_status launch_pass(hd_pool *pool, const hd_edit_desc *d_edits, uint32_t n, ui
 	mark();
 	HD_TRY(cudaMemsetAsync(W.ctr, 0, kWsCtrCount * sizeof(unsigned long long), st));
 	if (W.lc_key) { // the leaf-pattern cache names leaves of this pool state only
-		HD_TRY(cudaMemsetAsync(W.lc_key, 0, (W.lc_mask + 1ull) * sizeof(unsigned long long), st));
-		HD_TRY(cudaMemsetAsync(W.lc_val, 0xFF, (W.lc_mask + 1ull) * sizeof(uint32_t), st));
+		HD_TRY(cudaMemsetAsync(W.lc_key, 0, 2ull * (W.lc_mask + 1ull) * sizeof(unsigned long long), st));
 	}
 	k_root<<<1, kLongBlock, 0, st>>>(P, W, root_val, root_ptr);
 	dbg("root", 0);
