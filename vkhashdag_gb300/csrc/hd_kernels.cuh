@@ -150,18 +150,18 @@ template <bool Identity> __device__ __forceinline__ u32 list_at(const Workspace 
 	return Identity ? p : W.lists[off + p];
 }
 
-// A level-(L-2) item with a single edit stores that edit's index in lst_off
-// instead of the offset of a one-entry list: the leaf kernels (the only
-// readers of level-(L-2) lists) skip a dependent load per node, and the
-// expand kernel writes one list entry less.  Every other item stores the
-// offset of its list.
-__device__ __forceinline__ bool direct_edit(u32 L, u32 level, u32 len) { return level + 2u == L && len == 1u; }
-// Edit p of a level-(L-2) item's list.
-__device__ __forceinline__ u32 leaf_list_at(const Workspace &W, u32 off, u32 len, u32 p) {
+// An item with a single edit stores that edit's index in lst_off instead of
+// the offset of a one-entry list: the kernel that expands it (or rebuilds its
+// leaves) skips a dependent load, and the kernel that emits it writes one
+// list entry less.  Every other item stores the offset of its list.  Lists
+// longer than long_threshold (at least 1) are never direct.
+__device__ __forceinline__ bool direct_edit(u32 len) { return len == 1u; }
+// Edit p of an item's list.
+__device__ __forceinline__ u32 item_list_at(const Workspace &W, u32 off, u32 len, u32 p) {
 	return len == 1u ? off : W.lists[off + p];
 }
-// Consistency check of a level-(L-2) item's edit list (or direct edit index).
-__device__ __forceinline__ bool leaf_list_ok(Workspace &W, u32 off, u32 len) {
+// Consistency check of an item's edit list (or direct edit index).
+__device__ __forceinline__ bool item_list_ok(Workspace &W, u32 off, u32 len) {
 	if (len == 1u) {
 		if (off >= W.n_edits) {
 			ws_error(W, kErrInternal);
@@ -246,7 +246,7 @@ __device__ __forceinline__ void expand_short_phase(const DevPool &P, Workspace &
 			b = W.inner.base[i];
 			pos = W.inner.pos[i];
 		}
-		const bool mine = valid && len <= T && list_ok(W, off, len);
+		const bool mine = valid && len <= T && item_list_ok(W, off, len);
 		u32 cbase[8], cfirst[8], ccnt[8], old[8], part[8];
 		u32 n_emit = 0, n_list = 0, n_long = 0;
 		if (mine) {
@@ -260,7 +260,7 @@ __device__ __forceinline__ void expand_short_phase(const DevPool &P, Workspace &
 				for (u32 c = 0; c < 8; ++c)
 					full[c] = part[c] = 0;
 				for (u32 p = 0; p < len; ++p) {
-					const hd_edit_desc e = W.edits[W.lists[off + p]];
+					const hd_edit_desc e = W.edits[item_list_at(W, off, len, p)];
 					const u32 k = classify_children(e, shift, pos_x(pos), pos_y(pos), pos_z(pos));
 					fills |= (e.op == HD_OP_FILL ? 1u : 0u) << p;
 #pragma unroll
@@ -286,7 +286,7 @@ __device__ __forceinline__ void expand_short_phase(const DevPool &P, Workspace &
 					part[c] = cand & (f ? (~0u << cfirst[c]) : 0u); // the kept edits
 					if (ccnt[c]) {
 						++n_emit;
-						n_list += direct_edit(L, cl, ccnt[c]) ? 0u : ccnt[c];
+						n_list += direct_edit(ccnt[c]) ? 0u : ccnt[c];
 						n_long += ccnt[c] > T ? 1u : 0u;
 					}
 				}
@@ -299,7 +299,7 @@ __device__ __forceinline__ void expand_short_phase(const DevPool &P, Workspace &
 					part[c] = 0;
 					if (ccnt[c]) {
 						++n_emit;
-						n_list += direct_edit(L, cl, ccnt[c]) ? 0u : ccnt[c];
+						n_list += direct_edit(ccnt[c]) ? 0u : ccnt[c];
 						n_long += ccnt[c] > T ? 1u : 0u;
 					}
 				}
@@ -321,7 +321,7 @@ __device__ __forceinline__ void expand_short_phase(const DevPool &P, Workspace &
 			res[c] = kNull; // overwritten by the child's commit
 			u32 cx, cy, cz;
 			child_pos(pos, c, cx, cy, cz);
-			const bool direct = direct_edit(L, cl, ccnt[c]);
+			const bool direct = direct_edit(ccnt[c]);
 			const u32 n_entries = direct ? 0u : ccnt[c];
 			if (it < W.inner.cap && lo + n_entries <= W.list_cap) {
 				W.inner.pos[it] = pack_pos(cx, cy, cz);
@@ -329,14 +329,14 @@ __device__ __forceinline__ void expand_short_phase(const DevPool &P, Workspace &
 				W.inner.parent[it] = (u32)(i * 8u + c);
 				W.inner.lst_len[it] = ccnt[c];
 				if (direct) // the one kept edit: the first set bit of part / position cfirst
-					W.inner.lst_off[it] = len <= 32u ? W.lists[off + (u32)(__ffs(part[c]) - 1)] : W.lists[off + cfirst[c]];
+					W.inner.lst_off[it] = len <= 32u ? item_list_at(W, off, len, (u32)(__ffs(part[c]) - 1)) : W.lists[off + cfirst[c]];
 				else
 					W.inner.lst_off[it] = (u32)lo;
 				if (direct) {
 				} else if (len <= 32u) {
 					u32 k = 0;
 					for (u32 m = part[c]; m; m &= m - 1u)
-						W.lists[lo + k++] = W.lists[off + (u32)(__ffs(m) - 1)];
+						W.lists[lo + k++] = item_list_at(W, off, len, (u32)(__ffs(m) - 1));
 				} else {
 					write_child_list_thread(W, off, len, cfirst[c], shift, cx, cy, cz, W.lists + lo);
 				}
@@ -470,9 +470,9 @@ __device__ void emit_child_block(Workspace &W, u32 L, u32 cl, u64 child_begin, u
 			W.inner.pos[it] = pack_pos(cx, cy, cz);
 			W.inner.base[it] = base;
 			W.inner.parent[it] = parent_slot;
-			// a one-edit level-(L-2) item holds the edit's index (written to
-			// the list by this block before the barrier of the last iteration)
-			W.inner.lst_off[it] = direct_edit(L, cl, k) ? W.lists[lo] : lo;
+			// a one-edit item holds the edit's index (written to the list by
+			// this block before the barrier of the last iteration)
+			W.inner.lst_off[it] = direct_edit(k) ? W.lists[lo] : lo;
 			W.inner.lst_len[it] = k;
 			if (k > W.long_threshold) {
 				const unsigned long long lg = atomicAdd(&W.ctr[kWsLong + cl], 1ull);
@@ -558,7 +558,7 @@ __device__ __forceinline__ u64 apply_edit_leaf(const hd_edit_desc &e, u32 lx, u3
 // 6: 26.5, 7: 27.0, 8: 27.1).
 __device__ __forceinline__ u64 rebuild_leaf(const Workspace &W, u32 off, u32 len, u32 lx, u32 ly, u32 lz, u64 bits) {
 	for (u32 p = 0; p < len; ++p)
-		bits = apply_edit_leaf(W.edits[leaf_list_at(W, off, len, p)], lx, ly, lz, bits);
+		bits = apply_edit_leaf(W.edits[item_list_at(W, off, len, p)], lx, ly, lz, bits);
 	return bits;
 }
 
@@ -762,7 +762,7 @@ __device__ __forceinline__ void leafparent_short_phase(const DevPool &P, Workspa
 			b = W.inner.base[i];
 			pos = W.inner.pos[i];
 		}
-		const bool mine = valid && len <= T && leaf_list_ok(W, off, len);
+		const bool mine = valid && len <= T && item_list_ok(W, off, len);
 		u32 old[8], res[8];
 		u64 cb[8];
 		u32 cand_mask = 0;
@@ -899,7 +899,7 @@ __device__ __forceinline__ void leafparent_compact_phase(const DevPool &P, Works
 			b = W.inner.base[i];
 			pos = W.inner.pos[i];
 		}
-		const bool mine = valid && len <= T && leaf_list_ok(W, off, len);
+		const bool mine = valid && len <= T && item_list_ok(W, off, len);
 		u32 old[8], res[8];
 		u32 defer = 0;
 		// A: leaves without a partly covering edit
@@ -919,7 +919,7 @@ __device__ __forceinline__ void leafparent_compact_phase(const DevPool &P, Works
 				u64 staged = bits;
 				bool partial = false;
 				for (u32 p = 0; p < len; ++p) {
-					const hd_edit_desc &e = W.edits[leaf_list_at(W, off, len, p)];
+					const hd_edit_desc &e = W.edits[item_list_at(W, off, len, p)];
 					const u32 cls = classify(e, 2u, cx, cy, cz);
 					if (cls == kClsPartial) {
 						partial = true;
