@@ -203,13 +203,13 @@ hd_status hd_edit_last_leaf_work(hd_pool *pool, uint64_t *out);
  * (level L-2: a warp) instead of a thread.  Results never depend on them. */
 typedef struct hd_tuning {
 	uint32_t expand_blocks_per_sm;     /* k_expand_short (default 8) */
-	uint32_t leaf_blocks_per_sm;       /* k_leafparent_short (default 12) */
+	uint32_t leaf_blocks_per_sm;       /* k_leafparent_compact / k_leafparent_short (default 12) */
 	uint32_t dedup_blocks_per_sm;      /* k_dedup (default 32) */
 	uint32_t long_blocks_per_sm;       /* k_expand_long / k_leafparent_long (default 4) */
 	uint32_t long_threshold;           /* default 16, at least 1 */
-	uint32_t leaf_compact;             /* level-(L-2) leaves: 0 = thread per node (k_leafparent_short, default),
-	                                      1 = a warp's partly covered leaves compacted onto all its lanes
-	                                      (k_leafparent_compact; measured no faster on the benchmark) */
+	uint32_t leaf_compact;             /* level-(L-2) leaves: 1 = a warp's deferred leaves (partly covered ones)
+	                                      compacted onto all its lanes (k_leafparent_compact, default),
+	                                      0 = thread per node (k_leafparent_short) */
 } hd_tuning;
 hd_status hd_edit_get_tuning(const hd_pool *pool, hd_tuning *out);
 hd_status hd_edit_set_tuning(hd_pool *pool, const hd_tuning *tuning);

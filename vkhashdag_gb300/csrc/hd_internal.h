@@ -28,7 +28,7 @@ struct hd_pool {
 	std::mutex mtx;
 	uint64_t last_items[HD_MAX_LEVELS] = {}, last_cand[HD_MAX_LEVELS] = {}, last_ins[HD_MAX_LEVELS] = {};
 	std::atomic<uint64_t> kernel_launches{0}; // kernels launched by this pool since creation (any thread)
-	hd_tuning tune{8, 12, 32, 4, 16, 0};      // launch shape of the batched pass (the autotuner's pick on the benchmark)
+	hd_tuning tune{8, 12, 32, 4, 16, 1};      // launch shape of the batched pass (the autotuner's pick on the benchmark)
 	// CUDA graph of the multi-kernel pass of hd_edit, valid for one workspace
 	// allocation and launch shape (shape_gen changes with either)
 	uint64_t shape_gen = 0, graph_gen = ~0ull;

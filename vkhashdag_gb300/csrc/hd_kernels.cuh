@@ -852,25 +852,29 @@ __device__ __forceinline__ void leafparent_short_phase(const DevPool &P, Workspa
 	}
 	add_leaf_work(W, st_nodes, work);
 }
-// The same work with the partly covered leaves of a warp's 32 nodes compacted
-// onto all 32 lanes.  Rebuilding a partly covered leaf (its 64-voxel mask
-// under every edit of the list) is the kernel's costly step, and in the
-// thread-per-node form the lanes of a warp reach it for different leaves at
-// different times, so it ran with about half the lanes active.  Here:
-//   A. every lane classifies its node's 8 leaves against the node's edit list
-//      (EditNode of the leaf cell) and settles the leaves that no edit covers
-//      partly (unchanged, or set / cleared by the last full cover); a leaf
-//      that some edit covers partly is deferred, its old bits staged;
+// The same work with the deferred leaves of a warp's 32 nodes compacted onto
+// all 32 lanes.  The 64-voxel mask of a partly covered leaf and its read-only
+// lookup are the costly steps, and in the thread-per-node form the lanes of a
+// warp reach them for different child slots, so they ran with about a third
+// of the lanes active.  Here:
+//   A. every lane classifies its node's 8 leaves at once (classify_children,
+//      one-edit nodes) and settles the leaves the edit leaves untouched or
+//      covers fully; a leaf covered partly (or fully with a resident leaf
+//      under it, or any leaf of a node with several edits) is deferred;
 //   B. the warp's deferred leaves (at most 256) are queued in shared memory
-//      and each lane rebuilds every 32nd of them: the whole edit list applied
-//      to the staged bits in order, exactly as the per-leaf rule does;
-//   C. every lane takes its 8 leaves' bits back and goes on as the
-//      thread-per-node form does (result, read-only lookup, node resolution).
-// The per-leaf rule applied is the same (rebuild_leaf), so the result is too.
+//      and taken 32 at a time, one per lane: rebuilt (the one edit's mask, or
+//      the whole list in order), resolved (unchanged / Null / filled / found
+//      by the read-only lookup), and a new leaf gets its candidate slot;
+//   C. every lane takes its 8 results back and goes on as the thread-per-node
+//      form does (node resolution, todo record, the candidates' parent slots).
+// The per-leaf rules are the thread-per-node form's, so the results are too;
+// only the order of the leaf candidates differs (a node's candidates need not
+// be adjacent: each records its parent slot).
 struct LeafWarpStage {
-	u64 bits[32 * 8];   // lane * 8 + leaf: bits after phase A / B
-	u64 pos[32];        // the lane's node
-	u32 off[32], len[32];
+	u32 res[32 * 8];      // lane * 8 + leaf: the old child, then the leaf's result (a new leaf: its candidate slot)
+	u64 pos[32];          // the lane's node
+	u32 off[32], len[32], cls8[32];
+	u32 cand[32];         // leaves of the lane's node that are new leaves
 	unsigned char q[256]; // deferred leaves: lane << 3 | leaf
 };
 static constexpr int kLeafWarps = kBlock / 32;
@@ -883,6 +887,7 @@ __device__ __forceinline__ void leafparent_compact_phase(const DevPool &P, Works
 	u64 begin, n;
 	level_range(W, L, l, begin, n);
 	const u32 T = W.long_threshold;
+	const u32 fl = P.cfg.filled[L - 1];
 	const u64 stride = tstride;
 	const u32 lane = lane_id();
 	u32 st_nodes = 0;
@@ -900,42 +905,33 @@ __device__ __forceinline__ void leafparent_compact_phase(const DevPool &P, Works
 			pos = W.inner.pos[i];
 		}
 		const bool mine = valid && len <= T && item_list_ok(W, off, len);
-		u32 old[8], res[8];
+		u32 old[8];
 		u32 defer = 0;
-		// A: leaves without a partly covering edit
+		// A: settle what the classification settles, defer the rest
 		if (mine) {
 			base_children(P, l, b, old);
 			st_nodes += 1;
 			work.pairs(len);
 			if (b != kNull && b != P.cfg.filled[l])
 				work.base_words(1u + __popc(__ldg(node_addr(P, b)) & 0xFFu));
-#pragma unroll 1
+			const u32 cls8 = len == 1u ? classify_children(W.edits[off], 2u, pos_x(pos), pos_y(pos), pos_z(pos)) : 0u;
+			const bool fill = len == 1u && W.edits[off].op == HD_OP_FILL;
+#pragma unroll
 			for (u32 c = 0; c < 8; ++c) {
-				u32 cx, cy, cz;
-				child_pos(pos, c, cx, cy, cz);
-				u64 bits = leaf_bits(P, old[c]);
-				if (old[c] != kNull && old[c] != P.cfg.filled[L - 1])
+				const u32 cls = (cls8 >> (2u * c)) & 3u;
+				const bool real = old[c] != kNull && old[c] != fl;
+				if (real)
 					work.old_leaf();
-				u64 staged = bits;
-				bool partial = false;
-				for (u32 p = 0; p < len; ++p) {
-					const hd_edit_desc &e = W.edits[item_list_at(W, off, len, p)];
-					const u32 cls = classify(e, 2u, cx, cy, cz);
-					if (cls == kClsPartial) {
-						partial = true;
-						break;
-					}
-					if (cls == kClsFull)
-						bits = e.op == HD_OP_FILL ? ~0ull : 0ull;
-				}
-				S.bits[lane * 8u + c] = partial ? staged : bits;
-				defer |= (partial ? 1u : 0u) << c;
+				const bool d = len != 1u || cls == kClsPartial || (cls == kClsFull && real);
+				defer |= (d ? 1u : 0u) << c;
+				S.res[lane * 8u + c] = (d || cls == kClsNone) ? old[c] : (fill ? fl : kNull);
 			}
 			S.pos[lane] = pos;
 			S.off[lane] = off;
 			S.len[lane] = len;
+			S.cls8[lane] = cls8;
 		}
-		// B: the warp's deferred leaves on all lanes
+		S.cand[lane] = 0u;
 		const u32 nd = __popc(defer);
 		u32 incl = nd;
 #pragma unroll
@@ -949,54 +945,74 @@ __device__ __forceinline__ void leafparent_compact_phase(const DevPool &P, Works
 		for (u32 m = defer; m; m &= m - 1u)
 			S.q[qpos++] = (unsigned char)((lane << 3) | (u32)(__ffs(m) - 1));
 		__syncwarp();
-		for (u32 j = lane; j < total; j += 32u) {
-			const u32 e = S.q[j], src = e >> 3, c = e & 7u;
-			u32 cx, cy, cz;
-			child_pos(S.pos[src], c, cx, cy, cz);
-			S.bits[e] = rebuild_leaf(W, S.off[src], S.len[src], cx, cy, cz, S.bits[e]);
-		}
-		__syncwarp();
-		// C: results, read-only lookups, node resolution
-		u64 cb[8];
-		u32 cand_mask = 0;
-		if (mine) {
-#pragma unroll 1
-			for (u32 c = 0; c < 8; ++c) {
-				const u64 b0 = leaf_bits(P, old[c]);
-				const u64 bits = S.bits[lane * 8u + c];
+		// B: the deferred leaves, one per lane
+		for (u32 j0 = 0; j0 < total; j0 += 32u) {
+			const u32 j = j0 + lane;
+			u32 e = 0;
+			u64 nb = 0;
+			bool fresh = false;
+			if (j < total) {
+				e = S.q[j];
+				const u32 src = e >> 3, c = e & 7u;
+				const u32 oldc = S.res[e], sl = S.len[src], so = S.off[src];
+				u32 cx, cy, cz;
+				child_pos(S.pos[src], c, cx, cy, cz);
+				const u64 b0 = leaf_bits(P, oldc);
+				u64 bits;
+				if (sl == 1u) {
+					const hd_edit_desc &ed = W.edits[so];
+					if (((S.cls8[src] >> (2u * c)) & 3u) == kClsFull) {
+						bits = ed.op == HD_OP_FILL ? ~0ull : 0ull;
+					} else {
+						const u64 m = shape_mask(ed, cx << 2, cy << 2, cz << 2);
+						bits = ed.op == HD_OP_FILL ? (b0 | m) : (b0 & ~m);
+					}
+				} else {
+					bits = rebuild_leaf(W, so, sl, cx, cy, cz, b0);
+				}
 				bool cand;
-				u32 r = leaf_result(P, bits, b0, old[c], &cand);
+				u32 r = leaf_result(P, bits, b0, oldc, &cand);
 				if (cand) {
 					r = lookup_leaf_cached(P, W, bits, work);
 					work.lookup();
 					if (r == kNull) {
-						cb[c] = bits;
-						cand_mask |= 1u << c;
+						fresh = true;
+						nb = bits;
 					}
 				}
-				res[c] = r;
+				S.res[e] = r;
+			}
+			// a new leaf takes its candidate slot now; its node's lane writes the parent slot
+			const u64 ci = warp_reserve(&W.ctr[kWsItems + L - 1], fresh ? 1u : 0u);
+			if (fresh) {
+				const bool fits = ci < W.leaf.cap && ci < (u64)kNull;
+				if (fits)
+					W.leaf_new[ci] = nb;
+				else
+					ws_error(W, kErrCapacity);
+				S.res[e] = fits ? (u32)ci : kNull;
+				atomicOr(&S.cand[e >> 3], 1u << (e & 7u));
 			}
 		}
-		__syncwarp(); // the stage is rewritten by the next iteration
+		__syncwarp();
+		// C: the lane's own node
+		u32 res[8];
+#pragma unroll
+		for (u32 c = 0; c < 8; ++c)
+			res[c] = S.res[lane * 8u + c];
+		const u32 cand_mask = mine ? S.cand[lane] : 0u;
+		__syncwarp(); // every lane has read the stage before the next iteration rewrites it
 		u32 done = kNull;
-		const bool resolved = mine && !cand_mask && resolve_node(P, l, b, old, res, &done, work);
-		const u64 c0 = warp_reserve(&W.ctr[kWsItems + L - 1], __popc(cand_mask));
+		const bool resolved = mine && !cand_mask && resolve_node(P, l, b, old, res, &done, work); // no dedup round trip
 		const u64 tq = warp_reserve(&W.ctr[kWsTodo], (mine && !resolved) ? 1u : 0u);
 		if (!mine)
 			continue;
 		const u64 ri = begin + tq;
-		u64 ci = c0;
-#pragma unroll 1
-		for (u32 c = 0; c < 8; ++c) {
-			if (!((cand_mask >> c) & 1u))
-				continue;
-			if (ci < W.leaf.cap) {
-				W.leaf_new[ci] = cb[c];
-				W.leaf.parent[ci] = (u32)(ri * 8u + c);
-			} else {
-				ws_error(W, kErrCapacity);
-			}
-			++ci;
+		for (u32 m = cand_mask; m; m &= m - 1u) {
+			const u32 c = (u32)(__ffs(m) - 1);
+			if (res[c] != kNull)
+				W.leaf.parent[res[c]] = (u32)(ri * 8u + c);
+			res[c] = kNull; // written by the leaf dedup launch
 		}
 		if (resolved) {
 			hand_to_parent(W, i, done);
