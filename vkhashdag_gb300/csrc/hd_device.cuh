@@ -374,6 +374,7 @@ struct Workspace {
 	u32 *long_q;       // per inner level: items with long edit lists (same index space as inner)
 	u32 *todo;         // [inner.cap] level-(L-2) items that still need the claiming probe
 	u32 *todo_parent;  // [inner.cap] their parents' child slots (todo record t: bchild/cnew slot begin(L-2)+t)
+	u32 *leaf_cls;     // [inner.cap] one-edit level-(L-2) items: their 8 leaves' classes | fill << 16 (leaf_classes)
 	// Leaf-pattern cache of the leaf kernels: leaf bits -> pointer of the
 	// resident leaf with those bits, 2-way sets of slots (2k, 2k+1), a slot
 	// 16 bytes (key, then the pointer's complement), cleared to zero at the

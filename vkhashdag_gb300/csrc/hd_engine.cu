@@ -125,7 +125,7 @@ hd_status ws_reserve(hd_pool *pool, uint64_t inner_cap, uint64_t leaf_cap, uint6
 	    (s = ws_alloc(ws, &d.bchild, inner_cap * 8)) || (s = ws_alloc(ws, &d.cnew, inner_cap * 8)) ||
 	    (s = ws_alloc(ws, &d.leaf_new, leaf_cap)) || (s = ws_alloc(ws, &d.lists, list_cap)) ||
 	    (s = ws_alloc(ws, &d.long_q, inner_cap)) || (s = ws_alloc(ws, &d.todo, inner_cap)) ||
-	    (s = ws_alloc(ws, &d.todo_parent, inner_cap)) ||
+	    (s = ws_alloc(ws, &d.todo_parent, inner_cap)) || (s = ws_alloc(ws, &d.leaf_cls, inner_cap)) ||
 	    (s = ws_alloc(ws, &d.lc_key, 2ull * kLeafCacheSlots)) ||
 	    (s = ws_alloc(ws, &d.ctr, (uint64_t)kWsCtrCount)) ||
 	    (s = ws_alloc(ws, &ws.edits, (uint64_t)edit_cap))) {

@@ -172,6 +172,15 @@ __device__ __forceinline__ bool item_list_ok(Workspace &W, u32 off, u32 len) {
 	return list_ok(W, off, len);
 }
 
+// The classes of a level-(L-2) node's 8 leaves under its one edit
+// (classify_children at leaf size, 2 bits per leaf) and the edit's fill bit
+// at bit 16: written by the kernel that emits the item, read by the
+// compacted leaf kernel, which then needs neither the classification nor the
+// edit record for the leaves it settles.
+__device__ __forceinline__ u32 leaf_classes(const hd_edit_desc &e, u32 x, u32 y, u32 z) {
+	return classify_children(e, 2u, x, y, z) | (e.op == HD_OP_FILL ? 1u << 16 : 0u);
+}
+
 __device__ __forceinline__ void child_pos(u64 pos, u32 c, u32 &cx, u32 &cy, u32 &cz) {
 	cx = (pos_x(pos) << 1) | (c & 1u);
 	cy = (pos_y(pos) << 1) | ((c >> 1) & 1u);
@@ -328,10 +337,14 @@ __device__ __forceinline__ void expand_short_phase(const DevPool &P, Workspace &
 				W.inner.base[it] = cbase[c];
 				W.inner.parent[it] = (u32)(i * 8u + c);
 				W.inner.lst_len[it] = ccnt[c];
-				if (direct) // the one kept edit: the first set bit of part / position cfirst
-					W.inner.lst_off[it] = len <= 32u ? item_list_at(W, off, len, (u32)(__ffs(part[c]) - 1)) : W.lists[off + cfirst[c]];
-				else
+				if (direct) { // the one kept edit: the first set bit of part / position cfirst
+					const u32 id = len <= 32u ? item_list_at(W, off, len, (u32)(__ffs(part[c]) - 1)) : W.lists[off + cfirst[c]];
+					W.inner.lst_off[it] = id;
+					if (cl + 2u == L)
+						W.leaf_cls[it] = leaf_classes(W.edits[id], cx, cy, cz);
+				} else {
 					W.inner.lst_off[it] = (u32)lo;
+				}
 				if (direct) {
 				} else if (len <= 32u) {
 					u32 k = 0;
@@ -473,6 +486,8 @@ __device__ void emit_child_block(Workspace &W, u32 L, u32 cl, u64 child_begin, u
 			// a one-edit item holds the edit's index (written to the list by
 			// this block before the barrier of the last iteration)
 			W.inner.lst_off[it] = direct_edit(k) ? W.lists[lo] : lo;
+			if (direct_edit(k) && cl + 2u == L)
+				W.leaf_cls[it] = leaf_classes(W.edits[W.lists[lo]], cx, cy, cz);
 			W.inner.lst_len[it] = k;
 			if (k > W.long_threshold) {
 				const unsigned long long lg = atomicAdd(&W.ctr[kWsLong + cl], 1ull);
@@ -914,8 +929,9 @@ __device__ __forceinline__ void leafparent_compact_phase(const DevPool &P, Works
 			work.pairs(len);
 			if (b != kNull && b != P.cfg.filled[l])
 				work.base_words(1u + __popc(__ldg(node_addr(P, b)) & 0xFFu));
-			const u32 cls8 = len == 1u ? classify_children(W.edits[off], 2u, pos_x(pos), pos_y(pos), pos_z(pos)) : 0u;
-			const bool fill = len == 1u && W.edits[off].op == HD_OP_FILL;
+			const u32 lc = len == 1u ? W.leaf_cls[i] : 0u; // written by the kernel that emitted the item
+			const u32 cls8 = lc & 0xFFFFu;
+			const bool fill = (lc >> 16) & 1u;
 #pragma unroll
 			for (u32 c = 0; c < 8; ++c) {
 				const u32 cls = (cls8 >> (2u * c)) & 3u;
