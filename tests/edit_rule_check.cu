@@ -10,8 +10,9 @@
 //     leaf) against a per-voxel brute force: the box mask's per-axis runs and
 //     spread multiplies for all 16^3 combinations of axis masks and for every run
 //     of a small coordinate range; boxes (empty, thin, large) and spheres sampled
-//     around their surfaces, in the 32-bit paths (centre and bounds below 2^15,
-//     r2 <= 2^30) and the 64-bit ones (coordinates up to 2^21, r2 above 2^30);
+//     around their surfaces, in the 32-bit paths (centre and bounds below 2^15;
+//     the sign-bit mask for r2 <= 2^29, the compare mask up to 2^30) and the
+//     64-bit ones (coordinates up to 2^21, r2 above 2^30);
 //   * the expand kernel's classify_children (the 8 children of a node against
 //     one edit, each axis's terms shared by the children on the same half)
 //     against classify of each child, at every cell size from 4 to 2^20 voxels.
@@ -148,8 +149,8 @@ static void check_spheres(u32 world, double max_r, int n_edits, int leaves_per_e
 			e.p0[a] = below(world);
 		const double r = std::exp(unit() * std::log(max_r));
 		e.r2 = (u64)(r * r) + below(3);
-		if (r2_exact_edges && t % 4 == 0)
-			e.r2 = (1ull << 30) + (u64)(t / 4 % 3) - 1; // 2^30 - 1, 2^30, 2^30 + 1
+		if (r2_exact_edges && t % 4 == 0) // 2^30 - 1, 2^30, 2^30 + 1, 2^29 - 1, 2^29, 2^29 + 1
+			e.r2 = (1ull << (t / 4 % 2 ? 29 : 30)) + (u64)(t / 8 % 3) - 1;
 		const double rr = std::sqrt((double)e.r2);
 		for (int s = 0; s < leaves_per_edit; ++s) {
 			double d[3], n = 0;
@@ -265,7 +266,8 @@ int main(int argc, char **argv) {
 	check_boxes(1u << 15, 2048, 4000, 64);
 	check_boxes(1u << 21, 1u << 20, 2000, 64);
 	check_spheres(1u << 15, 16384.0, 4000, 64, false); // 32-bit classify and mask
-	check_spheres(1u << 15, 32768.0, 1000, 64, true);  // r2 around 2^30
+	check_spheres(1u << 15, 32768.0, 1000, 64, true);  // r2 around 2^29 and 2^30
+	check_spheres(1u << 15, 24000.0, 2000, 64, false); // r2 up to 2^29 and a little above
 	check_spheres(1u << 21, 32768.0, 2000, 64, true);  // 64-bit classify, 32-bit mask
 	check_spheres(1u << 21, 1u << 20, 2000, 64, false); // 64-bit classify and mask
 	check_children_all(15, 16384.0, 4000);   // 32-bit child classification

@@ -282,6 +282,15 @@ __host__ __device__ __forceinline__ u64 spread_z(u32 m) {
 	return ((u64)((m & 1u) | ((m & 2u) << 3)) | ((u64)(m & 4u) << 30) | ((u64)(m & 8u) << 33)) * 0x0F0F0F0Full;
 }
 
+// acc shifted left by one with the sign bit of t appended (a funnel shift).
+__host__ __device__ __forceinline__ u32 push_sign(u32 acc, u32 t) {
+#ifdef __CUDA_ARCH__
+	return __funnelshift_l(t, acc, 1);
+#else
+	return (acc << 1) | (t >> 31);
+#endif
+}
+
 __host__ __device__ __forceinline__ u64 shape_mask(const hd_edit_desc &e, u32 ox, u32 oy, u32 oz) {
 	// The leaf's voxels are 16 x-rows of 4 (one per (y,z) offset pair).  Row
 	// (yo,zo) holds voxel indices base+{0,1,8,9} for x offsets 0..3, with
@@ -293,6 +302,31 @@ __host__ __device__ __forceinline__ u64 shape_mask(const hd_edit_desc &e, u32 ox
 	// A leaf that the sphere only partially covers lies within r+4 of the centre
 	// on every axis, so for r2 <= 2^30 every square and every sum of three fits
 	// in 32 bits (3 * 32772^2 < 2^32); the wider form handles the rest.
+	if (e.r2 <= (1ull << 29)) {
+		// Here every square is below 2^29 + 2^18 and a voxel's
+		// t = dx^2 + dy^2 + dz^2 - r2 - 1 lies in (-2^30, 2^31): it is negative
+		// exactly when the voxel is inside, so its sign bit is the voxel's bit.
+		// One three-input add per voxel, and the sign bits shifted into each
+		// half of the mask in voxel order (index 63 first).
+		u32 sx[4], sy[4], sz[4];
+		const int cx = (int)e.p0[0], cy = (int)e.p0[1], cz = (int)e.p0[2];
+		const u32 r2m = (u32)e.r2 + 1u;
+#pragma unroll
+		for (u32 k = 0; k < 4; ++k) {
+			const int dx = (int)(ox + k) - cx, dy = (int)(oy + k) - cy, dz = (int)(oz + k) - cz;
+			sx[k] = (u32)(dx * dx);
+			sy[k] = (u32)(dy * dy);
+			sz[k] = (u32)(dz * dz) - r2m;
+		}
+		u32 hi = 0, lo = 0;
+#pragma unroll
+		for (int i = 63; i >= 32; --i)
+			hi = push_sign(hi, sx[((i >> 2) & 2) | (i & 1)] + sy[((i >> 3) & 2) | ((i >> 1) & 1)] + sz[((i >> 4) & 2) | ((i >> 2) & 1)]);
+#pragma unroll
+		for (int i = 31; i >= 0; --i)
+			lo = push_sign(lo, sx[((i >> 2) & 2) | (i & 1)] + sy[((i >> 3) & 2) | ((i >> 1) & 1)] + sz[((i >> 4) & 2) | ((i >> 2) & 1)]);
+		return (u64)lo | ((u64)hi << 32);
+	}
 	if (e.r2 <= (1ull << 30)) {
 		u32 dx2[4], dy2[4], dz2[4];
 		const int cx = (int)e.p0[0], cy = (int)e.p0[1], cz = (int)e.p0[2];
