@@ -220,10 +220,11 @@ def replica_seed_of(rank, batch):
 
 
 def leaf_roofline(counters, work, L, n_edits, leaf_ms, hbm, peak_kind):
-    """Roofline of the level-(L-2) leaf kernels (k_leafparent_short/_long) from
-    the pass's own work counters.  Algorithmic bytes: per level-(L-2) node its
-    item record (24 B: position, base, list offset and length, parent slot),
-    per (node, edit) pair its list entry (4 B), the base node's words, every
+    """Roofline of the level-(L-2) leaf kernels (k_leafparent_compact/_long)
+    from the pass's own work counters.  Algorithmic bytes: per level-(L-2) node
+    its item record (24 B: position, base, list offset and length, parent
+    slot), per (node, edit) pair 4 B (a one-edit node's leaf classes, else the
+    pair's list entry), the base node's words, every
     old leaf read (8 B), per changed leaf its index slot (8 B) and, when found,
     the resident leaf (8 B); per read-only lookup of a level-(L-2) node whose
     children are all known, its index slot (8 B) and one resident copy (the
@@ -240,13 +241,14 @@ def leaf_roofline(counters, work, L, n_edits, leaf_ms, hbm, peak_kind):
            8 * found + (8 + 4 * node_words) * work["inner_lookups"] + 12 * cand_leaf + 72 * todo +
            4 * max(0, nodes - todo) + 40 * n_edits)
     achieved = alg / (leaf_ms / 1e3) / 1e9
-    return {"bound": "hbm", "kernel": "leaf kernels (k_leafparent_short/_long)", "achieved": achieved, "peak": hbm,
+    return {"bound": "hbm", "kernel": "leaf kernels (k_leafparent_compact/_long)", "achieved": achieved, "peak": hbm,
             "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / hbm, "algorithmic_bytes_per_step": float(alg),
             "leaf_ms_per_step": leaf_ms, "work_last_step": work,
             "leaf_edit_evaluations_per_s": 8.0 * pairs / (leaf_ms / 1e3),
             "issue_efficiency": _profile_value("leaf_issue.json", "active_lanes_per_inst", 1.0 / 32.0),
-            "note": "integer voxel-mask work with divergent lanes, not DRAM bound; issue_efficiency = active lanes "
-                    "per issued instruction / 32 from the committed ncu capture"}
+            "note": "integer voxel-mask work (a warp's partly covered leaves compacted onto its lanes), not DRAM "
+                    "bound; issue_efficiency = active lanes per issued instruction / 32 from the committed ncu "
+                    "capture"}
 
 
 def batched_config(cfg, res, n_edits, ve_per_step, world):
