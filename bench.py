@@ -347,17 +347,25 @@ def run_reference(args):
     L = cfg.get_node_levels()
     threads = os.cpu_count() or 1
     mtl = max(0, L - 4)
+    t_start = time.perf_counter()
+
+    def phase(what):
+        print(f"[reference] {what}: {time.perf_counter() - t_start:.1f} s", file=sys.stderr, flush=True)
+
     base, batches = workload(0, args.warmup + args.steps + 1, args.n_edits, args.resolution)
     serial_batch = batches.pop()  # edits no step applies: the serial editor's sample
     ve_timed = [oracle.count_voxel_edits(b, args.resolution) for b in batches[args.warmup:]]
+    phase("workload and voxel-edit counts")
     pool = oracle.OraclePool.from_config(cfg)
     t0 = time.perf_counter()
     root0 = pool.threaded_edit(oracle.NULL, base, mtl, threads)
     t_base = time.perf_counter() - t0
+    phase(f"seeded scene on {threads} threads")
     rates, samples = [], []
     for k in range(args.warmup + args.steps):
         rate, n_done, t_used, _ = cpu_sample_rate(pool, root0, batches[k], args.resolution, args.ref_step_seconds,
                                                  threads, mtl)
+        phase(f"step {k}: {n_done} edits in {t_used:.1f} s")
         if k >= args.warmup:
             rates.append(rate)
             samples.append((n_done, t_used))
@@ -365,6 +373,7 @@ def run_reference(args):
     n_done = sum(s[0] for s in samples)
     t_all = sum(s[1] for s in samples)
     serial = serial_baseline(pool, root0, serial_batch, args.resolution, args.ref_step_seconds)
+    phase("serial sample")
     sample = (f"first {n_done // max(1, len(samples))} edits (on average) of each of {args.steps} batches of "
               f"{args.n_edits}, applied one by one by the threaded CPU editor to the seeded {args.resolution}^3 scene "
               f"(scene build {t_base:.1f} s untimed)")
