@@ -1960,11 +1960,15 @@ uint32_t orc_hash_leaf(uint32_t w0, uint32_t w1) { return orc::murmur_leaf(w0, w
 // sphere is counted row by row: for every (y, z) row the x extent is
 // cx +- isqrt(r2 - dy^2 - dz^2), clipped to the grid; spheres that lie inside
 // the grid depend only on r2 and are counted once per r2.
+// floor(sqrt(v)): a double estimate corrected in integers (no long double:
+// on aarch64 that is a software quad-precision type, about 30x slower here).
 static uint64_t isqrt_u64(uint64_t v) {
-	uint64_t r = (uint64_t)std::sqrt((long double)v);
+	uint64_t r = (uint64_t)std::sqrt((double)v);
+	if (r > 0xFFFFFFFFull)
+		r = 0xFFFFFFFFull;
 	while (r * r > v)
 		--r;
-	while ((r + 1) * (r + 1) <= v)
+	while (r < 0xFFFFFFFFull && (r + 1) * (r + 1) <= v)
 		++r;
 	return r;
 }

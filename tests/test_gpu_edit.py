@@ -40,13 +40,13 @@ def test_batched_pass_matches_reference(golden, orc, hd, name):
 
 
 @pytest.mark.parametrize("name", ["scene1024", "mixed512", "terrain256", "full_then_dig"])
-def test_batched_pass_compacted_leaves_matches_reference(golden, orc, hd, name):
-    """The same batched pass with the level-(L-2) leaves that an edit covers
-    partly compacted onto whole warps (k_leafparent_compact) instead of
-    rebuilt thread per node."""
+def test_batched_pass_thread_per_node_leaves_matches_reference(golden, orc, hd, name):
+    """The same batched pass with the level-(L-2) leaves rebuilt thread per
+    node (k_leafparent_short) instead of the default form, whose partly
+    covered leaves are compacted onto whole warps (k_leafparent_compact)."""
     s = scenario(golden, name)
     pool = pool_for(hd, s)
-    pool.set_tuning(leaf_compact=1)
+    pool.set_tuning(leaf_compact=0)
     root = pool.edit(hd.NULL, scenario_edits(s))
     check_against_golden(orc, pool, root, s)
 

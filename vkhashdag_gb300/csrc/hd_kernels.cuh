@@ -672,45 +672,18 @@ __device__ __forceinline__ u32 lookup_leaf_cached(const DevPool &P, const Worksp
 	return r;
 }
 
-// Read-only lookup of an inner node (packed words) at level l among the resident nodes.
-__device__ __forceinline__ u32 lookup_inner(const DevPool &P, u32 l, const u32 *w, u32 n, u32 h) {
-	const u32 bucket = P.cfg.bucket_base[l] + ((P.cfg.hasher == HD_HASHER_ZERO ? 0u : h) & ((1u << P.cfg.bucket_bits[l]) - 1u));
-	const u32 bucket_shift = P.cfg.wbpp + P.cfg.pbpb;
-	const u64 mask = P.index_mask;
-	const unsigned long long tag = h & 0x7FFFFFFFu;
-	u64 s = index_start(h, l, mask);
-	for (u32 probe = 0; probe < 32u; ++probe, s = (s + 1) & mask) {
-		const unsigned long long v = __ldg(&P.index[s]);
-		if (v == kSlotEmpty)
-			return kNull;
-		if ((v >> 63) || ((v >> 32) & 0x7FFFFFFFull) != tag)
-			continue;
-		const u32 val = (u32)v;
-		if ((val >> bucket_shift) != bucket)
-			continue;
-		const u32 *p = node_addr(P, val);
-		bool eq = true;
-		for (u32 k = 0; k < n; ++k)
-			eq = eq && p[k] == w[k];
-		if (eq)
-			return val;
-	}
-	return kNull;
-}
-
 // A level-(L-2) node whose 8 children are all known: unchanged, empty, or an
 // existing node found read-only.  Returns false if it needs the dedup launch.
+// The node's words (mask, then the non-null children in child order) are
+// hashed and compared straight from res[], with no word array to index.
 __device__ __forceinline__ bool resolve_node(const DevPool &P, u32 l, u32 base, const u32 old[8], const u32 res[8],
                                              u32 *out, LeafWork &work) {
 	bool unchanged = true;
-	u32 mask = 0, w[9], k = 1;
+	u32 mask = 0;
 #pragma unroll
 	for (int c = 0; c < 8; ++c) {
 		unchanged = unchanged && res[c] == old[c];
-		if (res[c] != kNull) {
-			mask |= 1u << c;
-			w[k++] = res[c];
-		}
+		mask |= (res[c] != kNull ? 1u : 0u) << c;
 	}
 	if (unchanged) {
 		*out = base;
@@ -720,12 +693,44 @@ __device__ __forceinline__ bool resolve_node(const DevPool &P, u32 l, u32 base, 
 		*out = kNull;
 		return true;
 	}
-	w[0] = mask;
 	Murmur mm;
-	for (u32 q = 0; q < k; ++q)
-		mm.add(w[q]);
+	mm.add(mask);
+#pragma unroll
+	for (int c = 0; c < 8; ++c)
+		if (res[c] != kNull)
+			mm.add(res[c]);
+	const u32 n = 1u + __popc(mask);
+	const u32 h = mm.finish(n);
 	work.inner();
-	const u32 r = lookup_inner(P, l, w, k, mm.finish(k));
+	const u32 bucket = P.cfg.bucket_base[l] + ((P.cfg.hasher == HD_HASHER_ZERO ? 0u : h) & ((1u << P.cfg.bucket_bits[l]) - 1u));
+	const u32 bucket_shift = P.cfg.wbpp + P.cfg.pbpb;
+	const u64 imask = P.index_mask;
+	const unsigned long long tag = h & 0x7FFFFFFFu;
+	u64 s = index_start(h, l, imask);
+	u32 r = kNull;
+	for (u32 probe = 0; probe < 32u; ++probe, s = (s + 1) & imask) {
+		const unsigned long long v = __ldg(&P.index[s]);
+		if (v == kSlotEmpty)
+			break;
+		if ((v >> 63) || ((v >> 32) & 0x7FFFFFFFull) != tag)
+			continue;
+		const u32 val = (u32)v;
+		if ((val >> bucket_shift) != bucket)
+			continue;
+		const u32 *p = node_addr(P, val);
+		bool eq = p[0] == mask;
+		u32 j = 1;
+#pragma unroll
+		for (int c = 0; c < 8; ++c)
+			if (res[c] != kNull) {
+				eq = eq && p[j] == res[c];
+				++j;
+			}
+		if (eq) {
+			r = val;
+			break;
+		}
+	}
 	*out = r;
 	return r != kNull;
 }
@@ -887,6 +892,7 @@ __device__ __forceinline__ void leafparent_short_phase(const DevPool &P, Workspa
 // be adjacent: each records its parent slot).
 struct LeafWarpStage {
 	u32 res[32 * 8];      // lane * 8 + leaf: the old child, then the leaf's result (a new leaf: its candidate slot)
+	u32 old[32 * 8];      // lane * 8 + leaf: the node's old children (kept here, not in registers, across B)
 	u64 pos[32];          // the lane's node
 	u32 off[32], len[32], cls8[32];
 	u32 cand[32];         // leaves of the lane's node that are new leaves
@@ -946,6 +952,9 @@ __device__ __forceinline__ void leafparent_compact_phase(const DevPool &P, Works
 			S.off[lane] = off;
 			S.len[lane] = len;
 			S.cls8[lane] = cls8;
+#pragma unroll
+			for (u32 c = 0; c < 8; ++c)
+				S.old[lane * 8u + c] = old[c];
 		}
 		S.cand[lane] = 0u;
 		const u32 nd = __popc(defer);
@@ -1014,8 +1023,10 @@ __device__ __forceinline__ void leafparent_compact_phase(const DevPool &P, Works
 		// C: the lane's own node
 		u32 res[8];
 #pragma unroll
-		for (u32 c = 0; c < 8; ++c)
+		for (u32 c = 0; c < 8; ++c) {
 			res[c] = S.res[lane * 8u + c];
+			old[c] = S.old[lane * 8u + c];
+		}
 		const u32 cand_mask = mine ? S.cand[lane] : 0u;
 		__syncwarp(); // every lane has read the stage before the next iteration rewrites it
 		u32 done = kNull;
