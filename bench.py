@@ -1272,9 +1272,16 @@ def run_serving(args):
 # ---------------------------------------------------------------------- garbage collection
 def _gc_workload(hd, W, res, n_batches, n_edits, device, heap_pages):
     """Seeded scene plus n_batches batches applied one after another (no
-    rollback): every batch leaves the nodes it replaced behind."""
-    from vkhashdag_gb300 import Config
+    rollback): every batch leaves the nodes it replaced behind.  The batched
+    benchmark's bucket counts hold the seeded scene and one batch; with the
+    scene and two batches kept, the fullest level-11 bucket comes within a
+    few words of its 2,048 (2,000 to 2,032 over runs on the device, the
+    insertion order moving the page padding; 2,005 in the reference's
+    sequential build of the same edits), so at 32768^3 this workload doubles
+    the level-11 buckets."""
     cfg = bench_config() if res == RES else W.config_for_resolution(res, bottom_bits=16, top_levels=6)
+    if res == RES:
+        cfg.bucket_bits_each_level[11] += 1
     pool = hd.NodePool(cfg, heap_pages=min(cfg.get_total_pages(), heap_pages), device=device)
     root = pool.edit(hd.NULL, W.sphere_scene(res, 64, seed=0))
     for k in range(n_batches):
@@ -1336,7 +1343,8 @@ def run_gc(args):
         "ms_per_step": 1e3 * t_gc, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "u32", "data": "synthetic",
         "config": {"workload": f"{res}^3 sphere scene + {args.gc_batches} x {args.n_edits} mixed edits, "
-                               f"collect keeping the last root", "node_levels": cfg.get_node_levels()},
+                               f"collect keeping the last root", "node_levels": cfg.get_node_levels(),
+                   "bucket_bits": list(cfg.bucket_bits_each_level)},
         "gc": st, "live_bytes_moved_gbs": moved / t_gc / 1e9, "queries_equal_after": same,
         "cpu_baseline": cpu, "clocks": clocks.summary(),
     }
