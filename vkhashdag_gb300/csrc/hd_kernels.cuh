@@ -231,7 +231,24 @@ __device__ __forceinline__ void write_child_list_thread(const Workspace &W, u32 
 // ------------------------------------------------------------------ k_expand_short
 // Thread per level-l inner node (l <= L-3) with an edit list of at most
 // long_threshold edits.  Children are inner items of level l+1.
-__device__ __forceinline__ void expand_short_phase(const DevPool &P, Workspace &W, u32 l, u64 tbase, u64 tstride) {
+//
+// Staged form (k_expand_short): a warp's emitted children are written by all
+// 32 lanes together instead of each node's lane walking its 8 child slots.
+// The warp's children take consecutive item slots in lane order, so child q
+// of the warp is item (warp base + q): every lane plans its node and stages
+// what each of its children needs (base, edit count, kept edits, list
+// offset) at that position in shared memory, then the lanes write the items
+// 32 at a time (coalesced), with their edit lists, the long-list queue
+// entries and, at level L-2, the leaf classes of one-edit items.
+struct ExpandWarpStage {
+	u64 pos[32];                       // the lane's node
+	u32 item[32], off[32], len[32];    // its item index and edit list
+	u32 base[256], cnt[256], keep[256], lo[256]; // per child of the warp, in item order
+	unsigned char q[256];              // lane << 3 | child slot
+};
+template <bool Staged>
+__device__ __forceinline__ void expand_short_phase(const DevPool &P, Workspace &W, u32 l, u64 tbase, u64 tstride,
+                                                   ExpandWarpStage *S = nullptr) {
 	if (ws_failed(W)) // an earlier launch overflowed: some items were never written
 		return;
 	const u32 L = P.cfg.L;
@@ -316,6 +333,86 @@ __device__ __forceinline__ void expand_short_phase(const DevPool &P, Workspace &
 		}
 		const u64 item0 = warp_reserve(&W.ctr[kWsItems + cl], n_emit);
 		const u64 list0 = warp_reserve(&W.ctr[kWsList], n_list);
+		if (Staged) {
+			const u32 lane = lane_id();
+			const u64 wbase = __shfl_sync(kFullMask, item0, 0); // lane 0's slot opens the warp's range
+			if (mine) {
+				S->pos[lane] = pos;
+				S->item[lane] = (u32)i;
+				S->off[lane] = off;
+				S->len[lane] = len;
+				u32 q = (u32)(item0 - wbase);
+				u64 lo = list0;
+#pragma unroll 1
+				for (u32 c = 0; c < 8; ++c) {
+					if (!ccnt[c])
+						continue;
+					S->q[q] = (unsigned char)((lane << 3) | c);
+					S->base[q] = cbase[c];
+					S->cnt[q] = ccnt[c];
+					S->keep[q] = len <= 32u ? part[c] : cfirst[c];
+					S->lo[q] = lo < 0xFFFFFFFFull ? (u32)lo : 0xFFFFFFFFu; // past list_cap: fails the check below
+					lo += direct_edit(ccnt[c]) ? 0u : ccnt[c];
+					++q;
+				}
+				uint4 *bc = reinterpret_cast<uint4 *>(W.bchild + i * 8u);
+				uint4 *cn = reinterpret_cast<uint4 *>(W.cnew + i * 8u);
+				bc[0] = make_uint4(old[0], old[1], old[2], old[3]);
+				bc[1] = make_uint4(old[4], old[5], old[6], old[7]);
+				u32 res[8];
+#pragma unroll
+				for (u32 c = 0; c < 8; ++c)
+					res[c] = ccnt[c] ? kNull : cbase[c]; // an emitted child's slot is written by its commit
+				cn[0] = make_uint4(res[0], res[1], res[2], res[3]);
+				cn[1] = make_uint4(res[4], res[5], res[6], res[7]);
+			}
+			const u32 total = __shfl_sync(kFullMask, (u32)(item0 - wbase) + n_emit, 31);
+			__syncwarp();
+			for (u32 j0 = 0; j0 < total; j0 += 32u) {
+				const u32 j = j0 + lane;
+				if (j >= total)
+					continue;
+				const u32 e = S->q[j], src = e >> 3, c = e & 7u;
+				const u64 it = child_begin + wbase + j;
+				const u32 cnt = S->cnt[j], slen = S->len[src], soff = S->off[src], kp = S->keep[j], lo = S->lo[j];
+				const bool direct = direct_edit(cnt);
+				const u32 n_entries = direct ? 0u : cnt;
+				u32 cx, cy, cz;
+				child_pos(S->pos[src], c, cx, cy, cz);
+				if (it < W.inner.cap && (u64)lo + n_entries <= W.list_cap) {
+					W.inner.pos[it] = pack_pos(cx, cy, cz);
+					W.inner.base[it] = S->base[j];
+					W.inner.parent[it] = S->item[src] * 8u + c;
+					W.inner.lst_len[it] = cnt;
+					if (direct) { // the one kept edit: the first set bit of keep / position keep
+						const u32 id = slen <= 32u ? item_list_at(W, soff, slen, (u32)(__ffs(kp) - 1)) : W.lists[soff + kp];
+						W.inner.lst_off[it] = id;
+						if (cl + 2u == L)
+							W.leaf_cls[it] = leaf_classes(W.edits[id], cx, cy, cz);
+					} else {
+						W.inner.lst_off[it] = lo;
+						if (slen <= 32u) {
+							u32 k = 0;
+							for (u32 m = kp; m; m &= m - 1u)
+								W.lists[lo + k++] = item_list_at(W, soff, slen, (u32)(__ffs(m) - 1));
+						} else {
+							write_child_list_thread(W, soff, slen, kp, shift, cx, cy, cz, W.lists + lo);
+						}
+					}
+					if (cnt > T) { // rare: one queue slot each
+						const unsigned long long lg = atomicAdd(&W.ctr[kWsLong + cl], 1ull);
+						if (child_begin + lg < W.inner.cap)
+							W.long_q[child_begin + lg] = (u32)it;
+						else
+							ws_error(W, kErrCapacity);
+					}
+				} else {
+					ws_error(W, kErrCapacity);
+				}
+			}
+			__syncwarp(); // the stage is rewritten by the next iteration
+			continue;
+		}
 		const u64 long0 = warp_reserve(&W.ctr[kWsLong + cl], n_long);
 		if (!mine)
 			continue;
@@ -375,8 +472,10 @@ __device__ __forceinline__ void expand_short_phase(const DevPool &P, Workspace &
 	}
 }
 static __global__ void __launch_bounds__(kBlock) k_expand_short(DevPool P, Workspace W, u32 l) {
+	__shared__ ExpandWarpStage s_stage[kBlock / 32];
 	apply_pass_desc(W);
-	expand_short_phase(P, W, l, (u64)blockIdx.x * blockDim.x, (u64)gridDim.x * blockDim.x);
+	expand_short_phase<true>(P, W, l, (u64)blockIdx.x * blockDim.x, (u64)gridDim.x * blockDim.x,
+	                         &s_stage[threadIdx.x >> 5]);
 }
 
 // ------------------------------------------------------------------ block planning (long lists)
@@ -1750,7 +1849,7 @@ static __global__ void __launch_bounds__(kBlock) k_small_pass(DevPool P, Workspa
 	root_phase(P, W, root_val, root_ptr);
 	__syncthreads();
 	for (u32 l = 0; l + 2 < L; ++l) {
-		expand_short_phase(P, W, l, tb, ts);
+		expand_short_phase<false>(P, W, l, tb, ts);
 		__syncthreads();
 	}
 	if (L >= 2) {
